@@ -1,0 +1,82 @@
+"""ctypes binding of ``libhermes_gb300.so`` (the C ABI in include/hermes_gb300.h).
+
+The library is required: there is no CPU fallback.  If it is missing the
+first call raises ``HermesLibraryError`` telling the user to build it.
+"""
+
+import ctypes
+import os
+import re
+
+from .build import LIB_PATH, PKG_DIR
+
+HEADER_PATH = os.path.join(PKG_DIR, "..", "include", "hermes_gb300.h")
+
+_c_int = ctypes.c_int
+_c_i64 = ctypes.c_int64
+_c_sz = ctypes.c_size_t
+_p = ctypes.c_void_p
+_dbl = ctypes.c_double
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "hermes_version": (ctypes.c_char_p, []),
+    "hermes_last_error": (ctypes.c_char_p, []),
+    "hermes_deposit_workspace_size": (_c_int, [_c_i64, _c_int, ctypes.POINTER(_c_sz)]),
+    "hermes_deposit": (_c_int, [_p, _p, _c_i64, _c_int, _dbl, _p, _c_int, _c_int,
+                                _p, _p, _p, _p, _c_sz, _p]),
+    "hermes_deposit_sort": (_c_int, [_p, _p, _c_i64, _c_int, _dbl, _p, _c_int, _c_int, _p, _c_sz, _p]),
+    "hermes_deposit_accumulate": (_c_int, [_c_i64, _c_int, _dbl, _p, _c_int, _c_int, _p, _p, _p,
+                                           _p, _c_sz, _p]),
+    "hermes_deposit_status": (_c_int, [_p, ctypes.POINTER(_c_i64), _p]),
+}
+
+
+class HermesLibraryError(RuntimeError):
+    """The CUDA library is missing or could not be loaded."""
+
+
+class HermesError(RuntimeError):
+    """A hermes_* call returned a non-zero status."""
+
+    def __init__(self, code, message):
+        super().__init__(f"hermes error {code}: {message}")
+        self.code = code
+
+
+_LIB = None
+
+
+def header_symbols():
+    """Every function name declared in include/hermes_gb300.h."""
+    text = open(HEADER_PATH).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(hermes_[a-z0-9_]+)\s*\(", text)))
+
+
+def load():
+    """Load (once) and return the library with argument types declared."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(LIB_PATH):
+        raise HermesLibraryError(
+            f"{LIB_PATH} is not built; run `python -c 'import __graft_entry__ as g; g.build()'` "
+            "or `python -m pyhermes_gb300.build`."
+        )
+    try:
+        lib = ctypes.CDLL(LIB_PATH)
+    except OSError as exc:
+        raise HermesLibraryError(f"cannot load {LIB_PATH}: {exc}") from exc
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = lib
+    return lib
+
+
+def check(rc, what=""):
+    if rc != 0:
+        msg = load().hermes_last_error().decode(errors="replace")
+        raise HermesError(rc, f"{what}: {msg}" if what else msg)

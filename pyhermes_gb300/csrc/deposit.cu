@@ -1,0 +1,563 @@
+// SFC deposit: particles -> scaling-function coefficients eps[L,L,L].
+//
+// Restates pyhermes/utils/wavelet_grid.py:17-55 (_project_scaling_grid_impl)
+// for one GB300.  The reference walks particles sequentially and does 27
+// float64 read-modify-writes per particle into the grid.  Here:
+//
+//   K0 dep_max_kernel     max|w| and max|phi| (order-independent bound)
+//   K1 dep_bin_kernel     per particle: float64 cell/frac (bit-identical to the
+//                         reference's floor/astype(int32)), packed 16-byte
+//                         record, histogram over (home tile, region) buckets
+//   K2 dep_scan_*         exclusive scan of the bucket histogram
+//   K3 dep_scatter_kernel counting-sort scatter (warp-aggregated slots)
+//   K4 dep_accum_kernel   one CTA per output tile: gathers the records of its
+//                         own tile and of the <=7 upper-neighbour tiles whose
+//                         support reaches it, accumulates each particle's
+//                         27-cell stencil into shared-memory int64 fixed-point
+//                         cells, then writes the tile once, coalesced.
+//
+// Each output cell is written exactly once (no zero-fill pass, no global
+// atomics on the grid).  Integer accumulation is associative, so the result
+// is bitwise independent of particle order and scheduling.  The region code
+// of a record marks the axes along which its stencil crosses into the lower
+// neighbour tile, so a CTA reads only records that reach it.
+#include <math.h>
+
+#include "hermes_common.cuh"
+
+namespace {
+
+constexpr int kMaxSupport = 4;
+constexpr int kTileX = 8, kTileY = 16, kTileZ = 32;
+constexpr int kAccThreads = 512;
+constexpr int kScanChunk = 4096;  // elements per scan block (1024 threads x 4)
+constexpr unsigned kRejected = 0xFFFFFFFFu;
+
+struct __align__(16) DepRec {
+  uint32_t cell;  // cx << 20 | cy << 10 | cz
+  uint32_t frac;  // fx << 20 | fy << 10 | fz
+  float w;
+  uint32_t key;   // home_tile * 8 + region, or kRejected
+};
+
+struct DepGeom {
+  int L, S, res;
+  int tx, ty, tz;     // tile extents (cells)
+  int ntx, nty, ntz;  // tiles per axis
+  double scale;       // L / box
+};
+
+struct DepStatus {
+  unsigned long long rejected;  // non-finite or out-of-range particles
+  unsigned int wmax_bits;       // max |w| (float, rounded up) as bits
+  unsigned int phimax_bits;     // max |phi| (float, rounded up) as bits
+};
+
+__device__ __forceinline__ float warp_max(float v) {
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+__global__ void dep_max_kernel(const double* __restrict__ w, int64_t n,
+                               const double* __restrict__ phi, int n_phi,
+                               DepStatus* st) {
+  float m = 0.f, pm = 0.f;
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    double v = fabs(w[i]);
+    if (isfinite(v)) m = fmaxf(m, __double2float_ru(v));
+  }
+  if (blockIdx.x == 0) {
+    for (int i = threadIdx.x; i < n_phi; i += blockDim.x)
+      pm = fmaxf(pm, __double2float_ru(fabs(phi[i])));
+  }
+  m = warp_max(m);
+  pm = warp_max(pm);
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(&st->wmax_bits, __float_as_uint(m));
+    atomicMax(&st->phimax_bits, __float_as_uint(pm));
+  }
+}
+
+// float64 cell / fraction index of one coordinate, exactly as the reference:
+// scaled = x * (L/box); c = floor(scaled); f = int((scaled - c) * res).
+__device__ __forceinline__ bool dep_axis(double x, const DepGeom& g, int& c, int& f) {
+  double s = __dmul_rn(x, g.scale);
+  if (!(fabs(s) < 1073741824.0)) return false;
+  double fl = floor(s);
+  c = (int)fl;
+  f = (int)__dmul_rn(__dsub_rn(s, fl), (double)g.res);
+  if (f < 0) f = 0;
+  if (f >= g.res) f = g.res - 1;
+  c &= (g.L - 1);  // periodic wrap (matches the reference's negative-index wrap)
+  return true;
+}
+
+__device__ __forceinline__ unsigned dep_key(int cx, int cy, int cz, const DepGeom& g) {
+  int hx = cx / g.tx, hy = cy / g.ty, hz = cz / g.tz;
+  unsigned region = 0;
+  if (g.ntx > 1 && (cx - hx * g.tx) < g.S - 1) region |= 1u;
+  if (g.nty > 1 && (cy - hy * g.ty) < g.S - 1) region |= 2u;
+  if (g.ntz > 1 && (cz - hz * g.tz) < g.S - 1) region |= 4u;
+  unsigned tile = ((unsigned)hx * g.nty + hy) * g.ntz + hz;
+  return tile * 8u + region;
+}
+
+// Warp-aggregated atomicAdd of 1 per lane on ctr[key]; returns each lane's
+// slot.  All 32 lanes must call it; lanes with key == kRejected get nothing.
+__device__ __forceinline__ unsigned warp_agg_slot(unsigned* ctr, unsigned key) {
+  unsigned lane = threadIdx.x & 31;
+  unsigned peers = __match_any_sync(0xffffffffu, key);
+  int leader = __ffs(peers) - 1;
+  unsigned rank = __popc(peers & ((1u << lane) - 1u));
+  unsigned base = 0;
+  if ((int)lane == leader && key != kRejected) base = atomicAdd(&ctr[key], (unsigned)__popc(peers));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  return base + rank;
+}
+
+__global__ void dep_bin_kernel(const double* __restrict__ pos, const double* __restrict__ w,
+                               int64_t n, DepGeom g, DepRec* __restrict__ rec,
+                               unsigned* __restrict__ counts, DepStatus* st) {
+  int64_t warp_stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += warp_stride) {
+    int64_t i = base + threadIdx.x;
+    unsigned key = kRejected;
+    if (i < n) {
+      double x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
+      double wi = w[i];
+      int cx, cy, cz, fx, fy, fz;
+      bool ok = isfinite(x) && isfinite(y) && isfinite(z) && isfinite(wi) &&
+                dep_axis(x, g, cx, fx) && dep_axis(y, g, cy, fy) && dep_axis(z, g, cz, fz);
+      DepRec r;
+      if (ok) {
+        key = dep_key(cx, cy, cz, g);
+        r.cell = ((unsigned)cx << 20) | ((unsigned)cy << 10) | (unsigned)cz;
+        r.frac = ((unsigned)fx << 20) | ((unsigned)fy << 10) | (unsigned)fz;
+        r.w = (float)wi;
+      } else {
+        r.cell = 0;
+        r.frac = 0;
+        r.w = 0.f;
+        atomicAdd(&st->rejected, 1ULL);
+      }
+      r.key = key;
+      rec[i] = r;
+    }
+    warp_agg_slot(counts, key);
+  }
+}
+
+// Scan phase 1: per-chunk sums.
+__global__ void dep_scan_sums_kernel(const unsigned* __restrict__ counts, int nb,
+                                     unsigned* __restrict__ chunk_sums) {
+  __shared__ unsigned warp_tot[32];
+  int beg = blockIdx.x * kScanChunk;
+  unsigned s = 0;
+  for (int k = 0; k < 4; ++k) {
+    int i = beg + k * 1024 + threadIdx.x;
+    if (i < nb) s += counts[i];
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) warp_tot[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    unsigned v = warp_tot[threadIdx.x];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (threadIdx.x == 0) chunk_sums[blockIdx.x] = v;
+  }
+}
+
+// Block-wide exclusive scan of one value per thread (1024 threads).
+__device__ unsigned block_excl_scan_1024(unsigned v, unsigned* total) {
+  __shared__ unsigned warp_part[32];
+  unsigned lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  unsigned inc = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    unsigned t = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= (unsigned)o) inc += t;
+  }
+  if (lane == 31) warp_part[wid] = inc;
+  __syncthreads();
+  if (wid == 0) {
+    unsigned p = warp_part[lane];
+    unsigned pinc = p;
+    for (int o = 1; o < 32; o <<= 1) {
+      unsigned t = __shfl_up_sync(0xffffffffu, pinc, o);
+      if (lane >= (unsigned)o) pinc += t;
+    }
+    warp_part[lane] = pinc - p;  // exclusive warp prefix
+    if (lane == 31) *total = pinc;
+  }
+  __syncthreads();
+  unsigned r = warp_part[wid] + inc - v;
+  __syncthreads();
+  return r;
+}
+
+// Scan phase 2: exclusive scan of chunk sums (single block, serial over
+// groups of 1024).
+__global__ void dep_scan_chunks_kernel(unsigned* chunk_sums, int nchunks) {
+  __shared__ unsigned total;
+  unsigned carry = 0;
+  for (int beg = 0; beg < nchunks; beg += 1024) {
+    int i = beg + threadIdx.x;
+    unsigned v = i < nchunks ? chunk_sums[i] : 0u;
+    unsigned ex = block_excl_scan_1024(v, &total);
+    if (i < nchunks) chunk_sums[i] = carry + ex;
+    carry += total;
+    __syncthreads();
+  }
+}
+
+// Scan phase 3: rescan each chunk with its prefix; writes offsets and the
+// scatter cursor, and offsets[nb] = grand total.
+__global__ void dep_scan_apply_kernel(const unsigned* __restrict__ counts, int nb,
+                                      const unsigned* __restrict__ chunk_prefix,
+                                      unsigned* __restrict__ offsets,
+                                      unsigned* __restrict__ cursor) {
+  __shared__ unsigned total;
+  int beg = blockIdx.x * kScanChunk + threadIdx.x * 4;
+  unsigned v[4];
+  unsigned s = 0;
+  for (int k = 0; k < 4; ++k) {
+    v[k] = (beg + k < nb) ? counts[beg + k] : 0u;
+    s += v[k];
+  }
+  unsigned ex = block_excl_scan_1024(s, &total) + chunk_prefix[blockIdx.x];
+  for (int k = 0; k < 4; ++k) {
+    if (beg + k < nb) {
+      offsets[beg + k] = ex;
+      cursor[beg + k] = ex;
+    }
+    ex += v[k];
+  }
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 1023) offsets[nb] = ex;
+}
+
+__global__ void dep_scatter_kernel(const DepRec* __restrict__ rec, int64_t n,
+                                   unsigned* __restrict__ cursor,
+                                   DepRec* __restrict__ sorted) {
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
+    int64_t i = base + threadIdx.x;
+    DepRec r;
+    unsigned key = kRejected;
+    if (i < n) {
+      r = rec[i];
+      key = r.key;
+    }
+    unsigned slot = warp_agg_slot(cursor, key);
+    if (key != kRejected) sorted[slot] = r;
+  }
+}
+
+__device__ __forceinline__ double dep_fixed_scale(const DepStatus* st, int64_t n) {
+  double wmax = (double)__uint_as_float(st->wmax_bits);
+  double pmax = (double)__uint_as_float(st->phimax_bits);
+  double bound = (double)n * wmax * pmax * pmax * pmax;
+  int e = -60;
+  if (bound > 0.0) {
+    frexp(bound, &e);  // bound < 2^e
+    if (e < -60) e = -60;
+  }
+  return ldexp(1.0, 62 - e);  // bound * scale < 2^62
+}
+
+template <int S, bool kF64Out>
+__global__ void __launch_bounds__(kAccThreads)
+dep_accum_kernel(const DepRec* __restrict__ sorted, const unsigned* __restrict__ offsets,
+                 const double* __restrict__ phi, int n_phi, DepGeom g, int64_t n,
+                 const DepStatus* __restrict__ st, float* __restrict__ out32,
+                 double* __restrict__ out64, unsigned* __restrict__ counts_out) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int ncell = g.tx * g.ty * g.tz;
+  long long* acc = reinterpret_cast<long long*>(smem);
+  unsigned* cnt = reinterpret_cast<unsigned*>(acc + ncell);
+  float* phis = reinterpret_cast<float*>(cnt + (counts_out ? ncell : 0));
+  __shared__ unsigned r_start[27], r_pref[28], r_home[27];
+  __shared__ int n_ranges;
+
+  const int tile = blockIdx.x;
+  const int hz = tile % g.ntz, hy = (tile / g.ntz) % g.nty, hx = tile / (g.ntz * g.nty);
+  const int x0 = hx * g.tx, y0 = hy * g.ty, z0 = hz * g.tz;
+
+  for (int i = threadIdx.x; i < n_phi; i += blockDim.x) phis[i] = __double2float_rn(phi[i]);
+  for (int i = threadIdx.x; i < ncell; i += blockDim.x) {
+    acc[i] = 0;
+    if (counts_out) cnt[i] = 0;
+  }
+  if (threadIdx.x == 0) {
+    int nr = 0;
+    unsigned run = 0;
+    for (int d = 0; d < 8; ++d) {
+      int dx = d & 1, dy = (d >> 1) & 1, dz = (d >> 2) & 1;
+      if ((dx && g.ntx == 1) || (dy && g.nty == 1) || (dz && g.ntz == 1)) continue;
+      int nx_ = (hx + dx) % g.ntx, ny_ = (hy + dy) % g.nty, nz_ = (hz + dz) % g.ntz;
+      unsigned nt = ((unsigned)nx_ * g.nty + ny_) * g.ntz + nz_;
+      unsigned D = (unsigned)d;
+      for (unsigned r = 0; r < 8; ++r) {
+        if ((r & D) != D) continue;
+        unsigned b = nt * 8u + r;
+        unsigned s0 = offsets[b], s1 = offsets[b + 1];
+        if (s1 > s0) {
+          r_start[nr] = s0;
+          r_pref[nr] = run;
+          r_home[nr] = (d == 0);
+          run += s1 - s0;
+          ++nr;
+        }
+      }
+    }
+    r_pref[nr] = run;
+    n_ranges = nr;
+  }
+  __syncthreads();
+
+  const double scale = dep_fixed_scale(st, n);
+  const float scale_f = (float)scale;
+  const int nr = n_ranges;
+  const unsigned total = r_pref[nr];
+  const int Lm = g.L - 1;
+  for (unsigned k = threadIdx.x; k < total; k += blockDim.x) {
+    int r = 0;
+    while (r + 1 < nr && r_pref[r + 1] <= k) ++r;
+    const DepRec rec = sorted[r_start[r] + (k - r_pref[r])];
+    const int cx = rec.cell >> 20, cy = (rec.cell >> 10) & 1023, cz = rec.cell & 1023;
+    const int fx = rec.frac >> 20, fy = (rec.frac >> 10) & 1023, fz = rec.frac & 1023;
+    int lx[S], ly[S], lz[S];
+    float px[S], py[S], pz[S];
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+      lx[s] = (cx - s - x0) & Lm;
+      ly[s] = (cy - s - y0) & Lm;
+      lz[s] = (cz - s - z0) & Lm;
+      px[s] = rec.w * phis[fx + g.res * s];
+      py[s] = phis[fy + g.res * s];
+      pz[s] = phis[fz + g.res * s];
+    }
+#pragma unroll
+    for (int a = 0; a < S; ++a) {
+      if (lx[a] >= g.tx) continue;
+#pragma unroll
+      for (int b = 0; b < S; ++b) {
+        if (ly[b] >= g.ty) continue;
+        const float pxy = px[a] * py[b];
+        const int row = (lx[a] * g.ty + ly[b]) * g.tz;
+#pragma unroll
+        for (int c = 0; c < S; ++c) {
+          if (lz[c] >= g.tz) continue;
+          const long long q = __float2ll_rn(pxy * pz[c] * scale_f);
+          atomicAdd(reinterpret_cast<unsigned long long*>(&acc[row + lz[c]]),
+                    static_cast<unsigned long long>(q));
+        }
+      }
+    }
+    if (counts_out && r_home[r]) {
+      atomicAdd(&cnt[((cx - x0) * g.ty + (cy - y0)) * g.tz + (cz - z0)], 1u);
+    }
+  }
+  __syncthreads();
+
+  const float inv_f = (float)(1.0 / scale);
+  const double inv_d = 1.0 / scale;
+  for (int i = threadIdx.x; i < ncell; i += blockDim.x) {
+    const int lz_ = i % g.tz, ly_ = (i / g.tz) % g.ty, lx_ = i / (g.tz * g.ty);
+    const size_t gi = ((size_t)(x0 + lx_) * g.L + (y0 + ly_)) * g.L + (z0 + lz_);
+    if (kF64Out) {
+      out64[gi] = (double)acc[i] * inv_d;
+    } else {
+      out32[gi] = __ll2float_rn(acc[i]) * inv_f;
+    }
+    if (counts_out) counts_out[gi] = cnt[i];
+  }
+}
+
+template <int S>
+int dep_launch_accum(const DepRec* sorted, const unsigned* offsets, const double* phi, int n_phi,
+                     const DepGeom& g, int64_t n, const DepStatus* st, float* eps_out,
+                     double* eps_f64_out, unsigned* counts_out, int ntiles, size_t smem,
+                     cudaStream_t s) {
+  if (eps_f64_out) {
+    HERMES_CUDA_TRY(cudaFuncSetAttribute(dep_accum_kernel<S, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dep_accum_kernel<S, true><<<ntiles, kAccThreads, smem, s>>>(sorted, offsets, phi, n_phi, g, n, st,
+                                                                nullptr, eps_f64_out, counts_out);
+  } else {
+    HERMES_CUDA_TRY(cudaFuncSetAttribute(dep_accum_kernel<S, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dep_accum_kernel<S, false><<<ntiles, kAccThreads, smem, s>>>(sorted, offsets, phi, n_phi, g, n, st,
+                                                                 eps_out, nullptr, counts_out);
+  }
+  return HERMES_OK;
+}
+
+struct DepPlan {
+  DepGeom g;
+  int nbuckets;
+  int nchunks;
+  size_t ws_bytes;
+};
+
+int dep_plan(int64_t n, int J, int S, int res, DepPlan* p) {
+  if (J < 2 || J > 10) return hermes::fail(HERMES_ERR_INVALID, "deposit: J=%d outside [2,10]", J);
+  if (n < 0 || n > 0x7FFFFFFFLL) return hermes::fail(HERMES_ERR_INVALID, "deposit: n=%lld outside [0,2^31)", (long long)n);
+  if (S < 1 || S > kMaxSupport) return hermes::fail(HERMES_ERR_INVALID, "deposit: phi support %d outside [1,%d]", S, kMaxSupport);
+  if (res < 1 || res > 1024) return hermes::fail(HERMES_ERR_INVALID, "deposit: phi_res %d outside [1,1024]", res);
+  DepGeom& g = p->g;
+  g.L = 1 << J;
+  g.S = S;
+  g.res = res;
+  g.tx = g.L < kTileX ? g.L : kTileX;
+  g.ty = g.L < kTileY ? g.L : kTileY;
+  g.tz = g.L < kTileZ ? g.L : kTileZ;
+  if (S - 1 > g.tx) return hermes::fail(HERMES_ERR_INVALID, "deposit: grid too small for support");
+  g.ntx = g.L / g.tx;
+  g.nty = g.L / g.ty;
+  g.ntz = g.L / g.tz;
+  const int ntiles = g.ntx * g.nty * g.ntz;
+  p->nbuckets = ntiles * 8;
+  p->nchunks = (p->nbuckets + kScanChunk - 1) / kScanChunk;
+  hermes::Carver c(nullptr, 0);
+  c.take<DepStatus>(1);
+  c.take<unsigned>(p->nbuckets);      // counts
+  c.take<unsigned>(p->nbuckets + 1);  // offsets
+  c.take<unsigned>(p->nbuckets);      // cursor
+  c.take<unsigned>(p->nchunks);       // chunk sums
+  c.take<DepRec>((size_t)(n > 0 ? n : 1));  // unsorted records
+  c.take<DepRec>((size_t)(n > 0 ? n : 1));  // sorted records
+  p->ws_bytes = c.used;
+  return HERMES_OK;
+}
+
+}  // namespace
+
+extern "C" int hermes_deposit_workspace_size(int64_t n, int J, size_t* bytes) {
+  if (!bytes) return hermes::fail(HERMES_ERR_INVALID, "deposit: bytes is NULL");
+  DepPlan p;
+  int rc = dep_plan(n, J, 3, 1024, &p);
+  if (rc) return rc;
+  *bytes = p.ws_bytes;
+  return HERMES_OK;
+}
+
+namespace {
+
+struct DepBuffers {
+  DepStatus* st;
+  unsigned* counts;
+  unsigned* offsets;
+  unsigned* cursor;
+  unsigned* chunk_sums;
+  DepRec* rec;
+  DepRec* sorted;
+};
+
+int dep_prepare(int64_t n, int J, double box, int n_phi, int phi_res, const double* phi,
+                void* workspace, size_t workspace_bytes, DepPlan* p, DepBuffers* b) {
+  if (!(box > 0.0) || !isfinite(box)) return hermes::fail(HERMES_ERR_INVALID, "deposit: box must be finite and > 0");
+  if (!phi || phi_res <= 0 || n_phi <= 0 || n_phi % phi_res)
+    return hermes::fail(HERMES_ERR_INVALID, "deposit: n_phi=%d must be a positive multiple of phi_res=%d", n_phi, phi_res);
+  int rc = dep_plan(n, J, n_phi / phi_res, phi_res, p);
+  if (rc) return rc;
+  p->g.scale = (double)p->g.L / box;
+  if (!workspace || workspace_bytes < p->ws_bytes)
+    return hermes::fail(HERMES_ERR_WORKSPACE, "deposit: workspace %zu < required %zu", workspace_bytes, p->ws_bytes);
+  hermes::Carver c(workspace, workspace_bytes);
+  b->st = c.take<DepStatus>(1);
+  b->counts = c.take<unsigned>(p->nbuckets);
+  b->offsets = c.take<unsigned>(p->nbuckets + 1);
+  b->cursor = c.take<unsigned>(p->nbuckets);
+  b->chunk_sums = c.take<unsigned>(p->nchunks);
+  b->rec = c.take<DepRec>((size_t)(n > 0 ? n : 1));
+  b->sorted = c.take<DepRec>((size_t)(n > 0 ? n : 1));
+  return HERMES_OK;
+}
+
+}  // namespace
+
+extern "C" int hermes_deposit_sort(const double* pos, const double* w, int64_t n, int J,
+                                   double box, const double* phi, int n_phi, int phi_res,
+                                   void* workspace, size_t workspace_bytes, void* stream) {
+  if (n > 0 && (!pos || !w)) return hermes::fail(HERMES_ERR_INVALID, "deposit: pos/w NULL");
+  DepPlan p;
+  DepBuffers b;
+  int rc = dep_prepare(n, J, box, n_phi, phi_res, phi, workspace, workspace_bytes, &p, &b);
+  if (rc) return rc;
+  cudaStream_t s = hermes::as_stream(stream);
+  HERMES_CUDA_TRY(cudaMemsetAsync(b.st, 0, sizeof(DepStatus), s));
+  HERMES_CUDA_TRY(cudaMemsetAsync(b.counts, 0, sizeof(unsigned) * p.nbuckets, s));
+  int dev = 0, nsm = 148;
+  HERMES_CUDA_TRY(cudaGetDevice(&dev));
+  HERMES_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  const int64_t want = (n + 255) / 256;
+  const int grid_p = (int)(want < 1 ? 1 : (want < (int64_t)nsm * 8 ? want : (int64_t)nsm * 8));
+
+  dep_max_kernel<<<grid_p, 256, 0, s>>>(w, n, phi, n_phi, b.st);
+  HERMES_LAUNCH_CHECK("dep_max_kernel");
+  if (n > 0) {
+    dep_bin_kernel<<<grid_p, 256, 0, s>>>(pos, w, n, p.g, b.rec, b.counts, b.st);
+    HERMES_LAUNCH_CHECK("dep_bin_kernel");
+  }
+  dep_scan_sums_kernel<<<p.nchunks, 1024, 0, s>>>(b.counts, p.nbuckets, b.chunk_sums);
+  HERMES_LAUNCH_CHECK("dep_scan_sums_kernel");
+  dep_scan_chunks_kernel<<<1, 1024, 0, s>>>(b.chunk_sums, p.nchunks);
+  HERMES_LAUNCH_CHECK("dep_scan_chunks_kernel");
+  dep_scan_apply_kernel<<<p.nchunks, 1024, 0, s>>>(b.counts, p.nbuckets, b.chunk_sums, b.offsets, b.cursor);
+  HERMES_LAUNCH_CHECK("dep_scan_apply_kernel");
+  if (n > 0) {
+    dep_scatter_kernel<<<grid_p, 256, 0, s>>>(b.rec, n, b.cursor, b.sorted);
+    HERMES_LAUNCH_CHECK("dep_scatter_kernel");
+  }
+  return HERMES_OK;
+}
+
+extern "C" int hermes_deposit_accumulate(int64_t n, int J, double box, const double* phi,
+                                         int n_phi, int phi_res, float* eps_out,
+                                         double* eps_f64_out, uint32_t* counts_out,
+                                         void* workspace, size_t workspace_bytes, void* stream) {
+  if ((eps_out == nullptr) == (eps_f64_out == nullptr))
+    return hermes::fail(HERMES_ERR_INVALID, "deposit: give exactly one of eps_out / eps_f64_out");
+  DepPlan p;
+  DepBuffers b;
+  int rc = dep_prepare(n, J, box, n_phi, phi_res, phi, workspace, workspace_bytes, &p, &b);
+  if (rc) return rc;
+  cudaStream_t s = hermes::as_stream(stream);
+  const int ncell = p.g.tx * p.g.ty * p.g.tz;
+  const size_t smem = (size_t)ncell * 8 + (counts_out ? (size_t)ncell * 4 : 0) + (size_t)n_phi * 4;
+  if (smem > 227 * 1024) return hermes::fail(HERMES_ERR_UNSUPPORTED, "deposit: shared memory %zu too large", smem);
+  const int ntiles = p.g.ntx * p.g.nty * p.g.ntz;
+  DepRec* sorted = b.sorted;
+  unsigned* offsets = b.offsets;
+  DepStatus* st = b.st;
+  int lrc = HERMES_OK;
+  switch (p.g.S) {
+    case 1: lrc = dep_launch_accum<1>(sorted, offsets, phi, n_phi, p.g, n, st, eps_out, eps_f64_out, counts_out, ntiles, smem, s); break;
+    case 2: lrc = dep_launch_accum<2>(sorted, offsets, phi, n_phi, p.g, n, st, eps_out, eps_f64_out, counts_out, ntiles, smem, s); break;
+    case 3: lrc = dep_launch_accum<3>(sorted, offsets, phi, n_phi, p.g, n, st, eps_out, eps_f64_out, counts_out, ntiles, smem, s); break;
+    default: lrc = dep_launch_accum<4>(sorted, offsets, phi, n_phi, p.g, n, st, eps_out, eps_f64_out, counts_out, ntiles, smem, s); break;
+  }
+  if (lrc) return lrc;
+  HERMES_LAUNCH_CHECK("dep_accum_kernel");
+  return HERMES_OK;
+}
+
+extern "C" int hermes_deposit(const double* pos, const double* w, int64_t n, int J,
+                              double box, const double* phi, int n_phi, int phi_res,
+                              float* eps_out, double* eps_f64_out, uint32_t* counts_out,
+                              void* workspace, size_t workspace_bytes, void* stream) {
+  if ((eps_out == nullptr) == (eps_f64_out == nullptr))
+    return hermes::fail(HERMES_ERR_INVALID, "deposit: give exactly one of eps_out / eps_f64_out");
+  int rc = hermes_deposit_sort(pos, w, n, J, box, phi, n_phi, phi_res, workspace, workspace_bytes, stream);
+  if (rc) return rc;
+  return hermes_deposit_accumulate(n, J, box, phi, n_phi, phi_res, eps_out, eps_f64_out, counts_out,
+                                   workspace, workspace_bytes, stream);
+}
+
+extern "C" int hermes_deposit_status(const void* workspace, int64_t* n_rejected, void* stream) {
+  if (!workspace || !n_rejected) return hermes::fail(HERMES_ERR_INVALID, "deposit_status: NULL argument");
+  DepStatus st;
+  cudaStream_t s = hermes::as_stream(stream);
+  HERMES_CUDA_TRY(cudaMemcpyAsync(&st, workspace, sizeof(st), cudaMemcpyDeviceToHost, s));
+  HERMES_CUDA_TRY(cudaStreamSynchronize(s));
+  *n_rejected = (int64_t)st.rejected;
+  return HERMES_OK;
+}

@@ -1,0 +1,129 @@
+"""Task parameter defaults and merging, mirroring the reference's
+``TaskBase`` + ``ParamBase.recursive_update`` behaviour
+(pyhermes/pipeline/pipeline.py:12-49, pyhermes/param/parambase.py:116-172):
+a user dict ``{TaskName: {...}}`` is merged into the task defaults; keys in
+``REPLACE_KEYS`` are replaced wholesale instead of merged.
+
+The defaults restate the values of the reference's per-package
+default_params.json files for the keys this package reads.
+"""
+
+import copy
+
+REPLACE_KEYS = {
+    "Corr_2PCF.binning_window",
+    "Corr_2PCF.sampling",
+    "Corr_3PCF_Multipole.binning_window12",
+    "Corr_3PCF_Multipole.binning_window13",
+    "Corr_3PCF_Multipole.sampling",
+    "Corr_3PCF_Multipole.sample_mpi",
+}
+
+_EMPTY_WINDOW = {"type": "", "len_args": {}, "los_args": {}, "other_args": {}}
+
+DEFAULTS = {
+    "SFCProjection": {
+        "fin": {"path": "", "format": "bin", "download": {}, "reader_params": {},
+                "catalog_weight_key": None, "field_value_key": None},
+        "particle_pos": None,
+        "catalog_weight": None,
+        "field_value": None,
+        "weight_normalization": "catalog",
+        "box_size": 1000,
+        "J": 8,
+        "wavelet_mode": "db2",
+        "wavelet_level": 10,
+        "phi_resolution": 1024,
+        "save_particle_data": False,
+        "particle_data_path": "",
+        "threads": 1,
+        "fout_path": "",
+    },
+    "Corr_2PCF": {
+        "sfc_field": "", "sfc_field1": "", "sfc_field2": "",
+        "random": None, "random1": "", "random2": "",
+        "weight_normalization": "catalog",
+        "window": dict(_EMPTY_WINDOW), "window1": dict(_EMPTY_WINDOW), "window2": dict(_EMPTY_WINDOW),
+        "binning_window": {"type": "shell", "len_args": ["R"], "los_args": {}, "other_args": {},
+                           "mapping": "s_to_R", "kernel_mode": ""},
+        "sampling": {"s": {"min": 1.0, "max": 150.0, "n": 30}},
+        "threads": 1,
+        "products": "xi",
+        "memory_strategy": "speed",
+        "binning_window_cache": False,
+        "binning_window_cache_dir": "",
+        "fout_path": "",
+    },
+    "Corr_3PCF_Multipole": {
+        "sfc_field": "", "sfc_field1": "", "sfc_field2": "", "sfc_field3": "",
+        "random": None, "random1": "", "random2": "", "random3": "",
+        "weight_normalization": "catalog",
+        "window": dict(_EMPTY_WINDOW), "window1": dict(_EMPTY_WINDOW),
+        "window2": dict(_EMPTY_WINDOW), "window3": dict(_EMPTY_WINDOW),
+        "binning_window12": {"type": "shell", "len_args": {}, "other_args": {}, "mapping": {}},
+        "binning_window13": {"type": "shell", "len_args": {}, "other_args": {}, "mapping": {}},
+        "sampling": {},
+        "l_min": 0,
+        "l_max": 4,
+        "gpu_device_id": 0,
+        "gpu_threads_per_block": [8, 8, 8],
+        "summation_backend": "gb300",
+        "execution_mode": "serial",
+        "sample_mpi": {"ranks_per_sample": 1, "gpu_device_ids": []},
+        "cache_multipole_fields": False,
+        "cache_dir": "",
+        "verbose_m_progress": False,
+        "verbose_profile": False,
+        "zeta_condition_warning": 1.0e12,
+        "threads": 1,
+        "products": "zeta_l",
+        "fout_path": "",
+        "contraction": "mixed",
+    },
+    "Corr_3PCF": {
+        "sfc_field": "", "sfc_field1": "", "sfc_field2": "", "sfc_field3": "",
+        "particle_pos1": None, "particle_weight1": None,
+        "random": None, "random1": "", "random2": "", "random3": "",
+        "weight_normalization": "catalog",
+        "r12": 20.0, "r13": 40.0,
+        "angle_param": "theta",
+        "theta": {"theta_min": 0.0, "theta_max": 3.141592653589793, "n_theta": 20},
+        "mu": {"mu_min": -1.0, "mu_max": 1.0, "n_mu": 20},
+        "n_rot": 100,
+        "center": "box_random",
+        "n_box_centers": 5000000,
+        "base_seed": 42,
+        "threads": 1,
+        "products": "Q",
+        "fout_path": "",
+    },
+}
+
+
+def _is_array_like(v):
+    return hasattr(v, "shape") and hasattr(v, "dtype")
+
+
+def recursive_update(default, new, section):
+    """Merge ``new`` into ``default`` in place (REPLACE_KEYS replaced whole)."""
+    for key, value in new.items():
+        path = f"{section}.{key}"
+        if (isinstance(value, dict) and isinstance(default.get(key), dict)
+                and path not in REPLACE_KEYS):
+            recursive_update(default[key], value, path)
+        else:
+            default[key] = value if _is_array_like(value) else copy.deepcopy(value)
+    return default
+
+
+def task_params(task_name, param_task):
+    """Return the merged parameter dict for ``task_name``."""
+    if param_task is None:
+        param_task = {task_name: {}}
+    if task_name not in param_task:
+        raise ValueError(
+            f"Mismatch of task name, expected <{task_name}>, but it was not found in "
+            f"the provided task(s) <{list(param_task)}>"
+        )
+    merged = copy.deepcopy(DEFAULTS[task_name])
+    return recursive_update(merged, param_task[task_name], task_name)

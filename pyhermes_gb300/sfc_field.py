@@ -1,0 +1,347 @@
+"""``SFCField``: a scaling-function-coefficient field resident in GB300 HBM.
+
+Mirrors the reference container ``pyhermes/io/sfc_field.py:50-584``:
+``sfc_info`` metadata (every key is also an attribute), ``epsilon``,
+``field @ window`` convolution, + - * / algebra, weight-normalisation
+switches, ``field_mean_density`` and NumPy-framed pickle save/load.
+
+Differences by design: the coefficients live on the GPU as a float32 torch
+tensor (``epsilon_device``); ``epsilon`` returns a float64 NumPy copy made
+on first access (the reference's dtype), so reference tools that read
+``.epsilon`` keep working.  Arithmetic stays on the device.
+"""
+
+import copy
+import os
+import pickle
+from io import BytesIO
+
+import numpy as np
+import torch
+
+REQUIRED_ARGV = ("J", "box_size", "phi_resolution", "wavelet_mode", "wavelet_level")
+
+
+def normalize_weight_normalization(weight_normalization):
+    """pyhermes/io/sfc_field.py:21-29."""
+    if weight_normalization is None:
+        raise ValueError("weight_normalization must be one of 'raw', 'catalog', 'field', or 'unit'.")
+    mode = str(weight_normalization).strip().lower()
+    if mode == "unit":
+        return "field"
+    if mode not in {"raw", "catalog", "field"}:
+        raise ValueError("weight_normalization must be one of 'raw', 'catalog', 'field', or 'unit'.")
+    return mode
+
+
+def normalize_task_weight_normalization(weight_normalization):
+    """pyhermes/io/sfc_field.py:32-38."""
+    if weight_normalization is None:
+        raise ValueError("task weight_normalization must be one of 'raw', 'catalog', 'field', or 'unit'.")
+    mode = str(weight_normalization).strip().lower()
+    if mode not in {"raw", "catalog", "field", "unit"}:
+        raise ValueError("task weight_normalization must be one of 'raw', 'catalog', 'field', or 'unit'.")
+    return mode
+
+
+def normalize_field_value_normalization(normalization):
+    """pyhermes/io/sfc_field.py:41-47."""
+    if normalization is None:
+        return None
+    mode = str(normalization).strip().lower()
+    if mode not in {"raw", "catalog", "field", "unit"}:
+        raise ValueError("normalization must be None, 'raw', 'catalog', 'field', or 'unit'.")
+    return mode
+
+
+def write_numpy_pickle(file_obj, value, protocol=4):
+    """NumPy-framed pickle (pyhermes/io/pickle_compat.py:87-90): the pickle
+    bytes stored as a uint8 .npy array."""
+    payload = pickle.dumps(_normalize_pathlike(value), protocol=protocol)
+    np.lib.format.write_array(file_obj, np.frombuffer(payload, dtype=np.uint8))
+
+
+def read_numpy_pickle(file_obj):
+    """pyhermes/io/pickle_compat.py:81-84."""
+    serialized = np.lib.format.read_array(file_obj, allow_pickle=False)
+    return pickle.load(BytesIO(serialized.tobytes()))
+
+
+def _normalize_pathlike(value):
+    if isinstance(value, os.PathLike):
+        return os.fsdecode(os.fspath(value))
+    if isinstance(value, dict):
+        return {_normalize_pathlike(k): _normalize_pathlike(v) for k, v in value.items()}
+    if isinstance(value, list):
+        return [_normalize_pathlike(v) for v in value]
+    if isinstance(value, tuple):
+        return tuple(_normalize_pathlike(v) for v in value)
+    return value
+
+
+class SFCField:
+    _REQUIRED_ARGV = REQUIRED_ARGV
+
+    def __init__(self, *args, threads=None, data_path=None, device=None, **kwargs):
+        self.threads = threads
+        self.sfc_info = {}
+        self.task_params = {}
+        self.saveflag = False
+        self.device = torch.device(device) if device is not None else torch.device("cuda")
+        self._eps_dev = None
+        self._eps_host = None
+        if data_path:
+            self.sfc_info["sfc_field_path"] = data_path
+            self.load_sfc_field(data_path)
+
+    # ---- coefficient storage -------------------------------------------
+    @property
+    def epsilon_device(self):
+        if self._eps_dev is None and self._eps_host is not None:
+            self._eps_dev = torch.as_tensor(self._eps_host, device=self.device).to(
+                torch.float32 if not np.iscomplexobj(self._eps_host) else torch.complex64)
+        return self._eps_dev
+
+    @epsilon_device.setter
+    def epsilon_device(self, t):
+        self._eps_dev = t
+        self._eps_host = None
+
+    @property
+    def epsilon(self):
+        if self._eps_host is None and self._eps_dev is not None:
+            t = self._eps_dev
+            t = t.to(torch.complex128) if t.is_complex() else t.to(torch.float64)
+            self._eps_host = t.cpu().numpy()
+        return self._eps_host
+
+    @epsilon.setter
+    def epsilon(self, value):
+        if value is None:
+            self._eps_dev = None
+            self._eps_host = None
+        elif isinstance(value, torch.Tensor):
+            self.epsilon_device = value
+        else:
+            self._eps_host = np.asarray(value)
+            self._eps_dev = None
+
+    def as_array(self):
+        return self.epsilon
+
+    # ---- metadata ----------------------------------------------------------
+    def format_sfc_params(self):
+        missing = [k for k in self._REQUIRED_ARGV if k not in self.sfc_info]
+        if missing:
+            raise ValueError(f"SFCField missing required keys: {missing}")
+        for key, value in self.sfc_info.items():
+            setattr(self, key, value)
+
+    def _spawn_like(self):
+        new = self.__class__.__new__(self.__class__)
+        new.threads = self.threads
+        new.sfc_info = copy.deepcopy(self.sfc_info)
+        new.task_params = copy.deepcopy(getattr(self, "task_params", {}))
+        new.saveflag = False
+        new.device = self.device
+        new._eps_dev = None
+        new._eps_host = None
+        return new
+
+    def copy(self):
+        new = self._spawn_like()
+        if self._eps_dev is not None:
+            new._eps_dev = self._eps_dev.clone()
+        elif self._eps_host is not None:
+            new._eps_host = self._eps_host.copy()
+        new.format_sfc_params()
+        return new
+
+    def _derived_field_integral(self, field):
+        t = field.epsilon_device
+        if t is None:
+            return None
+        total = t.to(torch.complex128 if t.is_complex() else torch.float64).sum().item()
+        if isinstance(total, complex):
+            if not (np.isfinite(total.real) and np.isfinite(total.imag)):
+                return None
+            if abs(total.imag) <= 1e-12 * max(1.0, abs(total.real)):
+                return float(total.real)
+            return complex(total)
+        return float(total) if np.isfinite(total) else None
+
+    def _mark_derived(self, field):
+        """pyhermes/io/sfc_field.py:326-338."""
+        field.sfc_info.update({
+            "catalog_weight_sum": None,
+            "catalog_weight_sq_sum": None,
+            "raw_field_weighted_sum": None,
+            "field_integral": self._derived_field_integral(field),
+            "weight_normalization": None,
+            "particle_count": None,
+            "particle_data_retrievable": False,
+            "particle_data_path": "",
+            "particle_data_format": "",
+            "field_kind": "derived_field",
+        })
+
+    # ---- algebra (device) ----------------------------------------------------
+    def _binary(self, other, op):
+        if isinstance(other, SFCField):
+            a, b = self.epsilon_device, other.epsilon_device
+            if a is None or b is None:
+                raise ValueError("Cannot operate on a field whose epsilon is None.")
+            if a.shape != b.shape:
+                raise ValueError(f"Shape mismatch: {tuple(a.shape)} vs {tuple(b.shape)}")
+            res = op(a, b)
+        elif np.isscalar(other) and not isinstance(other, (str, bytes)):
+            if self.epsilon_device is None:
+                raise ValueError("Cannot operate on a field whose epsilon is None.")
+            res = op(self.epsilon_device, other)
+        else:
+            return NotImplemented
+        new = self._spawn_like()
+        new._eps_dev = res
+        self._mark_derived(new)
+        new.format_sfc_params()
+        return new
+
+    def __add__(self, other):
+        return self._binary(other, lambda a, b: a + b)
+
+    def __radd__(self, other):
+        return self._binary(other, lambda a, b: b + a)
+
+    def __sub__(self, other):
+        return self._binary(other, lambda a, b: a - b)
+
+    def __rsub__(self, other):
+        return self._binary(other, lambda a, b: b - a)
+
+    def __mul__(self, other):
+        return self._binary(other, lambda a, b: a * b)
+
+    def __rmul__(self, other):
+        return self._binary(other, lambda a, b: b * a)
+
+    def __truediv__(self, other):
+        if np.isscalar(other) and float(other) == 0.0:
+            raise ZeroDivisionError("Cannot divide SFCField by zero.")
+        if isinstance(other, SFCField):
+            return NotImplemented
+        return self._binary(other, lambda a, b: a / b)
+
+    def __matmul__(self, other):
+        from .window import convolve_field
+
+        if hasattr(other, "as_array") and not isinstance(other, SFCField) or getattr(other, "is_window", False):
+            return convolve_field(self, other)
+        return NotImplemented
+
+    # ---- normalisation -----------------------------------------------------
+    def _normalization_denominator(self, weight_normalization):
+        """pyhermes/io/sfc_field.py:340-352."""
+        mode = normalize_weight_normalization(weight_normalization)
+        if mode == "raw":
+            return 1.0
+        if mode == "catalog":
+            value, label = getattr(self, "catalog_weight_sum", None), "catalog_weight_sum"
+        else:
+            value, label = getattr(self, "raw_field_weighted_sum", None), "raw_field_weighted_sum"
+        if value is None or not np.isfinite(value) or np.isclose(value, 0.0):
+            raise ValueError(f"Cannot use weight_normalization='{mode}' without a finite, non-zero {label}.")
+        return float(value)
+
+    def _field_integral_for_normalization(self, weight_normalization):
+        raw_sum = getattr(self, "raw_field_weighted_sum", None)
+        if raw_sum is None or not np.isfinite(raw_sum):
+            return None
+        return float(raw_sum / self._normalization_denominator(weight_normalization))
+
+    def switch_weight_normalization(self, weight_normalization):
+        """pyhermes/io/sfc_field.py:360-378 (rescale by old_den/new_den)."""
+        mode = normalize_weight_normalization(weight_normalization)
+        if getattr(self, "field_kind", None) != "catalog_field":
+            raise ValueError("weight normalization can only be switched for catalog fields.")
+        new = self.copy()
+        current = normalize_weight_normalization(getattr(self, "weight_normalization", "raw"))
+        if current == mode:
+            return new
+        factor = self._normalization_denominator(current) / new._normalization_denominator(mode)
+        new._eps_dev = new.epsilon_device * factor
+        new._eps_host = None
+        new.sfc_info["weight_normalization"] = mode
+        new.sfc_info["field_integral"] = new._field_integral_for_normalization(mode)
+        new.format_sfc_params()
+        return new
+
+    def to_unit_weight(self):
+        if getattr(self, "field_kind", None) == "catalog_field":
+            return self.switch_weight_normalization("field")
+        total = getattr(self, "field_integral", None)
+        if total is None:
+            total = self._derived_field_integral(self)
+        if total is None or not np.isfinite(total) or np.isclose(total, 0.0):
+            raise ValueError("Cannot rescale a derived field with zero or non-finite epsilon sum.")
+        new = self.copy()
+        new._eps_dev = new.epsilon_device / total
+        self._mark_derived(new)
+        new.format_sfc_params()
+        return new
+
+    def with_normalization(self, normalization=None):
+        mode = normalize_field_value_normalization(normalization)
+        if mode is None:
+            return self
+        if mode == "unit":
+            return self.to_unit_weight()
+        if getattr(self, "field_kind", None) != "catalog_field":
+            raise ValueError("normalization='raw', 'catalog', or 'field' can only be applied to catalog fields.")
+        return self.switch_weight_normalization(mode)
+
+    def switch_normalization(self, weight_normalization):
+        return self.with_normalization(weight_normalization)
+
+    def _resolve_value_unit(self, value_unit, sample_field=None):
+        field = self if sample_field is None else sample_field
+        value_unit = str(value_unit).strip().lower()
+        if value_unit not in {"auto", "grid", "physical"}:
+            raise ValueError("value_unit must be 'auto', 'grid', or 'physical'.")
+        if value_unit == "auto":
+            value_unit = "physical" if getattr(field, "field_kind", None) == "catalog_field" else "grid"
+        return value_unit
+
+    def field_mean_density(self, normalization=None, value_unit="auto"):
+        """pyhermes/io/sfc_field.py:416-423."""
+        field = self if normalization is None else self.with_normalization(normalization)
+        value_unit = self._resolve_value_unit(value_unit, sample_field=field)
+        value = getattr(field, "field_integral", None)
+        if value is None:
+            return None
+        volume = float(field.V) if value_unit == "grid" else float(field.box_size) ** 3
+        return value / volume
+
+    # ---- persistence (byte-compatible with the reference) -------------------
+    def save_sfc_field(self, f_out, single=True, overwrite=False):
+        """pyhermes/io/sfc_field.py:565-584: {'sfc_info', 'epsilon'} framed pickle."""
+        if os.path.exists(f_out) and not overwrite:
+            raise FileExistsError(f"{f_out} exists; pass overwrite=True")
+        d = os.path.dirname(f_out)
+        if d:
+            os.makedirs(d, exist_ok=True)
+        if not self.sfc_info:
+            raise ValueError('The dictionary "sfc_info" is empty.')
+        with open(f_out, "wb") as f:
+            write_numpy_pickle(f, {"sfc_info": self.sfc_info, "epsilon": self.epsilon})
+
+    def load_sfc_field(self, f_in, single=True):
+        """pyhermes/io/sfc_field.py:549-563."""
+        with open(f_in, "rb") as f:
+            dataset = read_numpy_pickle(f)
+        if "epsilon" not in dataset:
+            raise ValueError("Failed to load the dataset. The file is missing the 'epsilon' key.")
+        self.epsilon = dataset["epsilon"]
+        info = dataset.get("sfc_info")
+        if info:
+            self.sfc_info.update(info)
+        self.format_sfc_params()
