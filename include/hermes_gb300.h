@@ -78,6 +78,89 @@ int hermes_deposit_accumulate(int64_t n, int J, double box, const double* phi,
 int hermes_deposit_status(const void* workspace, int64_t* n_rejected,
                           void* stream);
 
+/* ---- spectral windows ------------------------------------------------------
+ * Built-in window transfer functions (utils/window_functions.py:441-458),
+ * evaluated on the fly inside the passes below instead of being materialised
+ * as an L^3 kernel array.  Lengths are in grid units (the reference's
+ * WindowFunc rescales len_args by L/box, io/window.py:112).
+ */
+#define HERMES_WIN_SPHERE 0                 /* len = {R}                 */
+#define HERMES_WIN_GAUSSIAN 1               /* len = {R}                 */
+#define HERMES_WIN_SHELL 2                  /* len = {R}                 */
+#define HERMES_WIN_THICK_SHELL 3            /* len = {R, delta_R}        */
+#define HERMES_WIN_GAUSSIAN_SHELL 4         /* len = {R_shell, R_smooth} */
+#define HERMES_WIN_CUBIC 5                  /* len = {Lx, Ly, Lz}        */
+#define HERMES_WIN_RING 6                   /* len = {R, H}, los         */
+#define HERMES_WIN_DISK 7                   /* len = {R, H}, los         */
+#define HERMES_WIN_CYLSHELL 8               /* len = {R, H}, los         */
+#define HERMES_WIN_CYLINDER 9               /* len = {R, H}, los         */
+#define HERMES_WIN_CW 10                    /* len = {R}                 */
+#define HERMES_WIN_CWS 11                   /* len = {R}                 */
+#define HERMES_WIN_GDW 12                   /* len = {R}                 */
+#define HERMES_WIN_DIRECTIONAL_DERIVATIVE 13 /* los                      */
+#define HERMES_WIN_LAPLACIAN 14
+#define HERMES_WIN_INVERSE_LAPLACIAN 15
+
+/* Kernel modes (io/window.py:172-195, utils/window_params.py:75-84). */
+#define HERMES_KMODE_OCTANT 0        /* real, mirror-symmetric images      */
+#define HERMES_KMODE_FULL_RFFT 1     /* real, signed images                */
+#define HERMES_KMODE_COMPLEX_RFFT 2  /* complex, signed images             */
+
+typedef struct hermes_window {
+  int32_t type;           /* HERMES_WIN_*                                   */
+  int32_t kernel_mode;    /* HERMES_KMODE_*                                 */
+  int32_t zero_mode_zero; /* 1: K(0,0,0) = 0 (io/window.py:266-272)         */
+  int32_t reserved;
+  double len[4];          /* length arguments in grid units                 */
+  double los[3];          /* line of sight / direction (any non-zero norm)  */
+  double scale;           /* multiplies the kernel (composite scalar ops)   */
+} hermes_window_t;
+
+/* Forward / inverse 3D FFTs in float32 (the reference's scipy.fft rfftn,
+ * irfftn, fftn, ifftn in utils/convolution.py:284-295).  Unnormalised like
+ * cuFFT (the inverse passes below fold in 1/L^3).  C2R overwrites `spec`. */
+int hermes_fft_r2c(const float* field, void* spec /* float2 [L,L,L/2+1] */,
+                   int J, void* stream);
+int hermes_fft_c2r(void* spec, float* field, int J, void* stream);
+
+/* field @ window for a real field and an rFFT-grid window
+ * (utils/convolution.py:284-288 + io/sfc_field.py:93-150): rfftn, multiply by
+ * the window kernel evaluated on the fly (phi_power: L*bandwidth+1 float64
+ * samples of |phi_hat|^2, wavelet_grid.py:94-100), irfftn.  `out` may alias
+ * `eps`.  Workspace: hermes_window_workspace_size. */
+int hermes_window_workspace_size(int J, size_t* bytes);
+int hermes_window_apply(const float* eps, float* out, int J,
+                        const hermes_window_t* win, const double* phi_power,
+                        int bandwidth, void* workspace, size_t workspace_bytes,
+                        void* stream);
+
+/* Materialise a window kernel on the rFFT grid (io/window.py:274-343):
+ * k_real float [L,L,L/2+1] for real modes, or k_cplx float2 for
+ * HERMES_KMODE_COMPLEX_RFFT (give the one that matches). */
+int hermes_window_materialize(const hermes_window_t* win, const double* phi_power,
+                              int bandwidth, int J, float* k_real, void* k_cplx,
+                              void* stream);
+/* spec *= K (materialised kernel, real or complex) -- for composite windows. */
+int hermes_spectrum_multiply(void* spec, const float* k_real, const void* k_cplx,
+                             int J, double factor, void* stream);
+
+/* Pair products for many bins in one pass over the spectra
+ * (theory/corr2pcf.py:366-372 pair_product_with_window, by Parseval):
+ *   out[b*n_pairs+p] = (1/L^6) sum_k F_i(k) K_b(k) conj(F_j(k))
+ * over the full k grid (half spectrum with Hermitian weights), where
+ * (i, j) = pairs[2p], pairs[2p+1] index into `spectra`, an array of
+ * n_spec device pointers to float2 [L,L,L/2+1] half spectra (host array).
+ * If exclude_k0 != 0 the k = 0 term is left out (added by the caller in
+ * float64 for mean-subtracted fields).  bins: host array of n_bins windows.
+ * out: host float64 [n_bins * n_pairs]; k0_out (nullable): host float64
+ * [n_bins] kernel values K_b(0); the call synchronises `stream`. */
+int hermes_pair_products_workspace_size(int J, int n_bins, int n_pairs, size_t* bytes);
+int hermes_pair_products(const void* const* spectra, int n_spec, const int32_t* pairs,
+                         int n_pairs, const hermes_window_t* bins, int n_bins,
+                         const double* phi_power, int bandwidth, int J, int exclude_k0,
+                         double* out, double* k0_out, void* workspace,
+                         size_t workspace_bytes, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

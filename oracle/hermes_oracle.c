@@ -113,3 +113,231 @@ int oracle_num_threads(void) {
   return 1;
 #endif
 }
+
+/* ------------------------------------------------------------------------
+ * Window transfer functions: utils/window_functions.py:29-438 and the
+ * special functions they call, utils/special_functions.py:131-270.
+ * ------------------------------------------------------------------------ */
+enum {
+  W_SPHERE = 0, W_GAUSSIAN, W_SHELL, W_THICK_SHELL, W_GAUSSIAN_SHELL, W_CUBIC, W_RING, W_DISK,
+  W_CYLSHELL, W_CYLINDER, W_CW, W_CWS, W_GDW, W_DIRDERIV, W_LAPLACIAN, W_INVLAPLACIAN
+};
+
+static const double PI = 3.141592653589793;
+
+static double j0_ref(double x) { /* special_functions.py:131-170 */
+  double ax = fabs(x);
+  if (ax < 8.0) {
+    double y = x * x;
+    double a1 = 57568490574.0 + y * (-13362590354.0 + y * (651619640.7 + y * (-11214424.18 + y * (77392.33017 + y * -184.9052456))));
+    double a2 = 57568490411.0 + y * (1029532985.0 + y * (9494680.718 + y * (59272.64853 + y * (267.8532712 + y))));
+    return a1 / a2;
+  }
+  double z = 8.0 / ax, y = z * z, xx = ax - 0.785398164;
+  double a1 = 1.0 + y * (-0.1098628627e-2 + y * (0.2734510407e-4 + y * (-0.2073370639e-5 + y * 0.2093887211e-6)));
+  double a2 = -0.1562499995e-1 + y * (0.1430488765e-3 + y * (-0.6911147651e-5 + y * (0.7621095161e-6 - y * 0.934945152e-7)));
+  return sqrt(0.636619772 / ax) * (cos(xx) * a1 - z * sin(xx) * a2);
+}
+
+static double j1_ref(double x) { /* special_functions.py:173-215 */
+  double ax = fabs(x);
+  if (ax < 8.0) {
+    double y = x * x;
+    double a1 = x * (72362614232.0 + y * (-7895059235.0 + y * (242396853.1 + y * (-2972611.439 + y * (15704.48260 + y * -30.16036606)))));
+    double a2 = 144725228442.0 + y * (2300535178.0 + y * (18583304.74 + y * (99447.43394 + y * (376.9991397 + y))));
+    return a1 / a2;
+  }
+  double z = 8.0 / ax, y = z * z, xx = ax - 2.356194491;
+  double a1 = 1.0 + y * (0.183105e-2 + y * (-0.3516396496e-4 + y * (0.2457520174e-5 + y * -0.240337019e-6)));
+  double a2 = 0.04687499995 + y * (-0.2002690873e-3 + y * (0.8449199096e-5 + y * (-0.88228987e-6 + y * 0.105787412e-6)));
+  double ans = sqrt(0.636619772 / ax) * (cos(xx) * a1 - z * sin(xx) * a2);
+  return x < 0.0 ? -ans : ans;
+}
+
+static double jn01_ref(int n, double x) { /* jn_numba for n in {0,1}: special_functions.py:218-235 */
+  double sign = 1.0;
+  if (x < 0.0) {
+    x = -x;
+    if (n % 2 == 1) sign = -sign;
+  }
+  return n == 0 ? sign * j0_ref(x) : sign * j1_ref(x);
+}
+
+static double w_sphere(double ki, double kj, double kk, double R) {
+  double k = sqrt(ki * ki + kj * kj + kk * kk);
+  double q = 2 * PI * k * R;
+  if (q == 0.0) return 1.0;
+  return 3 * (sin(q) - q * cos(q)) / (q * q * q);
+}
+
+static double cw_g(double q) { /* window_functions.py:324-332 */
+  double a = fabs(q);
+  if (a == 0.0) return 0.0;
+  if (a < 1.0e-4) return a * a * a * a / 3.0;
+  if (a > 50.0) return 0.0;
+  return a * (a * cosh(a) - sinh(a)) * exp(-0.5 * a * a);
+}
+
+static void los_norm(const double* los, double* n) {
+  double nr = sqrt(los[0] * los[0] + los[1] * los[1] + los[2] * los[2]);
+  n[0] = los[0] / nr;
+  n[1] = los[1] / nr;
+  n[2] = los[2] / nr;
+}
+
+/* W(k) for the built-in types; returns the real part, *im the imaginary. */
+static double window_value(int type, const double* a, const double* los, double ki, double kj, double kk,
+                           double* im) {
+  *im = 0.0;
+  switch (type) {
+    case W_SPHERE: return w_sphere(ki, kj, kk, a[0]);
+    case W_GAUSSIAN: {
+      double k = sqrt(ki * ki + kj * kj + kk * kk), q = 2 * PI * k * a[0];
+      return exp(-(q * q) / 2);
+    }
+    case W_SHELL: {
+      double k = sqrt(ki * ki + kj * kj + kk * kk), q = 2 * PI * k * a[0];
+      return q == 0.0 ? 1.0 : sin(q) / q;
+    }
+    case W_THICK_SHELL: {
+      double rin = a[0] - 0.5 * a[1];
+      if (rin < 0.0) rin = 0.0;
+      double rout = a[0] + 0.5 * a[1];
+      double den = rout * rout * rout - rin * rin * rin;
+      if (den == 0.0) return 1.0;
+      return (rout * rout * rout * w_sphere(ki, kj, kk, rout) - rin * rin * rin * w_sphere(ki, kj, kk, rin)) / den;
+    }
+    case W_GAUSSIAN_SHELL: {
+      double k = sqrt(ki * ki + kj * kj + kk * kk);
+      if (k == 0) return 1.0;
+      double qs = 2 * PI * k * a[0], qm = 2 * PI * k * a[1];
+      double den = a[0] * a[0] + a[1] * a[1];
+      if (den == 0.0) return 1.0;
+      double sinc = qs == 0.0 ? 1.0 : sin(qs) / qs;
+      return (a[1] * a[1] * cos(qs) + a[0] * a[0] * sinc) / den * exp(-(qm * qm) / 2);
+    }
+    case W_CUBIC: {
+      double q[3] = {PI * ki * a[0], PI * kj * a[1], PI * kk * a[2]}, r = 1.0;
+      for (int i = 0; i < 3; ++i) r *= q[i] == 0.0 ? 1.0 : sin(q[i]) / q[i];
+      return r;
+    }
+    case W_RING: case W_DISK: case W_CYLSHELL: case W_CYLINDER: {
+      double n[3];
+      los_norm(los, n);
+      double kpar = ki * n[0] + kj * n[1] + kk * n[2];
+      double k2 = ki * ki + kj * kj + kk * kk;
+      double kp2 = k2 - kpar * kpar;
+      if (kp2 < 0.0) kp2 = 0.0;
+      double qperp = 2.0 * PI * sqrt(kp2) * a[0], qpar = 2.0 * PI * kpar * a[1];
+      double perp, par;
+      if (type == W_RING || type == W_CYLSHELL) perp = jn01_ref(0, qperp);
+      else perp = qperp == 0.0 ? 1.0 : 2.0 * jn01_ref(1, qperp) / qperp;
+      if (type == W_RING || type == W_DISK) par = cos(qpar);
+      else par = qpar == 0.0 ? 1.0 : sin(qpar) / qpar;
+      return perp * par;
+    }
+    case W_CW: {
+      double k = sqrt(ki * ki + kj * kj + kk * kk), q = 2 * PI * k * a[0];
+      double c = 2 * sqrt(2.0) / (sqrt(1.0 + 5.0 * 2.718281828459045) * pow(PI, 0.25));
+      return sqrt(2.0 * PI) * c * pow(a[0], 0.5) * cw_g(q);
+    }
+    case W_CWS: {
+      double k = sqrt(ki * ki + kj * kj + kk * kk), q = 2 * PI * k * a[0];
+      double c = 2 * sqrt(2.0) / (sqrt(9.0 + 55.0 * 2.718281828459045) * pow(PI, 0.75));
+      return pow(2.0 * PI, 1.5) * c * pow(a[0], 1.5) * cw_g(q);
+    }
+    case W_GDW: {
+      double k = sqrt(ki * ki + kj * kj + kk * kk), q = 2 * PI * k * a[0];
+      return pow(2.0, 2.5) * pow(PI, 0.75) / sqrt(15.0) * pow(a[0], 1.5) * q * q * exp(-(q * q) / 2);
+    }
+    case W_DIRDERIV: {
+      double n[3];
+      los_norm(los, n);
+      *im = 2.0 * PI * (ki * n[0] + kj * n[1] + kk * n[2]);
+      return 0.0;
+    }
+    case W_LAPLACIAN: return -((2.0 * PI) * (2.0 * PI)) * (ki * ki + kj * kj + kk * kk);
+    case W_INVLAPLACIAN: {
+      double k2 = ki * ki + kj * kj + kk * kk;
+      return k2 == 0.0 ? 0.0 : -1.0 / (((2.0 * PI) * (2.0 * PI)) * k2);
+    }
+  }
+  return NAN;
+}
+
+/* Octant kernel (convolution.py:14-38) folded to the rFFT grid (:263-281).
+ * out: float64 [L, L, L/2+1]; P: L*bw+1 samples. */
+int oracle_window_octant(int type, const double* args, const double* los, int L, int bw, const double* P,
+                         double* out) {
+  const int64_t M = L + 1;
+  double* wa = (double*)malloc(sizeof(double) * (size_t)(M * M * M));
+  if (!wa) return -1;
+  const double invL = 1.0 / L;
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < M; ++i)
+    for (int64_t j = 0; j < M; ++j)
+      for (int64_t k = 0; k < M; ++k) {
+        double t = 0.0, im;
+        for (int ii = 0; ii < bw; ++ii)
+          for (int jj = 0; jj < bw; ++jj)
+            for (int kk = 0; kk < bw; ++kk) {
+              t += P[ii * L + i] * P[jj * L + j] * P[kk * L + k] *
+                   window_value(type, args, los, (ii * L + i) * invL, (jj * L + j) * invL, (kk * L + k) * invL, &im);
+            }
+        wa[(i * M + j) * M + k] = t;
+      }
+  const int64_t H = L / 2 + 1;
+#define WA(a, b, c) wa[((int64_t)(a) * M + (b)) * M + (c)]
+#pragma omp parallel for schedule(static)
+  for (int64_t x = 0; x < L; ++x)
+    for (int64_t y = 0; y < L; ++y)
+      for (int64_t z = 0; z < H; ++z)
+        out[(x * L + y) * H + z] = WA(x, y, z) + WA(L - x, y, z) + WA(x, L - y, z) + WA(x, y, L - z) +
+                                   WA(L - x, L - y, z) + WA(L - x, y, L - z) + WA(x, L - y, L - z) +
+                                   WA(L - x, L - y, L - z);
+#undef WA
+  free(wa);
+  return 0;
+}
+
+/* Full real / complex rFFT kernels (convolution.py:73-157, :168-252).
+ * out: float64 [L, L, L/2+1, 2] (re, im). */
+int oracle_window_rfft(int type, const double* args, const double* los, int L, int bw, const double* P,
+                       double* out) {
+  const int64_t H = L / 2 + 1;
+  const double invL = 1.0 / L;
+#pragma omp parallel for schedule(static)
+  for (int64_t x = 0; x < L; ++x)
+    for (int64_t y = 0; y < L; ++y)
+      for (int64_t z = 0; z < H; ++z) {
+        double tr = 0.0, ti = 0.0;
+        for (int ii = 0; ii < bw; ++ii) {
+          const int64_t xpi = ii * L + x, xni = ii * L + (L - x);
+          const double xp = xpi * invL, xn = -xni * invL;
+          for (int jj = 0; jj < bw; ++jj) {
+            const int64_t ypi = jj * L + y, yni = jj * L + (L - y);
+            const double yp = ypi * invL, yn = -yni * invL;
+            for (int kk = 0; kk < bw; ++kk) {
+              const int64_t zpi = kk * L + z, zni = kk * L + (L - z);
+              const double zp = zpi * invL, zn = -zni * invL;
+              const double px = P[xpi], nx = P[xni], py = P[ypi], ny = P[yni], pz = P[zpi], nz = P[zni];
+              const double wx[8] = {px, nx, px, px, nx, nx, px, nx};
+              const double wy[8] = {py, py, ny, py, ny, py, ny, ny};
+              const double wz[8] = {pz, pz, pz, nz, pz, nz, nz, nz};
+              const double ax[8] = {xp, xn, xp, xp, xn, xn, xp, xn};
+              const double ay[8] = {yp, yp, yn, yp, yn, yp, yn, yn};
+              const double az[8] = {zp, zp, zp, zn, zp, zn, zn, zn};
+              for (int t = 0; t < 8; ++t) {
+                double im, re = window_value(type, args, los, ax[t], ay[t], az[t], &im);
+                double w = wx[t] * wy[t] * wz[t];
+                tr += w * re;
+                ti += w * im;
+              }
+            }
+          }
+        }
+        out[2 * ((x * L + y) * H + z)] = tr;
+        out[2 * ((x * L + y) * H + z) + 1] = ti;
+      }
+  return 0;
+}

@@ -88,3 +88,74 @@ def projection_weights(catalog_weight, field_value, mode="catalog"):
     else:
         den = raw
     return cw * fv / den, raw / den
+
+
+WIN_CODES = {
+    "sphere": 0, "gaussian": 1, "shell": 2, "thick_shell": 3, "gaussian_shell": 4, "cubic": 5,
+    "ring": 6, "disk": 7, "cylshell": 8, "cylinder": 9, "cw": 10, "cws": 11, "gdw": 12,
+    "directional_derivative": 13, "laplacian": 14, "inverse_laplacian": 15,
+}
+WIN_ARGS = {
+    "sphere": ("R",), "gaussian": ("R",), "shell": ("R",), "thick_shell": ("R", "delta_R"),
+    "gaussian_shell": ("R_shell", "R_smooth"), "cubic": ("Lx", "Ly", "Lz"),
+    "ring": ("R", "H"), "disk": ("R", "H"), "cylshell": ("R", "H"), "cylinder": ("R", "H"),
+    "cw": ("R",), "cws": ("R",), "gdw": ("R",), "directional_derivative": (),
+    "laplacian": (), "inverse_laplacian": (),
+}
+
+
+def fourier_power(phi, k_max, k_count, res=1024):
+    """utils/wavelet_grid.py:94-118: |phi_hat|^2 by direct DFT (float64)."""
+    phi = np.asarray(phi, dtype=np.float64)
+    n = phi.shape[0]
+    dx = (n / res) / n
+    k = np.arange(k_count + 1) * (k_max / k_count)
+    x = np.arange(n) * dx
+    arg = (-2 * np.pi * k)[:, None] * x[None, :]
+    re = np.sum(phi * dx * np.cos(arg), axis=1)
+    im = np.sum(phi * dx * np.sin(arg), axis=1)
+    return re ** 2 + im ** 2
+
+
+def window_kernel(wtype, len_args, L, P, mode="octant", los=(0.0, 0.0, 1.0), bandwidth=1, box=1000.0):
+    """The reference WindowFunc kernel (io/window.py:274-332) in float64.
+
+    len_args are physical lengths (rescaled here by L/box like io/window.py:112).
+    mode: 'octant' (convolution.py:14-38 + 263-281), 'full_rfft' (:73-157) or
+    'complex_rfft' (:168-252).  Returns [L, L, L/2+1] real or complex."""
+    args = np.zeros(4)
+    for i, nm in enumerate(WIN_ARGS[wtype]):
+        args[i] = float(len_args[nm]) * L / box
+    los = np.ascontiguousarray(los, dtype=np.float64)
+    P = np.ascontiguousarray(P, dtype=np.float64)
+    H = L // 2 + 1
+    code = WIN_CODES[wtype]
+    lb = lib()
+    lb.oracle_window_octant.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                        ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    lb.oracle_window_rfft.argtypes = lb.oracle_window_octant.argtypes
+    if mode == "octant":
+        out = np.empty((L, L, H), dtype=np.float64)
+        lb.oracle_window_octant(code, _p(args), _p(los), L, bandwidth, _p(P), _p(out))
+    else:
+        out2 = np.empty((L, L, H, 2), dtype=np.float64)
+        lb.oracle_window_rfft(code, _p(args), _p(los), L, bandwidth, _p(P), _p(out2))
+        out = out2[..., 0] + 1j * out2[..., 1] if mode == "complex_rfft" else out2[..., 0].copy()
+    if wtype == "inverse_laplacian":
+        out[0, 0, 0] = 0.0
+    return out
+
+
+def convolve(eps, kernel):
+    """utils/convolution.py:284-288: irfftn(rfftn(eps) * K)."""
+    from scipy.fft import irfftn, rfftn
+
+    sc = rfftn(np.asarray(eps, dtype=np.float64))
+    sc *= kernel
+    return irfftn(sc, s=eps.shape)
+
+
+def pair_product(eps1, eps2, kernel):
+    """theory/corr2pcf.py:366-372: mean((eps1 conv K) * eps2)."""
+    conv = convolve(eps1, kernel)
+    return float(np.einsum("ijk,ijk->", conv, eps2, optimize=True) / conv.size)

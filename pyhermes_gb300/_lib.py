@@ -29,6 +29,15 @@ SIGNATURES = {
     "hermes_deposit_accumulate": (_c_int, [_c_i64, _c_int, _dbl, _p, _c_int, _c_int, _p, _p, _p,
                                            _p, _c_sz, _p]),
     "hermes_deposit_status": (_c_int, [_p, ctypes.POINTER(_c_i64), _p]),
+    "hermes_fft_r2c": (_c_int, [_p, _p, _c_int, _p]),
+    "hermes_fft_c2r": (_c_int, [_p, _p, _c_int, _p]),
+    "hermes_window_workspace_size": (_c_int, [_c_int, ctypes.POINTER(_c_sz)]),
+    "hermes_window_apply": (_c_int, [_p, _p, _c_int, _p, _p, _c_int, _p, _c_sz, _p]),
+    "hermes_window_materialize": (_c_int, [_p, _p, _c_int, _c_int, _p, _p, _p]),
+    "hermes_spectrum_multiply": (_c_int, [_p, _p, _p, _c_int, _dbl, _p]),
+    "hermes_pair_products_workspace_size": (_c_int, [_c_int, _c_int, _c_int, ctypes.POINTER(_c_sz)]),
+    "hermes_pair_products": (_c_int, [_p, _c_int, _p, _c_int, _p, _c_int, _p, _c_int, _c_int, _c_int,
+                                      _p, _p, _p, _c_sz, _p]),
 }
 
 

@@ -42,6 +42,8 @@ struct __align__(16) DepRec {
 
 struct DepGeom {
   int L, S, res;
+  int res_log2;       // log2(res) when res is a power of two, else -1
+  int tx_log2, ty_log2, tz_log2;
   int tx, ty, tz;     // tile extents (cells)
   int ntx, nty, ntz;  // tiles per axis
   double scale;       // L / box
@@ -51,6 +53,9 @@ struct DepStatus {
   unsigned long long rejected;  // non-finite or out-of-range particles
   unsigned int wmax_bits;       // max |w| (float, rounded up) as bits
   unsigned int phimax_bits;     // max |phi| (float, rounded up) as bits
+  double scale_d;               // fixed-point scale (power of two)
+  double inv_d;                 // 1 / scale_d
+  float scale_f, inv_f;         // the same as float
 };
 
 __device__ __forceinline__ float warp_max(float v) {
@@ -93,6 +98,25 @@ __device__ __forceinline__ bool dep_axis(double x, const DepGeom& g, int& c, int
   return true;
 }
 
+// Same result as dep_axis for s = x*scale >= 0 and a power-of-two res, from
+// the bits of s: the integer part and the top log2(res) fraction bits of the
+// float64 mantissa are exactly floor(s) and int((s - floor(s)) * res).
+// Only the multiply is float64 (GB300 float64 throughput is low).
+__device__ __forceinline__ bool dep_axis_fast(double x, const DepGeom& g, int& c, int& f) {
+  const double s = __dmul_rn(x, g.scale);
+  const unsigned long long b = (unsigned long long)__double_as_longlong(s);
+  if ((b >> 63) || g.res_log2 < 0) return dep_axis(x, g, c, f);
+  const int ex = (int)(b >> 52);
+  if (ex >= 1023 + 30) return false;  // >= 2^30, inf or nan
+  const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | (ex ? (1ull << 52) : 0ull);
+  const int sh = ex ? 1075 - ex : 1074;  // s = m * 2^-sh, sh >= 23
+  c = sh >= 64 ? 0 : (int)(m >> sh);
+  const int t = sh - g.res_log2;
+  f = t >= 64 ? 0 : (int)((m >> t) & (unsigned long long)(g.res - 1));
+  c &= (g.L - 1);
+  return true;
+}
+
 __device__ __forceinline__ unsigned dep_key(int cx, int cy, int cz, const DepGeom& g) {
   int hx = cx / g.tx, hy = cy / g.ty, hz = cz / g.tz;
   unsigned region = 0;
@@ -128,7 +152,7 @@ __global__ void dep_bin_kernel(const double* __restrict__ pos, const double* __r
       double wi = w[i];
       int cx, cy, cz, fx, fy, fz;
       bool ok = isfinite(x) && isfinite(y) && isfinite(z) && isfinite(wi) &&
-                dep_axis(x, g, cx, fx) && dep_axis(y, g, cy, fy) && dep_axis(z, g, cz, fz);
+                dep_axis_fast(x, g, cx, fx) && dep_axis_fast(y, g, cy, fy) && dep_axis_fast(z, g, cz, fz);
       DepRec r;
       if (ok) {
         key = dep_key(cx, cy, cz, g);
@@ -195,9 +219,32 @@ __device__ unsigned block_excl_scan_1024(unsigned v, unsigned* total) {
   return r;
 }
 
+__device__ __forceinline__ double dep_fixed_scale(const DepStatus* st, int64_t n) {
+  double wmax = (double)__uint_as_float(st->wmax_bits);
+  double pmax = (double)__uint_as_float(st->phimax_bits);
+  double bound = (double)n * wmax * pmax * pmax * pmax;
+  int e = -60;
+  if (bound > 0.0) {
+    frexp(bound, &e);  // bound < 2^e
+    if (e < -60) e = -60;
+  }
+  return ldexp(1.0, 62 - e);  // bound * scale < 2^62
+}
+
 // Scan phase 2: exclusive scan of chunk sums (single block, serial over
-// groups of 1024).
-__global__ void dep_scan_chunks_kernel(unsigned* chunk_sums, int nchunks) {
+// groups of 1024).  Also fixes the fixed-point scale and the float32 copy of
+// phi used by the accumulation.
+__global__ void dep_scan_chunks_kernel(unsigned* chunk_sums, int nchunks, DepStatus* st, int64_t n,
+                                       const double* __restrict__ phi, int n_phi,
+                                       float* __restrict__ phi_f) {
+  if (threadIdx.x == 0) {
+    const double sc = dep_fixed_scale(st, n);
+    st->scale_d = sc;
+    st->inv_d = 1.0 / sc;
+    st->scale_f = (float)sc;
+    st->inv_f = (float)(1.0 / sc);
+  }
+  for (int i = threadIdx.x; i < n_phi; i += blockDim.x) phi_f[i] = __double2float_rn(phi[i]);
   __shared__ unsigned total;
   unsigned carry = 0;
   for (int beg = 0; beg < nchunks; beg += 1024) {
@@ -252,41 +299,24 @@ __global__ void dep_scatter_kernel(const DepRec* __restrict__ rec, int64_t n,
   }
 }
 
-__device__ __forceinline__ double dep_fixed_scale(const DepStatus* st, int64_t n) {
-  double wmax = (double)__uint_as_float(st->wmax_bits);
-  double pmax = (double)__uint_as_float(st->phimax_bits);
-  double bound = (double)n * wmax * pmax * pmax * pmax;
-  int e = -60;
-  if (bound > 0.0) {
-    frexp(bound, &e);  // bound < 2^e
-    if (e < -60) e = -60;
-  }
-  return ldexp(1.0, 62 - e);  // bound * scale < 2^62
-}
-
 template <int S, bool kF64Out>
 __global__ void __launch_bounds__(kAccThreads)
 dep_accum_kernel(const DepRec* __restrict__ sorted, const unsigned* __restrict__ offsets,
-                 const double* __restrict__ phi, int n_phi, DepGeom g, int64_t n,
+                 const float* __restrict__ phif, DepGeom g,
                  const DepStatus* __restrict__ st, float* __restrict__ out32,
                  double* __restrict__ out64, unsigned* __restrict__ counts_out) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int ncell = g.tx * g.ty * g.tz;
   long long* acc = reinterpret_cast<long long*>(smem);
   unsigned* cnt = reinterpret_cast<unsigned*>(acc + ncell);
-  float* phis = reinterpret_cast<float*>(cnt + (counts_out ? ncell : 0));
   __shared__ unsigned r_start[27], r_pref[28], r_home[27];
   __shared__ int n_ranges;
 
   const int tile = blockIdx.x;
   const int hz = tile % g.ntz, hy = (tile / g.ntz) % g.nty, hx = tile / (g.ntz * g.nty);
   const int x0 = hx * g.tx, y0 = hy * g.ty, z0 = hz * g.tz;
+  const int tzl = g.tz_log2, tyzl = g.ty_log2 + g.tz_log2;
 
-  for (int i = threadIdx.x; i < n_phi; i += blockDim.x) phis[i] = __double2float_rn(phi[i]);
-  for (int i = threadIdx.x; i < ncell; i += blockDim.x) {
-    acc[i] = 0;
-    if (counts_out) cnt[i] = 0;
-  }
   if (threadIdx.x == 0) {
     int nr = 0;
     unsigned run = 0;
@@ -313,11 +343,26 @@ dep_accum_kernel(const DepRec* __restrict__ sorted, const unsigned* __restrict__
     n_ranges = nr;
   }
   __syncthreads();
-
-  const double scale = dep_fixed_scale(st, n);
-  const float scale_f = (float)scale;
   const int nr = n_ranges;
   const unsigned total = r_pref[nr];
+
+  if (total == 0) {  // empty tile: write zeros, skip shared memory
+    for (int i = threadIdx.x; i < ncell; i += blockDim.x) {
+      const int lz_ = i & (g.tz - 1), ly_ = (i >> tzl) & (g.ty - 1), lx_ = i >> tyzl;
+      const size_t gi = ((size_t)(x0 + lx_) * g.L + (y0 + ly_)) * g.L + (z0 + lz_);
+      if (kF64Out) out64[gi] = 0.0; else out32[gi] = 0.f;
+      if (counts_out) counts_out[gi] = 0u;
+    }
+    return;
+  }
+
+  for (int i = threadIdx.x; i < ncell; i += blockDim.x) {
+    acc[i] = 0;
+    if (counts_out) cnt[i] = 0;
+  }
+  __syncthreads();
+
+  const float scale_f = st->scale_f;
   const int Lm = g.L - 1;
   for (unsigned k = threadIdx.x; k < total; k += blockDim.x) {
     int r = 0;
@@ -332,9 +377,9 @@ dep_accum_kernel(const DepRec* __restrict__ sorted, const unsigned* __restrict__
       lx[s] = (cx - s - x0) & Lm;
       ly[s] = (cy - s - y0) & Lm;
       lz[s] = (cz - s - z0) & Lm;
-      px[s] = rec.w * phis[fx + g.res * s];
-      py[s] = phis[fy + g.res * s];
-      pz[s] = phis[fz + g.res * s];
+      px[s] = rec.w * __ldg(&phif[fx + g.res * s]);
+      py[s] = __ldg(&phif[fy + g.res * s]);
+      pz[s] = __ldg(&phif[fz + g.res * s]);
     }
 #pragma unroll
     for (int a = 0; a < S; ++a) {
@@ -343,7 +388,7 @@ dep_accum_kernel(const DepRec* __restrict__ sorted, const unsigned* __restrict__
       for (int b = 0; b < S; ++b) {
         if (ly[b] >= g.ty) continue;
         const float pxy = px[a] * py[b];
-        const int row = (lx[a] * g.ty + ly[b]) * g.tz;
+        const int row = (lx[a] << tyzl) + (ly[b] << tzl);
 #pragma unroll
         for (int c = 0; c < S; ++c) {
           if (lz[c] >= g.tz) continue;
@@ -354,15 +399,15 @@ dep_accum_kernel(const DepRec* __restrict__ sorted, const unsigned* __restrict__
       }
     }
     if (counts_out && r_home[r]) {
-      atomicAdd(&cnt[((cx - x0) * g.ty + (cy - y0)) * g.tz + (cz - z0)], 1u);
+      atomicAdd(&cnt[((cx - x0) << tyzl) + ((cy - y0) << tzl) + (cz - z0)], 1u);
     }
   }
   __syncthreads();
 
-  const float inv_f = (float)(1.0 / scale);
-  const double inv_d = 1.0 / scale;
+  const float inv_f = st->inv_f;
+  const double inv_d = st->inv_d;
   for (int i = threadIdx.x; i < ncell; i += blockDim.x) {
-    const int lz_ = i % g.tz, ly_ = (i / g.tz) % g.ty, lx_ = i / (g.tz * g.ty);
+    const int lz_ = i & (g.tz - 1), ly_ = (i >> tzl) & (g.ty - 1), lx_ = i >> tyzl;
     const size_t gi = ((size_t)(x0 + lx_) * g.L + (y0 + ly_)) * g.L + (z0 + lz_);
     if (kF64Out) {
       out64[gi] = (double)acc[i] * inv_d;
@@ -374,17 +419,17 @@ dep_accum_kernel(const DepRec* __restrict__ sorted, const unsigned* __restrict__
 }
 
 template <int S>
-int dep_launch_accum(const DepRec* sorted, const unsigned* offsets, const double* phi, int n_phi,
-                     const DepGeom& g, int64_t n, const DepStatus* st, float* eps_out,
+int dep_launch_accum(const DepRec* sorted, const unsigned* offsets, const float* phif,
+                     const DepGeom& g, const DepStatus* st, float* eps_out,
                      double* eps_f64_out, unsigned* counts_out, int ntiles, size_t smem,
                      cudaStream_t s) {
   if (eps_f64_out) {
     HERMES_CUDA_TRY(cudaFuncSetAttribute(dep_accum_kernel<S, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    dep_accum_kernel<S, true><<<ntiles, kAccThreads, smem, s>>>(sorted, offsets, phi, n_phi, g, n, st,
+    dep_accum_kernel<S, true><<<ntiles, kAccThreads, smem, s>>>(sorted, offsets, phif, g, st,
                                                                 nullptr, eps_f64_out, counts_out);
   } else {
     HERMES_CUDA_TRY(cudaFuncSetAttribute(dep_accum_kernel<S, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    dep_accum_kernel<S, false><<<ntiles, kAccThreads, smem, s>>>(sorted, offsets, phi, n_phi, g, n, st,
+    dep_accum_kernel<S, false><<<ntiles, kAccThreads, smem, s>>>(sorted, offsets, phif, g, st,
                                                                  eps_out, nullptr, counts_out);
   }
   return HERMES_OK;
@@ -410,6 +455,10 @@ int dep_plan(int64_t n, int J, int S, int res, DepPlan* p) {
   g.ty = g.L < kTileY ? g.L : kTileY;
   g.tz = g.L < kTileZ ? g.L : kTileZ;
   if (S - 1 > g.tx) return hermes::fail(HERMES_ERR_INVALID, "deposit: grid too small for support");
+  g.res_log2 = (res & (res - 1)) == 0 ? __builtin_ctz((unsigned)res) : -1;
+  g.tx_log2 = __builtin_ctz((unsigned)g.tx);
+  g.ty_log2 = __builtin_ctz((unsigned)g.ty);
+  g.tz_log2 = __builtin_ctz((unsigned)g.tz);
   g.ntx = g.L / g.tx;
   g.nty = g.L / g.ty;
   g.ntz = g.L / g.tz;
@@ -422,6 +471,7 @@ int dep_plan(int64_t n, int J, int S, int res, DepPlan* p) {
   c.take<unsigned>(p->nbuckets + 1);  // offsets
   c.take<unsigned>(p->nbuckets);      // cursor
   c.take<unsigned>(p->nchunks);       // chunk sums
+  c.take<float>(kMaxSupport * 1024);  // float32 phi
   c.take<DepRec>((size_t)(n > 0 ? n : 1));  // unsorted records
   c.take<DepRec>((size_t)(n > 0 ? n : 1));  // sorted records
   p->ws_bytes = c.used;
@@ -447,6 +497,7 @@ struct DepBuffers {
   unsigned* offsets;
   unsigned* cursor;
   unsigned* chunk_sums;
+  float* phif;
   DepRec* rec;
   DepRec* sorted;
 };
@@ -467,6 +518,7 @@ int dep_prepare(int64_t n, int J, double box, int n_phi, int phi_res, const doub
   b->offsets = c.take<unsigned>(p->nbuckets + 1);
   b->cursor = c.take<unsigned>(p->nbuckets);
   b->chunk_sums = c.take<unsigned>(p->nchunks);
+  b->phif = c.take<float>(kMaxSupport * 1024);
   b->rec = c.take<DepRec>((size_t)(n > 0 ? n : 1));
   b->sorted = c.take<DepRec>((size_t)(n > 0 ? n : 1));
   return HERMES_OK;
@@ -499,7 +551,7 @@ extern "C" int hermes_deposit_sort(const double* pos, const double* w, int64_t n
   }
   dep_scan_sums_kernel<<<p.nchunks, 1024, 0, s>>>(b.counts, p.nbuckets, b.chunk_sums);
   HERMES_LAUNCH_CHECK("dep_scan_sums_kernel");
-  dep_scan_chunks_kernel<<<1, 1024, 0, s>>>(b.chunk_sums, p.nchunks);
+  dep_scan_chunks_kernel<<<1, 1024, 0, s>>>(b.chunk_sums, p.nchunks, b.st, n, phi, n_phi, b.phif);
   HERMES_LAUNCH_CHECK("dep_scan_chunks_kernel");
   dep_scan_apply_kernel<<<p.nchunks, 1024, 0, s>>>(b.counts, p.nbuckets, b.chunk_sums, b.offsets, b.cursor);
   HERMES_LAUNCH_CHECK("dep_scan_apply_kernel");
@@ -522,7 +574,7 @@ extern "C" int hermes_deposit_accumulate(int64_t n, int J, double box, const dou
   if (rc) return rc;
   cudaStream_t s = hermes::as_stream(stream);
   const int ncell = p.g.tx * p.g.ty * p.g.tz;
-  const size_t smem = (size_t)ncell * 8 + (counts_out ? (size_t)ncell * 4 : 0) + (size_t)n_phi * 4;
+  const size_t smem = (size_t)ncell * 8 + (counts_out ? (size_t)ncell * 4 : 0);
   if (smem > 227 * 1024) return hermes::fail(HERMES_ERR_UNSUPPORTED, "deposit: shared memory %zu too large", smem);
   const int ntiles = p.g.ntx * p.g.nty * p.g.ntz;
   DepRec* sorted = b.sorted;
@@ -530,10 +582,10 @@ extern "C" int hermes_deposit_accumulate(int64_t n, int J, double box, const dou
   DepStatus* st = b.st;
   int lrc = HERMES_OK;
   switch (p.g.S) {
-    case 1: lrc = dep_launch_accum<1>(sorted, offsets, phi, n_phi, p.g, n, st, eps_out, eps_f64_out, counts_out, ntiles, smem, s); break;
-    case 2: lrc = dep_launch_accum<2>(sorted, offsets, phi, n_phi, p.g, n, st, eps_out, eps_f64_out, counts_out, ntiles, smem, s); break;
-    case 3: lrc = dep_launch_accum<3>(sorted, offsets, phi, n_phi, p.g, n, st, eps_out, eps_f64_out, counts_out, ntiles, smem, s); break;
-    default: lrc = dep_launch_accum<4>(sorted, offsets, phi, n_phi, p.g, n, st, eps_out, eps_f64_out, counts_out, ntiles, smem, s); break;
+    case 1: lrc = dep_launch_accum<1>(sorted, offsets, b.phif, p.g, st, eps_out, eps_f64_out, counts_out, ntiles, smem, s); break;
+    case 2: lrc = dep_launch_accum<2>(sorted, offsets, b.phif, p.g, st, eps_out, eps_f64_out, counts_out, ntiles, smem, s); break;
+    case 3: lrc = dep_launch_accum<3>(sorted, offsets, b.phif, p.g, st, eps_out, eps_f64_out, counts_out, ntiles, smem, s); break;
+    default: lrc = dep_launch_accum<4>(sorted, offsets, b.phif, p.g, st, eps_out, eps_f64_out, counts_out, ntiles, smem, s); break;
   }
   if (lrc) return lrc;
   HERMES_LAUNCH_CHECK("dep_accum_kernel");

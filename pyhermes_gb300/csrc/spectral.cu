@@ -1,0 +1,517 @@
+// Spectral window passes around cuFFT: `field @ window`, kernel
+// materialisation, and multi-bin pair products by Parseval.
+//
+// Reference path (pyhermes/utils/convolution.py, io/window.py,
+// theory/corr2pcf.py:366-372): materialise a float64 kernel array of
+// L^2 (L/2+1) values per window (8 images x W(k) per mode), then
+// irfftn(rfftn(eps) * K), then mean(conv * eps2) -- two FFTs and a kernel
+// build per bin.  Here the kernel is evaluated on the fly in the pass that
+// touches the spectrum, and the 2PCF products of every bin are one pass over
+// the half spectra:  sum_x (f1 * K)(x) f2(x) / L^3 = sum_k F1 K conj(F2) / L^6.
+#include <cufft.h>
+
+#include <map>
+#include <mutex>
+#include <tuple>
+#include <vector>
+
+#include "hermes_common.cuh"
+#include "window_eval.cuh"
+
+namespace hermes {
+
+// ---- cuFFT plan cache ----------------------------------------------------
+enum PlanKind { kR2C = 0, kC2R = 1, kC2C = 2 };
+
+static std::mutex g_plan_mu;
+static std::map<std::tuple<int, int, int, int>, cufftHandle> g_plans;
+
+int get_plan(int J, PlanKind kind, int batch, cufftHandle* out) {
+  int dev = 0;
+  HERMES_CUDA_TRY(cudaGetDevice(&dev));
+  auto key = std::make_tuple(dev, J, (int)kind, batch);
+  std::lock_guard<std::mutex> lk(g_plan_mu);
+  auto it = g_plans.find(key);
+  if (it != g_plans.end()) {
+    *out = it->second;
+    return HERMES_OK;
+  }
+  cufftHandle h;
+  const int L = 1 << J;
+  int n[3] = {L, L, L};
+  cufftType t = kind == kR2C ? CUFFT_R2C : (kind == kC2R ? CUFFT_C2R : CUFFT_C2C);
+  long long dist_in = kind == kC2R ? (long long)L * L * (L / 2 + 1) : (long long)L * L * L;
+  long long dist_out = kind == kR2C ? (long long)L * L * (L / 2 + 1) : (long long)L * L * L;
+  cufftResult r = cufftPlanMany(&h, 3, n, nullptr, 1, (int)dist_in, nullptr, 1, (int)dist_out, t, batch);
+  if (r != CUFFT_SUCCESS) return fail(HERMES_ERR_CUFFT, "cufftPlanMany(J=%d, kind=%d, batch=%d) failed: %d", J, (int)kind, batch, (int)r);
+  g_plans[key] = h;
+  *out = h;
+  return HERMES_OK;
+}
+
+#define HERMES_CUFFT_TRY(expr)                                                   \
+  do {                                                                           \
+    cufftResult _r = (expr);                                                     \
+    if (_r != CUFFT_SUCCESS) return hermes::fail(HERMES_ERR_CUFFT, "%s failed: %d", #expr, (int)_r); \
+  } while (0)
+
+// ---- host-side window preparation ---------------------------------------
+static void split_df(double v, float& hi, float& lo) {
+  hi = (float)v;
+  lo = (float)(v - (double)hi);
+}
+
+int prepare_window(const hermes_window_t& in, int L, WinDev* out) {
+  WinDev w;
+  memset(&w, 0, sizeof(w));
+  w.type = in.type;
+  w.mode = in.kernel_mode;
+  w.zero_k0 = in.zero_mode_zero ? 1 : 0;
+  w.los_axis = -1;
+  w.scale = (float)(in.scale == 0.0 ? 1.0 : in.scale);
+  if (in.type < 0 || in.type > HERMES_WIN_INVERSE_LAPLACIAN)
+    return fail(HERMES_ERR_INVALID, "window: unknown type %d", in.type);
+  if (in.kernel_mode < 0 || in.kernel_mode > HERMES_KMODE_COMPLEX_RFFT)
+    return fail(HERMES_ERR_INVALID, "window: unknown kernel_mode %d", in.kernel_mode);
+  const double invL = 1.0 / (double)L;
+  for (int i = 0; i < 4; ++i) {
+    w.len[i] = (float)in.len[i];
+    split_df(in.len[i] * invL, w.rho_hi[i], w.rho_lo[i]);
+  }
+  const double e = 2.718281828459045;
+  const double pi = 3.141592653589793;
+  switch (in.type) {
+    case HERMES_WIN_THICK_SHELL: {
+      double R = in.len[0], dR = in.len[1];
+      if (!(R >= 0.0) || !(dR > 0.0)) return fail(HERMES_ERR_INVALID, "thick_shell requires R >= 0 and delta_R > 0");
+      double rin = R - 0.5 * dR;
+      if (rin < 0.0) rin = 0.0;
+      double rout = R + 0.5 * dR;
+      double den = rout * rout * rout - rin * rin * rin;
+      if (den == 0.0) {
+        w.c0 = 0.f;
+        w.c1 = 0.f;
+      } else {
+        w.c0 = (float)(rout * rout * rout / den);
+        w.c1 = (float)(rin * rin * rin / den);
+      }
+      split_df(rout * invL, w.rho_hi[0], w.rho_lo[0]);
+      split_df(rin * invL, w.rho_hi[1], w.rho_lo[1]);
+      break;
+    }
+    case HERMES_WIN_GAUSSIAN_SHELL: {
+      double rs = in.len[0], rm = in.len[1];
+      double den = rs * rs + rm * rm;
+      if (den == 0.0) {
+        w.c0 = -1.f;
+        w.c1 = -1.f;
+      } else {
+        w.c0 = (float)(rm * rm / den);
+        w.c1 = (float)(rs * rs / den);
+      }
+      break;
+    }
+    case HERMES_WIN_CW: {
+      double ccw = 2.0 * sqrt(2.0) / (sqrt(1.0 + 5.0 * e) * pow(pi, 0.25));
+      w.c0 = (float)(sqrt(2.0 * pi) * ccw * pow(in.len[0], 0.5));
+      break;
+    }
+    case HERMES_WIN_CWS: {
+      double ccws = 2.0 * sqrt(2.0) / (sqrt(9.0 + 55.0 * e) * pow(pi, 0.75));
+      w.c0 = (float)(pow(2.0 * pi, 1.5) * ccws * pow(in.len[0], 1.5));
+      break;
+    }
+    case HERMES_WIN_GDW:
+      w.c0 = (float)(pow(2.0, 2.5) * pow(pi, 0.75) / sqrt(15.0) * pow(in.len[0], 1.5));
+      break;
+    case HERMES_WIN_LAPLACIAN:
+    case HERMES_WIN_INVERSE_LAPLACIAN:
+      w.c0 = (float)(invL * invL);
+      break;
+    default:
+      break;
+  }
+  if (in.type >= HERMES_WIN_RING && in.type <= HERMES_WIN_CYLINDER ||
+      in.type == HERMES_WIN_DIRECTIONAL_DERIVATIVE) {
+    double nx = in.los[0], ny = in.los[1], nz = in.los[2];
+    double nrm = sqrt(nx * nx + ny * ny + nz * nz);
+    if (!(nrm > 0.0)) return fail(HERMES_ERR_INVALID, "window: line of sight must be non-zero");
+    nx /= nrm;
+    ny /= nrm;
+    nz /= nrm;
+    w.los[0] = (float)nx;
+    w.los[1] = (float)ny;
+    w.los[2] = (float)nz;
+    const double v[3] = {nx, ny, nz};
+    for (int a = 0; a < 3; ++a) {
+      if (fabs(fabs(v[a]) - 1.0) == 0.0 && v[(a + 1) % 3] == 0.0 && v[(a + 2) % 3] == 0.0) w.los_axis = a;
+    }
+    if (in.type == HERMES_WIN_DIRECTIONAL_DERIVATIVE) w.c0 = (float)invL;
+  }
+  *out = w;
+  return HERMES_OK;
+}
+
+// ---- kernels -------------------------------------------------------------
+__global__ void phi_power_to_f32(const double* __restrict__ p, int n, float* __restrict__ out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (float)p[i];
+}
+
+// spec[k] *= K(k) * factor on the half spectrum [L][L][L/2+1].
+__global__ void spec_apply_window_kernel(float2* __restrict__ spec, WinDev w, int L,
+                                         const double* __restrict__ pd, int np, int bw, float factor) {
+  extern __shared__ float P[];
+  for (int i = threadIdx.x; i < np; i += blockDim.x) P[i] = (float)pd[i];
+  __syncthreads();
+  const int H = L / 2 + 1;
+  const long long total = (long long)L * L * H;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x; m < total; m += stride) {
+    const int z = (int)(m % H);
+    const long long r = m / H;
+    const int y = (int)(r % L), x = (int)(r / L);
+    const float2 K = kernel_value(w, x, y, z, L, P, bw);
+    const float2 s = spec[m];
+    spec[m] = make_float2((s.x * K.x - s.y * K.y) * factor, (s.x * K.y + s.y * K.x) * factor);
+  }
+}
+
+__global__ void materialize_kernel(WinDev w, int L, const double* __restrict__ pd, int np, int bw,
+                                   float* __restrict__ kr, float2* __restrict__ kc) {
+  extern __shared__ float P[];
+  for (int i = threadIdx.x; i < np; i += blockDim.x) P[i] = (float)pd[i];
+  __syncthreads();
+  const int H = L / 2 + 1;
+  const long long total = (long long)L * L * H;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x; m < total; m += stride) {
+    const int z = (int)(m % H);
+    const long long r = m / H;
+    const int y = (int)(r % L), x = (int)(r / L);
+    const float2 K = kernel_value(w, x, y, z, L, P, bw);
+    if (kr) kr[m] = K.x;
+    if (kc) kc[m] = K;
+  }
+}
+
+__global__ void spec_multiply_kernel(float2* __restrict__ spec, const float* __restrict__ kr,
+                                     const float2* __restrict__ kc, long long total, float factor) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x; m < total; m += stride) {
+    const float2 s = spec[m];
+    float2 K = kc ? kc[m] : make_float2(kr[m], 0.f);
+    spec[m] = make_float2((s.x * K.x - s.y * K.y) * factor, (s.x * K.y + s.y * K.x) * factor);
+  }
+}
+
+constexpr int kPPThreads = 256;
+constexpr int kPPModesPerThread = 16;
+constexpr int kMaxPairs = 4;
+constexpr int kBinsPerGroup = 4;
+
+struct PPArgs {
+  const float2* si[kMaxPairs];  // first spectrum of pair p
+  const float2* sj[kMaxPairs];  // second spectrum of pair p
+  int n_pairs;
+  int L;
+  int bw, np;
+  int n_bins;
+  int exclude_k0;
+  int complex_k;  // any bin with a complex kernel
+};
+
+// grid.x: mode blocks; grid.y: bin groups.  partial[(blockIdx.x * n_bins + b) * n_pairs + p].
+// NP = number of (i, j) spectrum pairs handled together (compile-time).
+template <int NP>
+__global__ void __launch_bounds__(kPPThreads)
+pair_products_kernel(PPArgs a, const WinDev* __restrict__ wins, const double* __restrict__ pd,
+                     double* __restrict__ partial, double* __restrict__ k0) {
+  extern __shared__ float P[];
+  __shared__ double red[kPPThreads / 32][kBinsPerGroup * NP];
+  for (int i = threadIdx.x; i < a.np; i += blockDim.x) P[i] = (float)pd[i];
+  __syncthreads();
+  const int L = a.L, H = L / 2 + 1;
+  const long long total = (long long)L * L * H;
+  const int b0 = blockIdx.y * kBinsPerGroup;
+  const int nb = min(kBinsPerGroup, a.n_bins - b0);
+  if (blockIdx.x == 0 && threadIdx.x < nb) k0[b0 + threadIdx.x] = (double)kernel_value(wins[b0 + threadIdx.x], 0, 0, 0, L, P, a.bw).x;
+  double acc[kBinsPerGroup][NP];
+#pragma unroll
+  for (int b = 0; b < kBinsPerGroup; ++b)
+#pragma unroll
+    for (int p = 0; p < NP; ++p) acc[b][p] = 0.0;
+
+  const long long base = (long long)blockIdx.x * kPPThreads * kPPModesPerThread;
+  float fac[kBinsPerGroup][NP];
+#pragma unroll
+  for (int b = 0; b < kBinsPerGroup; ++b)
+#pragma unroll
+    for (int p = 0; p < NP; ++p) fac[b][p] = 0.f;
+  for (int it = 0; it < kPPModesPerThread; ++it) {
+    const long long m = base + (long long)it * kPPThreads + threadIdx.x;
+    if (m >= total) break;
+    const int z = (int)(m % H);
+    const long long r = m / H;
+    const int y = (int)(r % L), x = (int)(r / L);
+    if (a.exclude_k0 && m == 0) continue;
+    const float wgt = (z == 0 || z == L / 2) ? 1.f : 2.f;
+    float tr[NP], ti[NP];
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+      if (true) {
+        const float2 u = a.si[p][m], v = a.sj[p][m];
+        tr[p] = wgt * (u.x * v.x + u.y * v.y);   // Re(u conj v)
+        ti[p] = wgt * (u.y * v.x - u.x * v.y);   // Im(u conj v)
+      } else {
+        tr[p] = 0.f;
+        ti[p] = 0.f;
+      }
+    }
+#pragma unroll
+    for (int b = 0; b < kBinsPerGroup; ++b) {
+      if (b < nb) {
+        const float2 K = kernel_value(wins[b0 + b], x, y, z, L, P, a.bw);
+#pragma unroll
+        for (int p = 0; p < NP; ++p)
+          fac[b][p] += tr[p] * K.x - ti[p] * K.y;
+      }
+    }
+    if ((it & 3) == 3) {  // fold float32 partials into float64 every 4 modes
+#pragma unroll
+      for (int b = 0; b < kBinsPerGroup; ++b)
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+          acc[b][p] += (double)fac[b][p];
+          fac[b][p] = 0.f;
+        }
+    }
+  }
+#pragma unroll
+  for (int b = 0; b < kBinsPerGroup; ++b)
+#pragma unroll
+    for (int p = 0; p < NP; ++p) acc[b][p] += (double)fac[b][p];
+
+  // block reduction (fixed order -> deterministic)
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int b = 0; b < kBinsPerGroup; ++b)
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+      double v = acc[b][p];
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) red[wid][b * NP + p] = v;
+    }
+  __syncthreads();
+  if (threadIdx.x < nb * NP) {
+    const int b = threadIdx.x / NP, p = threadIdx.x % NP;
+    double s = 0.0;
+    for (int w = 0; w < kPPThreads / 32; ++w) s += red[w][b * NP + p];
+    partial[((long long)blockIdx.x * a.n_bins + b0 + b) * a.n_pairs + p] = s;
+  }
+}
+
+__global__ void reduce_partials_kernel(const double* __restrict__ partial, int nblocks, int nout,
+                                       double scale, double* __restrict__ out) {
+  const int o = blockIdx.x;
+  double s = 0.0;
+  for (int b = threadIdx.x; b < nblocks; b += blockDim.x) s += partial[(long long)b * nout + o];
+  __shared__ double sh[256];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[o] = sh[0] * scale;
+}
+
+int grid_for(long long total, int threads) {
+  int dev = 0, nsm = 148;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  long long want = (total + threads - 1) / threads;
+  long long cap = (long long)nsm * 16;
+  return (int)(want < 1 ? 1 : (want < cap ? want : cap));
+}
+
+int check_power(int J, int bw) {
+  if (J < 2 || J > 10) return fail(HERMES_ERR_INVALID, "J=%d outside [2,10]", J);
+  if (bw < 1) return fail(HERMES_ERR_INVALID, "bandwidth must be >= 1");
+  long long n = (long long)(1 << J) * bw;
+  if (3 * n * n >= (1LL << 24)) return fail(HERMES_ERR_UNSUPPORTED, "bandwidth*L too large for exact float frequencies");
+  return HERMES_OK;
+}
+
+}  // namespace hermes
+
+using namespace hermes;
+
+extern "C" int hermes_fft_r2c(const float* field, void* spec, int J, void* stream) {
+  if (J < 2 || J > 10) return fail(HERMES_ERR_INVALID, "fft: J=%d outside [2,10]", J);
+  cufftHandle h;
+  int rc = get_plan(J, kR2C, 1, &h);
+  if (rc) return rc;
+  HERMES_CUFFT_TRY(cufftSetStream(h, as_stream(stream)));
+  HERMES_CUFFT_TRY(cufftExecR2C(h, const_cast<cufftReal*>(field), reinterpret_cast<cufftComplex*>(spec)));
+  return HERMES_OK;
+}
+
+extern "C" int hermes_fft_c2r(void* spec, float* field, int J, void* stream) {
+  if (J < 2 || J > 10) return fail(HERMES_ERR_INVALID, "fft: J=%d outside [2,10]", J);
+  cufftHandle h;
+  int rc = get_plan(J, kC2R, 1, &h);
+  if (rc) return rc;
+  HERMES_CUFFT_TRY(cufftSetStream(h, as_stream(stream)));
+  HERMES_CUFFT_TRY(cufftExecC2R(h, reinterpret_cast<cufftComplex*>(spec), field));
+  return HERMES_OK;
+}
+
+extern "C" int hermes_window_workspace_size(int J, size_t* bytes) {
+  if (!bytes) return fail(HERMES_ERR_INVALID, "bytes is NULL");
+  if (J < 2 || J > 10) return fail(HERMES_ERR_INVALID, "J=%d outside [2,10]", J);
+  const size_t L = (size_t)1 << J;
+  *bytes = L * L * (L / 2 + 1) * sizeof(float2);
+  return HERMES_OK;
+}
+
+extern "C" int hermes_window_apply(const float* eps, float* out, int J, const hermes_window_t* win,
+                                   const double* phi_power, int bandwidth, void* workspace,
+                                   size_t workspace_bytes, void* stream) {
+  if (!eps || !out || !win || !phi_power) return fail(HERMES_ERR_INVALID, "window_apply: NULL argument");
+  int rc = check_power(J, bandwidth);
+  if (rc) return rc;
+  size_t need = 0;
+  hermes_window_workspace_size(J, &need);
+  if (!workspace || workspace_bytes < need)
+    return fail(HERMES_ERR_WORKSPACE, "window_apply: workspace %zu < %zu", workspace_bytes, need);
+  const int L = 1 << J;
+  WinDev w;
+  rc = prepare_window(*win, L, &w);
+  if (rc) return rc;
+  float2* spec = static_cast<float2*>(workspace);
+  rc = hermes_fft_r2c(eps, spec, J, stream);
+  if (rc) return rc;
+  const int np = L * bandwidth + 1;
+  const long long total = (long long)L * L * (L / 2 + 1);
+  const float factor = (float)(1.0 / ((double)L * L * L));
+  spec_apply_window_kernel<<<grid_for(total, 256), 256, np * sizeof(float), as_stream(stream)>>>(
+      spec, w, L, phi_power, np, bandwidth, factor);
+  HERMES_LAUNCH_CHECK("spec_apply_window_kernel");
+  return hermes_fft_c2r(spec, out, J, stream);
+}
+
+extern "C" int hermes_window_materialize(const hermes_window_t* win, const double* phi_power, int bandwidth,
+                                         int J, float* k_real, void* k_cplx, void* stream) {
+  if (!win || !phi_power) return fail(HERMES_ERR_INVALID, "materialize: NULL argument");
+  if ((k_real == nullptr) == (k_cplx == nullptr))
+    return fail(HERMES_ERR_INVALID, "materialize: give exactly one of k_real / k_cplx");
+  int rc = check_power(J, bandwidth);
+  if (rc) return rc;
+  const int L = 1 << J;
+  WinDev w;
+  rc = prepare_window(*win, L, &w);
+  if (rc) return rc;
+  const int np = L * bandwidth + 1;
+  const long long total = (long long)L * L * (L / 2 + 1);
+  materialize_kernel<<<grid_for(total, 256), 256, np * sizeof(float), as_stream(stream)>>>(
+      w, L, phi_power, np, bandwidth, k_real, static_cast<float2*>(k_cplx));
+  HERMES_LAUNCH_CHECK("materialize_kernel");
+  return HERMES_OK;
+}
+
+extern "C" int hermes_spectrum_multiply(void* spec, const float* k_real, const void* k_cplx, int J,
+                                        double factor, void* stream) {
+  if (!spec || ((k_real == nullptr) == (k_cplx == nullptr)))
+    return fail(HERMES_ERR_INVALID, "spectrum_multiply: give spec and exactly one kernel");
+  if (J < 2 || J > 10) return fail(HERMES_ERR_INVALID, "J=%d outside [2,10]", J);
+  const long long L = 1LL << J;
+  const long long total = L * L * (L / 2 + 1);
+  spec_multiply_kernel<<<grid_for(total, 256), 256, 0, as_stream(stream)>>>(
+      static_cast<float2*>(spec), k_real, static_cast<const float2*>(k_cplx), total, (float)factor);
+  HERMES_LAUNCH_CHECK("spec_multiply_kernel");
+  return HERMES_OK;
+}
+
+static long long pp_mode_blocks(int J) {
+  const long long L = 1LL << J;
+  const long long total = L * L * (L / 2 + 1);
+  const long long per = (long long)kPPThreads * kPPModesPerThread;
+  return (total + per - 1) / per;
+}
+
+extern "C" int hermes_pair_products_workspace_size(int J, int n_bins, int n_pairs, size_t* bytes) {
+  if (!bytes) return fail(HERMES_ERR_INVALID, "bytes is NULL");
+  if (J < 2 || J > 10) return fail(HERMES_ERR_INVALID, "J=%d outside [2,10]", J);
+  if (n_bins < 1 || n_pairs < 1 || n_pairs > kMaxPairs)
+    return fail(HERMES_ERR_INVALID, "pair_products: n_bins >= 1 and 1 <= n_pairs <= %d", kMaxPairs);
+  Carver c(nullptr, 0);
+  c.take<WinDev>(n_bins);
+  c.take<double>((size_t)pp_mode_blocks(J) * n_bins * n_pairs);
+  c.take<double>((size_t)n_bins * n_pairs);
+  c.take<double>((size_t)n_bins);
+  *bytes = c.used;
+  return HERMES_OK;
+}
+
+extern "C" int hermes_pair_products(const void* const* spectra, int n_spec, const int32_t* pairs, int n_pairs,
+                                    const hermes_window_t* bins, int n_bins, const double* phi_power,
+                                    int bandwidth, int J, int exclude_k0, double* out, double* k0_out,
+                                    void* workspace, size_t workspace_bytes, void* stream) {
+  if (!spectra || !pairs || !bins || !phi_power || !out) return fail(HERMES_ERR_INVALID, "pair_products: NULL argument");
+  size_t need = 0;
+  int rc = hermes_pair_products_workspace_size(J, n_bins, n_pairs, &need);
+  if (rc) return rc;
+  rc = check_power(J, bandwidth);
+  if (rc) return rc;
+  if (!workspace || workspace_bytes < need)
+    return fail(HERMES_ERR_WORKSPACE, "pair_products: workspace %zu < %zu", workspace_bytes, need);
+  const int L = 1 << J;
+  PPArgs a;
+  memset(&a, 0, sizeof(a));
+  if (n_spec < 1 || n_spec > 2 * kMaxPairs) return fail(HERMES_ERR_INVALID, "pair_products: n_spec=%d", n_spec);
+  for (int i = 0; i < n_spec; ++i)
+    if (!spectra[i]) return fail(HERMES_ERR_INVALID, "pair_products: spectra[%d] is NULL", i);
+  for (int p = 0; p < n_pairs; ++p) {
+    if (pairs[2 * p] < 0 || pairs[2 * p] >= n_spec || pairs[2 * p + 1] < 0 || pairs[2 * p + 1] >= n_spec)
+      return fail(HERMES_ERR_INVALID, "pair_products: pair %d indexes outside [0,%d)", p, n_spec);
+    a.si[p] = static_cast<const float2*>(spectra[pairs[2 * p]]);
+    a.sj[p] = static_cast<const float2*>(spectra[pairs[2 * p + 1]]);
+  }
+  a.n_pairs = n_pairs;
+  a.L = L;
+  a.bw = bandwidth;
+  a.np = L * bandwidth + 1;
+  a.n_bins = n_bins;
+  a.exclude_k0 = exclude_k0 ? 1 : 0;
+  std::vector<WinDev> hw(n_bins);
+  for (int b = 0; b < n_bins; ++b) {
+    rc = prepare_window(bins[b], L, &hw[b]);
+    if (rc) return rc;
+  }
+  Carver c(workspace, workspace_bytes);
+  WinDev* dwin = c.take<WinDev>(n_bins);
+  const long long nblk = pp_mode_blocks(J);
+  double* partial = c.take<double>((size_t)nblk * n_bins * n_pairs);
+  double* dout = c.take<double>((size_t)n_bins * n_pairs);
+  double* dk0 = c.take<double>((size_t)n_bins);
+  cudaStream_t s = as_stream(stream);
+  HERMES_CUDA_TRY(cudaMemcpyAsync(dwin, hw.data(), sizeof(WinDev) * n_bins, cudaMemcpyHostToDevice, s));
+  dim3 grid((unsigned)nblk, (unsigned)((n_bins + kBinsPerGroup - 1) / kBinsPerGroup));
+  const size_t sm = a.np * sizeof(float);
+  switch (n_pairs) {
+    case 1: pair_products_kernel<1><<<grid, kPPThreads, sm, s>>>(a, dwin, phi_power, partial, dk0); break;
+    case 2: pair_products_kernel<2><<<grid, kPPThreads, sm, s>>>(a, dwin, phi_power, partial, dk0); break;
+    case 3: pair_products_kernel<3><<<grid, kPPThreads, sm, s>>>(a, dwin, phi_power, partial, dk0); break;
+    case 4: pair_products_kernel<4><<<grid, kPPThreads, sm, s>>>(a, dwin, phi_power, partial, dk0); break;
+    default: return fail(HERMES_ERR_UNSUPPORTED, "pair_products: n_pairs=%d > 4", n_pairs);
+  }
+  HERMES_LAUNCH_CHECK("pair_products_kernel");
+  const double scale = 1.0 / ((double)L * L * L * (double)L * L * L);
+  reduce_partials_kernel<<<n_bins * n_pairs, 256, 0, s>>>(partial, (int)nblk, n_bins * n_pairs, scale, dout);
+  HERMES_LAUNCH_CHECK("reduce_partials_kernel");
+  HERMES_CUDA_TRY(cudaMemcpyAsync(out, dout, sizeof(double) * n_bins * n_pairs, cudaMemcpyDeviceToHost, s));
+  if (k0_out) HERMES_CUDA_TRY(cudaMemcpyAsync(k0_out, dk0, sizeof(double) * n_bins, cudaMemcpyDeviceToHost, s));
+  HERMES_CUDA_TRY(cudaStreamSynchronize(s));
+  return HERMES_OK;
+}

@@ -82,7 +82,97 @@ def gen_deposit():
               raw_field_weighted_sum=np.array(f.sfc_info["raw_field_weighted_sum"]))
 
 
-SECTIONS = {"phi": gen_phi, "deposit": gen_deposit}
+WINDOW_CASES = {
+    # name: (win_params, bandwidth)
+    "sphere": ({"type": "sphere", "len_args": {"R": 90.0}}, 1),
+    "gaussian": ({"type": "gaussian", "len_args": {"R": 70.0}}, 1),
+    "shell": ({"type": "shell", "len_args": {"R": 150.0}}, 1),
+    "thick_shell": ({"type": "thick_shell", "len_args": {"R": 120.0, "delta_R": 40.0}}, 1),
+    "thick_shell_inner0": ({"type": "thick_shell", "len_args": {"R": 10.0, "delta_R": 40.0}}, 1),
+    "gaussian_shell": ({"type": "gaussian_shell", "len_args": {"R_shell": 100.0, "R_smooth": 30.0}}, 1),
+    "cubic": ({"type": "cubic", "len_args": {"Lx": 80.0, "Ly": 120.0, "Lz": 200.0}}, 1),
+    "ring_z": ({"type": "ring", "len_args": {"R": 100.0, "H": 60.0}}, 1),
+    "disk_z": ({"type": "disk", "len_args": {"R": 100.0, "H": 60.0}}, 1),
+    "cylshell_z": ({"type": "cylshell", "len_args": {"R": 100.0, "H": 60.0}}, 1),
+    "cylinder_z": ({"type": "cylinder", "len_args": {"R": 100.0, "H": 60.0}}, 1),
+    "ring_tilted": ({"type": "ring", "len_args": {"R": 100.0, "H": 60.0},
+                     "los_args": {"nx": 1.0, "ny": 2.0, "nz": 2.0}}, 1),
+    "cw": ({"type": "cw", "len_args": {"R": 60.0}}, 1),
+    "cws": ({"type": "cws", "len_args": {"R": 60.0}}, 1),
+    "gdw": ({"type": "gdw", "len_args": {"R": 60.0}}, 1),
+    "dirderiv": ({"type": "directional_derivative", "los_args": {"nx": 0.0, "ny": 1.0, "nz": 1.0}}, 1),
+    "laplacian": ({"type": "laplacian"}, 1),
+    "inverse_laplacian": ({"type": "inverse_laplacian"}, 1),
+    "gaussian_bw2": ({"type": "gaussian", "len_args": {"R": 40.0}}, 2),
+}
+
+
+def _sfc_params(J):
+    return {"J": J, "box_size": 1000.0, "phi_resolution": 1024, "wavelet_mode": "db2", "wavelet_level": 10}
+
+
+def gen_windows():
+    from pyhermes.io.window import WindowFunc
+
+    out = {}
+    for name, (wp, bw) in WINDOW_CASES.items():
+        w = WindowFunc(dict(wp), _sfc_params(4), bandwidth=bw)
+        out[name] = np.asarray(w.as_array())
+    _save("windows_J4", **out)
+
+
+def gen_convolution():
+    from pyhermes.io.window import WindowFunc
+
+    rng = np.random.default_rng(7)
+    pos = rng.uniform(0.0, 1000.0, (4000, 3))
+    f = _projection(pos, 5, weights=rng.lognormal(0.0, 0.3, 4000))
+    res = {"pos": pos, "epsilon": f.epsilon}
+    for name in ("gaussian", "thick_shell", "ring_tilted", "dirderiv", "inverse_laplacian"):
+        w = WindowFunc(dict(WINDOW_CASES[name][0]), f.sfc_info)
+        res["conv_" + name] = (f @ w).epsilon
+    _save("convolution_J5", **res)
+
+
+def gen_corr2pcf():
+    from pyhermes.theory.corr2pcf import Corr_2PCF
+
+    rng = np.random.default_rng(11)
+    pos = rng.uniform(0.0, 1000.0, (6000, 3))
+    pos[:2000] = (pos[:2000] * 0.25 + 300.0)  # a clump so xi is not pure noise
+    w = rng.lognormal(0.0, 0.3, 6000)
+    f = _projection(pos, 5, weights=w)
+    out = {"pos": pos, "weights": w}
+    task = Corr_2PCF({"Corr_2PCF": {
+        "sfc_field": f, "random": "uniform",
+        "binning_window": {"type": "thick_shell", "len_args": {"R": None, "delta_R": 40.0},
+                           "mapping": "s_to_R"},
+        "sampling": {"s": {"min": 60.0, "max": 300.0, "n": 5}},
+        "products": ["dd", "dr", "delta_dd", "rr", "xi"]}})
+    d = task.run(save_result=False)
+    for k in ("dd", "dr", "delta_dd", "rr", "xi"):
+        out["iso_" + k] = np.asarray(getattr(d, k))
+    task = Corr_2PCF({"Corr_2PCF": {
+        "sfc_field": f, "random": "uniform",
+        "binning_window": {"type": "ring"},
+        "sampling": {"s": {"min": 80.0, "max": 240.0, "n": 3}, "mu": {"min": 0.1, "max": 0.9, "n": 3}},
+        "products": ["delta_dd", "xi"]}})
+    d = task.run(save_result=False)
+    out["smu_delta_dd"] = np.asarray(d.delta_dd)
+    out["smu_xi"] = np.asarray(d.xi)
+    task = Corr_2PCF({"Corr_2PCF": {
+        "sfc_field": f, "random": "uniform", "window": {"type": "gaussian", "len_args": {"R": 40.0}},
+        "binning_window": {"type": "shell", "len_args": ["R"], "mapping": "s_to_R"},
+        "sampling": {"s": {"min": 80.0, "max": 200.0, "n": 3}},
+        "products": ["xi"]}})
+    d = task.run(save_result=False)
+    out["smooth_xi"] = np.asarray(d.xi)
+    out["smooth_delta_dd"] = np.asarray(d.delta_dd)
+    _save("corr2pcf_J5", **out)
+
+
+SECTIONS = {"phi": gen_phi, "deposit": gen_deposit, "windows": gen_windows,
+            "convolution": gen_convolution, "corr2pcf": gen_corr2pcf}
 
 
 def main(argv):
