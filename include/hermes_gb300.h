@@ -161,6 +161,43 @@ int hermes_pair_products(const void* const* spectra, int n_spec, const int32_t* 
                          double* out, double* k0_out, void* workspace,
                          size_t workspace_bytes, void* stream);
 
+/* ---- 3PCF multipoles ---------------------------------------------------------
+ * Replaces, per (l, m), the per-sample loop of
+ * utils/corr3pcf_multipoles.py:505-555 (_stream_convolution_fields +
+ * compute_multipole_m_summand) for all radial bins at once.
+ *
+ * hermes_multipole_fields: for a real field with half spectrum `half_spec`
+ * (float2 [L,L,L/2+1], from hermes_fft_r2c) and thin-shell radii `radii`
+ * (host, grid units, nb <= 16), writes
+ *   fields_out[b] = ifftn(fftn(eps) * K_lm^b)   (complex64 [L^3] each)
+ * with K_lm^b the radial-multipole window of radial_multipole_windows.py:
+ * 128-183 (shell profile: j_l(2 pi |k| R_b) Y_lm(khat), 8 phi-weighted
+ * images; phi_power: L+1 float64 samples).
+ *
+ * hermes_multipole_contract: S[b2][b3] (host float64 complex, [nb2][nb3][2])
+ *   = 4 pi / L^3 sum_x eps1(x) sum_{l1,l2} Gamma3(l1,l2) a2^{b2}(x-l1) a3^{b3}(x-l2)
+ * for every bin pair (corr3pcf_multipoles.py:33-58 + :451), with
+ * a2 = fields2 and a3 = fields3, or a3 = conj_sign * conj(fields2) when
+ * fields3 is NULL (the a_{l,-m} = (-1)^{l+m} conj(a_{lm}) identity for a
+ * shared field and shared bins).  gamma: host float64 [3][3] triple overlaps
+ * (corr3pcf_multipoles.py:22-30).  Synchronises `stream`.
+ *
+ * hermes_multipole_contract_plain: the same sum for one (a2, a3) pair in the
+ * reference's per-cell loop form (workspace >= 16*(#SM*8+1) bytes).
+ */
+int hermes_multipole_workspace_size(int J, int nb, size_t* bytes);
+int hermes_multipole_fields(const void* half_spec, int J, int l, int m,
+                            const double* radii, int nb, const double* phi_power,
+                            void* fields_out, void* workspace, size_t workspace_bytes,
+                            void* stream);
+int hermes_multipole_contract(const float* eps1, const void* fields2, int nb2,
+                              const void* fields3, int nb3, int conj_sign,
+                              const double* gamma, int J, double* out,
+                              void* workspace, size_t workspace_bytes, void* stream);
+int hermes_multipole_contract_plain(const float* eps1, const void* a2, const void* a3,
+                                    const double* gamma, int J, double* out,
+                                    void* workspace, size_t workspace_bytes, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

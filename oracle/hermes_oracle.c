@@ -341,3 +341,234 @@ int oracle_window_rfft(int type, const double* args, const double* los, int L, i
       }
   return 0;
 }
+
+/* ------------------------------------------------------------------------
+ * 3PCF multipoles: special functions (utils/special_functions.py:49-128,
+ * 273-334), radial multipole windows (utils/radial_multipole_windows.py:
+ * 66-183) and the triple-product contraction
+ * (utils/corr3pcf_multipoles.py:134-170).
+ * ------------------------------------------------------------------------ */
+double oracle_spherical_jn(int l, double x) {
+  if (l < 0) return NAN;
+  if (x == 0.0) return l == 0 ? 1.0 : 0.0;
+  double ax = fabs(x);
+  if (ax <= 5.0e-2) {
+    if (l == 0) {
+      double x2 = x * x;
+      return 1.0 - x2 / 6.0 + x2 * x2 / 120.0;
+    }
+    double denom = 1.0;
+    for (int n = 1; n <= l; ++n) denom *= 2.0 * n + 1.0;
+    double x2 = x * x;
+    return (pow(x, l) / denom) * (1.0 - x2 / (2.0 * (2.0 * l + 3.0)) + x2 * x2 / (8.0 * (2.0 * l + 3.0) * (2.0 * l + 5.0)));
+  }
+  double sx = sin(x), cx = cos(x);
+  double j0 = sx / x;
+  if (l == 0) return j0;
+  double j1 = sx / (x * x) - cx / x;
+  if (l == 1) return j1;
+  if (ax < l + 1.0) {
+    int n_stop = l + 40;
+    double jp1 = 0.0, jcur = 1.0, jt = 0.0, jd0 = 0.0, jd1 = 0.0;
+    for (int n = n_stop; n > 0; --n) {
+      double jm1 = ((2.0 * n + 1.0) / x) * jcur - jp1;
+      if (n - 1 == l) jt = jm1;
+      if (n - 1 == 1) jd1 = jm1;
+      if (n - 1 == 0) jd0 = jm1;
+      jp1 = jcur;
+      jcur = jm1;
+      if (fabs(jcur) > 1.0e200) {
+        jp1 *= 1.0e-200; jcur *= 1.0e-200; jt *= 1.0e-200; jd0 *= 1.0e-200; jd1 *= 1.0e-200;
+      } else if (fabs(jcur) < 1.0e-200 && jcur != 0.0) {
+        jp1 *= 1.0e200; jcur *= 1.0e200; jt *= 1.0e200; jd0 *= 1.0e200; jd1 *= 1.0e200;
+      }
+    }
+    if (fabs(jd0) >= fabs(jd1) || jd1 == 0.0) return jt * (j0 / jd0);
+    return jt * (j1 / jd1);
+  }
+  double jm1 = j0, jc = j1;
+  for (int e = 1; e < l; ++e) {
+    double jn = ((2.0 * e + 1.0) / x) * jc - jm1;
+    jm1 = jc;
+    jc = jn;
+  }
+  return jc;
+}
+
+static double assoc_legendre(int l, int m, double x) {
+  double pmm = 1.0;
+  if (m > 0) {
+    double somx2 = sqrt(fmax(0.0, 1.0 - x * x)), fact = 1.0;
+    for (int i = 0; i < m; ++i) {
+      pmm *= -fact * somx2;
+      fact += 2.0;
+    }
+  }
+  if (l == m) return pmm;
+  double pmmp1 = x * (2.0 * m + 1.0) * pmm;
+  if (l == m + 1) return pmmp1;
+  double a = pmm, b = pmmp1, pll = 0.0;
+  for (int e = m + 2; e <= l; ++e) {
+    pll = ((2.0 * e - 1.0) * x * b - (e + m - 1.0) * a) / (e - m);
+    a = b;
+    b = pll;
+  }
+  return pll;
+}
+
+static double fact_small(int n) {
+  double o = 1.0;
+  for (int i = 2; i <= n; ++i) o *= i;
+  return o;
+}
+
+/* Y_l^m(khat) (special_functions.py:307-334); returns re, *im. */
+void oracle_sph_harm(int l, int m, double ki, double kj, double kk, double* re, double* im) {
+  *re = 0.0;
+  *im = 0.0;
+  if (abs(m) > l) return;
+  double k = sqrt(ki * ki + kj * kj + kk * kk);
+  if (k == 0.0) {
+    if (l == 0 && m == 0) *re = 1.0 / sqrt(4.0 * PI);
+    return;
+  }
+  double mu = kk / k;
+  if (mu > 1.0) mu = 1.0;
+  else if (mu < -1.0) mu = -1.0;
+  double theta = acos(mu), phi = atan2(kj, ki);
+  int mp = m < 0 ? -m : m;
+  double x = cos(theta);
+  double P = assoc_legendre(l, mp, x);
+  double norm = sqrt((2.0 * l + 1.0) / (4.0 * PI) * fact_small(l - mp) / fact_small(l + mp));
+  double r = norm * P * cos(mp * phi), i = norm * P * sin(mp * phi);
+  if (m >= 0) {
+    *re = r;
+    *im = i;
+  } else {
+    double sign = (mp % 2 == 1) ? -1.0 : 1.0;
+    *re = sign * r;
+    *im = -sign * i;
+  }
+}
+
+static double sphere_profile(double k, double R) {
+  double q = 2.0 * PI * k * R;
+  if (q == 0.0) return 1.0;
+  return 3.0 * (sin(q) - q * cos(q)) / (q * q * q);
+}
+
+/* _radial_profile (radial_multipole_windows.py:112-125); codes 0..4 =
+ * shell, gaussian_shell, thick_shell, sphere, gaussian. */
+static double radial_profile(double k, int code, const double* a, int l) {
+  switch (code) {
+    case 0: return oracle_spherical_jn(l, 2.0 * PI * k * a[0]);
+    case 1: {
+      if (k == 0.0) return 1.0;
+      double qs = 2.0 * PI * k * a[0], qm = 2.0 * PI * k * a[1];
+      double den = a[0] * a[0] + a[1] * a[1];
+      if (den == 0.0) return 1.0;
+      double sinc = qs == 0.0 ? 1.0 : sin(qs) / qs;
+      return (a[1] * a[1] * cos(qs) + a[0] * a[0] * sinc) / den * exp(-0.5 * qm * qm);
+    }
+    case 2: {
+      double rin = a[0] - 0.5 * a[1];
+      if (rin < 0.0) rin = 0.0;
+      double rout = a[0] + 0.5 * a[1];
+      double den = rout * rout * rout - rin * rin * rin;
+      if (den == 0.0) return 1.0;
+      return (rout * rout * rout * sphere_profile(k, rout) - rin * rin * rin * sphere_profile(k, rin)) / den;
+    }
+    case 3: return sphere_profile(k, a[0]);
+    case 4: {
+      double q = 2.0 * PI * k * a[0];
+      return exp(-0.5 * q * q);
+    }
+  }
+  return NAN;
+}
+
+/* calculate_radial_multipole_window_array_numba (radial_multipole_windows.py:
+ * 147-183): complex [L,L,L] (interleaved re, im), args in grid units. */
+int oracle_radial_multipole_window(int L, const double* P, int code, const double* args, int l, int m,
+                                   double* out) {
+  const double invL = 1.0 / L;
+#pragma omp parallel for schedule(static)
+  for (int x = 0; x < L; ++x) {
+    const double ki[2] = {(x - L) * invL, x * invL};
+    const double pi_[2] = {P[L - x], P[x]};
+    for (int y = 0; y < L; ++y) {
+      const double kj[2] = {(y - L) * invL, y * invL};
+      const double pj[2] = {P[L - y], P[y]};
+      for (int z = 0; z < L; ++z) {
+        const double kk[2] = {(z - L) * invL, z * invL};
+        const double pk[2] = {P[L - z], P[z]};
+        double sr = 0.0, si = 0.0;
+        for (int a = 0; a < 2; ++a)
+          for (int b = 0; b < 2; ++b)
+            for (int c = 0; c < 2; ++c) {
+              double yr = 0.0, yi = 0.0, rad = 0.0;
+              if (l >= 0 && abs(m) <= l) {
+                double kn = sqrt(ki[a] * ki[a] + kj[b] * kj[b] + kk[c] * kk[c]);
+                rad = radial_profile(kn, code, args, l);
+                oracle_sph_harm(l, m, ki[a], kj[b], kk[c], &yr, &yi);
+              }
+              double w = pi_[a] * pj[b] * pk[c];
+              sr += w * (rad * yr);
+              si += w * (rad * yi);
+            }
+        int64_t o = (((int64_t)x * L + y) * L + z) * 2;
+        out[o] = sr;
+        out[o + 1] = si;
+      }
+    }
+  }
+  return 0;
+}
+
+/* compute_3d_summand_cpu (corr3pcf_multipoles.py:134-170): sum over cells of
+ * data(x) * sum_{l1,l2} Gamma3(l1,l2) a1(x-l1) a2(x-l2); a1/a2 interleaved
+ * complex [L^3]; returns re/im. */
+int oracle_contract(const double* data, const double* a1, const double* a2, const double* gamma, int L, int S,
+                    double* out_re, double* out_im) {
+  const int64_t N = (int64_t)L * L * L, plane = (int64_t)L * L;
+  double tr = 0.0, ti = 0.0;
+#pragma omp parallel for reduction(+ : tr, ti) schedule(static)
+  for (int64_t idx = 0; idx < N; ++idx) {
+    const int64_t lx = idx / plane, rem = idx - lx * plane, ly = rem / L, lz = rem - ly * L;
+    double s1r = 0.0, s1i = 0.0;
+    for (int l1x = 0; l1x < S; ++l1x) {
+      const int64_t i1x = pmod(lx - l1x, L);
+      for (int l1y = 0; l1y < S; ++l1y) {
+        const int64_t i1y = pmod(ly - l1y, L);
+        for (int l1z = 0; l1z < S; ++l1z) {
+          const int64_t i1z = pmod(lz - l1z, L);
+          double s2r = 0.0, s2i = 0.0;
+          for (int l2x = 0; l2x < S; ++l2x) {
+            const int64_t i2x = pmod(lx - l2x, L);
+            const double gx = gamma[l1x * S + l2x];
+            for (int l2y = 0; l2y < S; ++l2y) {
+              const int64_t i2y = pmod(ly - l2y, L);
+              const double gxy = gx * gamma[l1y * S + l2y];
+              for (int l2z = 0; l2z < S; ++l2z) {
+                const int64_t i2z = pmod(lz - l2z, L);
+                const double w = gxy * gamma[l1z * S + l2z];
+                const int64_t o = ((i2x * L + i2y) * L + i2z) * 2;
+                s2r += w * a2[o];
+                s2i += w * a2[o + 1];
+              }
+            }
+          }
+          const int64_t o1 = ((i1x * L + i1y) * L + i1z) * 2;
+          s1r += a1[o1] * s2r - a1[o1 + 1] * s2i;
+          s1i += a1[o1] * s2i + a1[o1 + 1] * s2r;
+        }
+      }
+    }
+    const double d = data[idx];
+    tr += d * s1r;
+    ti += d * s1i;
+  }
+  *out_re = tr;
+  *out_im = ti;
+  return 0;
+}

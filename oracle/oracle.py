@@ -159,3 +159,120 @@ def pair_product(eps1, eps2, kernel):
     """theory/corr2pcf.py:366-372: mean((eps1 conv K) * eps2)."""
     conv = convolve(eps1, kernel)
     return float(np.einsum("ijk,ijk->", conv, eps2, optimize=True) / conv.size)
+
+
+def cal_gamma(phi, support=3, res=1024):
+    """utils/corr3pcf_multipoles.py:22-30."""
+    phi = np.asarray(phi, dtype=np.float64)
+    g = np.zeros((support, support))
+    for a in range(support):
+        for b in range(support):
+            g[a, b] = np.sum(phi * np.roll(phi, a * res) * np.roll(phi, b * res)) / res
+    return g
+
+
+def _setup_multipole_lib():
+    lb = lib()
+    P, I, D = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+    lb.oracle_radial_multipole_window.argtypes = [I, P, I, P, I, I, P]
+    lb.oracle_contract.argtypes = [P, P, P, P, I, I, ctypes.POINTER(D), ctypes.POINTER(D)]
+    lb.oracle_spherical_jn.argtypes = [I, D]
+    lb.oracle_spherical_jn.restype = D
+    lb.oracle_sph_harm.argtypes = [I, I, D, D, D, ctypes.POINTER(D), ctypes.POINTER(D)]
+    return lb
+
+
+RADIAL_CODES = {"shell": 0, "gaussian_shell": 1, "thick_shell": 2, "sphere": 3, "gaussian": 4}
+
+
+def radial_multipole_window(L, P, radius_grid, l, m, code=0, arg1=0.0):
+    """radial_multipole_windows.py:147-183 -> complex128 [L, L, L]."""
+    lb = _setup_multipole_lib()
+    out = np.empty((L, L, L, 2), dtype=np.float64)
+    args = np.array([radius_grid, arg1, 0.0, 0.0])
+    P = np.ascontiguousarray(P, dtype=np.float64)
+    lb.oracle_radial_multipole_window(L, _p(P), code, _p(args), l, m, _p(out))
+    return out[..., 0] + 1j * out[..., 1]
+
+
+def contract(data, a1, a2, gamma):
+    """compute_3d_summand_cpu (corr3pcf_multipoles.py:134-170)."""
+    lb = _setup_multipole_lib()
+    data = np.ascontiguousarray(data, dtype=np.float64)
+    a1 = np.ascontiguousarray(a1, dtype=np.complex128)
+    a2 = np.ascontiguousarray(a2, dtype=np.complex128)
+    gamma = np.ascontiguousarray(gamma, dtype=np.float64)
+    re, im = ctypes.c_double(0.0), ctypes.c_double(0.0)
+    lb.oracle_contract(_p(data), _p(a1), _p(a2), _p(gamma), data.shape[0], gamma.shape[0],
+                       ctypes.byref(re), ctypes.byref(im))
+    return complex(re.value, im.value)
+
+
+def combine_multipole_m_terms(m_values, l):
+    """corr3pcf_multipoles.py:173-180."""
+    coeff = complex(m_values[0])
+    for m in range(1, l + 1):
+        coeff += ((-1) ** m) * complex(m_values[m])
+        coeff += ((-1) ** (-m)) * np.conj(complex(m_values[m]))
+    coeff *= (-1) ** l
+    return coeff.real
+
+
+def multipole_m_summands(eps1, eps2, eps3, R12, R13, l, phi, res=1024, box=1000.0):
+    """S_m for m = 0..l at one (r12, r13) (corr3pcf_multipoles.py:505-555);
+    R12/R13 physical radii of thin shells."""
+    from scipy.fft import fftn, ifftn
+
+    L = eps1.shape[0]
+    P = fourier_power(phi, 1, L, res)
+    gamma = cal_gamma(phi, phi.shape[0] // res, res)
+    s2 = fftn(np.asarray(eps2, dtype=np.float64))
+    s3 = fftn(np.asarray(eps3, dtype=np.float64))
+    out = []
+    for m in range(0, l + 1):
+        w2 = radial_multipole_window(L, P, R12 * L / box, l, m)
+        w3 = radial_multipole_window(L, P, R13 * L / box, l, -m)
+        a2 = ifftn(s2 * w2)
+        a3 = ifftn(s3 * w3)
+        out.append((4.0 * np.pi) * contract(eps1, a2, a3, gamma) / eps1.size)
+    return out
+
+
+def calc_ddd_multipole(eps1, eps2, eps3, R12, R13, l_min, l_max, phi, res=1024, box=1000.0):
+    """calc_DDD_multipole (corr3pcf_multipoles.py:460-579) for thin shells."""
+    ddd = []
+    for l in range(l_min, l_max + 1):
+        ddd.append(combine_multipole_m_terms(multipole_m_summands(eps1, eps2, eps3, R12, R13, l, phi, res, box), l))
+    return np.arange(l_min, l_max + 1, dtype=np.int32), np.asarray(ddd)
+
+
+def legendre_triple_coeff(l, lp, k):
+    """special_functions.py:337-363."""
+    from scipy.special import gammaln
+
+    s = l + lp + k
+    if (k > l + lp) or (k < abs(l - lp)) or (s % 2 != 0):
+        return 0.0
+    g = s // 2
+    log_val = (gammaln(s - 2 * l + 1) + gammaln(s - 2 * lp + 1) + gammaln(s - 2 * k + 1) - gammaln(s + 2)
+               + 2 * (gammaln(g + 1) - gammaln(g - l + 1) - gammaln(g - lp + 1) - gammaln(g - k + 1)))
+    return float((2 * k + 1) * np.exp(log_val))
+
+
+def solve_multipoles_from_ratio(A, B, lmax):
+    """special_functions.py:366-409 (build_mixing_matrix + solve)."""
+    A = np.asarray(A, dtype=np.float64)[:lmax + 1]
+    B = np.asarray(B, dtype=np.float64)[:lmax + 1]
+    f = B / B[0]
+    M = np.zeros((lmax + 1, lmax + 1))
+    for l in range(lmax + 1):
+        for lp in range(1, lmax + 1):
+            if l == lp:
+                M[0, l] += f[lp] / (2 * l + 1)
+    for k in range(1, lmax + 1):
+        for l in range(lmax + 1):
+            for lp in range(1, lmax + 1):
+                M[k, l] += legendre_triple_coeff(l, lp, k) * f[lp]
+    M += np.eye(lmax + 1)
+    M *= B[0]
+    return np.linalg.solve(M, A), M, np.linalg.cond(M)

@@ -29,7 +29,7 @@ namespace {
 
 constexpr int kMaxSupport = 4;
 constexpr int kTileX = 8, kTileY = 16, kTileZ = 32;
-constexpr int kAccThreads = 512;
+constexpr int kAccThreads = 256;
 constexpr int kScanChunk = 4096;  // elements per scan block (1024 threads x 4)
 constexpr unsigned kRejected = 0xFFFFFFFFu;
 
@@ -299,6 +299,31 @@ __global__ void dep_scatter_kernel(const DepRec* __restrict__ rec, int64_t n,
   }
 }
 
+// Round-to-nearest int64 of a float32 value |v| < 2^62 with integer ops only
+// (float -> int64 conversion instructions are slow on this part).
+__device__ __forceinline__ long long f32_to_ll_rn(float v) {
+  const int b = __float_as_int(v);
+  const int e = (b >> 23) & 0xFF;
+  if (e == 0) return 0;  // zero / subnormal: below one quantum
+  const long long m = (long long)((b & 0x7FFFFF) | 0x800000);
+  long long q;
+  if (e >= 150) {
+    q = m << (e - 150);
+  } else {
+    const int sh = 150 - e;
+    q = sh >= 25 ? 0 : ((m + (1LL << (sh - 1))) >> sh);
+  }
+  return b < 0 ? -q : q;
+}
+
+// int64 -> float32 via two 32-bit conversions (at most one rounding step
+// beyond round-to-nearest; the result is a float32 field anyway).
+__device__ __forceinline__ float ll_to_f32(long long a) {
+  const float hi = (float)(int)(a >> 32);
+  const float lo = (float)(unsigned)(a & 0xFFFFFFFFLL);
+  return fmaf(hi, 4294967296.0f, lo);
+}
+
 template <int S, bool kF64Out>
 __global__ void __launch_bounds__(kAccThreads)
 dep_accum_kernel(const DepRec* __restrict__ sorted, const unsigned* __restrict__ offsets,
@@ -309,7 +334,7 @@ dep_accum_kernel(const DepRec* __restrict__ sorted, const unsigned* __restrict__
   const int ncell = g.tx * g.ty * g.tz;
   long long* acc = reinterpret_cast<long long*>(smem);
   unsigned* cnt = reinterpret_cast<unsigned*>(acc + ncell);
-  __shared__ unsigned r_start[27], r_pref[28], r_home[27];
+  __shared__ unsigned r_start[64], r_pref[65], r_home[64];
   __shared__ int n_ranges;
 
   const int tile = blockIdx.x;
@@ -317,56 +342,91 @@ dep_accum_kernel(const DepRec* __restrict__ sorted, const unsigned* __restrict__
   const int x0 = hx * g.tx, y0 = hy * g.ty, z0 = hz * g.tz;
   const int tzl = g.tz_log2, tyzl = g.ty_log2 + g.tz_log2;
 
-  if (threadIdx.x == 0) {
-    int nr = 0;
-    unsigned run = 0;
-    for (int d = 0; d < 8; ++d) {
-      int dx = d & 1, dy = (d >> 1) & 1, dz = (d >> 2) & 1;
-      if ((dx && g.ntx == 1) || (dy && g.nty == 1) || (dz && g.ntz == 1)) continue;
-      int nx_ = (hx + dx) % g.ntx, ny_ = (hy + dy) % g.nty, nz_ = (hz + dz) % g.ntz;
-      unsigned nt = ((unsigned)nx_ * g.nty + ny_) * g.ntz + nz_;
-      unsigned D = (unsigned)d;
-      for (unsigned r = 0; r < 8; ++r) {
-        if ((r & D) != D) continue;
-        unsigned b = nt * 8u + r;
-        unsigned s0 = offsets[b], s1 = offsets[b + 1];
-        if (s1 > s0) {
-          r_start[nr] = s0;
-          r_pref[nr] = run;
-          r_home[nr] = (d == 0);
-          run += s1 - s0;
-          ++nr;
-        }
+  // Range table: warp 0 handles the 64 (neighbour d, region r) combinations,
+  // two per lane, with independent loads, then compacts them with a ballot.
+  if (threadIdx.x < 32) {
+    const unsigned lane = threadIdx.x;
+    unsigned len[2], st0[2], home[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int combo = 2 * (int)lane + h;
+      const int d = combo >> 3;
+      const unsigned r = (unsigned)(combo & 7), D = (unsigned)d;
+      const int dx = d & 1, dy = (d >> 1) & 1, dz = (d >> 2) & 1;
+      len[h] = 0;
+      st0[h] = 0;
+      home[h] = (d == 0);
+      const bool ok = !((dx && g.ntx == 1) || (dy && g.nty == 1) || (dz && g.ntz == 1)) && ((r & D) == D);
+      if (ok) {
+        const int nx_ = (hx + dx) % g.ntx, ny_ = (hy + dy) % g.nty, nz_ = (hz + dz) % g.ntz;
+        const unsigned b = (((unsigned)nx_ * g.nty + ny_) * g.ntz + nz_) * 8u + r;
+        const unsigned s0 = offsets[b], s1 = offsets[b + 1];
+        st0[h] = s0;
+        len[h] = s1 - s0;
       }
     }
-    r_pref[nr] = run;
-    n_ranges = nr;
+    // inclusive scan over the 64 lengths (lane order, two per lane)
+    const unsigned pair_sum = len[0] + len[1];
+    unsigned inc = pair_sum;
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned t = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= (unsigned)o) inc += t;
+    }
+    const unsigned excl = inc - pair_sum;
+    const unsigned v0 = __ballot_sync(0xffffffffu, len[0] > 0), v1 = __ballot_sync(0xffffffffu, len[1] > 0);
+    const unsigned below = (1u << lane) - 1u;
+    unsigned slot = __popc(v0 & below) + __popc(v1 & below);
+    unsigned pref = excl;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      if (len[h] > 0) {
+        r_start[slot] = st0[h];
+        r_pref[slot] = pref;
+        r_home[slot] = home[h];
+        ++slot;
+      }
+      pref += len[h];
+    }
+    if (lane == 31) {
+      const int nr = __popc(v0) + __popc(v1);
+      r_pref[nr] = inc;
+      n_ranges = nr;
+    }
   }
   __syncthreads();
   const int nr = n_ranges;
   const unsigned total = r_pref[nr];
 
   if (total == 0) {  // empty tile: write zeros, skip shared memory
-    for (int i = threadIdx.x; i < ncell; i += blockDim.x) {
+    for (int i = 4 * threadIdx.x; i < ncell; i += 4 * blockDim.x) {
       const int lz_ = i & (g.tz - 1), ly_ = (i >> tzl) & (g.ty - 1), lx_ = i >> tyzl;
       const size_t gi = ((size_t)(x0 + lx_) * g.L + (y0 + ly_)) * g.L + (z0 + lz_);
-      if (kF64Out) out64[gi] = 0.0; else out32[gi] = 0.f;
-      if (counts_out) counts_out[gi] = 0u;
+      if (kF64Out) {
+        reinterpret_cast<double2*>(out64 + gi)[0] = make_double2(0.0, 0.0);
+        reinterpret_cast<double2*>(out64 + gi)[1] = make_double2(0.0, 0.0);
+      } else {
+        *reinterpret_cast<float4*>(out32 + gi) = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+      if (counts_out) *reinterpret_cast<uint4*>(counts_out + gi) = make_uint4(0u, 0u, 0u, 0u);
     }
     return;
   }
 
-  for (int i = threadIdx.x; i < ncell; i += blockDim.x) {
-    acc[i] = 0;
-    if (counts_out) cnt[i] = 0;
+  for (int i = 2 * threadIdx.x; i < ncell; i += 2 * blockDim.x) {
+    *reinterpret_cast<longlong2*>(acc + i) = make_longlong2(0, 0);
+    if (counts_out) *reinterpret_cast<uint2*>(cnt + i) = make_uint2(0u, 0u);
   }
   __syncthreads();
 
   const float scale_f = st->scale_f;
   const int Lm = g.L - 1;
   for (unsigned k = threadIdx.x; k < total; k += blockDim.x) {
-    int r = 0;
-    while (r + 1 < nr && r_pref[r + 1] <= k) ++r;
+    int lo = 0, hi = nr - 1;  // largest r with r_pref[r] <= k
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (r_pref[mid] <= k) lo = mid; else hi = mid - 1;
+    }
+    const int r = lo;
     const DepRec rec = sorted[r_start[r] + (k - r_pref[r])];
     const int cx = rec.cell >> 20, cy = (rec.cell >> 10) & 1023, cz = rec.cell & 1023;
     const int fx = rec.frac >> 20, fy = (rec.frac >> 10) & 1023, fz = rec.frac & 1023;
@@ -392,7 +452,7 @@ dep_accum_kernel(const DepRec* __restrict__ sorted, const unsigned* __restrict__
 #pragma unroll
         for (int c = 0; c < S; ++c) {
           if (lz[c] >= g.tz) continue;
-          const long long q = __float2ll_rn(pxy * pz[c] * scale_f);
+          const long long q = f32_to_ll_rn(pxy * pz[c] * scale_f);
           atomicAdd(reinterpret_cast<unsigned long long*>(&acc[row + lz[c]]),
                     static_cast<unsigned long long>(q));
         }
@@ -406,15 +466,20 @@ dep_accum_kernel(const DepRec* __restrict__ sorted, const unsigned* __restrict__
 
   const float inv_f = st->inv_f;
   const double inv_d = st->inv_d;
-  for (int i = threadIdx.x; i < ncell; i += blockDim.x) {
+  for (int i = 4 * threadIdx.x; i < ncell; i += 4 * blockDim.x) {
     const int lz_ = i & (g.tz - 1), ly_ = (i >> tzl) & (g.ty - 1), lx_ = i >> tyzl;
     const size_t gi = ((size_t)(x0 + lx_) * g.L + (y0 + ly_)) * g.L + (z0 + lz_);
+    const longlong2 a01 = *reinterpret_cast<const longlong2*>(acc + i);
+    const longlong2 a23 = *reinterpret_cast<const longlong2*>(acc + i + 2);
     if (kF64Out) {
-      out64[gi] = (double)acc[i] * inv_d;
+      reinterpret_cast<double2*>(out64 + gi)[0] = make_double2((double)a01.x * inv_d, (double)a01.y * inv_d);
+      reinterpret_cast<double2*>(out64 + gi)[1] = make_double2((double)a23.x * inv_d, (double)a23.y * inv_d);
     } else {
-      out32[gi] = __ll2float_rn(acc[i]) * inv_f;
+      *reinterpret_cast<float4*>(out32 + gi) =
+          make_float4(ll_to_f32(a01.x) * inv_f, ll_to_f32(a01.y) * inv_f,
+                      ll_to_f32(a23.x) * inv_f, ll_to_f32(a23.y) * inv_f);
     }
-    if (counts_out) counts_out[gi] = cnt[i];
+    if (counts_out) *reinterpret_cast<uint4*>(counts_out + gi) = *reinterpret_cast<const uint4*>(cnt + i);
   }
 }
 

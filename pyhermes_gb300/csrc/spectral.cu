@@ -49,6 +49,8 @@ int get_plan(int J, PlanKind kind, int batch, cufftHandle* out) {
   return HERMES_OK;
 }
 
+int get_plan_c2c_batch(int J, int batch, cufftHandle* out) { return get_plan(J, kC2C, batch, out); }
+
 #define HERMES_CUFFT_TRY(expr)                                                   \
   do {                                                                           \
     cufftResult _r = (expr);                                                     \

@@ -1,0 +1,495 @@
+"""3PCF spherical-harmonic multipoles on the GPU.
+
+``Corr_3PCF_Multipole`` mirrors ``pyhermes/theory/corr3pcf_multipole.py``
+(serial semantics): the same parameter dict (sampling in grid / paired mode,
+binning_window12/13 with a mapping from sampled names to ``len_args``),
+products ddd_l / rrr_l / delta_ddd_l / zeta_l, the all-uniform analytic
+rrr_l shortcut (:1389-1395), the physical rescale by scale_factor**9
+(:546-555, :944-952) and the zeta_l mixing-matrix solve (:1554-1589,
+utils/special_functions.py:337-409).
+
+Engine (``MultipoleEngine``): instead of rebuilding both side fields for
+every (r12, r13) sample as the reference does (calc_DDD_multipole per
+sample), each (l, m) produces the a_lm fields of every distinct radius once
+(``hermes_multipole_fields``) and contracts all radius pairs at once
+(``hermes_multipole_contract``).  When the second and third vertices share
+the field and the radii, a_{l,-m} = (-1)^{l+m} conj(a_lm) removes the
+second batch.  ``summation_backend='plain'`` runs the per-sample reference
+form on the GPU (the baseline the batched engine is measured against).
+"""
+
+import copy
+import ctypes
+import itertools
+import logging
+import time
+
+import numpy as np
+import torch
+
+from . import _lib
+from .kernels import _ptr, _stream_ptr
+from .params import task_params
+from .phi import cal_gamma, sample_scaling_function
+from .sfc_field import SFCField, normalize_task_weight_normalization, write_numpy_pickle
+from .window import WindowFunc, phi_power_device, rfft_field
+
+logger = logging.getLogger("pyhermes_gb300.Corr_3PCF_Multipole")
+
+MAX_BINS = 16
+_WS = {}
+
+
+def _workspace(nbytes, device):
+    key = ("multipole", str(device))
+    buf = _WS.get(key)
+    if buf is None or buf.numel() < nbytes:
+        if buf is not None:
+            del _WS[key]
+            buf = None
+            torch.cuda.empty_cache()
+        buf = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)
+        _WS[key] = buf
+    return buf
+
+
+def _ws_bytes(J, nb):
+    n = ctypes.c_size_t(0)
+    _lib.check(_lib.load().hermes_multipole_workspace_size(J, nb, ctypes.byref(n)), "multipole_workspace_size")
+    return n.value
+
+
+def multipole_fields(half_spec, J, l, m, radii_grid, phi_power, out=None):
+    """a_lm^b = ifftn(fftn(eps) K_lm^b) for thin-shell radii (grid units)."""
+    nb = len(radii_grid)
+    N = 1 << (3 * J)
+    dev = half_spec.device
+    if out is None:
+        out = torch.empty((nb, N), dtype=torch.complex64, device=dev)
+    ws = _workspace(_ws_bytes(J, nb), dev)
+    radii = (ctypes.c_double * nb)(*[float(r) for r in radii_grid])
+    _lib.check(_lib.load().hermes_multipole_fields(_ptr(half_spec), J, int(l), int(m), radii, nb, _ptr(phi_power),
+                                                   _ptr(out), _ptr(ws), ws.numel(), _stream_ptr(dev)),
+               "hermes_multipole_fields")
+    return out
+
+
+def multipole_contract(eps1, fields2, nb2, gamma, J, fields3=None, nb3=None, conj_sign=1):
+    """S[b2, b3] complex128 (see include/hermes_gb300.h)."""
+    nb3 = nb2 if fields3 is None else nb3
+    dev = eps1.device
+    ws = _workspace(_ws_bytes(J, max(nb2, nb3)), dev)
+    out = np.zeros((nb2, nb3, 2), dtype=np.float64)
+    g = (ctypes.c_double * 9)(*np.asarray(gamma, dtype=np.float64).ravel())
+    _lib.check(_lib.load().hermes_multipole_contract(_ptr(eps1), _ptr(fields2), nb2, _ptr(fields3), nb3,
+                                                     int(conj_sign), g, J, out.ctypes.data_as(ctypes.c_void_p),
+                                                     _ptr(ws), ws.numel(), _stream_ptr(dev)),
+               "hermes_multipole_contract")
+    return out[..., 0] + 1j * out[..., 1]
+
+
+def multipole_contract_plain(eps1, a2, a3, gamma, J):
+    dev = eps1.device
+    ws = _workspace(_ws_bytes(J, 1), dev)
+    out = np.zeros(2, dtype=np.float64)
+    g = (ctypes.c_double * 9)(*np.asarray(gamma, dtype=np.float64).ravel())
+    _lib.check(_lib.load().hermes_multipole_contract_plain(_ptr(eps1), _ptr(a2), _ptr(a3), g, J,
+                                                           out.ctypes.data_as(ctypes.c_void_p), _ptr(ws),
+                                                           ws.numel(), _stream_ptr(dev)),
+               "hermes_multipole_contract_plain")
+    return complex(out[0], out[1])
+
+
+def combine_multipole_m_terms(m_values, l):
+    """corr3pcf_multipoles.py:173-180."""
+    coeff = complex(m_values[0])
+    for m in range(1, l + 1):
+        coeff += ((-1) ** m) * complex(m_values[m])
+        coeff += ((-1) ** (-m)) * np.conj(complex(m_values[m]))
+    coeff *= (-1) ** l
+    return coeff.real
+
+
+class MultipoleEngine:
+    """Batched multipole contraction of three fields over radius pairs."""
+
+    def __init__(self, eps1, eps2, eps3, phi_array, J, box_size, phi_resolution=1024, share23=None):
+        self.J = int(J)
+        self.L = 1 << self.J
+        self.box = float(box_size)
+        self.dev = eps1.device
+        self.eps1 = eps1.to(torch.float32).contiguous()
+        self.spec2 = rfft_field(eps2.to(torch.float32).contiguous())
+        same = share23 if share23 is not None else (eps3 is eps2 or (eps3.data_ptr() == eps2.data_ptr()))
+        self.same23 = bool(same)
+        self.spec3 = self.spec2 if self.same23 else rfft_field(eps3.to(torch.float32).contiguous())
+        self.phi = np.asarray(phi_array, dtype=np.float64)
+        support = self.phi.shape[0] // phi_resolution
+        if support != 3:
+            raise NotImplementedError("The GPU contraction is specialised for a support-3 scaling function (db2).")
+        self.gamma = cal_gamma(self.phi, support, phi_resolution)
+        self.P = phi_power_device(self.phi, self.L, 1, phi_resolution, self.dev)
+        self.timing = {"fields_s": 0.0, "contract_s": 0.0}
+
+    def summands(self, l, m, r12_phys, r13_phys):
+        """S_m[i, j] for radius lists (physical units), complex128 [n12, n13]."""
+        g12 = [r * self.L / self.box for r in r12_phys]
+        g13 = [r * self.L / self.box for r in r13_phys]
+        out = np.zeros((len(g12), len(g13)), dtype=np.complex128)
+        shared = self.same23 and list(g12) == list(g13)
+        for i0 in range(0, len(g12), MAX_BINS):
+            c12 = g12[i0:i0 + MAX_BINS]
+            t0 = time.perf_counter()
+            f2 = multipole_fields(self.spec2, self.J, l, m, c12, self.P)
+            for j0 in range(0, len(g13), MAX_BINS):
+                c13 = g13[j0:j0 + MAX_BINS]
+                if shared and i0 == j0:
+                    t1 = time.perf_counter()
+                    self.timing["fields_s"] += t1 - t0
+                    S = multipole_contract(self.eps1, f2, len(c12), self.gamma, self.J,
+                                           conj_sign=(-1) ** ((l + m) % 2))
+                else:
+                    f3 = multipole_fields(self.spec3, self.J, l, -m, c13, self.P)
+                    t1 = time.perf_counter()
+                    self.timing["fields_s"] += t1 - t0
+                    S = multipole_contract(self.eps1, f2, len(c12), self.gamma, self.J, fields3=f3, nb3=len(c13))
+                    del f3
+                self.timing["contract_s"] += time.perf_counter() - t1
+                t0 = time.perf_counter()
+                out[i0:i0 + len(c12), j0:j0 + len(c13)] = S
+            del f2
+        return out
+
+    def ddd(self, pairs, l_min, l_max):
+        """DDD_l for samples given as (r12, r13) physical radii -> [n_samples, n_l]."""
+        r12 = sorted({p[0] for p in pairs})
+        r13 = sorted({p[1] for p in pairs})
+        i12 = {r: i for i, r in enumerate(r12)}
+        i13 = {r: i for i, r in enumerate(r13)}
+        if self.same23 and r12 != r13:
+            both = sorted(set(r12) | set(r13))
+            r12 = r13 = both
+            i12 = i13 = {r: i for i, r in enumerate(both)}
+        res = np.zeros((len(pairs), l_max - l_min + 1))
+        for li, l in enumerate(range(l_min, l_max + 1)):
+            Sm = [self.summands(l, m, r12, r13) for m in range(0, l + 1)]
+            for s, (a, b) in enumerate(pairs):
+                res[s, li] = combine_multipole_m_terms([Sm[m][i12[a], i13[b]] for m in range(l + 1)], l)
+        return res
+
+    def ddd_plain(self, pairs, l_min, l_max):
+        """The per-sample reference form: both side fields rebuilt per sample
+        and (l, m), reference-order contraction of one pair."""
+        res = np.zeros((len(pairs), l_max - l_min + 1))
+        for s, (a, b) in enumerate(pairs):
+            ga, gb = a * self.L / self.box, b * self.L / self.box
+            for li, l in enumerate(range(l_min, l_max + 1)):
+                vals = []
+                for m in range(0, l + 1):
+                    f2 = multipole_fields(self.spec2, self.J, l, m, [ga], self.P)
+                    f3 = multipole_fields(self.spec3, self.J, l, -m, [gb], self.P)
+                    vals.append(multipole_contract_plain(self.eps1, f2, f3, self.gamma, self.J))
+                    del f2, f3
+                res[s, li] = combine_multipole_m_terms(vals, l)
+        return res
+
+
+def legendre_triple_coeff(l, lp, k):
+    """utils/special_functions.py:337-363."""
+    from math import lgamma
+
+    s = l + lp + k
+    if (k > l + lp) or (k < abs(l - lp)) or (s % 2 != 0):
+        return 0.0
+    g = s // 2
+    log_val = (lgamma(s - 2 * l + 1) + lgamma(s - 2 * lp + 1) + lgamma(s - 2 * k + 1) - lgamma(s + 2)
+               + 2 * (lgamma(g + 1) - lgamma(g - l + 1) - lgamma(g - lp + 1) - lgamma(g - k + 1)))
+    return float((2 * k + 1) * np.exp(log_val))
+
+
+def mixing_solve(A, B, lmax, device="cuda"):
+    """zeta_l for A(mu) = B(mu) C(mu) (special_functions.py:366-409), float64
+    on the GPU for all samples at once.  A, B: [n_samples, >= lmax+1]."""
+    A = np.atleast_2d(np.asarray(A, dtype=np.float64))[:, :lmax + 1]
+    B = np.atleast_2d(np.asarray(B, dtype=np.float64))[:, :lmax + 1]
+    n = lmax + 1
+    G = np.zeros((n, n, n))
+    for k in range(n):
+        for l in range(n):
+            for lp in range(n):
+                G[k, l, lp] = legendre_triple_coeff(l, lp, k)
+    if np.any(B[:, 0] == 0):
+        raise ValueError("B[0] is zero.")
+    Bt = torch.as_tensor(B, device=device)
+    At = torch.as_tensor(A, device=device)
+    Gt = torch.as_tensor(G, device=device)
+    f = Bt / Bt[:, :1]
+    M = torch.zeros((A.shape[0], n, n), dtype=torch.float64, device=device)
+    idx = torch.arange(1, n, device=device)
+    M[:, 0, idx] += f[:, idx] / (2 * idx + 1).double()
+    fm = f.clone()
+    fm[:, 0] = 0.0
+    M[:, 1:, :] += torch.einsum("klp,sp->skl", Gt[1:], fm)
+    M += torch.eye(n, dtype=torch.float64, device=device)
+    M *= Bt[:, :1, None]
+    C = torch.linalg.solve(M, At)
+    cond = torch.linalg.cond(M)
+    return C.cpu().numpy(), M.cpu().numpy(), cond.cpu().numpy()
+
+
+class Corr3PCFMultipoleData:
+    """Result container (pyhermes/io/corr3pcf_multipole.py:9-30)."""
+
+    def __init__(self):
+        for k in ("sfc_info1", "sfc_info2", "sfc_info3", "sample_params", "binning_window12", "binning_window13",
+                  "r12", "r13", "l", "ddd_l", "rrr_l", "delta_ddd_l", "zeta_l", "zeta_condition"):
+            setattr(self, k, None)
+        self.corr3pcf_multipole_info = {}
+        self.timing = {}
+
+    def save_corr3pcf_multipole(self, f_out, overwrite=False):
+        import os
+
+        if os.path.exists(f_out) and not overwrite:
+            raise FileExistsError(f_out)
+        with open(f_out, "wb") as f:
+            write_numpy_pickle(f, {k: v for k, v in self.__dict__.items()})
+
+
+PRODUCTS = ("ddd_l", "rrr_l", "delta_ddd_l", "zeta_l")
+
+
+class Corr_3PCF_Multipole:
+    task_name = "Corr_3PCF_Multipole"
+
+    def __init__(self, param_task=None, device="cuda"):
+        self.task_params = task_params(self.task_name, param_task)
+        self.device = torch.device(device)
+        tp = self.task_params
+        self.sfc_field = tp.get("sfc_field", "")
+        for i in (1, 2, 3):
+            setattr(self, f"sfc_field{i}", tp.get(f"sfc_field{i}", "") or self.sfc_field)
+        self.random = tp.get("random")
+        for i in (1, 2, 3):
+            r = tp.get(f"random{i}")
+            setattr(self, f"random{i}", self.random if r in (None, "") else r)
+        self.weight_normalization = normalize_task_weight_normalization(tp.get("weight_normalization", "catalog"))
+        window = tp.get("window")
+        self.window = window if (isinstance(window, dict) and window.get("type")) else None
+        for i in (1, 2, 3):
+            wi = tp.get(f"window{i}")
+            wi = wi if (isinstance(wi, dict) and wi.get("type")) else None
+            setattr(self, f"window{i}", wi or (dict(self.window) if self.window else None))
+        self.sampling = self._normalize_sampling(tp.get("sampling"))
+        self.samples = self._expand_sampling(self.sampling)
+        self.binning_window12 = [self._sample_window(tp.get("binning_window12"), s) for s in self.samples]
+        self.binning_window13 = [self._sample_window(tp.get("binning_window13"), s) for s in self.samples]
+        self.l_min = int(tp["l_min"])
+        self.l_max = int(tp["l_max"])
+        if self.l_min < 0 or self.l_max < 0 or self.l_min > self.l_max:
+            raise ValueError("Corr_3PCF_Multipole requires 0 <= l_min <= l_max.")
+        backend = str(tp.get("summation_backend", "gb300")).strip().lower()
+        if backend not in {"gb300", "gpu", "plain", "cpu"}:
+            raise ValueError("summation_backend must be 'gb300', 'gpu', 'plain' or 'cpu'.")
+        self.summation_backend = "plain" if backend == "plain" else "gb300"
+        prods = tp.get("products", "zeta_l")
+        prods = [prods] if isinstance(prods, str) else list(prods)
+        self.products = []
+        for p in prods:
+            p = str(p).strip().lower()
+            if p not in PRODUCTS:
+                raise ValueError(f"Unsupported product '{p}'.")
+            if p not in self.products:
+                self.products.append(p)
+        self.fout_path = tp.get("fout_path", "")
+        self._fields_prepared = False
+
+    # ---- sampling (corr3pcf_multipole.py:229-322) ----------------------------
+    def _normalize_sampling(self, sampling):
+        if not isinstance(sampling, dict):
+            raise TypeError("Corr_3PCF_Multipole requires a 'sampling' dictionary.")
+        s = copy.deepcopy(sampling)
+        mode = str(s.pop("mode", "grid")).strip().lower()
+        if mode not in {"grid", "paired"}:
+            raise ValueError("sampling.mode must be 'grid' or 'paired'.")
+        values = {}
+        for name, spec in s.items():
+            if isinstance(spec, dict):
+                if "values" in spec:
+                    v = np.asarray(spec["values"], dtype=np.float64)
+                elif {"min", "max", "n"}.issubset(spec):
+                    v = np.linspace(float(spec["min"]), float(spec["max"]), int(spec["n"]))
+                elif {"start", "stop", "step"}.issubset(spec):
+                    st = float(spec["step"])
+                    v = np.arange(float(spec["start"]), float(spec["stop"]) + 0.5 * st, st)
+                else:
+                    raise ValueError(f"sampling.{name} must use 'values', 'min/max/n', 'start/stop/step'.")
+            elif isinstance(spec, (list, tuple, np.ndarray)):
+                v = np.asarray(spec, dtype=np.float64)
+            else:
+                v = np.asarray([spec], dtype=np.float64)
+            values[name] = v
+        if not values:
+            raise ValueError("sampling must contain at least one sampled parameter.")
+        return {"mode": mode, "values": values}
+
+    def _expand_sampling(self, sampling):
+        values = sampling["values"]
+        names = list(values)
+        if sampling["mode"] == "grid":
+            return [{n: float(v) for n, v in zip(names, combo)}
+                    for combo in itertools.product(*(values[n] for n in names))]
+        n = max(a.size for a in values.values())
+        if any(a.size not in (1, n) for a in values.values()):
+            raise ValueError("sampling.mode='paired' requires each parameter to have length 1 or the shared length.")
+        return [{k: float(a[0] if a.size == 1 else a[i]) for k, a in values.items()} for i in range(n)]
+
+    def _sample_window(self, template, sample):
+        params = copy.deepcopy(template)
+        mapping = params.pop("mapping", {}) or {}
+        params["len_args"] = copy.deepcopy(params.get("len_args", {}) or {})
+        params["other_args"] = copy.deepcopy(params.get("other_args", {}) or {})
+        for target, source in mapping.items():
+            value = float(sample[source]) if isinstance(source, str) else float(source)
+            if "." in target:
+                sec, key = target.split(".", 1)
+                params.setdefault(sec, {})[key] = value
+            else:
+                params["len_args"][target] = value
+        if not params["len_args"]:
+            raise ValueError("binning window produced an empty len_args dictionary.")
+        return params
+
+    # ---- inputs ----------------------------------------------------------------
+    def _resolve(self, value, what):
+        if isinstance(value, SFCField):
+            return value
+        if isinstance(value, str) and value:
+            return SFCField(data_path=value, device=self.device)
+        raise ValueError(f"Missing usable input for {what}.")
+
+    def _normalized(self, field):
+        self._density_physical_scale = float(field.scale_factor) ** 3
+        if self.weight_normalization == "unit":
+            return field.with_normalization("unit")
+        if getattr(field, "field_kind", None) != "catalog_field":
+            return field.copy()
+        return field.switch_weight_normalization(self.weight_normalization)
+
+    def _expanded(self):
+        out = list(self.products)
+        if "zeta_l" in out:
+            for d in ("delta_ddd_l", "rrr_l"):
+                if d not in out:
+                    out.append(d)
+        return out
+
+    def prepare_input_fields(self):
+        exp = self._expanded()
+        needs_data = any(p in exp for p in ("ddd_l", "delta_ddd_l", "zeta_l"))
+        needs_random = any(p in exp for p in ("rrr_l", "delta_ddd_l", "zeta_l"))
+        self.data, self.rand = {}, {}
+        ref = self._normalized(self._resolve(self.sfc_field1, "field vertex 1"))
+        self.reference = ref
+        self.rho = ref.field_mean_density(value_unit="grid")
+        for i in (1, 2, 3):
+            if needs_data:
+                base = self._normalized(self._resolve(getattr(self, f"sfc_field{i}"), f"field vertex {i}"))
+                w = getattr(self, f"window{i}")
+                self.data[i] = base @ WindowFunc(w, base.sfc_info, device=self.device) if w else base.copy()
+            if needs_random:
+                r = getattr(self, f"random{i}")
+                if r is None or r == "":
+                    raise ValueError(f"Missing input for random vertex {i}.")
+                if r == "uniform":
+                    base = self.data.get(i) or ref
+                    rho_i = base.field_mean_density(value_unit="grid") if i in self.data else self.rho
+                    w = getattr(self, f"window{i}")
+                    if w:
+                        win = WindowFunc(w, base.sfc_info, device=self.device)
+                        k0 = float(np.asarray(win.as_array())[0, 0, 0].real)
+                        if not np.isclose(k0, 1.0, rtol=1e-10, atol=1e-12):
+                            raise NotImplementedError("uniform randoms with a window whose W(0) != 1")
+                    self.rand[i] = float(rho_i)
+                else:
+                    base = self._normalized(self._resolve(r, f"random vertex {i}"))
+                    w = getattr(self, f"window{i}")
+                    self.rand[i] = base @ WindowFunc(w, base.sfc_info, device=self.device) if w else base.copy()
+        self._fields_prepared = True
+
+    def _eps(self, product, i):
+        if product == "ddd_l":
+            return self.data[i].epsilon_device.to(torch.float32)
+        if product == "delta_ddd_l":
+            r = self.rand[i]
+            d = self.data[i].epsilon_device.double()
+            if isinstance(r, float):
+                return (d - r).to(torch.float32)
+            return (d - r.epsilon_device.double()).to(torch.float32)
+        r = self.rand[i]
+        if isinstance(r, float):
+            return torch.full((self.reference.L,) * 3, r, dtype=torch.float32, device=self.device)
+        return r.epsilon_device.to(torch.float32)
+
+    def _pairs(self):
+        pairs = []
+        for w12, w13 in zip(self.binning_window12, self.binning_window13):
+            for w in (w12, w13):
+                if str(w.get("type", "shell")).strip().lower() != "shell":
+                    raise NotImplementedError("Only thin-shell radial multipole windows run on the GPU.")
+            pairs.append((float(w12["len_args"]["R"]), float(w13["len_args"]["R"])))
+        return pairs
+
+    def run(self, save_result=True, overwrite=False):
+        t0 = time.perf_counter()
+        if not self._fields_prepared:
+            self.prepare_input_fields()
+        exp = self._expanded()
+        data = Corr3PCFMultipoleData()
+        data.l = np.arange(self.l_min, self.l_max + 1, dtype=np.int32)
+        data.binning_window12 = self.binning_window12
+        data.binning_window13 = self.binning_window13
+        names = list(self.samples[0])
+        data.sample_params = {n: np.asarray([s[n] for s in self.samples]) for n in names}
+        data.r12 = data.sample_params.get("r12")
+        data.r13 = data.sample_params.get("r13")
+        pairs = self._pairs()
+        scale = float(getattr(self, "_density_physical_scale", 1.0)) ** 3
+        ref = self.reference
+        phi = ref.sfc_info.get("phi_array")
+        if phi is None:
+            phi = sample_scaling_function(ref.wavelet_mode, ref.wavelet_level)
+        for product in exp:
+            if product == "zeta_l":
+                continue
+            if product == "rrr_l" and all(isinstance(self.rand[i], float) for i in (1, 2, 3)):
+                vals = np.zeros((len(pairs), self.l_max - self.l_min + 1))
+                if self.l_min == 0:
+                    vals[:, 0] = self.rand[1] * self.rand[2] * self.rand[3]
+                setattr(data, product, vals * scale)
+                continue
+            e1, e2, e3 = (self._eps(product, i) for i in (1, 2, 3))
+            same23 = (self.sfc_field2 is self.sfc_field3 or self.sfc_field2 == self.sfc_field3) and \
+                self.window2 == self.window3 and (product != "delta_ddd_l" or self.random2 == self.random3)
+            eng = MultipoleEngine(e1, e2, e2 if same23 else e3, phi, ref.J, ref.box_size, ref.phi_resolution,
+                                  share23=same23)
+            if self.summation_backend == "plain":
+                vals = eng.ddd_plain(pairs, self.l_min, self.l_max)
+            else:
+                vals = eng.ddd(pairs, self.l_min, self.l_max)
+            data.timing[product] = dict(eng.timing)
+            setattr(data, product, vals * scale)
+        if "zeta_l" in exp:
+            if self.l_min != 0:
+                raise ValueError("zeta_l requires l_min = 0.")
+            z, _, cond = mixing_solve(data.delta_ddd_l, data.rrr_l, self.l_max, device=self.device)
+            data.zeta_l = z
+            data.zeta_condition = cond
+        for i in (1, 2, 3):
+            if i in self.data:
+                setattr(data, f"sfc_info{i}", self.data[i].sfc_info)
+        self.corr3pcf_multipole_data = data
+        if save_result and self.fout_path:
+            data.save_corr3pcf_multipole(self.fout_path, overwrite=overwrite)
+        logger.info("Corr_3PCF_Multipole %d samples l<=%d in %.3f s", len(pairs), self.l_max, time.perf_counter() - t0)
+        return data

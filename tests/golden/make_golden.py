@@ -171,8 +171,47 @@ def gen_corr2pcf():
     _save("corr2pcf_J5", **out)
 
 
+def gen_multipole():
+    from pyhermes.theory.corr3pcf_multipole import Corr_3PCF_Multipole
+    from pyhermes.utils.radial_multipole_windows import calculate_radial_multipole_window_array
+    from pyhermes.utils.special_functions import spherical_harmonic_numba, spherical_jn_numba
+    from pyhermes.utils.wavelet_grid import fourier_power_spectrum
+
+    out = {}
+    # special functions on a grid of arguments
+    xs = np.array([0.0, 1e-3, 0.04, 0.3, 1.0, 2.5, 7.0, 12.0, 33.0, 80.0])
+    out["jn"] = np.array([[spherical_jn_numba(l, x) for x in xs] for l in range(11)])
+    out["jn_x"] = xs
+    ks = np.array([[0.1, 0.2, 0.3], [-0.4, 0.1, -0.2], [0.0, 0.0, 0.5], [0.3, -0.3, 0.0], [-0.1, -0.2, -0.3]])
+    out["ylm"] = np.array([[[spherical_harmonic_numba(l, m, *k) for k in ks] for m in range(-l, l + 1)]
+                           + [[0j] * len(ks)] * (10 - 2 * l) for l in range(5)])
+    out["ylm_k"] = ks
+    phi = np.load(os.path.join(HERE, "phi_db2.npz"))["phi"]
+    P = fourier_power_spectrum(phi, 0, 1, 16, 1024)
+    for (l, m) in [(0, 0), (2, 1), (3, -2), (4, 4)]:
+        out[f"window_l{l}_m{m}"] = calculate_radial_multipole_window_array(
+            16, P, {"R": 180.0}, "shell", l, m, box_size=1000.0)
+    # the task: J=4, clustered catalogue, two (r12, r13) samples, l <= 2
+    rng = np.random.default_rng(21)
+    pos = rng.uniform(0.0, 1000.0, (3000, 3))
+    pos[:1200] = pos[:1200] * 0.3 + 350.0
+    w = rng.lognormal(0.0, 0.3, 3000)
+    f = _projection(pos, 4, weights=w)
+    task = Corr_3PCF_Multipole({"Corr_3PCF_Multipole": {
+        "sfc_field": f, "random": "uniform",
+        "binning_window12": {"type": "shell", "len_args": {}, "other_args": {}, "mapping": {"R": "r12"}},
+        "binning_window13": {"type": "shell", "len_args": {}, "other_args": {}, "mapping": {"R": "r13"}},
+        "sampling": {"mode": "paired", "r12": [150.0, 200.0], "r13": [250.0, 300.0]},
+        "l_min": 0, "l_max": 2, "summation_backend": "cpu", "products": ["ddd_l", "zeta_l"]}})
+    d = task.run(save_result=False)
+    out.update({"pos": pos, "weights": w, "epsilon": f.epsilon, "l": d.l, "ddd_l": d.ddd_l,
+                "delta_ddd_l": d.delta_ddd_l, "rrr_l": d.rrr_l, "zeta_l": d.zeta_l,
+                "zeta_condition": d.zeta_condition})
+    _save("multipole_J4", **out)
+
+
 SECTIONS = {"phi": gen_phi, "deposit": gen_deposit, "windows": gen_windows,
-            "convolution": gen_convolution, "corr2pcf": gen_corr2pcf}
+            "convolution": gen_convolution, "corr2pcf": gen_corr2pcf, "multipole": gen_multipole}
 
 
 def main(argv):
