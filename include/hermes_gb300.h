@@ -73,6 +73,21 @@ int hermes_deposit_accumulate(int64_t n, int J, double box, const double* phi,
                               double* eps_f64_out, uint32_t* counts_out,
                               void* workspace, size_t workspace_bytes,
                               void* stream);
+/* hermes_deposit without any device allocation, for callers that cannot
+ * allocate device memory (code inside an allocator's callbacks, plug-ins of
+ * hosts that budget all of HBM, runs that must not fail on allocation).  No
+ * counterpart in the reference: it is an addition of this library.  Same
+ * arguments and result as hermes_deposit minus the workspace; the scratch
+ * is a 4.5 MiB array built into the library (held on every GPU that loads
+ * it until exit).  Limits: n <= 131072 particles, J <= 8; larger requests
+ * return HERMES_ERR_INVALID.  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress), so make that first call
+ * before any stream capture.  All calls share the one array: calls whose
+ * work overlaps on the GPU (other streams, other host threads) race. */
+int hermes_deposit_noalloc(const double* pos, const double* w, int64_t n, int J,
+                           double box, const double* phi, int n_phi, int phi_res,
+                           float* eps_out, double* eps_f64_out, uint32_t* counts_out,
+                           void* stream);
 /* Reads (synchronously) the count of skipped non-finite particles from the
  * workspace of the last hermes_deposit issued with it. */
 int hermes_deposit_status(const void* workspace, int64_t* n_rejected,

@@ -23,6 +23,8 @@
 // neighbour tile, so a CTA reads only records that reach it.
 #include <math.h>
 
+#include <mutex>
+
 #include "hermes_common.cuh"
 
 namespace {
@@ -677,4 +679,70 @@ extern "C" int hermes_deposit_status(const void* workspace, int64_t* n_rejected,
   HERMES_CUDA_TRY(cudaStreamSynchronize(s));
   *n_rejected = (int64_t)st.rejected;
   return HERMES_OK;
+}
+
+// ---- deposit without any device allocation ---------------------------------
+// Some callers cannot allocate device memory at all: code that runs inside an
+// allocator's own callbacks, plug-ins of hosts that own and budget every byte
+// of HBM, or programs that must never hit an allocation failure mid-run.  For
+// them hermes_deposit_noalloc runs the same deposit kernels with their scratch
+// (the sort buckets and particle records that hermes_deposit takes from a
+// caller workspace) in the fixed array below, compiled into this library.
+//
+// Limits: n <= kNoAllocMaxParticles and J <= kNoAllocMaxJ.  The array holds
+// kNoAllocScratchBytes (4.5 MiB) on every GPU that loads the library, until
+// the process exits.
+constexpr int64_t kNoAllocMaxParticles = 131072;
+constexpr int kNoAllocMaxJ = 8;
+constexpr size_t kNoAllocScratchBytes = 4718592;
+static __device__ __align__(256) unsigned char g_deposit_noalloc_scratch[kNoAllocScratchBytes];
+
+namespace {
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+// Device address of the scratch array on the current device.  The array's
+// name in host code is only a host-side stand-in, so the address is looked
+// up once per device with cudaGetSymbolAddress and cached.
+int noalloc_scratch(void** out) {
+  int dev = 0;
+  HERMES_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kNoAllocMaxDevices)
+    return hermes::fail(HERMES_ERR_UNSUPPORTED, "deposit_noalloc: device %d beyond the supported %d", dev,
+                        kNoAllocMaxDevices);
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_deposit_noalloc_scratch);
+    if (e != cudaSuccess) return hermes::cuda_fail(e, "cudaGetSymbolAddress(g_deposit_noalloc_scratch)");
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return HERMES_OK;
+}
+}  // namespace
+
+extern "C" int hermes_deposit_noalloc(const double* pos, const double* w, int64_t n, int J, double box,
+                                      const double* phi, int n_phi, int phi_res, float* eps_out,
+                                      double* eps_f64_out, uint32_t* counts_out, void* stream) {
+  if (n < 0 || n > kNoAllocMaxParticles)
+    return hermes::fail(HERMES_ERR_INVALID, "deposit_noalloc: n=%lld outside [0, %lld] (the built-in scratch limit)",
+                        (long long)n, (long long)kNoAllocMaxParticles);
+  if (J > kNoAllocMaxJ)
+    return hermes::fail(HERMES_ERR_INVALID, "deposit_noalloc: J=%d above %d (the built-in scratch limit)", J,
+                        kNoAllocMaxJ);
+  size_t need = 0;
+  int rc = hermes_deposit_workspace_size(n, J, &need);
+  if (rc) return rc;
+  if (need > kNoAllocScratchBytes)
+    return hermes::fail(HERMES_ERR_INVALID, "deposit_noalloc: needs %zu scratch bytes, built-in array has %zu",
+                        need, kNoAllocScratchBytes);
+  void* scratch = nullptr;
+  rc = noalloc_scratch(&scratch);
+  if (rc) return rc;
+  // hermes_deposit_sort clears the status word and bucket counts it relies on;
+  // everything else in the scratch is written before it is read.
+  return hermes_deposit(pos, w, n, J, box, phi, n_phi, phi_res, eps_out, eps_f64_out, counts_out, scratch,
+                        kNoAllocScratchBytes, stream);
 }
