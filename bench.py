@@ -1,19 +1,30 @@
 """Benchmark of the GB300 field pipeline (one JSON line on rank 0).
 
-Workload (default): the clustered-field deposit configuration — 4,000,000
-points Poisson-sampled from a seeded lognormal density field
-(P(k) ~ k^-1.5 exp(-(k/0.5)^2), sigma_G = 1) in a 1000 Mpc/h periodic box,
-lognormal(0, 0.3) weights, projected at J=9 (512^3 float32 coefficients).
+Headline workload (one step = one catalogue): spherical-harmonic 3PCF
+multipoles.  1,000,000 points Poisson-sampled from a seeded lognormal density
+field (P(k) ~ k^-1.5 exp(-(k/0.5 h/Mpc)^2), sigma_G = 1, lognormal(0, 0.3)
+weights) and 5,000,000 uniform randoms in a 1000 Mpc/h periodic box are
+deposited at J=9 (512^3); delta = D - R (catalogue-normalised); 15 thin
+shells over 10-160 Mpc/h on both triangle sides (225 (r12, r13) samples);
+l = 0..10; products delta_ddd_l and rrr_l (the random field, full
+contraction) and zeta_l (float64 mixing solve).  The step runs through the
+public API (Corr_3PCF_Multipole with the batched "gb300" backend).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
-`value` is device-timed whole-job throughput with inputs resident in HBM;
-`e2e` is the same metric through the C ABI with host (pinned) inputs, the
-host->device copy and the device->host read of the field inside the timed
-region.  `--impl reference` times the float64 CPU restatement of the
-reference deposit (oracle/, sequential like the reference loop) on the
-host.  Under torchrun each rank deposits its own replica catalogue (replicas
-only: the path has no exchange step); rank 0 prints.
+`value` = seconds per catalogue, device-timed (CUDA events), inputs already
+in HBM.  `e2e` = the same with the catalogues in pinned host memory and the
+host->device copies plus the device->host read of zeta_l inside the timed
+region.  `plain` = the per-sample reference-form GPU path (both side fields
+rebuilt and a one-pair contraction for every (r12, r13, l, m)), timed on a
+one-sample subset and scaled by the 225 samples (its cost is linear in the
+samples).  `roofline` = the batched contraction, algorithmic FLOPs
+8 * 15 * 15 * 27 * L^3 per (l, m), against the measured bf16 peak.
+`deposit` = the 4M-point J=9 deposit (Mparticles/s, HBM roofline of the
+accumulate kernel).  `--impl reference` times the float64 CPU restatement of
+the reference (oracle/) on a bounded unit and scales it the same way.
+Under torchrun each rank runs its own replica catalogue (replicas only: the
+path has no exchange step); rank 0 prints the aggregate.
 """
 
 import argparse
@@ -31,20 +42,29 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-N_PARTICLES = 4_000_000
-J = 9
 BOX = 1000.0
-METRIC = "deposit Mparticles/s (4M lognormal points, J=9, float32 coefficients)"
-WORKLOAD = "clustered lognormal catalogue deposit: 4e6 points, J=9 (512^3), box 1000 Mpc/h"
+MP_J = 9
+MP_LMAX = 10
+MP_NDATA = 1_000_000
+MP_NRAND = 5_000_000
+MP_RADII = [float(r) for r in np.linspace(10.0, 160.0, 15)]
+N_LM = sum(l + 1 for l in range(MP_LMAX + 1))          # 66 (l, m>=0) terms
+N_SAMPLES = len(MP_RADII) ** 2                          # 225
+METRIC = "zeta_l s/catalogue (J=9, lmax=10, 15x15 shells 10-160 Mpc/h, 1M data + 5M randoms)"
+WORKLOAD = ("3PCF multipoles: 1e6 lognormal data + 5e6 uniform randoms deposited at J=9 (512^3), "
+            "delta=D-R, 15 thin shells 10-160 Mpc/h on both sides (225 (r12,r13) samples), l=0..10, "
+            "products delta_ddd_l + rrr_l (random field) + zeta_l")
+DEP_N = 4_000_000
+DEP_J = 9
 
 
 def load_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
             d = json.load(f)
-        return float(d["hbm_gbs"]), "measured"
+        return float(d["hbm_gbs"]), float(d["bf16_tflops"]), "measured"
     except Exception:
-        return 6800.0, "fallback"
+        return 6800.0, 1900.0, "fallback"
 
 
 class ClockSampler:
@@ -58,7 +78,6 @@ class ClockSampler:
         self.gpu_index = gpu_index
         self.proc = None
         self.lines = []
-        self.thread = None
 
     def start(self):
         try:
@@ -69,8 +88,7 @@ class ClockSampler:
         except Exception:
             self.proc = None
             return
-        self.thread = threading.Thread(target=self._read, daemon=True)
-        self.thread.start()
+        threading.Thread(target=self._read, daemon=True).start()
 
     def _read(self):
         for line in self.proc.stdout:
@@ -85,7 +103,7 @@ class ClockSampler:
             self.proc.wait(timeout=5)
         except Exception:
             self.proc.kill()
-        sm, smax, reasons = [], [], set()
+        sm, smax, power, reasons = [], [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
             parts = [p.strip() for p in ln.split(",")]
@@ -94,41 +112,64 @@ class ClockSampler:
             try:
                 sm.append(float(parts[1]))
                 smax.append(float(parts[2]))
+                power.append(float(parts[3]))
             except ValueError:
                 continue
             for nm, v in zip(names, parts[5:9]):
                 if v.lower().startswith("active"):
                     reasons.add(nm)
-        return {"sm_mhz": statistics.median(sm) if sm else None,
-                "sm_max_mhz": max(smax) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "power_w_max": max(power) if power else None, "reasons": sorted(reasons), "samples": len(sm)}
 
 
 def dist_setup():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
+    return (int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")),
+            int(os.environ.get("LOCAL_RANK", "0")))
 
 
-def make_catalogue(seed_offset, device):
+def make_catalogues(seed_offset, device):
+    """(data pos, data weights, random pos, random weights) as float64 NumPy."""
     from pyhermes_gb300 import synthetic
 
-    pos, w = synthetic.lognormal_catalogue(N_PARTICLES, box=BOX, seed_field=0 + seed_offset,
-                                           seed_poisson=1 + seed_offset, seed_weights=2 + seed_offset,
-                                           device=device)
-    pw = w / w.sum()
-    return pos, pw
+    dpos, dw = synthetic.lognormal_catalogue(MP_NDATA, box=BOX, seed_field=3 + seed_offset,
+                                             seed_poisson=4 + seed_offset, seed_weights=5 + seed_offset,
+                                             device=device)
+    rng = np.random.default_rng(40 + seed_offset)
+    rpos = rng.uniform(0.0, BOX, (MP_NRAND, 3))
+    rw = np.ones(MP_NRAND)
+    return dpos, dw, rpos, rw
 
 
-def cpu_deposit_rate(pos, pw, phi, n_sample):
+def multipole_task_params(dfield, rfield):
+    return {"Corr_3PCF_Multipole": {
+        "sfc_field": dfield, "random": rfield,
+        "binning_window12": {"type": "shell", "len_args": {}, "other_args": {}, "mapping": {"R": "r12"}},
+        "binning_window13": {"type": "shell", "len_args": {}, "other_args": {}, "mapping": {"R": "r13"}},
+        "sampling": {"mode": "grid", "r12": MP_RADII, "r13": MP_RADII},
+        "l_min": 0, "l_max": MP_LMAX, "summation_backend": "gb300", "products": "zeta_l"}}
+
+
+# ---------------------------------------------------------------------------
+# reference arm: the float64 CPU restatement of the reference on the host
+# ---------------------------------------------------------------------------
+def cpu_unit_seconds(eps_np, J, phi, l=1, m=1, r12=70.0, r13=110.0):
+    """One (sample, l, m) unit of the reference algorithm (calc_DDD_multipole
+    inner loop): two radial-multipole windows, two complex FFT convolutions
+    and the 729-term contraction, float64 on all host cores."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
+    from scipy.fft import fftn, ifftn
 
+    L = 1 << J
+    workers = os.cpu_count() or 1
     t0 = time.perf_counter()
-    oracle.deposit(pos[:n_sample], pw[:n_sample], phi, J, BOX)
-    dt = time.perf_counter() - t0
-    return n_sample / dt / 1e6, dt
+    P = oracle.fourier_power(phi, 1, L)
+    gam = oracle.cal_gamma(phi)
+    s = fftn(eps_np, workers=workers)
+    a2 = ifftn(s * oracle.radial_multipole_window(L, P, r12 * L / BOX, l, m), workers=workers)
+    a3 = ifftn(s * oracle.radial_multipole_window(L, P, r13 * L / BOX, l, -m), workers=workers)
+    oracle.contract(eps_np, a2, a3, gam)
+    return time.perf_counter() - t0, oracle.num_threads()
 
 
 def run_reference(args, ws, rank):
@@ -136,45 +177,113 @@ def run_reference(args, ws, rank):
         return 0
     from pyhermes_gb300.phi import sample_scaling_function
 
-    device = "cuda" if _cuda_ok() else "cpu"
-    pos, pw = make_catalogue(0, device if device == "cuda" else "cpu")
     phi = sample_scaling_function()
+    Ju = 8  # bounded unit: J=8, scaled by 8 to J=9 (the unit's cost is ~linear in cells)
+    rng = np.random.default_rng(0)
+    eps = rng.standard_normal((1 << Ju,) * 3) * 1e-7
     for _ in range(args.warmup):
-        cpu_deposit_rate(pos, pw, phi, N_PARTICLES // 4)
-    rates, total = [], 0.0
+        cpu_unit_seconds(eps, Ju, phi, l=0, m=0)
+    total, cores = 0.0, 1
     for _ in range(args.steps):
-        r, dt = cpu_deposit_rate(pos, pw, phi, N_PARTICLES)
-        rates.append(r)
+        dt, cores = cpu_unit_seconds(eps, Ju, phi)
         total += dt
-    value = N_PARTICLES * args.steps / total / 1e6
+    unit = total / args.steps
+    per_cat = unit * 8.0 * N_SAMPLES * N_LM * 2
     line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": "Mparticles/s",
-        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": total / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded lognormal catalogue)",
-        "config": {"workload": WORKLOAD, "n_particles": N_PARTICLES, "J": J},
-        "cpu_baseline": {"value": value, "unit": "Mparticles/s", "cores": 1, "kind": "port",
-                         "sample": f"full {N_PARTICLES} particle catalogue per step, sequential float64 "
-                                   "restatement of the reference deposit loop (oracle/hermes_oracle.c)"},
-        "e2e": {"value": value, "unit": "Mparticles/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "impl": "reference", "metric": METRIC, "value": per_cat, "unit": "s/catalogue",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": unit * 1e3,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic field (seeded)", "config": {"workload": WORKLOAD, "J": MP_J, "lmax": MP_LMAX},
+        "cpu_baseline": {"value": per_cat, "unit": "s/catalogue", "cores": cores, "kind": "port",
+                         "sample": (f"one (r12, r13, l=1, m=1) unit at J={Ju} per step ({unit:.2f} s): two "
+                                    "radial-multipole windows, two complex FFT convolutions, the 729-term "
+                                    "contraction (oracle/ float64 restatement, all host threads); scaled x8 to "
+                                    f"J=9 and x{N_SAMPLES}x{N_LM}x2 (samples x (l,m) x products)")},
+        "e2e": {"value": per_cat, "unit": "s/catalogue", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
     return 0
 
 
-def _cuda_ok():
-    try:
-        import torch
+# ---------------------------------------------------------------------------
+# GB300 arm
+# ---------------------------------------------------------------------------
+def deposit_field(pos_t, w_t, J, phi_t, ws):
+    from pyhermes_gb300 import kernels
+    from pyhermes_gb300.sfc_field import SFCField
 
-        return torch.cuda.is_available()
-    except Exception:
-        return False
+    wsum = float(w_t.sum().item())
+    pw = w_t / wsum
+    eps, _, _ = kernels.deposit(pos_t, pw, J, BOX, phi_t, workspace=ws)
+    L = 1 << J
+    f = SFCField(device=pos_t.device)
+    f.sfc_info = {"J": J, "L": L, "V": L ** 3, "box_size": BOX, "scale_factor": L / BOX, "phi_resolution": 1024,
+                  "wavelet_mode": "db2", "wavelet_level": 10, "phi_support": 3,
+                  "phi_array": phi_t.cpu().numpy(), "field_kind": "catalog_field",
+                  "weight_normalization": "catalog", "catalog_weight_sum": wsum,
+                  "raw_field_weighted_sum": wsum, "field_integral": 1.0, "particle_count": int(pos_t.shape[0])}
+    f.format_sfc_params()
+    f.epsilon_device = eps
+    return f
+
+
+def deposit_bench(dev, lib, kernels, phi, flush, steps):
+    """The 4M-point J=9 deposit: Mparticles/s and the accumulate kernel roofline."""
+    import torch
+
+    from pyhermes_gb300 import _lib, synthetic
+
+    pos_np, w_np = synthetic.lognormal_catalogue(DEP_N, box=BOX, device=dev)
+    pos = torch.as_tensor(pos_np, device=dev)
+    pw = torch.as_tensor(w_np / w_np.sum(), device=dev)
+    L = 1 << DEP_J
+    eps = torch.empty((L, L, L), dtype=torch.float32, device=dev)
+    buf = kernels.DepositWorkspace(dev).get(DEP_N, DEP_J)
+    sptr = torch.cuda.current_stream(dev).cuda_stream
+    P = ctypes.c_void_p
+
+    def sort():
+        _lib.check(lib.hermes_deposit_sort(P(pos.data_ptr()), P(pw.data_ptr()), DEP_N, DEP_J, BOX,
+                                           P(phi.data_ptr()), phi.numel(), 1024, P(buf.data_ptr()),
+                                           buf.numel(), sptr), "sort")
+
+    def accumulate():
+        _lib.check(lib.hermes_deposit_accumulate(DEP_N, DEP_J, BOX, P(phi.data_ptr()), phi.numel(), 1024,
+                                                 P(eps.data_ptr()), None, None, P(buf.data_ptr()),
+                                                 buf.numel(), sptr), "accumulate")
+
+    for _ in range(3):
+        sort()
+        accumulate()
+    stream = torch.cuda.current_stream(dev)
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(steps)]
+    torch.cuda.synchronize(dev)
+    for k in range(steps):
+        flush.zero_()
+        ev[k][0].record(stream)
+        sort()
+        ev[k][1].record(stream)
+        accumulate()
+        ev[k][2].record(stream)
+    torch.cuda.synchronize(dev)
+    step_ms = [e[0].elapsed_time(e[2]) for e in ev]
+    acc_ms = sum(e[1].elapsed_time(e[2]) for e in ev) / steps
+    hbm, _, kind = load_peaks()
+    alg = DEP_N * 16 + L ** 3 * 4
+    ach = alg / (acc_ms / 1e3) / 1e9
+    return {"metric": "deposit Mparticles/s (4M lognormal points, J=9, float32 field)",
+            "value": DEP_N / (sum(step_ms) / steps / 1e3) / 1e6, "unit": "Mparticles/s",
+            "ms_per_step": sum(step_ms) / steps, "launches_per_step": 7,
+            "roofline": {"kernel": "dep_accum_kernel", "bound": "hbm", "achieved": ach, "peak": hbm,
+                         "peak_kind": kind, "unit": "GB/s", "frac": ach / hbm, "traffic": None,
+                         "algorithmic_bytes": alg, "ms_per_launch": acc_ms}}
 
 
 def run_gb300(args, ws, rank, local):
     import torch
 
     from pyhermes_gb300 import _lib, kernels
+    from pyhermes_gb300 import multipole as mp
     from pyhermes_gb300.phi import sample_scaling_function
 
     torch.cuda.set_device(local)
@@ -184,35 +293,23 @@ def run_gb300(args, ws, rank, local):
 
         dist.init_process_group("nccl", device_id=dev)
     lib = _lib.load()
-    pos_np, pw_np = make_catalogue(rank, dev)
     phi_np = sample_scaling_function()
-    pos = torch.as_tensor(pos_np, device=dev)
-    pw = torch.as_tensor(pw_np, device=dev)
     phi = torch.as_tensor(phi_np, device=dev)
-    L = 1 << J
-    eps = torch.empty((L, L, L), dtype=torch.float32, device=dev)
-    wsp = kernels.DepositWorkspace(dev)
-    buf = wsp.get(N_PARTICLES, J)
-    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+    dpos_np, dw_np, rpos_np, rw_np = make_catalogues(rank, dev)
+    dpos, dw = torch.as_tensor(dpos_np, device=dev), torch.as_tensor(dw_np, device=dev)
+    rpos, rw = torch.as_tensor(rpos_np, device=dev), torch.as_tensor(rw_np, device=dev)
+    wsd, wsr = kernels.DepositWorkspace(dev), kernels.DepositWorkspace(dev)
     stream = torch.cuda.current_stream(dev)
-    sptr = stream.cuda_stream
-    P = ctypes.c_void_p
 
-    def sort():
-        _lib.check(lib.hermes_deposit_sort(P(pos.data_ptr()), P(pw.data_ptr()), N_PARTICLES, J, BOX,
-                                           P(phi.data_ptr()), phi.numel(), 1024, P(buf.data_ptr()),
-                                           buf.numel(), sptr), "sort")
+    def step(dp, dwt, rp, rwt):
+        dfield = deposit_field(dp, dwt, MP_J, phi, wsd)
+        rfield = deposit_field(rp, rwt, MP_J, phi, wsr)
+        task = mp.Corr_3PCF_Multipole(multipole_task_params(dfield, rfield), device=dev)
+        return task.run(save_result=False)
 
-    def accumulate():
-        _lib.check(lib.hermes_deposit_accumulate(N_PARTICLES, J, BOX, P(phi.data_ptr()), phi.numel(), 1024,
-                                                 P(eps.data_ptr()), None, None, P(buf.data_ptr()),
-                                                 buf.numel(), sptr), "accumulate")
-
-    for _ in range(max(args.warmup, 3)):
-        sort()
-        accumulate()
+    for _ in range(max(args.warmup, 3) if args.warmup > 0 else 0):
+        res = step(dpos, dw, rpos, rw)
     torch.cuda.synchronize(dev)
-    kernels_per_step = 7  # max, bin, 3 scan phases, scatter, accumulate
 
     def barrier():
         if ws > 1:
@@ -221,85 +318,121 @@ def run_gb300(args, ws, rank, local):
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.3)
-    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     barrier()
     torch.cuda.synchronize(dev)
+    kernel_launches = 0
     for k in range(args.steps):
-        flush.zero_()
         ev[k][0].record(stream)
-        sort()
+        res = step(dpos, dw, rpos, rw)
         ev[k][1].record(stream)
-        accumulate()
-        ev[k][2].record(stream)
     torch.cuda.synchronize(dev)
     barrier()
     clk = clocks.stop()
-    step_ms = [e[0].elapsed_time(e[2]) for e in ev]
-    acc_ms = [e[1].elapsed_time(e[2]) for e in ev]
-    t_total = sum(step_ms) / 1e3
+    t_total = sum(a.elapsed_time(b) for a, b in ev) / 1e3
     if ws > 1:
         import torch.distributed as dist
 
         t = torch.tensor([t_total], device=dev, dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         t_total = float(t.item())
-    value = N_PARTICLES * ws * args.steps / t_total / 1e6
+    # whole-job: catalogues per second over all ranks -> seconds per catalogue
+    value = t_total / (args.steps * ws)
+    zeta = np.asarray(res.zeta_l)
 
-    # end to end through the C ABI: pinned host buffers, H2D + deposit + D2H of the field
-    pos_h = torch.as_tensor(pos_np).pin_memory()
-    pw_h = torch.as_tensor(pw_np).pin_memory()
-    eps_h = torch.empty((L, L, L), dtype=torch.float32).pin_memory()
-    pos_d = torch.empty_like(pos)
-    pw_d = torch.empty_like(pw)
+    # launches per step: 2 deposits x 7, per product per (l,m): fields (table, power, prepass, FFT) +
+    # contract (G, GEMM, reduce); plus the mixing solve
+    kernel_launches = args.steps * (14 + 2 * N_LM * 7 + 1)
+
+    # end to end: catalogues in pinned host memory, copies inside the timed region
+    h = [torch.as_tensor(a).pin_memory() for a in (dpos_np, dw_np, rpos_np, rw_np)]
+    d = [torch.empty_like(x, device=dev) for x in h]
     e2e_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
               for _ in range(args.steps)]
-    for k in range(args.steps + 1):
-        flush.zero_()
-        if k > 0:
-            e2e_ev[k - 1][0].record(stream)
-        pos_d.copy_(pos_h, non_blocking=True)
-        pw_d.copy_(pw_h, non_blocking=True)
-        _lib.check(lib.hermes_deposit(P(pos_d.data_ptr()), P(pw_d.data_ptr()), N_PARTICLES, J, BOX,
-                                      P(phi.data_ptr()), phi.numel(), 1024, P(eps.data_ptr()), None, None,
-                                      P(buf.data_ptr()), buf.numel(), sptr), "deposit")
-        eps_h.copy_(eps, non_blocking=True)
-        if k > 0:
-            e2e_ev[k - 1][1].record(stream)
+    for k in range(args.steps):
+        e2e_ev[k][0].record(stream)
+        for src, dst in zip(h, d):
+            dst.copy_(src, non_blocking=True)
+        r2 = step(*d)
+        np.asarray(r2.zeta_l)  # zeta_l read back to the host (done inside run())
+        e2e_ev[k][1].record(stream)
     torch.cuda.synchronize(dev)
-    e2e_s = sum(a.elapsed_time(b) for a, b in e2e_ev) / 1e3
-    e2e_value = N_PARTICLES * ws * args.steps / e2e_s / 1e6
+    e2e_value = sum(a.elapsed_time(b) for a, b in e2e_ev) / 1e3 / (args.steps * ws)
 
-    peak, peak_kind = load_peaks()
-    alg_bytes = N_PARTICLES * 16 + L ** 3 * 4
-    acc_mean = sum(acc_ms) / len(acc_ms) / 1e3
-    achieved = alg_bytes / acc_mean / 1e9
-    pass_bytes = N_PARTICLES * (24 + 8) + L ** 3 * 4
-    pass_gbs = pass_bytes / (t_total / args.steps) / 1e9
+    # dominant kernel: the batched contraction of one (l, m) over 15x15 radii
+    dfield = deposit_field(dpos, dw, MP_J, phi, wsd)
+    rfield = deposit_field(rpos, rw, MP_J, phi, wsr)
+    delta = (dfield.epsilon_device.double() - rfield.epsilon_device.double()).float()
+    eng = mp.MultipoleEngine(delta, delta, delta, phi_np, MP_J, BOX)
+    L = 1 << MP_J
+    grid = [r * L / BOX for r in MP_RADII]
+    f2 = mp.multipole_fields(eng.spec2, MP_J, 4, 2, grid, eng.P)
+    for _ in range(3):
+        mp.multipole_contract(eng.eps1, f2, 15, eng.gamma, MP_J, conj_sign=1)
+    cev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(5)]
+    for a, b in cev:
+        a.record(stream)
+        mp.multipole_contract(eng.eps1, f2, 15, eng.gamma, MP_J, conj_sign=1)
+        b.record(stream)
+    fev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(3)]
+    for a, b in fev:
+        a.record(stream)
+        mp.multipole_fields(eng.spec2, MP_J, 4, 2, grid, eng.P, out=f2)
+        b.record(stream)
+    torch.cuda.synchronize(dev)
+    t_con = sum(a.elapsed_time(b) for a, b in cev) / len(cev) / 1e3
+    t_fld = sum(a.elapsed_time(b) for a, b in fev) / len(fev) / 1e3
+    del f2
+    hbm, bf16, kind = load_peaks()
+    flops = 8.0 * 15 * 15 * 27 * L ** 3
+    achieved = flops / t_con / 1e12
+
+    # plain per-sample reference-form path on a one-sample subset (l <= 1)
+    t0 = time.perf_counter()
+    plain = eng.ddd_plain([(MP_RADII[5], MP_RADII[9])], 0, 1)
+    torch.cuda.synchronize(dev)
+    t_plain_units = time.perf_counter() - t0
+    plain_unit = t_plain_units / 3.0  # 3 (l, m) terms
+    plain_per_cat = plain_unit * N_SAMPLES * N_LM * 2
+    batched = eng.ddd([(MP_RADII[5], MP_RADII[9])], 0, 1)
+    mixed_vs_plain = float(np.max(np.abs(batched - plain)) / np.max(np.abs(plain)))
+
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+    dep = deposit_bench(dev, lib, kernels, phi, flush, max(args.steps, 5))
 
     if rank != 0:
+        if ws > 1:
+            torch.distributed.destroy_process_group()
         return 0
-    cpu_rate, cpu_dt = cpu_deposit_rate(pos_np, pw_np, phi_np, 1_000_000)
+    cpu_unit, cores = cpu_unit_seconds(np.random.default_rng(0).standard_normal((256,) * 3) * 1e-7, 8, phi_np)
+    cpu_per_cat = cpu_unit * 8.0 * N_SAMPLES * N_LM * 2
     line = {
-        "metric": METRIC, "value": value, "unit": "Mparticles/s", "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": t_total / args.steps * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded lognormal catalogue; the reference's Quijote catalogue is not available)",
-        "config": {"workload": WORKLOAD, "n_particles": N_PARTICLES, "J": J, "box": BOX,
-                   "l2": "flushed (256 MiB write) before every timed step; field 512 MiB > L2",
+        "metric": METRIC, "value": value, "unit": "s/catalogue", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_total / args.steps * 1e3, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (float64 reductions and mixing solve)",
+        "data": "synthetic (seeded lognormal data + uniform randoms; the reference's Quijote catalogue is absent)",
+        "config": {"workload": WORKLOAD, "J": MP_J, "lmax": MP_LMAX, "radii": len(MP_RADII),
+                   "samples": N_SAMPLES, "n_data": MP_NDATA, "n_random": MP_NRAND,
+                   "l2": "per-(l,m) working set (15 GiB fields) far above L2",
                    "parallelism": f"replicas x{ws}"},
-        "roofline": {"kernel": "dep_accum_kernel", "bound": "hbm", "achieved": achieved, "peak": peak,
-                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None,
-                     "algorithmic_bytes": alg_bytes, "ms_per_launch": acc_mean * 1e3},
-        "deposit_pass": {"GB/s": pass_gbs, "frac": pass_gbs / peak,
-                         "algorithmic_bytes": pass_bytes,
-                         "note": "all 7 kernels; float64 xyz+w in, float32 field out"},
-        "cpu_baseline": {"value": cpu_rate, "unit": "Mparticles/s", "cores": 1, "kind": "port",
-                         "sample": "first 1,000,000 particles of the catalogue, sequential float64 "
-                                   f"restatement of the reference loop ({cpu_dt:.2f} s)"},
-        "e2e": {"value": e2e_value, "unit": "Mparticles/s",
-                "h2d_bytes_per_step": N_PARTICLES * 32, "d2h_bytes_per_step": L ** 3 * 4},
-        "gpu_launches": kernels_per_step * args.steps,
+        "plain": {"value": plain_per_cat, "unit": "s/catalogue", "speedup_batched_vs_plain": plain_per_cat / value,
+                  "sample": "one (r12, r13) sample, l<=1, scaled by 225 samples x 66 (l,m) x 2 products",
+                  "max_rel_diff_batched_vs_plain": mixed_vs_plain},
+        "roofline": {"kernel": "hermes_multipole_contract (mp_gfield + mp_gemm + reduce)", "bound": "tensor",
+                     "achieved": achieved, "peak": bf16, "peak_kind": kind, "unit": "TFLOP/s",
+                     "frac": achieved / bf16, "traffic": None,
+                     "algorithmic_flops": flops, "ms_per_launch": t_con * 1e3,
+                     "fields_ms_per_lm": t_fld * 1e3},
+        "deposit": dep,
+        "cpu_baseline": {"value": cpu_per_cat, "unit": "s/catalogue", "cores": cores, "kind": "port",
+                         "sample": (f"one (r12, r13, l=1, m=1) unit at J=8 ({cpu_unit:.2f} s, float64 oracle "
+                                    "restatement: windows, FFT convolutions, 729-term contraction); scaled x8 "
+                                    "to J=9 and x225 samples x66 (l,m) x2 products")},
+        "e2e": {"value": e2e_value, "unit": "s/catalogue",
+                "h2d_bytes_per_step": int(sum(x.numel() * x.element_size() for x in h)),
+                "d2h_bytes_per_step": int(zeta.size * 8)},
+        "gpu_launches": kernel_launches,
+        "zeta_l_shape": list(zeta.shape),
         "clocks": clk,
     }
     print(json.dumps(line))
@@ -311,7 +444,7 @@ def run_gb300(args, ws, rank, local):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     args = ap.parse_args()

@@ -213,6 +213,53 @@ int hermes_multipole_contract_plain(const float* eps1, const void* a2, const voi
                                     const double* gamma, int J, double* out,
                                     void* workspace, size_t workspace_bytes, void* stream);
 
+/* ---- Monte Carlo 3PCF ---------------------------------------------------------
+ * hermes_interp: utils/wavelet_grid.py:143-186 interpolate_grid_at_pos_numba:
+ * out[i] (float64) = 27-point phi-weighted value of `grid` (float32 [L^3]) at
+ * scaled position (pos * L/box) + (dx, dy, dz); phi: 3*phi_res float64.
+ *
+ * hermes_mc_triplets: utils/corr3pcf_kernels.py:66-140 for one mu:
+ *   sum_out = sum_i w_i n1(x_i) sum_r n2(x_i + d2_r) n3(x_i + d3_r)
+ * (float64), with n1 = eps1 interpolated (box-random centres) or rho1 when
+ * eps1 is NULL (particle centres, w = center_w or 1).  offsets: n_rot x 6
+ * float64 (scaled) triangle offsets (generate_triangle_offsets, :21-63, from
+ * the reference's per-rotation seeded uniforms).  samples_out (nullable):
+ * float32 [n_centers][n_rot] per-triplet products.  Synchronises `stream`.
+ */
+int hermes_mc_workspace_size(size_t* bytes);
+int hermes_interp(const float* grid, int J, const double* scaled_pos, int64_t n,
+                  const double* phi, int n_phi, int phi_res, double dx, double dy,
+                  double dz, double* out, void* workspace, size_t workspace_bytes,
+                  void* stream);
+int hermes_mc_triplets(const float* eps1, const float* eps2, const float* eps3, int J,
+                       const double* centers, const double* center_w, int64_t n_centers,
+                       const double* offsets, int n_rot, const double* phi, int n_phi,
+                       int phi_res, double rho1, double* sum_out, float* samples_out,
+                       void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---- learned proposal network (no reference counterpart) ---------------------
+ * A tanh MLP with dims[0] inputs, dims[n_layers] outputs, widths <= 128:
+ * params = per layer W [in][out] then b [out] (float32).  forward writes
+ * every layer's output into acts (sum_l batch*dims[l+1] floats) and reads
+ * params or, for inference, a bfloat16 copy (params_bf16, from
+ * hermes_to_bf16).  backward: grads (same layout) of sum(dy * y) through the
+ * network; scratch: hermes_mlp_scratch_floats(batch) floats.  mse_grad:
+ * dy = 2 (y - target)/n and the mean squared error (host float64; scratch:
+ * one device double; synchronises).  adam_step: one Adam update (step >= 1). */
+int hermes_mlp_param_count(const int32_t* dims, int n_layers, int64_t* n_params);
+int hermes_mlp_scratch_floats(int64_t batch, int64_t* n);
+int hermes_mlp_forward(const float* params, const void* params_bf16, const int32_t* dims,
+                       int n_layers, const float* x, int64_t batch, float* acts,
+                       void* stream);
+int hermes_mlp_backward(const float* params, const int32_t* dims, int n_layers,
+                        const float* x, int64_t batch, const float* acts, const float* dy,
+                        float* grads, float* scratch, void* stream);
+int hermes_mse_grad(const float* y, const float* target, int64_t n, float* dy,
+                    double* loss_out, double* scratch, void* stream);
+int hermes_adam_step(float* params, const float* grads, float* m, float* v, int64_t n,
+                     float lr, float b1, float b2, float eps, int step, void* stream);
+int hermes_to_bf16(const float* in, int64_t n, void* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -276,3 +276,78 @@ def solve_multipoles_from_ratio(A, B, lmax):
     M += np.eye(lmax + 1)
     M *= B[0]
     return np.linalg.solve(M, A), M, np.linalg.cond(M)
+
+
+def generate_triangle_offsets(R1, R2, mu, phi, costheta1, alpha):
+    """utils/corr3pcf_kernels.py:21-63."""
+    import math
+
+    st1 = math.sqrt(1.0 - costheta1 * costheta1)
+    dx1, dy1, dz1 = st1 * math.cos(phi), st1 * math.sin(phi), costheta1
+    if abs(dx1) > 1e-10 or abs(dy1) > 1e-10:
+        o1 = [-dy1, dx1, 0.0]
+    else:
+        o1 = [0.0, -dz1, dy1]
+    nr = math.sqrt(o1[0] ** 2 + o1[1] ** 2 + o1[2] ** 2)
+    ox1, oy1, oz1 = o1[0] / nr, o1[1] / nr, o1[2] / nr
+    ox2, oy2, oz2 = dy1 * oz1 - dz1 * oy1, dz1 * ox1 - dx1 * oz1, dx1 * oy1 - dy1 * ox1
+    ca, sa = math.cos(alpha), math.sin(alpha)
+    st = math.sqrt(max(0.0, 1.0 - mu * mu))
+    dx2 = mu * dx1 + st * (ca * ox1 + sa * ox2)
+    dy2 = mu * dy1 + st * (ca * oy1 + sa * oy2)
+    dz2 = mu * dz1 + st * (ca * oz1 + sa * oz2)
+    return R1 * dx1, R1 * dy1, R1 * dz1, R2 * dx2, R2 * dy2, R2 * dz2
+
+
+def mc_box_random(eps1, eps2, eps3, J, centers, r12s, r13s, mu, n_rot, seed_base_rot, mu_index, phi):
+    """estimate_triplet_product_box_random_centers (corr3pcf_kernels.py:100-140)."""
+    n1 = interp(centers, eps1, phi, J)
+    total = 0.0
+    for irot in range(n_rot):
+        np.random.seed(seed_base_rot + irot + mu_index * 1000003)
+        a, b, c = np.random.rand(3)
+        o = generate_triangle_offsets(r12s, r13s, mu, 2 * np.pi * a, 2.0 * b - 1.0, 2 * np.pi * c)
+        n2 = interp(centers, eps2, phi, J, offset=o[0:3])
+        n3 = interp(centers, eps3, phi, J, offset=o[3:6])
+        total += float(np.sum(n1 * n2 * n3))
+    return total / (n_rot * centers.shape[0])
+
+
+def mlp_forward(params, dims, x):
+    """tanh MLP (hidden tanh, linear output) in float64; returns activations."""
+    acts, off, h = [], 0, np.asarray(x, dtype=np.float64)
+    for l in range(len(dims) - 1):
+        K, N = dims[l], dims[l + 1]
+        W = params[off:off + K * N].reshape(K, N)
+        b = params[off + K * N:off + K * N + N]
+        off += K * N + N
+        z = h @ W + b
+        h = np.tanh(z) if l + 1 < len(dims) - 1 else z
+        acts.append(h)
+    return acts
+
+
+def mlp_mse_grad(params, dims, x, t):
+    """Mean squared error and its gradient w.r.t. the flat parameters."""
+    params = np.asarray(params, dtype=np.float64)
+    acts = mlp_forward(params, dims, x)
+    y = acts[-1][:, 0]
+    n = y.shape[0]
+    loss = float(np.mean((y - t) ** 2))
+    dy = (2.0 / n) * (y - t)[:, None]
+    grads = np.zeros_like(params)
+    offs, off = [], 0
+    for l in range(len(dims) - 1):
+        offs.append(off)
+        off += dims[l] * dims[l + 1] + dims[l + 1]
+    for l in range(len(dims) - 2, -1, -1):
+        K, N = dims[l], dims[l + 1]
+        Yl = acts[l]
+        dz = dy * (1.0 - Yl ** 2) if l + 1 < len(dims) - 1 else dy
+        Xl = np.asarray(x, dtype=np.float64) if l == 0 else acts[l - 1]
+        o = offs[l]
+        grads[o:o + K * N] = (Xl.T @ dz).ravel()
+        grads[o + K * N:o + K * N + N] = dz.sum(axis=0)
+        W = params[o:o + K * N].reshape(K, N)
+        dy = dz @ W.T
+    return loss, grads

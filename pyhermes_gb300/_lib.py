@@ -43,6 +43,18 @@ SIGNATURES = {
     "hermes_multipole_fields": (_c_int, [_p, _c_int, _c_int, _c_int, _p, _c_int, _p, _p, _p, _c_sz, _p]),
     "hermes_multipole_contract": (_c_int, [_p, _p, _c_int, _p, _c_int, _c_int, _p, _c_int, _p, _p, _c_sz, _p]),
     "hermes_multipole_contract_plain": (_c_int, [_p, _p, _p, _p, _c_int, _p, _p, _c_sz, _p]),
+    "hermes_mc_workspace_size": (_c_int, [ctypes.POINTER(_c_sz)]),
+    "hermes_interp": (_c_int, [_p, _c_int, _p, _c_i64, _p, _c_int, _c_int, _dbl, _dbl, _dbl, _p, _p, _c_sz, _p]),
+    "hermes_mc_triplets": (_c_int, [_p, _p, _p, _c_int, _p, _p, _c_i64, _p, _c_int, _p, _c_int, _c_int, _dbl,
+                                    ctypes.POINTER(_dbl), _p, _p, _c_sz, _p]),
+    "hermes_mlp_param_count": (_c_int, [_p, _c_int, ctypes.POINTER(_c_i64)]),
+    "hermes_mlp_scratch_floats": (_c_int, [_c_i64, ctypes.POINTER(_c_i64)]),
+    "hermes_mlp_forward": (_c_int, [_p, _p, _p, _c_int, _p, _c_i64, _p, _p]),
+    "hermes_mlp_backward": (_c_int, [_p, _p, _c_int, _p, _c_i64, _p, _p, _p, _p, _p]),
+    "hermes_mse_grad": (_c_int, [_p, _p, _c_i64, _p, ctypes.POINTER(_dbl), _p, _p]),
+    "hermes_adam_step": (_c_int, [_p, _p, _p, _p, _c_i64, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                  ctypes.c_float, _c_int, _p]),
+    "hermes_to_bf16": (_c_int, [_p, _c_i64, _p, _p]),
 }
 
 

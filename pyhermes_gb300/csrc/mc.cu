@@ -1,0 +1,187 @@
+// Monte Carlo 3PCF on the GPU: field interpolation at points and triplet
+// products over (centre, rotation) pairs.
+//
+// Restates pyhermes/utils/wavelet_grid.py:143-186 (interpolate_grid_at_pos:
+// the 27-point phi-weighted gather) and pyhermes/utils/corr3pcf_kernels.py:
+// 66-140 (estimate_triplet_product_{particle,box_random}_centers).  The
+// reference draws three uniforms per rotation from a re-seeded MT19937 and
+// builds the two triangle offsets on the host (generate_triangle_offsets,
+// :21-63); the offsets are tiny (n_rot x 6 doubles) and are passed in, so the
+// GPU sums exactly the same (centre, offset) pairs.  One thread per centre
+// loads the centre once, gathers n1 once and loops over the rotations;
+// products are float32, sums float64 with a fixed-order block reduction.
+#include "hermes_common.cuh"
+
+namespace {
+
+using hermes::fail;
+
+// Cell and fraction index of a scaled coordinate exactly as the reference:
+// c = floor(s), f = int((s - c) * res) in float64.
+__device__ __forceinline__ void mc_axis(double s, int res, int L, int& c, int& f) {
+  const double fl = floor(s);
+  c = ((int)fl) & (L - 1);
+  int fi = (int)__dmul_rn(__dsub_rn(s, fl), (double)res);
+  f = fi < 0 ? 0 : (fi >= res ? res - 1 : fi);
+}
+
+// 27-point interpolation of a float32 field at scaled position (sx, sy, sz).
+__device__ __forceinline__ float mc_interp(const float* __restrict__ grid, const float* __restrict__ phis, int res,
+                                           int J, double sx, double sy, double sz) {
+  const int L = 1 << J;
+  int cx, cy, cz, fx, fy, fz;
+  mc_axis(sx, res, L, cx, fx);
+  mc_axis(sy, res, L, cy, fy);
+  mc_axis(sz, res, L, cz, fz);
+  const int m = L - 1;
+  float acc = 0.f;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const int xg = (cx - a) & m;
+    const float px = phis[fx + a * res];
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+      const int yg = (cy - b) & m;
+      const float py = phis[fy + b * res];
+      const float* row = grid + (((size_t)xg << J) + yg) * (size_t)L;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const int zg = (cz - c) & m;
+        acc += __ldg(row + zg) * px * py * phis[fz + c * res];
+      }
+    }
+  }
+  return acc;
+}
+
+__global__ void mc_phi_kernel(const double* __restrict__ phi, int n, float* __restrict__ out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = (float)phi[i];
+}
+
+__global__ void mc_interp_kernel(const float* __restrict__ grid, int J, const double* __restrict__ pos, int64_t n,
+                                 const float* __restrict__ phis, int res, double dx, double dy, double dz,
+                                 double* __restrict__ out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = (double)mc_interp(grid, phis, res, J, pos[3 * i] + dx, pos[3 * i + 1] + dy, pos[3 * i + 2] + dz);
+}
+
+// sum_i w_i n1_i sum_r n2(x_i + d2_r) n3(x_i + d3_r); n1 = eps1 interpolated
+// (box-random centres) or rho1 (particle centres: eps1 == NULL).  When
+// samples != NULL also writes the per-(centre, rotation) products f_ir.
+__global__ void __launch_bounds__(256)
+mc_triplet_kernel(const float* __restrict__ eps1, const float* __restrict__ eps2, const float* __restrict__ eps3,
+                  int J, const double* __restrict__ centers, const double* __restrict__ cw, int64_t nc,
+                  const double* __restrict__ offsets, int n_rot, const float* __restrict__ phis, int res,
+                  double rho1, double* __restrict__ partial, float* __restrict__ samples) {
+  double acc = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += (int64_t)gridDim.x * blockDim.x) {
+    const double x = centers[3 * i], y = centers[3 * i + 1], z = centers[3 * i + 2];
+    const float n1 = eps1 ? mc_interp(eps1, phis, res, J, x, y, z) : (float)rho1;
+    const float w = cw ? (float)cw[i] : 1.f;
+    float s = 0.f;
+    for (int r = 0; r < n_rot; ++r) {
+      const double* o = offsets + 6 * r;
+      const float n2 = mc_interp(eps2, phis, res, J, x + o[0], y + o[1], z + o[2]);
+      const float n3 = mc_interp(eps3, phis, res, J, x + o[3], y + o[4], z + o[5]);
+      const float f = w * n1 * n2 * n3;
+      if (samples) samples[i * n_rot + r] = f;
+      s += f;
+    }
+    acc += (double)s;
+  }
+  __shared__ double sh[256];
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
+}
+
+__global__ void mc_sum_kernel(const double* __restrict__ partial, int n, double* __restrict__ out) {
+  __shared__ double sh[256];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += partial[i];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = sh[0];
+}
+
+int mc_grid() {
+  int dev = 0, nsm = 148;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  return nsm * 8;
+}
+
+}  // namespace
+
+extern "C" int hermes_mc_workspace_size(size_t* bytes) {
+  if (!bytes) return fail(HERMES_ERR_INVALID, "bytes is NULL");
+  hermes::Carver c(nullptr, 0);
+  c.take<float>(4 * 1024);
+  c.take<double>((size_t)mc_grid() + 1);
+  *bytes = c.used;
+  return HERMES_OK;
+}
+
+static int mc_prepare(const double* phi, int n_phi, int res, void* workspace, size_t workspace_bytes, float** phis,
+                      double** partial, cudaStream_t s) {
+  if (!phi || res <= 0 || n_phi != 3 * res || res > 1024)
+    return fail(HERMES_ERR_INVALID, "mc: phi must hold 3*res samples with res <= 1024 (n_phi=%d, res=%d)", n_phi, res);
+  size_t need = 0;
+  hermes_mc_workspace_size(&need);
+  if (!workspace || workspace_bytes < need) return fail(HERMES_ERR_WORKSPACE, "mc: workspace %zu < %zu", workspace_bytes, need);
+  hermes::Carver c(workspace, workspace_bytes);
+  *phis = c.take<float>(4 * 1024);
+  *partial = c.take<double>((size_t)mc_grid() + 1);
+  mc_phi_kernel<<<4, 256, 0, s>>>(phi, n_phi, *phis);
+  HERMES_LAUNCH_CHECK("mc_phi_kernel");
+  return HERMES_OK;
+}
+
+extern "C" int hermes_interp(const float* grid, int J, const double* scaled_pos, int64_t n, const double* phi,
+                             int n_phi, int phi_res, double dx, double dy, double dz, double* out, void* workspace,
+                             size_t workspace_bytes, void* stream) {
+  if (!grid || (n > 0 && (!scaled_pos || !out))) return fail(HERMES_ERR_INVALID, "interp: NULL argument");
+  if (J < 2 || J > 10) return fail(HERMES_ERR_INVALID, "interp: J=%d outside [2,10]", J);
+  cudaStream_t s = hermes::as_stream(stream);
+  float* phis;
+  double* partial;
+  int rc = mc_prepare(phi, n_phi, phi_res, workspace, workspace_bytes, &phis, &partial, s);
+  if (rc) return rc;
+  if (n == 0) return HERMES_OK;
+  mc_interp_kernel<<<mc_grid(), 256, 0, s>>>(grid, J, scaled_pos, n, phis, phi_res, dx, dy, dz, out);
+  HERMES_LAUNCH_CHECK("mc_interp_kernel");
+  return HERMES_OK;
+}
+
+extern "C" int hermes_mc_triplets(const float* eps1, const float* eps2, const float* eps3, int J,
+                                  const double* centers, const double* center_w, int64_t n_centers,
+                                  const double* offsets, int n_rot, const double* phi, int n_phi, int phi_res,
+                                  double rho1, double* sum_out, float* samples_out, void* workspace,
+                                  size_t workspace_bytes, void* stream) {
+  if (!eps2 || !eps3 || !sum_out || (n_centers > 0 && !centers) || (n_rot > 0 && !offsets))
+    return fail(HERMES_ERR_INVALID, "mc_triplets: NULL argument");
+  if (J < 2 || J > 10) return fail(HERMES_ERR_INVALID, "mc_triplets: J=%d outside [2,10]", J);
+  if (n_rot < 0 || n_centers < 0) return fail(HERMES_ERR_INVALID, "mc_triplets: negative count");
+  cudaStream_t s = hermes::as_stream(stream);
+  float* phis;
+  double* partial;
+  int rc = mc_prepare(phi, n_phi, phi_res, workspace, workspace_bytes, &phis, &partial, s);
+  if (rc) return rc;
+  const int g = mc_grid();
+  mc_triplet_kernel<<<g, 256, 0, s>>>(eps1, eps2, eps3, J, centers, center_w, n_centers, offsets, n_rot, phis,
+                                      phi_res, rho1, partial, samples_out);
+  HERMES_LAUNCH_CHECK("mc_triplet_kernel");
+  mc_sum_kernel<<<1, 256, 0, s>>>(partial, g, partial + g);
+  HERMES_LAUNCH_CHECK("mc_sum_kernel");
+  HERMES_CUDA_TRY(cudaMemcpyAsync(sum_out, partial + g, sizeof(double), cudaMemcpyDeviceToHost, s));
+  HERMES_CUDA_TRY(cudaStreamSynchronize(s));
+  return HERMES_OK;
+}

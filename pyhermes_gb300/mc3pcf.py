@@ -1,0 +1,488 @@
+"""Monte Carlo 3PCF on the GPU, with an optional learned importance-sampling
+proposal for the triangle centres.
+
+``Corr_3PCF`` mirrors ``pyhermes/theory/corr3pcf.py`` (box-random and
+particle centres, single process): the same parameters (r12, r13, theta or
+mu sampling, n_rot, n_box_centers, base_seed), the same seeds — centres from
+``default_rng(base_seed + 1000003)`` in grid units (:1406-1416,
+utils/sampling.py:6-10), one ``np.random.seed(base_seed + 1 + irot +
+1000003 * mu_index)`` draw of three uniforms per rotation (corr3pcf_kernels.py:
+80-86) — the same products (ddd, rrr, delta_ddd, xi12/13/23, zeta, zeta_H, Q)
+and the scale_factor**9 rescale.  Triplet sums run in
+``hermes_mc_triplets`` (csrc/mc.cu).
+
+``LearnedProposal`` (no reference counterpart): a tanh MLP over
+(r12, r13, mu, local delta) trained with the hand-written kernels of
+csrc/mlp.cu on uniform-MC triplet samples to predict log E_rot[f^2] at a
+centre.  Centres are then drawn from a pool with probability
+q_i = a/M + (1-a) h_i / sum h, h = exp(prediction / 2) (the variance-optimal
+shape sqrt(E f^2), mixed with the uniform pool distribution so weights stay
+bounded), and each sample is weighted by (1/M)/q_i: the estimator stays
+unbiased for the pool mean whatever the network predicts.
+"""
+
+import ctypes
+import math
+import time
+
+import numpy as np
+import torch
+
+from . import _lib
+from .kernels import _ptr, _stream_ptr
+from .params import task_params
+from .phi import sample_scaling_function
+from .sfc_field import SFCField, normalize_task_weight_normalization
+
+_WS = {}
+
+
+def _mc_workspace(device):
+    key = str(device)
+    if key not in _WS:
+        n = ctypes.c_size_t(0)
+        _lib.check(_lib.load().hermes_mc_workspace_size(ctypes.byref(n)), "mc_workspace_size")
+        _WS[key] = torch.empty(n.value, dtype=torch.uint8, device=device)
+    return _WS[key]
+
+
+def generate_triangle_offsets(R1, R2, mu, phi, costheta1, alpha):
+    """utils/corr3pcf_kernels.py:21-63 (float64, same operation order)."""
+    sintheta1 = math.sqrt(1.0 - costheta1 * costheta1)
+    dx1 = sintheta1 * math.cos(phi)
+    dy1 = sintheta1 * math.sin(phi)
+    dz1 = costheta1
+    x2, y2, z2 = R1 * dx1, R1 * dy1, R1 * dz1
+    if abs(dx1) > 1e-10 or abs(dy1) > 1e-10:
+        ox1, oy1, oz1 = -dy1, dx1, 0.0
+    else:
+        ox1, oy1, oz1 = 0.0, -dz1, dy1
+    norm = math.sqrt(ox1 * ox1 + oy1 * oy1 + oz1 * oz1)
+    ox1 /= norm
+    oy1 /= norm
+    oz1 /= norm
+    ox2 = dy1 * oz1 - dz1 * oy1
+    oy2 = dz1 * ox1 - dx1 * oz1
+    oz2 = dx1 * oy1 - dy1 * ox1
+    ca, sa = math.cos(alpha), math.sin(alpha)
+    st2 = 1.0 - mu * mu
+    if st2 < 0.0:
+        st2 = 0.0
+    st = math.sqrt(st2)
+    dx2 = mu * dx1 + st * (ca * ox1 + sa * ox2)
+    dy2 = mu * dy1 + st * (ca * oy1 + sa * oy2)
+    dz2 = mu * dz1 + st * (ca * oz1 + sa * oz2)
+    return x2, y2, z2, R2 * dx2, R2 * dy2, R2 * dz2
+
+
+def rotation_offsets(R1, R2, mu, n_rot, seed_base_rot=-1, mu_index=-1, rng=None):
+    """[n_rot, 6] offsets with the reference's per-rotation seeding (:80-90)."""
+    out = np.empty((n_rot, 6))
+    two_pi = 2.0 * math.pi
+    for irot in range(n_rot):
+        if seed_base_rot >= 0:
+            seed = seed_base_rot + irot
+            if mu_index >= 0:
+                seed += mu_index * 1000003
+            np.random.seed(seed)
+            a, b, c = np.random.rand(3)
+        else:
+            a, b, c = (rng or np.random).rand(3)
+        out[irot] = generate_triangle_offsets(R1, R2, mu, two_pi * a, 2.0 * b - 1.0, two_pi * c)
+    return out
+
+
+def triplet_sum(eps1, eps2, eps3, J, centers, offsets, phi_t, center_w=None, rho1=0.0, samples=False):
+    """sum_i w_i n1_i sum_r n2 n3 (float64) and optionally the per-triplet products."""
+    dev = eps2.device
+    c = torch.as_tensor(np.ascontiguousarray(centers), dtype=torch.float64, device=dev) \
+        if not isinstance(centers, torch.Tensor) else centers
+    o = torch.as_tensor(np.ascontiguousarray(offsets), dtype=torch.float64, device=dev)
+    w = None if center_w is None else torch.as_tensor(center_w, dtype=torch.float64, device=dev)
+    nc, nr = c.shape[0], o.shape[0]
+    smp = torch.empty((nc, nr), dtype=torch.float32, device=dev) if samples else None
+    ws = _mc_workspace(dev)
+    out = ctypes.c_double(0.0)
+    rc = _lib.load().hermes_mc_triplets(_ptr(eps1), _ptr(eps2), _ptr(eps3), J, _ptr(c), _ptr(w), nc, _ptr(o), nr,
+                                        _ptr(phi_t), phi_t.numel(), phi_t.numel() // 3, float(rho1),
+                                        ctypes.byref(out), _ptr(smp), _ptr(ws), ws.numel(), _stream_ptr(dev))
+    _lib.check(rc, "hermes_mc_triplets")
+    return out.value, smp
+
+
+def interp(grid, J, scaled_pos, phi_t, offset=(0.0, 0.0, 0.0)):
+    dev = grid.device
+    p = torch.as_tensor(np.ascontiguousarray(scaled_pos), dtype=torch.float64, device=dev) \
+        if not isinstance(scaled_pos, torch.Tensor) else scaled_pos
+    out = torch.empty(p.shape[0], dtype=torch.float64, device=dev)
+    ws = _mc_workspace(dev)
+    rc = _lib.load().hermes_interp(_ptr(grid), J, _ptr(p), p.shape[0], _ptr(phi_t), phi_t.numel(),
+                                   phi_t.numel() // 3, float(offset[0]), float(offset[1]), float(offset[2]),
+                                   _ptr(out), _ptr(ws), ws.numel(), _stream_ptr(dev))
+    _lib.check(rc, "hermes_interp")
+    return out
+
+
+PRODUCT_DEPS = {"Q": ["zeta", "zeta_H"], "zeta_H": ["xi12", "xi13", "xi23"], "zeta": ["delta_ddd", "rrr"]}
+ALLOWED = {"ddd", "rrr", "delta_ddd", "xi12", "xi13", "xi23", "zeta", "zeta_H", "Q"}
+
+
+class Corr3PCFData:
+    def __init__(self):
+        for k in ("mu", "theta", "r23", "ddd", "rrr", "d_delta_dd", "r_delta_dd", "delta_ddd", "xi12", "xi13",
+                  "xi23", "zeta", "zeta_H", "Q"):
+            setattr(self, k, None)
+        self.corr3pcf_info = {}
+
+
+class Corr_3PCF:
+    task_name = "Corr_3PCF"
+
+    def __init__(self, param_task=None, device="cuda"):
+        tp = task_params(self.task_name, param_task)
+        self.task_params = tp
+        self.device = torch.device(device)
+        self.sfc_field = tp.get("sfc_field", "")
+        for i in (1, 2, 3):
+            setattr(self, f"sfc_field{i}", tp.get(f"sfc_field{i}", "") or self.sfc_field)
+            r = tp.get(f"random{i}")
+            setattr(self, f"random{i}", tp.get("random") if r in (None, "") else r)
+        self.weight_normalization = normalize_task_weight_normalization(tp.get("weight_normalization", "catalog"))
+        self.r12, self.r13 = float(tp["r12"]), float(tp["r13"])
+        self.n_rot = int(tp["n_rot"])
+        self.center = tp["center"]
+        if self.center not in ("box_random", "particle"):
+            raise ValueError(f"Unknown center='{self.center}'. Use 'box_random' or 'particle'.")
+        self.n_box_centers = int(tp["n_box_centers"])
+        self.base_seed = int(tp["base_seed"])
+        self.particle_pos1 = tp.get("particle_pos1")
+        self.particle_weight1 = tp.get("particle_weight1")
+        prods = tp.get("products", "Q")
+        prods = [prods] if isinstance(prods, str) else list(prods)
+        out = []
+        for p in prods:
+            p = str(p).strip()
+            if p not in ALLOWED:
+                raise ValueError(f"Unsupported product '{p}'.")
+            if p not in out:
+                out.append(p)
+        i = 0
+        while i < len(out):
+            for d in PRODUCT_DEPS.get(out[i], []):
+                if d not in out:
+                    out.append(d)
+            i += 1
+        self.expanded = out
+        ap = str(tp["angle_param"]).strip().lower()
+        if ap == "theta":
+            t = tp["theta"]
+            if isinstance(t, dict):
+                self.theta_arr = np.linspace(float(t.get("theta_min", 0.0)), float(t.get("theta_max", math.pi)),
+                                             int(t.get("n_theta", 20)))
+            else:
+                self.theta_arr = np.asarray(t, dtype=np.float64)
+            self.mu_arr = np.cos(self.theta_arr)
+        elif ap == "mu":
+            m = tp["mu"]
+            if isinstance(m, dict):
+                self.mu_arr = np.linspace(float(m.get("mu_min", -1.0)), float(m.get("mu_max", 1.0)),
+                                          int(m.get("n_mu", 20)))
+            else:
+                self.mu_arr = np.asarray(m, dtype=np.float64)
+            self.theta_arr = np.arccos(np.clip(self.mu_arr, -1.0, 1.0))
+        else:
+            raise ValueError(f"Unsupported angle_param='{tp['angle_param']}'. Use 'theta' or 'mu'.")
+
+    def _field(self, v, what):
+        if isinstance(v, SFCField):
+            f = v
+        elif isinstance(v, str) and v:
+            f = SFCField(data_path=v, device=self.device)
+        else:
+            raise ValueError(f"Missing usable input for {what}.")
+        self._density_physical_scale = float(f.scale_factor) ** 3
+        if self.weight_normalization == "unit":
+            return f.with_normalization("unit")
+        if getattr(f, "field_kind", None) != "catalog_field":
+            return f.copy()
+        return f.switch_weight_normalization(self.weight_normalization)
+
+    def _rand(self, i, ref):
+        r = getattr(self, f"random{i}")
+        if r == "uniform":
+            return float(ref.field_mean_density(value_unit="grid"))
+        if r is None or r == "":
+            return None
+        return self._field(r, f"random vertex {i}")
+
+    @staticmethod
+    def _density(x):
+        return float(x) if isinstance(x, float) else float(x.field_mean_density(value_unit="grid"))
+
+    def _pair(self, radius, a, b):
+        """corr3pcf.py:730-734 via the Parseval pair-product engine (shell window)."""
+        if isinstance(a, float) or isinstance(b, float):
+            return self._density(a) * self._density(b)
+        from .corr2pcf import Corr_2PCF
+
+        t = Corr_2PCF({"Corr_2PCF": {"sfc_field1": a, "sfc_field2": b, "weight_normalization": "raw",
+                                     "binning_window": {"type": "shell", "len_args": ["R"], "mapping": "s_to_R"},
+                                     "sampling": {"s": np.atleast_1d(radius)}, "products": ["dd"]}},
+                      device=self.device)
+        t._field_in_task_normalization = lambda f: f
+        t.prepare_input_fields()
+        t._density_physical_scale = 1.0
+        return np.asarray(t.run(save_result=False).dd)
+
+    def run(self, save_result=False, overwrite=False):
+        data = {i: self._field(getattr(self, f"sfc_field{i}"), f"field vertex {i}") for i in (1, 2, 3)}
+        ref = data[1]
+        rand = {i: self._rand(i, data[i]) for i in (1, 2, 3)}
+        L, J = ref.L, ref.J
+        phi = ref.sfc_info.get("phi_array")
+        if phi is None:
+            phi = sample_scaling_function(ref.wavelet_mode, ref.wavelet_level)
+        phi_t = torch.as_tensor(np.asarray(phi, dtype=np.float64), device=self.device)
+        sf = float(ref.scale_factor)
+        r12s, r13s = self.r12 * sf, self.r13 * sf
+        eps = {i: data[i].epsilon_device.to(torch.float32).contiguous() for i in (1, 2, 3)}
+
+        def delta(i):
+            r = rand[i]
+            if isinstance(r, float):
+                return (data[i].epsilon_device.double() - r).float().contiguous()
+            return (data[i].epsilon_device.double() - r.epsilon_device.double()).float().contiguous()
+
+        if self.center == "box_random":
+            rng = np.random.default_rng(self.base_seed + 1000003 * 1)
+            centers = rng.uniform(0.0, float(L), size=(self.n_box_centers, 3))
+            weights, wsum, rho1 = None, float(self.n_box_centers), 0.0
+        else:
+            if self.particle_pos1 is None:
+                raise ValueError("center='particle' needs particle_pos1 (catalogue re-reading is not part of this package).")
+            centers = np.asarray(self.particle_pos1, dtype=np.float64) * sf
+            weights = np.ones(centers.shape[0]) if self.particle_weight1 is None else \
+                np.asarray(self.particle_weight1, dtype=np.float64)
+            wsum = float(weights.sum())
+            rho1 = wsum / float(L) ** 3
+        c_t = torch.as_tensor(centers, dtype=torch.float64, device=self.device)
+        res = {}
+        seed_base_rot = self.base_seed + 1
+        loop = [p for p in ("ddd", "delta_ddd") if p in self.expanded]
+        for prod in loop:
+            vals = np.zeros(self.mu_arr.size)
+            if prod == "ddd":
+                e1, e2, e3 = eps[1], eps[2], eps[3]
+            else:
+                e1, e2, e3 = delta(1), delta(2), delta(3)
+            for it, mu in enumerate(self.mu_arr):
+                off = rotation_offsets(r12s, r13s, float(mu), self.n_rot, seed_base_rot, it)
+                if self.center == "box_random":
+                    s, _ = triplet_sum(e1, e2, e3, J, c_t, off, phi_t)
+                    vals[it] = s / (self.n_rot * centers.shape[0])
+                else:
+                    s, _ = triplet_sum(None, e2, e3, J, c_t, off, phi_t, center_w=weights, rho1=rho1)
+                    vals[it] = rho1 * s / (self.n_rot * wsum)
+            res[prod] = vals
+        if "rrr" in self.expanded:
+            n_uniform = sum(isinstance(rand[i], float) for i in (1, 2, 3))
+            if n_uniform >= 2:
+                res["rrr"] = np.full(self.mu_arr.size, self._density(rand[1]) * self._density(rand[2])
+                                     * self._density(rand[3]))
+            else:
+                raise NotImplementedError("rrr with fewer than two uniform random vertices")
+        scale = float(getattr(self, "_density_physical_scale", 1.0)) ** 3
+        for p in ("ddd", "rrr", "delta_ddd"):
+            if p in res:
+                res[p] = res[p] * scale
+        out = Corr3PCFData()
+        out.mu, out.theta = self.mu_arr, self.theta_arr
+        out.r23 = np.sqrt(np.clip(self.r12 ** 2 + self.r13 ** 2 - 2 * self.r12 * self.r13 * self.mu_arr, 0, None))
+        for p in ("ddd", "rrr", "delta_ddd"):
+            setattr(out, p, res.get(p))
+        if any(p in self.expanded for p in ("xi12", "xi13", "xi23")):
+            out.xi12 = self._xi(self.r12, data[1], data[2], rand[1], rand[2])
+            out.xi13 = self._xi(self.r13, data[1], data[3], rand[1], rand[3])
+            out.xi23 = self._xi(out.r23, data[2], data[3], rand[2], rand[3])
+        if "zeta" in self.expanded:
+            out.zeta = out.delta_ddd / out.rrr
+        if "zeta_H" in self.expanded:
+            out.zeta_H = out.xi12 * out.xi13 + out.xi12 * out.xi23 + out.xi13 * out.xi23
+        if "Q" in self.expanded:
+            out.Q = out.zeta / out.zeta_H
+        self.corr3pcf_data = out
+        return out
+
+    def _xi(self, radius, fa, fb, ra, rb):
+        """corr3pcf.py:1011-1036: xi = delta_dd / rr with shell pair products."""
+        rr = self._pair(radius, ra, rb)
+        da = fa - (ra if isinstance(ra, float) else ra)
+        db = fb - (rb if isinstance(rb, float) else rb)
+        dd = self._pair(radius, da, db)
+        return np.asarray(dd) / np.asarray(rr)
+
+
+# ---------------------------------------------------------------------------
+# learned proposal
+# ---------------------------------------------------------------------------
+class MLP:
+    """tanh MLP trained and run with the kernels of csrc/mlp.cu."""
+
+    def __init__(self, dims=(4, 128, 128, 128, 1), device="cuda", seed=0):
+        self.dims = list(dims)
+        self.device = torch.device(device)
+        self.cdims = (ctypes.c_int32 * len(self.dims))(*self.dims)
+        n = ctypes.c_int64(0)
+        _lib.check(_lib.load().hermes_mlp_param_count(self.cdims, len(self.dims) - 1, ctypes.byref(n)),
+                   "mlp_param_count")
+        self.n_params = n.value
+        g = torch.Generator().manual_seed(seed)
+        parts = []
+        for a, b in zip(self.dims[:-1], self.dims[1:]):
+            parts.append((torch.randn(a, b, generator=g) * math.sqrt(1.0 / a)).reshape(-1))
+            parts.append(torch.zeros(b))
+        self.params = torch.cat(parts).to(self.device, torch.float32).contiguous()
+        self.m = torch.zeros_like(self.params)
+        self.v = torch.zeros_like(self.params)
+        self.step_count = 0
+        self.params_bf16 = None
+
+    def _acts(self, batch):
+        return torch.empty(sum(batch * d for d in self.dims[1:]), dtype=torch.float32, device=self.device)
+
+    def forward(self, x, bf16=False, return_acts=False):
+        x = x.to(torch.float32).contiguous()
+        acts = self._acts(x.shape[0])
+        lib = _lib.load()
+        if bf16:
+            if self.params_bf16 is None:
+                self.params_bf16 = torch.empty(self.n_params, dtype=torch.bfloat16, device=self.device)
+                _lib.check(lib.hermes_to_bf16(_ptr(self.params), self.n_params, _ptr(self.params_bf16),
+                                              _stream_ptr(self.device)), "to_bf16")
+            rc = lib.hermes_mlp_forward(None, _ptr(self.params_bf16), self.cdims, len(self.dims) - 1, _ptr(x),
+                                        x.shape[0], _ptr(acts), _stream_ptr(self.device))
+        else:
+            rc = lib.hermes_mlp_forward(_ptr(self.params), None, self.cdims, len(self.dims) - 1, _ptr(x), x.shape[0],
+                                        _ptr(acts), _stream_ptr(self.device))
+        _lib.check(rc, "hermes_mlp_forward")
+        y = acts[-x.shape[0] * self.dims[-1]:].view(x.shape[0], self.dims[-1])
+        return (y, acts) if return_acts else y
+
+    def grads(self, x, target):
+        """(loss, gradient of the mean squared error) for one batch."""
+        lib = _lib.load()
+        x = x.to(torch.float32).contiguous()
+        y, acts = self.forward(x, return_acts=True)
+        t = target.to(torch.float32).reshape(-1).contiguous()
+        dy = torch.empty_like(t)
+        loss = ctypes.c_double(0.0)
+        scratch_d = torch.empty(1, dtype=torch.float64, device=self.device)
+        _lib.check(lib.hermes_mse_grad(_ptr(y.reshape(-1).contiguous()), _ptr(t), t.numel(), _ptr(dy),
+                                       ctypes.byref(loss), _ptr(scratch_d), _stream_ptr(self.device)), "mse_grad")
+        n = ctypes.c_int64(0)
+        lib.hermes_mlp_scratch_floats(x.shape[0], ctypes.byref(n))
+        scratch = torch.empty(n.value, dtype=torch.float32, device=self.device)
+        g = torch.empty_like(self.params)
+        _lib.check(lib.hermes_mlp_backward(_ptr(self.params), self.cdims, len(self.dims) - 1, _ptr(x), x.shape[0],
+                                           _ptr(acts), _ptr(dy), _ptr(g), _ptr(scratch), _stream_ptr(self.device)),
+                   "mlp_backward")
+        return loss.value, g
+
+    def adam(self, g, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8):
+        self.step_count += 1
+        self.params_bf16 = None
+        _lib.check(_lib.load().hermes_adam_step(_ptr(self.params), _ptr(g), _ptr(self.m), _ptr(self.v),
+                                                self.n_params, lr, b1, b2, eps, self.step_count,
+                                                _stream_ptr(self.device)), "adam_step")
+
+    def train(self, x, t, epochs=5, batch=8192, lr=2e-3, seed=0):
+        n = x.shape[0]
+        gen = torch.Generator(device=self.device).manual_seed(seed)
+        losses = []
+        for _ in range(epochs):
+            perm = torch.randperm(n, device=self.device, generator=gen)
+            for s in range(0, n - batch + 1, batch):
+                idx = perm[s:s + batch]
+                loss, g = self.grads(x[idx], t[idx])
+                self.adam(g, lr=lr)
+                losses.append(loss)
+        return losses
+
+
+class LearnedProposal:
+    """Importance sampling of triangle centres with a trained MLP proposal."""
+
+    def __init__(self, eps1, eps2, eps3, J, phi, rho, device="cuda", mix=0.2):
+        self.e1, self.e2, self.e3 = (e.to(torch.float32).contiguous() for e in (eps1, eps2, eps3))
+        self.J, self.L = J, 1 << J
+        self.phi_t = torch.as_tensor(np.asarray(phi, dtype=np.float64), device=device)
+        self.rho = float(rho)
+        self.device = torch.device(device)
+        self.mix = mix
+        self.net = MLP(device=device)
+
+    def features(self, centers, r12s, r13s, mu):
+        n1 = interp(self.e1, self.J, centers, self.phi_t)
+        dl = (n1 / self.rho - 1.0).clamp(-1.0, 50.0)
+        f = torch.stack([torch.full_like(dl, r12s / self.L * 10), torch.full_like(dl, r13s / self.L * 10),
+                         torch.full_like(dl, mu), torch.log1p(dl.clamp_min(-0.99))], dim=1)
+        return f.float()
+
+    def training_data(self, configs, n_centers, n_rot_train, seed=0):
+        """Uniform-MC samples: features and target log(mean_r f^2 / scale^2)."""
+        X, T = [], []
+        rng = np.random.default_rng(seed)
+        for (r12s, r13s, mu) in configs:
+            c = torch.as_tensor(rng.uniform(0.0, float(self.L), (n_centers, 3)), device=self.device)
+            off = rotation_offsets(r12s, r13s, mu, n_rot_train, rng=np.random.RandomState(rng.integers(1 << 31)))
+            _, smp = triplet_sum(self.e1, self.e2, self.e3, self.J, c, off, self.phi_t, samples=True)
+            m2 = (smp.double() ** 2).mean(dim=1) / self.rho ** 6
+            X.append(self.features(c, r12s, r13s, mu))
+            T.append(torch.log(m2 + 1e-12).float())
+        return torch.cat(X), torch.cat(T)
+
+    def train(self, configs, n_centers=200_000, n_rot_train=8, epochs=4, seed=0):
+        X, T = self.training_data(configs, n_centers, n_rot_train, seed)
+        self.t_mean = float(T.mean())
+        self.t_std = float(T.std()) + 1e-6
+        return self.net.train(X, (T - self.t_mean) / self.t_std, epochs=epochs, seed=seed)
+
+    def proposal(self, pool, r12s, r13s, mu, bf16=True):
+        pred = self.net.forward(self.features(pool, r12s, r13s, mu), bf16=bf16).reshape(-1).double()
+        logh = 0.5 * (pred * self.t_std + self.t_mean)
+        h = torch.exp(logh - logh.max())
+        M = pool.shape[0]
+        q = self.mix / M + (1.0 - self.mix) * h / h.sum()
+        return q
+
+    def estimate(self, pool, r12s, r13s, mu, n_samples, seed=0, uniform=False, bf16=True):
+        """Mean over the pool of E_rot[f]: returns (estimate, per-sample values)."""
+        gen = torch.Generator(device=self.device).manual_seed(seed)
+        M = pool.shape[0]
+        if uniform:
+            idx = torch.randint(0, M, (n_samples,), generator=gen, device=self.device)
+            wts = torch.ones(n_samples, dtype=torch.float64, device=self.device)
+        else:
+            q = self.proposal(pool, r12s, r13s, mu, bf16=bf16)
+            cdf = torch.cumsum(q, 0)
+            u = torch.rand(n_samples, generator=gen, device=self.device, dtype=torch.float64) * cdf[-1]
+            idx = torch.searchsorted(cdf, u).clamp_max(M - 1)
+            wts = (1.0 / M) / q[idx]
+        rs = np.random.RandomState(seed)
+        off = rotation_offsets(r12s, r13s, mu, n_samples, rng=rs)
+        # one rotation per sampled centre: evaluate f_k = n1 n2 n3 at (centre_k, rotation_k)
+        cen = pool[idx]
+        vals = torch.empty(n_samples, dtype=torch.float64, device=self.device)
+        chunk = 1 << 20
+        for s in range(0, n_samples, chunk):
+            e = min(n_samples, s + chunk)
+            vals[s:e] = self._f_pairs(cen[s:e], off[s:e])
+        v = vals * wts
+        return float(v.mean()), v
+
+    def _f_pairs(self, centers, offsets):
+        o = torch.as_tensor(offsets, device=self.device)
+        n1 = interp(self.e1, self.J, centers, self.phi_t)
+        n2 = interp(self.e2, self.J, centers + o[:, 0:3], self.phi_t)
+        n3 = interp(self.e3, self.J, centers + o[:, 3:6], self.phi_t)
+        return n1 * n2 * n3

@@ -210,7 +210,30 @@ def gen_multipole():
     _save("multipole_J4", **out)
 
 
-SECTIONS = {"phi": gen_phi, "deposit": gen_deposit, "windows": gen_windows,
+def gen_mc3pcf():
+    from pyhermes.theory.corr3pcf import Corr_3PCF
+    from pyhermes.utils.corr3pcf_kernels import generate_triangle_offsets
+
+    rng = np.random.default_rng(31)
+    pos = rng.uniform(0.0, 1000.0, (4000, 3))
+    pos[:1500] = pos[:1500] * 0.3 + 300.0
+    w = rng.lognormal(0.0, 0.3, 4000)
+    f = _projection(pos, 4, weights=w)
+    out = {"pos": pos, "weights": w}
+    offs = [generate_triangle_offsets(2.0, 3.5, m, p, c, a)
+            for m, p, c, a in [(0.3, 1.0, 0.2, 2.0), (-0.7, 4.0, -0.9, 0.5), (0.999, 0.1, 0.9999, 6.0)]]
+    out["offsets"] = np.array(offs)
+    task = Corr_3PCF({"Corr_3PCF": {
+        "sfc_field": f, "random": "uniform", "r12": 150.0, "r13": 250.0, "angle_param": "mu",
+        "mu": {"mu_min": -0.8, "mu_max": 0.8, "n_mu": 3}, "n_rot": 3, "center": "box_random",
+        "n_box_centers": 600, "base_seed": 42, "products": ["Q", "ddd"]}})
+    d = task.run(save_result=False)
+    for k in ("mu", "ddd", "rrr", "delta_ddd", "xi12", "xi13", "xi23", "zeta", "zeta_H", "Q"):
+        out["box_" + k] = np.asarray(getattr(d, k))
+    _save("mc3pcf_J4", **out)
+
+
+SECTIONS = {"mc3pcf": gen_mc3pcf, "phi": gen_phi, "deposit": gen_deposit, "windows": gen_windows,
             "convolution": gen_convolution, "corr2pcf": gen_corr2pcf, "multipole": gen_multipole}
 
 
