@@ -184,7 +184,10 @@ int hermes_pair_products(const void* const* spectra, int n_spec, const int32_t* 
  * hermes_multipole_fields: for a real field with half spectrum `half_spec`
  * (float2 [L,L,L/2+1], from hermes_fft_r2c) and thin-shell radii `radii`
  * (host, grid units, nb <= 16), writes
- *   fields_out[b] = ifftn(fftn(eps) * K_lm^b)   (complex64 [L^3] each)
+ *   a_lm^b = ifftn(fftn(eps) * K_lm^b)
+ * into fields_out, complex64 and bin-interleaved: [L^3][16] (cell c, bin b at
+ * c*16 + b; slots b >= nb are unspecified) when nb > 1, plain [L^3] when
+ * nb == 1,
  * with K_lm^b the radial-multipole window of radial_multipole_windows.py:
  * 128-183 (shell profile: j_l(2 pi |k| R_b) Y_lm(khat), 8 phi-weighted
  * images; phi_power: L+1 float64 samples).
@@ -192,7 +195,8 @@ int hermes_pair_products(const void* const* spectra, int n_spec, const int32_t* 
  * hermes_multipole_contract: S[b2][b3] (host float64 complex, [nb2][nb3][2])
  *   = 4 pi / L^3 sum_x eps1(x) sum_{l1,l2} Gamma3(l1,l2) a2^{b2}(x-l1) a3^{b3}(x-l2)
  * for every bin pair (corr3pcf_multipoles.py:33-58 + :451), with
- * a2 = fields2 and a3 = fields3, or a3 = conj_sign * conj(fields2) when
+ * a2 = fields2 and a3 = fields3 (each in the layout hermes_multipole_fields
+ * writes for its nb), or a3 = conj_sign * conj(fields2) when
  * fields3 is NULL (the a_{l,-m} = (-1)^{l+m} conj(a_{lm}) identity for a
  * shared field and shared bins).  gamma: host float64 [3][3] triple overlaps
  * (corr3pcf_multipoles.py:22-30).  Synchronises `stream`.

@@ -12,11 +12,15 @@
 //                        |k|^2 grid (float32, double-float phase)
 //   mp_prepass_kernel    eps_hat(k) K_lm^b(k) / L^3 for every bin b, Y_lm
 //                        shared by the bins, written as a batch of spectra
-//   cuFFT (batched C2C)  -> a_lm^b(x) for every bin
-//   mp_gfield_kernel     G^b(y) = sum_{l1,l2} Gamma3 eps1(y+l1) a3^b(y+l1-l2)
-//                        (separable shared-memory passes)
-//   mp_gemm_kernel       S[b1,b2] = sum_y a2^{b1}(y) G^{b2}(y): the bin x bin
-//                        product over cells, float32 tiles, float64 partials
+//   cuFFT (batched C2C)  -> a_lm^b(x) for every bin; fields are stored
+//                        bin-interleaved, [cell][16], so one cell's bins are
+//                        one 128-byte line (istride 16 for cuFFT)
+//   mp_contract_kernel   persistent: per output tile, for every bin b3,
+//                        G^b3(y) = sum_{l1,l2} Gamma3 eps1(y+l1) a3^b3(y+l1-l2)
+//                        by separable shared-memory passes into a tile of G in
+//                        shared memory, then S[b2,b3] += sum_y a2^{b2}(y) G^b3(y)
+//                        (the bin x bin product over cells), float32 per tile,
+//                        float64 per thread
 //   mp_reduce_kernel     float64 cross-block reduction
 // The identity S = sum_y a2(y) G3(y) is the reference sum with y = x - l1.
 // mp_plain_kernel is the reference-form contraction of one (a2, a3) pair
@@ -32,7 +36,7 @@
 #include "window_eval.cuh"
 
 namespace hermes {
-int get_plan_c2c_batch(int J, int batch, cufftHandle* out);
+int get_plan_c2c_interleaved(int J, int batch, int stride, cufftHandle* out);
 }
 
 namespace {
@@ -43,6 +47,7 @@ using hermes::df_sqrt_int;
 using hermes::fail;
 
 constexpr int kMaxBins = 16;
+constexpr int kBinStride = 16;  // interleaved field layout [cell][kBinStride]
 constexpr float kFourPiInvSqrt = 0.28209479177387814f;  // 1/sqrt(4 pi)
 
 // ---- spherical Bessel j_l in float32 --------------------------------------
@@ -98,13 +103,18 @@ __device__ float sph_jl_f32(int l, float xh, float xl) {
   return jc;
 }
 
-// T[n2 * nb + b] = j_l(2 pi sqrt(n2) R_b / L), n2 = 0 .. n2max.
+// T[n2 * kBinStride + b] = j_l(2 pi sqrt(n2) R_b / L), n2 = 0 .. n2max (rows
+// padded to 16 floats so one image's bins are four float4 loads).
 __global__ void mp_jl_table_kernel(float* __restrict__ T, int n2max, const float* __restrict__ rho,
                                    int nb, int l) {
-  const long long total = (long long)(n2max + 1) * nb;
+  const long long total = (long long)(n2max + 1) * kBinStride;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
        i += (long long)gridDim.x * blockDim.x) {
-    const int n2 = (int)(i / nb), b = (int)(i % nb);
+    const int n2 = (int)(i / kBinStride), b = (int)(i % kBinStride);
+    if (b >= nb) {
+      T[i] = 0.f;
+      continue;
+    }
     float nh, nl, xh, xl;
     df_sqrt_int(n2, nh, nl);
     df_mul(nh, nl, rho[2 * b], rho[2 * b + 1], xh, xl);
@@ -161,12 +171,15 @@ __device__ __forceinline__ float2 ylm_at(const YlmConst& Y, int a, int b, int c,
   return make_float2(yr, yi);
 }
 
-// out[b][k] = eps_hat(k) * K_lm^b(k) / L^3 on the full FFT grid; eps_hat
-// comes from the half spectrum of a real field (Hermitian expansion).
-template <int NB>
+// out[k * stride + b] = eps_hat(k) * K_lm^b(k) / L^3 on the full FFT grid;
+// eps_hat comes from the half spectrum of a real field (Hermitian expansion).
+// NB4 = number of float4 groups of bins handled (bins padded to 4*NB4).
+template <int NB4>
 __global__ void __launch_bounds__(256)
 mp_prepass_kernel(const float2* __restrict__ half, int J, const float* __restrict__ P,
-                  const float* __restrict__ T, YlmConst Y, int nb, float2* __restrict__ out, float inv_n) {
+                  const float4* __restrict__ T4, YlmConst Y, int nb, int stride, float2* __restrict__ out,
+                  float inv_n) {
+  constexpr int NB = 4 * NB4;
   const int L = 1 << J, H = L / 2 + 1, Lm = L - 1;
   const long long N = 1LL << (3 * J);
   for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < N;
@@ -194,192 +207,367 @@ mp_prepass_kernel(const float2* __restrict__ half, int J, const float* __restric
           const float pw = pa[i] * pb[j] * pc[k];
           const float2 yv = ylm_at(Y, ia[i], ib[j], ic[k], n2);
           const float yr = pw * yv.x, yi = pw * yv.y;
-          const float* tr = T + (long long)n2 * nb;
+          const float4* tr = T4 + (long long)n2 * (kBinStride / 4);
 #pragma unroll
-          for (int b = 0; b < NB; ++b) {
-            if (b < nb) {
-              const float jl = __ldg(tr + b);
-              accr[b] = fmaf(jl, yr, accr[b]);
-              acci[b] = fmaf(jl, yi, acci[b]);
-            }
+          for (int q = 0; q < NB4; ++q) {
+            const float4 jl = __ldg(tr + q);
+            accr[4 * q + 0] = fmaf(jl.x, yr, accr[4 * q + 0]);
+            acci[4 * q + 0] = fmaf(jl.x, yi, acci[4 * q + 0]);
+            accr[4 * q + 1] = fmaf(jl.y, yr, accr[4 * q + 1]);
+            acci[4 * q + 1] = fmaf(jl.y, yi, acci[4 * q + 1]);
+            accr[4 * q + 2] = fmaf(jl.z, yr, accr[4 * q + 2]);
+            acci[4 * q + 2] = fmaf(jl.z, yi, acci[4 * q + 2]);
+            accr[4 * q + 3] = fmaf(jl.w, yr, accr[4 * q + 3]);
+            acci[4 * q + 3] = fmaf(jl.w, yi, acci[4 * q + 3]);
           }
         }
     const float er = e.x * inv_n, ei = e.y * inv_n;
+    if (stride == 1) {
+      out[idx] = make_float2(er * accr[0] - ei * acci[0], er * acci[0] + ei * accr[0]);
+    } else {
+      float4* o4 = reinterpret_cast<float4*>(out + idx * stride);
 #pragma unroll
-    for (int b = 0; b < NB; ++b)
-      if (b < nb) out[(long long)b * N + idx] = make_float2(er * accr[b] - ei * acci[b], er * acci[b] + ei * accr[b]);
+      for (int q = 0; q < NB / 2; ++q) {
+        if (2 * q < nb)
+          o4[q] = make_float4(er * accr[2 * q] - ei * acci[2 * q], er * acci[2 * q] + ei * accr[2 * q],
+                              er * accr[2 * q + 1] - ei * acci[2 * q + 1], er * acci[2 * q + 1] + ei * accr[2 * q + 1]);
+      }
+    }
   }
 }
 
-// ---- G fields ------------------------------------------------------------
-// Output tile TXxTYxTZ cells; a3 halo [-2, +2]; eps1 halo [0, +2].
-constexpr int GX = 4, GY = 8, GZ = 16;
-constexpr int GThreads = 512;
-constexpr int AX_ = GX + 4, AY_ = GY + 4, AZ_ = GZ + 4;    // a3 halo 8x12x20
-constexpr int ZY_ = GY + 4, ZZ_ = GZ + 2;                    // z-pass region 8x12x18
-constexpr int YY_ = GY + 2;                                  // y-pass region 8x10x18
-constexpr int EX_ = GX + 2, EY_ = GY + 2, EZ_ = GZ + 2;      // eps halo 6x10x18
-constexpr int kA3 = AX_ * AY_ * AZ_;
-constexpr int kAz = AX_ * ZY_ * ZZ_;
-constexpr int kAyz = AX_ * YY_ * ZZ_;
-constexpr int kEps = EX_ * EY_ * EZ_;
+// ---- contraction: ε-weighted pair stencil + bin x bin product ----------------
+// With Gamma3 = Gx (x) Gy (x) Gz and x_e = y_x + l1x, delta = l2x:
+//   G(y)  = sum_{l1x, delta} Gx[l1x][delta] T_delta(y_x + l1x; y_y, y_z)
+//   T_d(x_e; c) = sum_{u in [-2,2]^2} V_u(x_e; c) a3(x_e - d, c + u)
+//   V_u(x_e; c) = sum_{l1y, l1z} Gy[l1y][l1y-uy] Gz[l1z][l1z-uz] eps1(x_e, c + l1)
+// (terms with l1 - u outside [0,2] vanish).  V is bin independent, so a CTA
+// computes it once per x-plane for its 8x8 column tile and every bin lane
+// reuses it.  The CTA marches along x over a chunk of CX planes: plane x_a of
+// a3 (12x12 cells x 16 bins, 128-byte rows) is staged with cp.async, T_d for
+// d = 0..2 comes from that one plane, and G(x_a - 2) is complete after the
+// step and is multiplied into S[b2][b3] += a2^{b2} G^{b3}.
+// Thread mapping: lane & 15 = bin b3, each half-warp owns 2x2 columns.
+// Per cell and bin: 75 + 9 complex*real FMAs for G, 16 complex FMAs for S.
+namespace ct {
+constexpr int TY = 8, TZ = 8;              // column tile (y, z)
+constexpr int HY = TY + 4, HZ = TZ + 4;    // a3 plane region (halo 2)
+constexpr int EY = TY + 2, EZ = TZ + 2;    // eps plane region (halo +2)
+constexpr int kCols = TY * TZ;
+constexpr int kGroups = kCols / 4;         // 2x2 column groups
+constexpr int kThreads = kGroups * 16;     // 256
+constexpr int kWarps = kThreads / 32;
+constexpr int kVRow = 8;                   // floats per (column, uy) row of V; 5 used
+constexpr int kVCol = 5 * kVRow + 4;       // floats per column (pad: conflict-free V stores)
+constexpr int kVPlane = kCols * kVCol;
+constexpr int kA3Plane = HY * HZ * kBinStride;  // float2
+constexpr int kA2Stride = kBinStride + 2;       // float2 per cell (pad: no bank conflicts)
+constexpr int kA2Plane = kCols * kA2Stride;
+constexpr int kEpsPlane = EY * EZ;
+constexpr int kMaxCX = 64;
+// a3 planes x2, a2 planes x3, V ring x3, eps planes x2, one G plane, float64 S
+constexpr size_t kSmem = sizeof(float2) * (2 * kA3Plane + 3 * kA2Plane + kA2Plane) +
+                         sizeof(float) * (3 * kVPlane + 2 * kEpsPlane) + sizeof(double) * 2 * kMaxBins * kMaxBins;
+}  // namespace ct
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
 
 struct GammaC {
   float g[9];  // Gamma[l1][l2], row-major
 };
 
-// a3 source: fields3 (nb3 fields) or sign * conj(fields2)
-__global__ void __launch_bounds__(GThreads)
-mp_gfield_kernel(const float* __restrict__ eps1, const float2* __restrict__ src, int conj_src, float sign,
-                 int nb, int J, GammaC gm, float2* __restrict__ gout) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  float2* a3 = reinterpret_cast<float2*>(smem_raw);          // kA3 (aliased by ayz)
-  float2* ayz = a3;                                            // 9 * kAyz
-  float2* az = ayz + 9 * kAyz;                                 // 3 * kAz
-  float* eh = reinterpret_cast<float*>(az + 3 * kAz);         // kEps
-  const int L = 1 << J, Lm = L - 1;
-  const long long N = 1LL << (3 * J);
-  const int ntz = L / GZ, nty = L / GY;
-  const int tile = blockIdx.x;
-  const int x0 = (tile / (ntz * nty)) * GX, y0 = ((tile / ntz) % nty) * GY, z0 = (tile % ntz) * GZ;
-  const int tid = threadIdx.x;
+struct ContractArgs {
+  const float* eps1;
+  const float2* f2;
+  const float2* src3;
+  int s2, s3;        // field strides (kBinStride, or 1 for a single bin)
+  int conj_src;      // a3 = sign * conj(src3)
+  float sign;
+  int J, CX;
+  GammaC gm;
+  double* partial;   // [gridDim.x][16][16][2]
+};
 
-  for (int i = tid; i < kEps; i += blockDim.x) {
-    const int z = i % EZ_, y = (i / EZ_) % EY_, x = i / (EZ_ * EY_);
-    eh[i] = eps1[(((long long)((x0 + x) & Lm)) * L + ((y0 + y) & Lm)) * L + ((z0 + z) & Lm)];
-  }
-  for (int b = 0; b < nb; ++b) {
-    const float2* f = src + (long long)b * N;
-    __syncthreads();  // previous bin's readers of ayz are done
-    for (int i = tid; i < kA3; i += blockDim.x) {
-      const int z = i % AZ_, y = (i / AZ_) % AY_, x = i / (AZ_ * AY_);
-      float2 v = f[(((long long)((x0 - 2 + x) & Lm)) * L + ((y0 - 2 + y) & Lm)) * L + ((z0 - 2 + z) & Lm)];
-      if (conj_src) v = make_float2(sign * v.x, -sign * v.y);
-      a3[i] = v;
+// a3 plane x_a (region rows y0-2.., cols z0-2..) -> buf [cell][16] float2.
+__device__ __forceinline__ void ct_stage_a3(const float2* __restrict__ src3, int s3, float2* buf, int xa, int y0, int z0, int L, int Lm) {
+  const long long xb = (long long)(xa & Lm) * L;
+  if (s3 == kBinStride) {
+    for (int c = threadIdx.x; c < ct::HY * ct::HZ * 8; c += ct::kThreads) {
+      const int cell = c >> 3, ch = c & 7;
+      const int hy = cell / ct::HZ, hz = cell - hy * ct::HZ;
+      const long long g = ((xb + ((y0 - 2 + hy) & Lm)) * L + ((z0 - 2 + hz) & Lm)) * kBinStride + 2 * ch;
+      cp_async16(buf + cell * kBinStride + 2 * ch, src3 + g);
     }
-    __syncthreads();
-    // z-pass: az[l1z][x][y][z'] = sum_l2z G[l1z][l2z] a3[x][y][z' + 2 - l2z], z' in [0, GZ+2)
-    for (int i = tid; i < AX_ * ZY_ * ZZ_; i += blockDim.x) {
-      const int z = i % ZZ_, y = (i / ZZ_) % ZY_, x = i / (ZZ_ * ZY_);
-      const float2* col = a3 + (x * AY_ + y) * AZ_ + z + 2;
-      const float2 v0 = col[0], v1 = col[-1], v2 = col[-2];
-#pragma unroll
-      for (int l1 = 0; l1 < 3; ++l1) {
-        const float g0 = gm.g[l1 * 3 + 0], g1 = gm.g[l1 * 3 + 1], g2 = gm.g[l1 * 3 + 2];
-        az[l1 * kAz + i] = make_float2(g0 * v0.x + g1 * v1.x + g2 * v2.x, g0 * v0.y + g1 * v1.y + g2 * v2.y);
-      }
-    }
-    __syncthreads();
-    // y-pass: ayz[l1y][l1z][x][y'][z'] = sum_l2y G[l1y][l2y] az[l1z][x][y' + 2 - l2y][z'], y' in [0, GY+2)
-    for (int i = tid; i < AX_ * YY_ * ZZ_; i += blockDim.x) {
-      const int z = i % ZZ_, y = (i / ZZ_) % YY_, x = i / (ZZ_ * YY_);
-      const int base = (x * ZY_ + y + 2) * ZZ_ + z;
-#pragma unroll
-      for (int l1z = 0; l1z < 3; ++l1z) {
-        const float2 v0 = az[l1z * kAz + base], v1 = az[l1z * kAz + base - ZZ_], v2 = az[l1z * kAz + base - 2 * ZZ_];
-#pragma unroll
-        for (int l1y = 0; l1y < 3; ++l1y) {
-          const float g0 = gm.g[l1y * 3 + 0], g1 = gm.g[l1y * 3 + 1], g2 = gm.g[l1y * 3 + 2];
-          ayz[(l1y * 3 + l1z) * kAyz + i] =
-              make_float2(g0 * v0.x + g1 * v1.x + g2 * v2.x, g0 * v0.y + g1 * v1.y + g2 * v2.y);
-        }
-      }
-    }
-    __syncthreads();
-    // x-pass + gather: G(y) = sum_l1 e(y+l1) sum_l2x G[l1x][l2x] ayz[l1y][l1z][x + 2 + l1x - l2x][y + l1y][z + l1z]
-    for (int i = tid; i < GX * GY * GZ; i += blockDim.x) {
-      const int z = i % GZ, y = (i / GZ) % GY, x = i / (GZ * GY);
-      float gr = 0.f, gi = 0.f;
-#pragma unroll
-      for (int l1y = 0; l1y < 3; ++l1y)
-#pragma unroll
-        for (int l1z = 0; l1z < 3; ++l1z) {
-          const float2* row = ayz + (l1y * 3 + l1z) * kAyz + (y + l1y) * ZZ_ + (z + l1z);
-          float2 v[5];
-#pragma unroll
-          for (int d = 0; d < 5; ++d) v[d] = row[(x + d) * (YY_ * ZZ_)];  // x offset d - 2
-#pragma unroll
-          for (int l1x = 0; l1x < 3; ++l1x) {
-            const float ev = eh[((x + l1x) * EY_ + (y + l1y)) * EZ_ + (z + l1z)];
-            // ayz x index: x + 2 + l1x - l2x  -> v[2 + l1x - l2x]
-            const float g0 = gm.g[l1x * 3 + 0], g1 = gm.g[l1x * 3 + 1], g2 = gm.g[l1x * 3 + 2];
-            const float ur = g0 * v[2 + l1x].x + g1 * v[1 + l1x].x + g2 * v[l1x].x;
-            const float ui = g0 * v[2 + l1x].y + g1 * v[1 + l1x].y + g2 * v[l1x].y;
-            gr = fmaf(ev, ur, gr);
-            gi = fmaf(ev, ui, gi);
-          }
-        }
-      gout[(long long)b * N + (((long long)(x0 + x)) * L + (y0 + y)) * L + (z0 + z)] = make_float2(gr, gi);
+  } else {  // single bin: slot 0 holds the value, other slots zero
+    for (int c = threadIdx.x; c < ct::HY * ct::HZ * kBinStride; c += ct::kThreads) {
+      const int cell = c >> 4, bb = c & 15;
+      const int hy = cell / ct::HZ, hz = cell - hy * ct::HZ;
+      float2 v = make_float2(0.f, 0.f);
+      if (bb == 0) v = src3[(xb + ((y0 - 2 + hy) & Lm)) * L + ((z0 - 2 + hz) & Lm)];
+      buf[c] = v;
     }
   }
 }
 
-// ---- bin x bin product over cells ----------------------------------------
-// S[b1][b2] = sum_y A[b1][y] * B[b2][y] (complex, no conjugation).
-constexpr int kGemmThreads = 256;
-constexpr int kGemmChunk = 64;
+// a2 plane x (the tile's 8x8 columns) -> buf [col][kA2Stride] float2.
+__device__ __forceinline__ void ct_stage_a2(const float2* __restrict__ f2, int s2, float2* buf, int x, int y0, int z0, int L, int Lm) {
+  const long long xb = (long long)(x & Lm) * L;
+  if (s2 == kBinStride) {
+    for (int c = threadIdx.x; c < ct::kCols * 8; c += ct::kThreads) {
+      const int col = c >> 3, ch = c & 7;
+      const int cy = col / ct::TZ, cz = col - cy * ct::TZ;
+      const long long g = ((xb + y0 + cy) * L + z0 + cz) * kBinStride + 2 * ch;
+      cp_async16(buf + col * ct::kA2Stride + 2 * ch, f2 + g);
+    }
+  } else {
+    for (int c = threadIdx.x; c < ct::kCols * kBinStride; c += ct::kThreads) {
+      const int col = c >> 4, bb = c & 15;
+      const int cy = col / ct::TZ, cz = col - cy * ct::TZ;
+      float2 v = make_float2(0.f, 0.f);
+      if (bb == 0) v = f2[(xb + y0 + cy) * L + z0 + cz];
+      buf[col * ct::kA2Stride + bb] = v;
+    }
+  }
+}
 
-__global__ void __launch_bounds__(kGemmThreads)
-mp_gemm_kernel(const float2* __restrict__ A, int na, const float2* __restrict__ B, int nbb, long long N,
-               double* __restrict__ partial) {
-  __shared__ float2 sa[kMaxBins][kGemmChunk + 1];
-  __shared__ float2 sb[kMaxBins][kGemmChunk + 1];
-  // thread -> (b1 pair, b2 pair): 8 x 8 = 64 blocks of 2x2, 4 threads per block split the chunk
-  const int blk = threadIdx.x >> 2, part = threadIdx.x & 3;
-  const int r0 = (blk >> 3) * 2, c0 = (blk & 7) * 2;
-  double acc[2][2][2];
+__device__ __forceinline__ void ct_stage_eps(const float* __restrict__ eps1, float* buf, int xe, int y0, int z0, int L, int Lm) {
+  const long long xb = (long long)(xe & Lm) * L;
+  for (int c = threadIdx.x; c < ct::kEpsPlane; c += ct::kThreads) {
+    const int ey = c / ct::EZ, ez = c - ey * ct::EZ;
+    cp_async4(buf + c, eps1 + (xb + ((y0 + ey) & Lm)) * L + ((z0 + ez) & Lm));
+  }
+}
+
+// V plane from a staged eps plane: V[col][uy+2][uz+2].  Four threads per
+// column; w[a][l1] = Gamma[l1][l1 - a + 2] (0 outside [0,2]) in shared memory.
+// Each thread filters the column's 3x3 eps neighbourhood along z for the five
+// uz, then along y for its uy rows (uy+2 = part, and 4 for part 0).
+__device__ __forceinline__ void ct_compute_v(const float* __restrict__ w, const float* __restrict__ e,
+                                             float* __restrict__ v) {
+  const int col = threadIdx.x >> 2, part = threadIdx.x & 3;
+  const int cy = col / ct::TZ, cz = col - cy * ct::TZ;
+  float ev[3][3];
 #pragma unroll
-  for (int i = 0; i < 2; ++i)
+  for (int i = 0; i < 3; ++i)
 #pragma unroll
-    for (int j = 0; j < 2; ++j) acc[i][j][0] = acc[i][j][1] = 0.0;
-  for (long long base = (long long)blockIdx.x * kGemmChunk; base < N; base += (long long)gridDim.x * kGemmChunk) {
-    __syncthreads();
-    for (int i = threadIdx.x; i < kMaxBins * kGemmChunk; i += blockDim.x) {
-      const int b = i / kGemmChunk, k = i % kGemmChunk;
-      const long long y = base + k;
-      sa[b][k] = (b < na && y < N) ? A[(long long)b * N + y] : make_float2(0.f, 0.f);
-      sb[b][k] = (b < nbb && y < N) ? B[(long long)b * N + y] : make_float2(0.f, 0.f);
-    }
-    __syncthreads();
-    float f[2][2][2] = {};
-    for (int k = part; k < kGemmChunk; k += 4) {
-      const float2 a0 = sa[r0][k], a1 = sa[r0 + 1][k], b0 = sb[c0][k], b1 = sb[c0 + 1][k];
-      f[0][0][0] += a0.x * b0.x - a0.y * b0.y; f[0][0][1] += a0.x * b0.y + a0.y * b0.x;
-      f[0][1][0] += a0.x * b1.x - a0.y * b1.y; f[0][1][1] += a0.x * b1.y + a0.y * b1.x;
-      f[1][0][0] += a1.x * b0.x - a1.y * b0.y; f[1][0][1] += a1.x * b0.y + a1.y * b0.x;
-      f[1][1][0] += a1.x * b1.x - a1.y * b1.y; f[1][1][1] += a1.x * b1.y + a1.y * b1.x;
-    }
+    for (int j = 0; j < 3; ++j) ev[i][j] = e[(cy + i) * ct::EZ + cz + j];
+  float ez[3][5];
 #pragma unroll
-    for (int i = 0; i < 2; ++i)
+  for (int i = 0; i < 3; ++i)
 #pragma unroll
-      for (int j = 0; j < 2; ++j) {
-        acc[i][j][0] += (double)f[i][j][0];
-        acc[i][j][1] += (double)f[i][j][1];
+    for (int a = 0; a < 5; ++a) ez[i][a] = fmaf(w[a * 3 + 2], ev[i][2], fmaf(w[a * 3 + 1], ev[i][1], w[a * 3] * ev[i][0]));
+#pragma unroll
+  for (int rep = 0; rep < 2; ++rep) {
+    const int ay = rep == 0 ? part : 4;
+    if (rep == 1 && part != 0) break;
+    const float w0 = w[ay * 3], w1 = w[ay * 3 + 1], w2 = w[ay * 3 + 2];
+    float o[5];
+#pragma unroll
+    for (int a = 0; a < 5; ++a) o[a] = fmaf(w2, ez[2][a], fmaf(w1, ez[1][a], w0 * ez[0][a]));
+    float* dst = v + col * ct::kVCol + ay * ct::kVRow;
+    *reinterpret_cast<float4*>(dst) = make_float4(o[0], o[1], o[2], o[3]);
+    dst[4] = o[4];
+  }
+}
+
+__global__ void __launch_bounds__(ct::kThreads, 2) mp_contract_kernel(ContractArgs A) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* abuf = reinterpret_cast<float2*>(smem_raw);     // [2][kA3Plane]
+  float2* a2buf = abuf + 2 * ct::kA3Plane;                // [3][kA2Plane]
+  float2* gpl = a2buf + 3 * ct::kA2Plane;                 // [kCols][kA2Stride] completed G plane
+  double* dacc = reinterpret_cast<double*>(gpl + ct::kA2Plane);  // [16][16][2]
+  float* vring = reinterpret_cast<float*>(dacc + 2 * kMaxBins * kMaxBins);  // [3][kVPlane]
+  float* epsb = vring + 3 * ct::kVPlane;                  // [2][kEpsPlane]
+  const int J = A.J, L = 1 << J, Lm = L - 1, CX = A.CX;
+  const int tid = threadIdx.x;
+  // stencil mapping: lane & 15 = bin, half-warp = 2x2 column group
+  const int b = tid & 15;
+  const int grp = tid >> 4;
+  const int cy = 2 * (grp / (ct::TZ / 2)), cz = 2 * (grp % (ct::TZ / 2));
+  // product mapping: warp -> b2 quad (w >> 1), lane >> 2 -> b3 pair, cells 8k + slice
+  const int bq = tid >> 6, b3p = (tid >> 2) & 7;
+  const int slice = ((tid >> 5) & 1) * 4 + (tid & 3);
+  const int nty = L / ct::TY, ntz = L / ct::TZ;
+  const int n_items = (L / CX) * nty * ntz;
+  const int nsteps = CX + 4;
+  __shared__ float gsm[15];    // V-pass weights w[a][l1] = Gamma[l1][l1 - a + 2]
+  if (tid == 0) {
+#pragma unroll
+    for (int a = 0; a < 5; ++a)
+#pragma unroll
+      for (int l1 = 0; l1 < 3; ++l1) {
+        const int l2 = l1 - a + 2;  // static indices keep A in parameter space
+        gsm[a * 3 + l1] = (l2 >= 0 && l2 <= 2) ? A.gm.g[l1 * 3 + (l2 < 0 ? 0 : (l2 > 2 ? 2 : l2))] : 0.f;
       }
   }
-  // combine the 4 parts of each block (adjacent lanes)
+  for (int i = tid; i < 2 * kMaxBins * kMaxBins; i += ct::kThreads) dacc[i] = 0.0;
+  __syncthreads();
+
+  for (int item = blockIdx.x; item < n_items; item += gridDim.x) {
+    const int tz = item % ntz, ty = (item / ntz) % nty, xc = item / (ntz * nty);
+    const int x0 = xc * CX, y0 = ty * ct::TY, z0 = tz * ct::TZ;
+    // prologue: V(x0-2), V(x0-1) into ring slots 0, 1; first a3 plane; eps plane x0
+    ct_stage_eps(A.eps1, epsb, x0 - 2, y0, z0, L, Lm);
+    ct_stage_eps(A.eps1, epsb + ct::kEpsPlane, x0 - 1, y0, z0, L, Lm);
+    cp_async_commit();
+    cp_async_wait<0>();
+    __syncthreads();
+    ct_compute_v(gsm, epsb, vring);
+    ct_compute_v(gsm, epsb + ct::kEpsPlane, vring + ct::kVPlane);
+    __syncthreads();
+    ct_stage_a3(A.src3, A.s3, abuf, x0 - 2, y0, z0, L, Lm);
+    ct_stage_eps(A.eps1, epsb, x0, y0, z0, L, Lm);
+    cp_async_commit();
+
+    float2 G[5][4];
+    float2 S[8];  // S[4 bq + i][2 b3p + j] at i * 2 + j
 #pragma unroll
-  for (int i = 0; i < 2; ++i)
+    for (int q = 0; q < 5; ++q)
 #pragma unroll
-    for (int j = 0; j < 2; ++j)
+      for (int c = 0; c < 4; ++c) G[q][c] = make_float2(0.f, 0.f);
 #pragma unroll
-      for (int c = 0; c < 2; ++c) {
-        double v = acc[i][j][c];
-        v += __shfl_xor_sync(0xffffffffu, v, 1);
-        v += __shfl_xor_sync(0xffffffffu, v, 2);
-        acc[i][j][c] = v;
+    for (int q = 0; q < 8; ++q) S[q] = make_float2(0.f, 0.f);
+
+    for (int st = 0; st < nsteps; ++st) {
+      const int xa = x0 - 2 + st;
+      // (1) prefetch: a3 plane xa+1, eps plane xa+3, a2 plane of the next step's product.
+      // Readers of the overwritten buffers finished before the previous step's
+      // third barrier (a3, eps) or before this step's first barrier of the step
+      // before (a2, three buffers).
+      if (st + 1 < nsteps) {
+        ct_stage_a3(A.src3, A.s3, abuf + ((st + 1) & 1) * ct::kA3Plane, xa + 1, y0, z0, L, Lm);
+        ct_stage_eps(A.eps1, epsb + ((st + 1) & 1) * ct::kEpsPlane, xa + 3, y0, z0, L, Lm);
+        if (st + 1 >= 4) ct_stage_a2(A.f2, A.s2, a2buf + ((st + 1) % 3) * ct::kA2Plane, xa - 1, y0, z0, L, Lm);
       }
-  if (part == 0) {
+      cp_async_commit();
+      cp_async_wait<1>();
+      __syncthreads();
+      // (2) V(xa + 2) from eps plane xa + 2
+      ct_compute_v(gsm, epsb + (st & 1) * ct::kEpsPlane, vring + ((st + 2) % 3) * ct::kVPlane);
+      __syncthreads();
+      // (3) T_d(xa + d) for this group's 2x2 columns, bin b
+      {
+        const float2* ap = abuf + (st & 1) * ct::kA3Plane;
+        const float* vp0 = vring + (st % 3) * ct::kVPlane;
+        const float* vp1 = vring + ((st + 1) % 3) * ct::kVPlane;
+        const float* vp2 = vring + ((st + 2) % 3) * ct::kVPlane;
+        float2 T[3][4];
 #pragma unroll
-    for (int i = 0; i < 2; ++i)
+        for (int d = 0; d < 3; ++d)
 #pragma unroll
-      for (int j = 0; j < 2; ++j) {
-        const int b1 = r0 + i, b2 = c0 + j;
-        double* o = partial + ((long long)blockIdx.x * kMaxBins * kMaxBins + b1 * kMaxBins + b2) * 2;
-        o[0] = acc[i][j][0];
-        o[1] = acc[i][j][1];
+          for (int c = 0; c < 4; ++c) T[d][c] = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int r = 0; r < 6; ++r) {
+          float2 av[6];
+#pragma unroll
+          for (int k = 0; k < 6; ++k) av[k] = ap[((cy + r) * ct::HZ + cz + k) * kBinStride + b];
+#pragma unroll
+          for (int dy = 0; dy < 2; ++dy) {
+            const int uy = r - 2 - dy;
+            if (uy < -2 || uy > 2) continue;
+#pragma unroll
+            for (int dz = 0; dz < 2; ++dz) {
+              const int voff = ((cy + dy) * ct::TZ + cz + dz) * ct::kVCol + (uy + 2) * ct::kVRow;
+#pragma unroll
+              for (int d = 0; d < 3; ++d) {
+                const float* vp = (d == 0 ? vp0 : (d == 1 ? vp1 : vp2)) + voff;
+                const float4 v4 = *reinterpret_cast<const float4*>(vp);
+                const float v5 = vp[4];
+                float2 t = T[d][dy * 2 + dz];
+                t = __ffma2_rn(make_float2(v4.x, v4.x), av[dz], t);
+                t = __ffma2_rn(make_float2(v4.y, v4.y), av[dz + 1], t);
+                t = __ffma2_rn(make_float2(v4.z, v4.z), av[dz + 2], t);
+                t = __ffma2_rn(make_float2(v4.w, v4.w), av[dz + 3], t);
+                t = __ffma2_rn(make_float2(v5, v5), av[dz + 4], t);
+                T[d][dy * 2 + dz] = t;
+              }
+            }
+          }
+        }
+        // (4) G(xa + d - l1x) += Gx[l1x][d] T_d; ring slot q <-> x = xa - 2 + q
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+#pragma unroll
+          for (int l1x = 0; l1x < 3; ++l1x) {
+            const float gx = A.gm.g[l1x * 3 + d];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) G[d - l1x + 2][c] = __ffma2_rn(make_float2(gx, gx), T[d][c], G[d - l1x + 2][c]);
+          }
       }
+      // (5) G(xa - 2) is complete: publish it, then S[b2][b3] += a2^{b2} G^{b3}
+      const bool full = st >= 4;
+      if (full) {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          float2 g = G[0][c];
+          if (A.conj_src) g = make_float2(A.sign * g.x, -A.sign * g.y);
+          gpl[((cy + (c >> 1)) * ct::TZ + cz + (c & 1)) * ct::kA2Stride + b] = g;
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) G[q][c] = G[q + 1][c];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) G[4][c] = make_float2(0.f, 0.f);
+      __syncthreads();
+      if (full) {
+        const float2* a2p = a2buf + (st % 3) * ct::kA2Plane;
+#pragma unroll 2
+        for (int k = 0; k < ct::kCols / 8; ++k) {
+          const int cell = 8 * k + slice;
+          const float4* ar = reinterpret_cast<const float4*>(a2p + cell * ct::kA2Stride + 4 * bq);
+          const float4 a01 = ar[0], a23 = ar[1];
+          const float4 gg = *reinterpret_cast<const float4*>(gpl + cell * ct::kA2Stride + 2 * b3p);
+          const float2 g0 = make_float2(gg.x, gg.y), g1 = make_float2(gg.z, gg.w);
+          const float2 h0 = make_float2(-gg.y, gg.x), h1 = make_float2(-gg.w, gg.z);  // i g
+          const float ar_[4] = {a01.x, a01.z, a23.x, a23.z}, ai_[4] = {a01.y, a01.w, a23.y, a23.w};
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            const float2 re = make_float2(ar_[i], ar_[i]), im = make_float2(ai_[i], ai_[i]);
+            S[2 * i] = __ffma2_rn(im, h0, __ffma2_rn(re, g0, S[2 * i]));
+            S[2 * i + 1] = __ffma2_rn(im, h1, __ffma2_rn(re, g1, S[2 * i + 1]));
+          }
+        }
+      }
+    }
+    cp_async_wait<0>();
+    // fixed-order reduction of the eight cell slices (lanes, then the warp
+    // pair in two ordered rounds), float64 per CTA
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      S[q].x += __shfl_xor_sync(0xffffffffu, S[q].x, 1);
+      S[q].y += __shfl_xor_sync(0xffffffffu, S[q].y, 1);
+      S[q].x += __shfl_xor_sync(0xffffffffu, S[q].x, 2);
+      S[q].y += __shfl_xor_sync(0xffffffffu, S[q].y, 2);
+    }
+#pragma unroll
+    for (int round = 0; round < 2; ++round) {
+      if ((tid & 3) == 0 && ((tid >> 5) & 1) == round) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const int o = ((4 * bq + (q >> 1)) * kMaxBins + 2 * b3p + (q & 1)) * 2;
+          dacc[o] += (double)S[q].x;
+          dacc[o + 1] += (double)S[q].y;
+        }
+      }
+      __syncthreads();  // round 1 after round 0; all buffers idle before the next item
+    }
   }
+  for (int i = tid; i < 2 * kMaxBins * kMaxBins; i += ct::kThreads)
+    A.partial[(long long)blockIdx.x * 2 * kMaxBins * kMaxBins + i] = dacc[i];
 }
 
 // out[o] = sum over blocks of partial[blk * nout + o]
@@ -499,24 +687,22 @@ YlmConst make_ylm(int l, int m) {
   return Y;
 }
 
-size_t table_floats(int J, int nb) {
+size_t table_floats(int J) {
   const long long L = 1LL << J;
-  return (size_t)(3 * L * L + 1) * nb;
+  return (size_t)(3 * L * L + 1) * kBinStride;
 }
 
 }  // namespace
 
 extern "C" int hermes_multipole_workspace_size(int J, int nb, size_t* bytes) {
   if (!bytes) return fail(HERMES_ERR_INVALID, "bytes is NULL");
-  if (J < 3 || J > 10) return fail(HERMES_ERR_INVALID, "multipole: J=%d outside [3,10]", J);
+  if (J < 4 || J > 10) return fail(HERMES_ERR_INVALID, "multipole: J=%d outside [4,10]", J);
   if (nb < 1 || nb > kMaxBins) return fail(HERMES_ERR_INVALID, "multipole: nb=%d outside [1,%d]", nb, kMaxBins);
-  const size_t N = (size_t)1 << (3 * J);
   hermes::Carver c(nullptr, 0);
   c.take<float>(2 * kMaxBins);         // rho double-float
-  c.take<float>(table_floats(J, nb));  // j_l table
+  c.take<float>(table_floats(J));      // j_l table
   c.take<float>((1 << J) + 1);         // phi power float
-  c.take<float2>((size_t)nb * N);      // G fields
-  c.take<double>((size_t)4096 * kMaxBins * kMaxBins * 2);  // partials
+  c.take<double>((size_t)1024 * kMaxBins * kMaxBins * 2);  // partials
   c.take<double>((size_t)kMaxBins * kMaxBins * 2);
   *bytes = c.used;
   return HERMES_OK;
@@ -538,10 +724,11 @@ extern "C" int hermes_multipole_fields(const void* half_spec, int J, int l, int 
   if (!workspace || workspace_bytes < need) return fail(HERMES_ERR_WORKSPACE, "multipole_fields: workspace %zu < %zu", workspace_bytes, need);
   const int L = 1 << J;
   const long long N = 1LL << (3 * J);
+  const int stride = nb == 1 ? 1 : kBinStride;
   cudaStream_t s = hermes::as_stream(stream);
   hermes::Carver c(workspace, workspace_bytes);
   float* rho = c.take<float>(2 * kMaxBins);
-  float* T = c.take<float>(table_floats(J, nb));
+  float* T = c.take<float>(table_floats(J));
   float* Pf = c.take<float>(L + 1);
   float hrho[2 * kMaxBins];
   for (int b = 0; b < nb; ++b) {
@@ -562,12 +749,13 @@ extern "C" int hermes_multipole_fields(const void* half_spec, int J, int l, int 
   float2* out = static_cast<float2*>(fields_out);
   const int grid = nsm * 8;
   const float2* half = static_cast<const float2*>(half_spec);
-  if (nb <= 4) mp_prepass_kernel<4><<<grid, 256, 0, s>>>(half, J, Pf, T, Y, nb, out, inv_n);
-  else if (nb <= 8) mp_prepass_kernel<8><<<grid, 256, 0, s>>>(half, J, Pf, T, Y, nb, out, inv_n);
-  else mp_prepass_kernel<16><<<grid, 256, 0, s>>>(half, J, Pf, T, Y, nb, out, inv_n);
+  const float4* T4 = reinterpret_cast<const float4*>(T);
+  if (nb <= 4) mp_prepass_kernel<1><<<grid, 256, 0, s>>>(half, J, Pf, T4, Y, nb, stride, out, inv_n);
+  else if (nb <= 8) mp_prepass_kernel<2><<<grid, 256, 0, s>>>(half, J, Pf, T4, Y, nb, stride, out, inv_n);
+  else mp_prepass_kernel<4><<<grid, 256, 0, s>>>(half, J, Pf, T4, Y, nb, stride, out, inv_n);
   HERMES_LAUNCH_CHECK("mp_prepass_kernel");
   cufftHandle h;
-  rc = hermes::get_plan_c2c_batch(J, nb, &h);
+  rc = hermes::get_plan_c2c_interleaved(J, nb, stride, &h);
   if (rc) return rc;
   cufftResult r = cufftSetStream(h, s);
   if (r != CUFFT_SUCCESS) return fail(HERMES_ERR_CUFFT, "cufftSetStream failed: %d", (int)r);
@@ -596,23 +784,31 @@ extern "C" int hermes_multipole_contract(const float* eps1, const void* fields2,
   cudaStream_t s = hermes::as_stream(stream);
   hermes::Carver c(workspace, workspace_bytes);
   c.take<float>(2 * kMaxBins);
-  c.take<float>(table_floats(J, nb2 > nb3 ? nb2 : nb3));
+  c.take<float>(table_floats(J));
   c.take<float>(L + 1);
-  float2* G = c.take<float2>((size_t)(nb2 > nb3 ? nb2 : nb3) * N);
-  double* partial = c.take<double>((size_t)4096 * kMaxBins * kMaxBins * 2);
+  double* partial = c.take<double>((size_t)1024 * kMaxBins * kMaxBins * 2);
   double* dout = c.take<double>((size_t)kMaxBins * kMaxBins * 2);
-  const GammaC gm = make_gamma(gamma);
-  const int ntiles = (L / GX) * (L / GY) * (L / GZ);
-  const size_t smem = sizeof(float2) * (9 * kAyz + 3 * kAz) + sizeof(float) * kEps;
-  static_assert(9 * kAyz >= kA3, "a3 halo must fit in the aliased y-pass buffer");
-  HERMES_CUDA_TRY(cudaFuncSetAttribute(mp_gfield_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  const float2* src = static_cast<const float2*>(conj_src ? fields2 : fields3);
-  mp_gfield_kernel<<<ntiles, GThreads, smem, s>>>(eps1, src, conj_src, (float)conj_sign, nb3, J, gm, G);
-  HERMES_LAUNCH_CHECK("mp_gfield_kernel");
-  int nblk = sm_count() * 8;
-  if (nblk > 4096) nblk = 4096;
-  mp_gemm_kernel<<<nblk, kGemmThreads, 0, s>>>(static_cast<const float2*>(fields2), nb2, G, nb3, N, partial);
-  HERMES_LAUNCH_CHECK("mp_gemm_kernel");
+  HERMES_CUDA_TRY(cudaFuncSetAttribute(mp_contract_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)ct::kSmem));
+  // field layout follows hermes_multipole_fields: [cell][16] for nb > 1, [cell] for nb == 1
+  ContractArgs A;
+  A.eps1 = eps1;
+  A.f2 = static_cast<const float2*>(fields2);
+  A.src3 = static_cast<const float2*>(conj_src ? fields2 : fields3);
+  A.s2 = nb2 == 1 ? 1 : kBinStride;
+  A.s3 = conj_src ? A.s2 : (nb3 == 1 ? 1 : kBinStride);
+  A.conj_src = conj_src;
+  A.sign = (float)conj_sign;
+  A.J = J;
+  A.CX = L < ct::kMaxCX ? L : ct::kMaxCX;
+  A.gm = make_gamma(gamma);
+  A.partial = partial;
+  const int n_items = (L / A.CX) * (L / ct::TY) * (L / ct::TZ);
+  int nblk = 2 * sm_count();  // two resident CTAs per SM
+  if (nblk > n_items) nblk = n_items;
+  if (nblk > 1024) nblk = 1024;
+  mp_contract_kernel<<<nblk, ct::kThreads, ct::kSmem, s>>>(A);
+  HERMES_LAUNCH_CHECK("mp_contract_kernel");
   mp_reduce_kernel<<<kMaxBins * kMaxBins * 2, 256, 0, s>>>(partial, nblk, kMaxBins * kMaxBins * 2, dout);
   HERMES_LAUNCH_CHECK("mp_reduce_kernel");
   std::vector<double> h((size_t)kMaxBins * kMaxBins * 2);
@@ -631,7 +827,7 @@ extern "C" int hermes_multipole_contract_plain(const float* eps1, const void* a2
                                                const double* gamma, int J, double* out, void* workspace,
                                                size_t workspace_bytes, void* stream) {
   if (!eps1 || !a2 || !a3 || !gamma || !out) return fail(HERMES_ERR_INVALID, "contract_plain: NULL argument");
-  if (J < 3 || J > 10) return fail(HERMES_ERR_INVALID, "contract_plain: J=%d outside [3,10]", J);
+  if (J < 4 || J > 10) return fail(HERMES_ERR_INVALID, "contract_plain: J=%d outside [4,10]", J);
   const int nblk = sm_count() * 8;
   if (!workspace || workspace_bytes < sizeof(double) * (2 * (size_t)nblk + 2))
     return fail(HERMES_ERR_WORKSPACE, "contract_plain: workspace too small");

@@ -59,13 +59,20 @@ def _ws_bytes(J, nb):
     return n.value
 
 
+BIN_STRIDE = 16
+
+
 def multipole_fields(half_spec, J, l, m, radii_grid, phi_power, out=None):
-    """a_lm^b = ifftn(fftn(eps) K_lm^b) for thin-shell radii (grid units)."""
+    """a_lm^b = ifftn(fftn(eps) K_lm^b) for thin-shell radii (grid units).
+
+    Returns complex64 [L^3, 16] (bin-interleaved; bins >= nb unused) for
+    several radii, or [L^3] for a single radius."""
     nb = len(radii_grid)
     N = 1 << (3 * J)
     dev = half_spec.device
     if out is None:
-        out = torch.empty((nb, N), dtype=torch.complex64, device=dev)
+        shape = (N,) if nb == 1 else (N, BIN_STRIDE)
+        out = torch.empty(shape, dtype=torch.complex64, device=dev)
     ws = _workspace(_ws_bytes(J, nb), dev)
     radii = (ctypes.c_double * nb)(*[float(r) for r in radii_grid])
     _lib.check(_lib.load().hermes_multipole_fields(_ptr(half_spec), J, int(l), int(m), radii, nb, _ptr(phi_power),

@@ -51,7 +51,7 @@ def test_multipole_fields_match_oracle(l, m):
     s = fftn(eps)
     for b, r in enumerate(radii):
         ref = ifftn(s * oracle.radial_multipole_window(L, Pn, r, l, m)).ravel()
-        assert _rel(f[b], ref) < 2e-5, (l, m, b, _rel(f[b], ref))
+        assert _rel(f[:, b], ref) < 2e-5, (l, m, b, _rel(f[:, b], ref))
 
 
 def test_contract_batched_and_plain_match_oracle():
@@ -82,9 +82,23 @@ def test_contract_batched_and_plain_match_oracle():
     S1 = mp.multipole_contract(et, f2, 3, gam, J, fields3=f3b, nb3=3)
     S2 = mp.multipole_contract(et, f2, 3, gam, J, conj_sign=(-1) ** ((l + m) % 2))
     assert _rel(S2, S1) < 1e-5
-    # plain reference-form path for one pair
-    p = mp.multipole_contract_plain(et, f2[1], f3[0], gam, J)
+    # plain reference-form path for one pair (single-radius fields)
+    g2 = mp.multipole_fields(spec, J, l, m, [r2[1]], P)
+    g3 = mp.multipole_fields(spec, J, l, -m, [r3[0]], P)
+    assert _rel(g2.cpu().numpy(), f2[:, 1].cpu().numpy()) < 1e-5
+    p = mp.multipole_contract_plain(et, g2, g3, gam, J)
     assert abs(p - ref[1, 0]) < 1e-4 * np.abs(ref).max()
+    # batched contraction with single-bin ([cell]-layout) fields on one or both sides
+    S11 = mp.multipole_contract(et, g2, 1, gam, J, fields3=g3, nb3=1)
+    assert abs(S11[0, 0] - ref[1, 0]) < 1e-4 * np.abs(ref).max()
+    S31 = mp.multipole_contract(et, f2, 3, gam, J, fields3=g3, nb3=1)
+    assert _rel(S31[:, 0], ref[:, 0]) < 1e-4
+    S13 = mp.multipole_contract(et, g2, 1, gam, J, fields3=f3, nb3=2)
+    assert _rel(S13[0], ref[1]) < 1e-4
+    g3b = mp.multipole_fields(spec, J, l, -m, [r2[1]], P)
+    Sc = mp.multipole_contract(et, g2, 1, gam, J, conj_sign=(-1) ** ((l + m) % 2))
+    Se = mp.multipole_contract(et, g2, 1, gam, J, fields3=g3b, nb3=1)
+    assert abs(Sc[0, 0] - Se[0, 0]) < 1e-5 * abs(Se[0, 0])
 
 
 def test_corr3pcf_multipole_matches_reference(golden_dir):
