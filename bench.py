@@ -18,8 +18,12 @@ host->device copies plus the device->host read of zeta_l inside the timed
 region.  `plain` = the per-sample reference-form GPU path (both side fields
 rebuilt and a one-pair contraction for every (r12, r13, l, m)), timed on a
 one-sample subset and scaled by the 225 samples (its cost is linear in the
-samples).  `roofline` = the batched contraction, algorithmic FLOPs
-8 * 15 * 15 * 27 * L^3 per (l, m), against the measured bf16 peak.
+samples).  `roofline` = the batched contraction (mp_contract_kernel), with
+the algorithmic FLOPs of the 27-term separable form, 8 * 15 * 15 * 27 * L^3
+per (l, m), against the measured bf16 peak; the kernel itself runs a
+restructured stencil on FP32 paired-FMA pipes (about 1.2e12 real FLOPs per
+(l, m) at J=9).  `traffic` is the DRAM bytes of one J=9 launch from the
+committed ncu summary profiles/mp_contract_kernel_J9.md.
 `deposit` = the 4M-point J=9 deposit (Mparticles/s, HBM roofline of the
 accumulate kernel).  `--impl reference` times the float64 CPU restatement of
 the reference (oracle/) on a bounded unit and scales it the same way.
@@ -65,6 +69,19 @@ def load_peaks():
         return float(d["hbm_gbs"]), float(d["bf16_tflops"]), "measured"
     except Exception:
         return 6800.0, 1900.0, "fallback"
+
+
+def contract_traffic():
+    """DRAM bytes of one J=9 15x15 contraction launch (ncu, committed summary)."""
+    path = os.path.join(ROOT, "profiles", "mp_contract_kernel_J9.md")
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.startswith("traffic_bytes_per_launch:"):
+                    return float(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
 
 
 class ClockSampler:
@@ -340,9 +357,10 @@ def run_gb300(args, ws, rank, local):
     value = t_total / (args.steps * ws)
     zeta = np.asarray(res.zeta_l)
 
-    # launches per step: 2 deposits x 7, per product per (l,m): fields (table, power, prepass, FFT) +
-    # contract (G, GEMM, reduce); plus the mixing solve
-    kernel_launches = args.steps * (14 + 2 * N_LM * 7 + 1)
+    # our kernels per step: 2 deposits x 7; per product per (l, m): fields (power, j_l table,
+    # prepass, interleave; the inverse FFT is cuFFT) + contract (contraction, reduce); the
+    # mixing solve
+    kernel_launches = args.steps * (14 + 2 * N_LM * 6 + 1)
 
     # end to end: catalogues in pinned host memory, copies inside the timed region
     h = [torch.as_tensor(a).pin_memory() for a in (dpos_np, dw_np, rpos_np, rw_np)]
@@ -418,9 +436,10 @@ def run_gb300(args, ws, rank, local):
         "plain": {"value": plain_per_cat, "unit": "s/catalogue", "speedup_batched_vs_plain": plain_per_cat / value,
                   "sample": "one (r12, r13) sample, l<=1, scaled by 225 samples x 66 (l,m) x 2 products",
                   "max_rel_diff_batched_vs_plain": mixed_vs_plain},
-        "roofline": {"kernel": "hermes_multipole_contract (mp_gfield + mp_gemm + reduce)", "bound": "tensor",
+        "roofline": {"kernel": "mp_contract_kernel (+ mp_reduce_kernel)", "bound": "tensor",
                      "achieved": achieved, "peak": bf16, "peak_kind": kind, "unit": "TFLOP/s",
-                     "frac": achieved / bf16, "traffic": None,
+                     "frac": achieved / bf16, "traffic": contract_traffic(),
+                     "executes_on": "FP32 paired-FMA pipes (separable pair stencil + 4x2-blocked bin product)",
                      "algorithmic_flops": flops, "ms_per_launch": t_con * 1e3,
                      "fields_ms_per_lm": t_fld * 1e3},
         "deposit": dep,

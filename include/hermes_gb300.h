@@ -203,6 +203,10 @@ int hermes_pair_products(const void* const* spectra, int n_spec, const int32_t* 
  *
  * hermes_multipole_contract_plain: the same sum for one (a2, a3) pair in the
  * reference's per-cell loop form (workspace >= 16*(#SM*8+1) bytes).
+ *
+ * hermes_multipole_workspace_size(J, nb): bytes of device workspace for
+ * fields/contract calls with up to nb bins (for nb > 1 this includes the
+ * nb * L^3 complex64 bin-major fields that cuFFT transforms).
  */
 int hermes_multipole_workspace_size(int J, int nb, size_t* bytes);
 int hermes_multipole_fields(const void* half_spec, int J, int l, int m,
@@ -216,6 +220,17 @@ int hermes_multipole_contract(const float* eps1, const void* fields2, int nb2,
 int hermes_multipole_contract_plain(const float* eps1, const void* a2, const void* a3,
                                     const double* gamma, int J, double* out,
                                     void* workspace, size_t workspace_bytes, void* stream);
+
+/* hermes_mixing_solve: replaces solve_multipoles_from_ratio +
+ * build_mixing_matrix (utils/special_functions.py:366-409) for n_sys samples
+ * at once, float64 on the device.  A, B: [n_sys][n] (n = lmax + 1 <= 32,
+ * B[s][0] != 0, checked by the caller as the reference raises ValueError);
+ * gaunt: [n][n][n], gaunt[k][l][l'] = legendre_triple_coeff(l, l', k).
+ * Writes zeta_out [n_sys][n] = M^{-1} A and, when non-NULL, m_out
+ * [n_sys][n][n] (the mixing matrices) and cond_out [n_sys] (2-norm condition
+ * numbers).  All pointers are device memory; asynchronous on `stream`. */
+int hermes_mixing_solve(const double* A, const double* B, const double* gaunt, int n_sys, int n,
+                        double* zeta_out, double* m_out, double* cond_out, void* stream);
 
 /* ---- Monte Carlo 3PCF ---------------------------------------------------------
  * hermes_interp: utils/wavelet_grid.py:143-186 interpolate_grid_at_pos_numba:

@@ -12,9 +12,10 @@
 //                        |k|^2 grid (float32, double-float phase)
 //   mp_prepass_kernel    eps_hat(k) K_lm^b(k) / L^3 for every bin b, Y_lm
 //                        shared by the bins, written as a batch of spectra
-//   cuFFT (batched C2C)  -> a_lm^b(x) for every bin; fields are stored
-//                        bin-interleaved, [cell][16], so one cell's bins are
-//                        one 128-byte line (istride 16 for cuFFT)
+//   cuFFT (batched C2C)  -> a_lm^b(x) for every bin, one contiguous field per
+//                        bin (cuFFT is far slower on strided batches)
+//   mp_interleave_kernel bin-major -> bin-interleaved [cell][16], so one
+//                        cell's bins are one 128-byte row for the contraction
 //   mp_contract_kernel   persistent: per output tile, for every bin b3,
 //                        G^b3(y) = sum_{l1,l2} Gamma3 eps1(y+l1) a3^b3(y+l1-l2)
 //                        by separable shared-memory passes into a tile of G in
@@ -36,7 +37,7 @@
 #include "window_eval.cuh"
 
 namespace hermes {
-int get_plan_c2c_interleaved(int J, int batch, int stride, cufftHandle* out);
+int get_plan_c2c_batch(int J, int batch, cufftHandle* out);
 }
 
 namespace {
@@ -171,14 +172,13 @@ __device__ __forceinline__ float2 ylm_at(const YlmConst& Y, int a, int b, int c,
   return make_float2(yr, yi);
 }
 
-// out[k * stride + b] = eps_hat(k) * K_lm^b(k) / L^3 on the full FFT grid;
+// out[b * L^3 + k] = eps_hat(k) * K_lm^b(k) / L^3 on the full FFT grid;
 // eps_hat comes from the half spectrum of a real field (Hermitian expansion).
 // NB4 = number of float4 groups of bins handled (bins padded to 4*NB4).
 template <int NB4>
 __global__ void __launch_bounds__(256)
 mp_prepass_kernel(const float2* __restrict__ half, int J, const float* __restrict__ P,
-                  const float4* __restrict__ T4, YlmConst Y, int nb, int stride, float2* __restrict__ out,
-                  float inv_n) {
+                  const float4* __restrict__ T4, YlmConst Y, int nb, float2* __restrict__ out, float inv_n) {
   constexpr int NB = 4 * NB4;
   const int L = 1 << J, H = L / 2 + 1, Lm = L - 1;
   const long long N = 1LL << (3 * J);
@@ -222,17 +222,32 @@ mp_prepass_kernel(const float2* __restrict__ half, int J, const float* __restric
           }
         }
     const float er = e.x * inv_n, ei = e.y * inv_n;
-    if (stride == 1) {
-      out[idx] = make_float2(er * accr[0] - ei * acci[0], er * acci[0] + ei * accr[0]);
-    } else {
-      float4* o4 = reinterpret_cast<float4*>(out + idx * stride);
 #pragma unroll
-      for (int q = 0; q < NB / 2; ++q) {
-        if (2 * q < nb)
-          o4[q] = make_float4(er * accr[2 * q] - ei * acci[2 * q], er * acci[2 * q] + ei * accr[2 * q],
-                              er * accr[2 * q + 1] - ei * acci[2 * q + 1], er * acci[2 * q + 1] + ei * accr[2 * q + 1]);
-      }
+    for (int b = 0; b < NB; ++b)
+      if (b < nb) out[b * N + idx] = make_float2(er * accr[b] - ei * acci[b], er * acci[b] + ei * accr[b]);
+  }
+}
+
+// dst[c * 16 + b] = src[b * N + c] for b < nb, 0 for nb <= b < 16.  A block
+// moves 128 cells: coalesced per-bin reads into a padded shared tile, then
+// 16 KB of contiguous 16-byte writes.
+constexpr int kIlCells = 128;
+__global__ void __launch_bounds__(256)
+mp_interleave_kernel(const float2* __restrict__ src, int nb, long long N, float2* __restrict__ dst) {
+  __shared__ float2 tile[kIlCells][kBinStride + 1];
+  const int tid = threadIdx.x;
+  for (long long c0 = (long long)blockIdx.x * kIlCells; c0 < N; c0 += (long long)gridDim.x * kIlCells) {
+    for (int i = tid; i < kIlCells * kBinStride; i += blockDim.x) {
+      const int b = i / kIlCells, c = i % kIlCells;
+      tile[c][b] = b < nb ? src[(long long)b * N + c0 + c] : make_float2(0.f, 0.f);
     }
+    __syncthreads();
+    float4* d4 = reinterpret_cast<float4*>(dst + c0 * kBinStride);
+    for (int i = tid; i < kIlCells * kBinStride / 2; i += blockDim.x) {
+      const int c = i >> 3, q = i & 7;
+      d4[i] = make_float4(tile[c][2 * q].x, tile[c][2 * q].y, tile[c][2 * q + 1].x, tile[c][2 * q + 1].y);
+    }
+    __syncthreads();
   }
 }
 
@@ -694,6 +709,8 @@ size_t table_floats(int J) {
 
 }  // namespace
 
+// Workspace: j_l table, partial sums and, for nb > 1, the bin-major fields
+// (nb * L^3 complex64) that cuFFT transforms before they are interleaved.
 extern "C" int hermes_multipole_workspace_size(int J, int nb, size_t* bytes) {
   if (!bytes) return fail(HERMES_ERR_INVALID, "bytes is NULL");
   if (J < 4 || J > 10) return fail(HERMES_ERR_INVALID, "multipole: J=%d outside [4,10]", J);
@@ -704,6 +721,7 @@ extern "C" int hermes_multipole_workspace_size(int J, int nb, size_t* bytes) {
   c.take<float>((1 << J) + 1);         // phi power float
   c.take<double>((size_t)1024 * kMaxBins * kMaxBins * 2);  // partials
   c.take<double>((size_t)kMaxBins * kMaxBins * 2);
+  if (nb > 1) c.take<float2>((size_t)nb << (3 * J));     // bin-major fields
   *bytes = c.used;
   return HERMES_OK;
 }
@@ -724,12 +742,14 @@ extern "C" int hermes_multipole_fields(const void* half_spec, int J, int l, int 
   if (!workspace || workspace_bytes < need) return fail(HERMES_ERR_WORKSPACE, "multipole_fields: workspace %zu < %zu", workspace_bytes, need);
   const int L = 1 << J;
   const long long N = 1LL << (3 * J);
-  const int stride = nb == 1 ? 1 : kBinStride;
   cudaStream_t s = hermes::as_stream(stream);
   hermes::Carver c(workspace, workspace_bytes);
   float* rho = c.take<float>(2 * kMaxBins);
   float* T = c.take<float>(table_floats(J));
   float* Pf = c.take<float>(L + 1);
+  c.take<double>((size_t)1024 * kMaxBins * kMaxBins * 2);
+  c.take<double>((size_t)kMaxBins * kMaxBins * 2);
+  float2* binmajor = nb > 1 ? c.take<float2>((size_t)nb * N) : static_cast<float2*>(fields_out);
   float hrho[2 * kMaxBins];
   for (int b = 0; b < nb; ++b) {
     if (!(radii[b] >= 0.0)) return fail(HERMES_ERR_INVALID, "multipole_fields: radius %d must be >= 0", b);
@@ -750,17 +770,24 @@ extern "C" int hermes_multipole_fields(const void* half_spec, int J, int l, int 
   const int grid = nsm * 8;
   const float2* half = static_cast<const float2*>(half_spec);
   const float4* T4 = reinterpret_cast<const float4*>(T);
-  if (nb <= 4) mp_prepass_kernel<1><<<grid, 256, 0, s>>>(half, J, Pf, T4, Y, nb, stride, out, inv_n);
-  else if (nb <= 8) mp_prepass_kernel<2><<<grid, 256, 0, s>>>(half, J, Pf, T4, Y, nb, stride, out, inv_n);
-  else mp_prepass_kernel<4><<<grid, 256, 0, s>>>(half, J, Pf, T4, Y, nb, stride, out, inv_n);
+  if (nb <= 4) mp_prepass_kernel<1><<<grid, 256, 0, s>>>(half, J, Pf, T4, Y, nb, binmajor, inv_n);
+  else if (nb <= 8) mp_prepass_kernel<2><<<grid, 256, 0, s>>>(half, J, Pf, T4, Y, nb, binmajor, inv_n);
+  else mp_prepass_kernel<4><<<grid, 256, 0, s>>>(half, J, Pf, T4, Y, nb, binmajor, inv_n);
   HERMES_LAUNCH_CHECK("mp_prepass_kernel");
   cufftHandle h;
-  rc = hermes::get_plan_c2c_interleaved(J, nb, stride, &h);
+  rc = hermes::get_plan_c2c_batch(J, nb, &h);
   if (rc) return rc;
   cufftResult r = cufftSetStream(h, s);
   if (r != CUFFT_SUCCESS) return fail(HERMES_ERR_CUFFT, "cufftSetStream failed: %d", (int)r);
-  r = cufftExecC2C(h, reinterpret_cast<cufftComplex*>(out), reinterpret_cast<cufftComplex*>(out), CUFFT_INVERSE);
+  r = cufftExecC2C(h, reinterpret_cast<cufftComplex*>(binmajor), reinterpret_cast<cufftComplex*>(binmajor),
+                   CUFFT_INVERSE);
   if (r != CUFFT_SUCCESS) return fail(HERMES_ERR_CUFFT, "cufftExecC2C failed: %d", (int)r);
+  if (nb > 1) {
+    long long nblk = N / kIlCells;
+    if (nblk > (long long)nsm * 16) nblk = (long long)nsm * 16;
+    mp_interleave_kernel<<<(int)nblk, 256, 0, s>>>(binmajor, nb, N, out);
+    HERMES_LAUNCH_CHECK("mp_interleave_kernel");
+  }
   return HERMES_OK;
 }
 

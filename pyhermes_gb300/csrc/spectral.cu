@@ -51,29 +51,9 @@ int get_plan(int J, PlanKind kind, int batch, cufftHandle* out) {
 
 // Batched C2C plan over `batch` interleaved fields: element (cell, b) at
 // cell * stride + b (stride >= batch), i.e. istride = stride, idist = 1.
-static std::map<std::tuple<int, int, int, int>, cufftHandle> g_plans_il;
 
-int get_plan_c2c_interleaved(int J, int batch, int stride, cufftHandle* out) {
-  if (stride == 1 && batch == 1) return get_plan(J, kC2C, 1, out);
-  int dev = 0;
-  HERMES_CUDA_TRY(cudaGetDevice(&dev));
-  auto key = std::make_tuple(dev, J, batch, stride);
-  std::lock_guard<std::mutex> lk(g_plan_mu);
-  auto it = g_plans_il.find(key);
-  if (it != g_plans_il.end()) {
-    *out = it->second;
-    return HERMES_OK;
-  }
-  cufftHandle h;
-  const int L = 1 << J;
-  int n[3] = {L, L, L};
-  cufftResult r = cufftPlanMany(&h, 3, n, n, stride, 1, n, stride, 1, CUFFT_C2C, batch);
-  if (r != CUFFT_SUCCESS)
-    return fail(HERMES_ERR_CUFFT, "cufftPlanMany(J=%d, interleaved batch=%d stride=%d) failed: %d", J, batch, stride, (int)r);
-  g_plans_il[key] = h;
-  *out = h;
-  return HERMES_OK;
-}
+// Batched contiguous complex-to-complex plan (batch fields of L^3, distance L^3).
+int get_plan_c2c_batch(int J, int batch, cufftHandle* out) { return get_plan(J, kC2C, batch, out); }
 
 #define HERMES_CUFFT_TRY(expr)                                                   \
   do {                                                                           \

@@ -214,33 +214,44 @@ def legendre_triple_coeff(l, lp, k):
     return float((2 * k + 1) * np.exp(log_val))
 
 
+_GAUNT = {}
+
+
+def _gaunt_device(n, device):
+    key = (n, str(device))
+    g = _GAUNT.get(key)
+    if g is None:
+        G = np.zeros((n, n, n))
+        for k in range(n):
+            for l in range(n):
+                for lp in range(n):
+                    G[k, l, lp] = legendre_triple_coeff(l, lp, k)
+        g = torch.as_tensor(G, device=device)
+        _GAUNT[key] = g
+    return g
+
+
 def mixing_solve(A, B, lmax, device="cuda"):
     """zeta_l for A(mu) = B(mu) C(mu) (special_functions.py:366-409), float64
-    on the GPU for all samples at once.  A, B: [n_samples, >= lmax+1]."""
-    A = np.atleast_2d(np.asarray(A, dtype=np.float64))[:, :lmax + 1]
-    B = np.atleast_2d(np.asarray(B, dtype=np.float64))[:, :lmax + 1]
+    on the GPU for all samples at once (hermes_mixing_solve).  A, B:
+    [n_samples, >= lmax+1].  Returns (C, M, cond) as numpy arrays."""
+    A = np.atleast_2d(np.asarray(A, dtype=np.float64))
+    B = np.atleast_2d(np.asarray(B, dtype=np.float64))
     n = lmax + 1
-    G = np.zeros((n, n, n))
-    for k in range(n):
-        for l in range(n):
-            for lp in range(n):
-                G[k, l, lp] = legendre_triple_coeff(l, lp, k)
+    if A.shape[1] < n or B.shape[1] < n:
+        raise ValueError("A and B must have length at least lmax+1.")
+    A, B = A[:, :n], B[:, :n]
     if np.any(B[:, 0] == 0):
         raise ValueError("B[0] is zero.")
-    Bt = torch.as_tensor(B, device=device)
-    At = torch.as_tensor(A, device=device)
-    Gt = torch.as_tensor(G, device=device)
-    f = Bt / Bt[:, :1]
-    M = torch.zeros((A.shape[0], n, n), dtype=torch.float64, device=device)
-    idx = torch.arange(1, n, device=device)
-    M[:, 0, idx] += f[:, idx] / (2 * idx + 1).double()
-    fm = f.clone()
-    fm[:, 0] = 0.0
-    M[:, 1:, :] += torch.einsum("klp,sp->skl", Gt[1:], fm)
-    M += torch.eye(n, dtype=torch.float64, device=device)
-    M *= Bt[:, :1, None]
-    C = torch.linalg.solve(M, At)
-    cond = torch.linalg.cond(M)
+    ns = A.shape[0]
+    At = torch.as_tensor(np.ascontiguousarray(A), device=device)
+    Bt = torch.as_tensor(np.ascontiguousarray(B), device=device)
+    C = torch.empty((ns, n), dtype=torch.float64, device=device)
+    M = torch.empty((ns, n, n), dtype=torch.float64, device=device)
+    cond = torch.empty(ns, dtype=torch.float64, device=device)
+    _lib.check(_lib.load().hermes_mixing_solve(_ptr(At), _ptr(Bt), _ptr(_gaunt_device(n, At.device)), ns, n,
+                                               _ptr(C), _ptr(M), _ptr(cond), _stream_ptr(At.device)),
+               "hermes_mixing_solve")
     return C.cpu().numpy(), M.cpu().numpy(), cond.cpu().numpy()
 
 

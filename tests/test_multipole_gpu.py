@@ -133,3 +133,19 @@ def test_multipole_J6_grid_vs_oracle():
     for s, (a, b) in enumerate(pairs[:3]):
         _, ref = oracle.calc_ddd_multipole(eps, eps, eps, a, b, 0, 4, PHI)
         assert _rel(got[s], ref) < 1e-4, (s, got[s], ref)
+
+
+def test_mixing_solve_matches_oracle():
+    """FP64 GPU mixing solve vs the float64 restatement of
+    solve_multipoles_from_ratio: zeta, M and cond(M) to 1e-10 relative."""
+    rng = np.random.default_rng(11)
+    lmax, ns = 10, 40
+    B = rng.standard_normal((ns, lmax + 1)) * 0.05
+    B[:, 0] = rng.uniform(0.5, 2.0, ns)
+    A = rng.standard_normal((ns, lmax + 1))
+    C, M, cond = mp.mixing_solve(A, B, lmax)
+    for s in range(ns):
+        c_ref, m_ref, cond_ref = oracle.solve_multipoles_from_ratio(A[s], B[s], lmax)
+        np.testing.assert_allclose(M[s], m_ref, rtol=1e-13, atol=1e-15)
+        assert _rel(C[s], c_ref) < 1e-10
+        assert abs(cond[s] - cond_ref) < 1e-10 * cond_ref
