@@ -23,7 +23,8 @@ the algorithmic FLOPs of the 27-term separable form, 8 * 15 * 15 * 27 * L^3
 per (l, m), against the measured bf16 peak; the kernel itself runs a
 restructured stencil on FP32 paired-FMA pipes (about 1.2e12 real FLOPs per
 (l, m) at J=9).  `traffic` is the DRAM bytes of one J=9 launch from the
-committed ncu summary profiles/mp_contract_kernel_J9.md.
+committed ncu summary profiles/mp_contract_kernel_J9.md (the deposit's from
+profiles/dep_accum_kernel_J9.md).
 `deposit` = the 4M-point J=9 deposit (Mparticles/s, HBM roofline of the
 accumulate kernel).  `--impl reference` times the float64 CPU restatement of
 the reference (oracle/) on a bounded unit and scales it the same way.
@@ -71,9 +72,10 @@ def load_peaks():
         return 6800.0, 1900.0, "fallback"
 
 
-def contract_traffic():
-    """DRAM bytes of one J=9 15x15 contraction launch (ncu, committed summary)."""
-    path = os.path.join(ROOT, "profiles", "mp_contract_kernel_J9.md")
+def profile_traffic(name):
+    """DRAM bytes per launch of a kernel from its committed ncu summary
+    (profiles/<name>.md, line `traffic_bytes_per_launch: N`), else None."""
+    path = os.path.join(ROOT, "profiles", name + ".md")
     try:
         with open(path) as f:
             for line in f:
@@ -292,8 +294,54 @@ def deposit_bench(dev, lib, kernels, phi, flush, steps):
             "value": DEP_N / (sum(step_ms) / steps / 1e3) / 1e6, "unit": "Mparticles/s",
             "ms_per_step": sum(step_ms) / steps, "launches_per_step": 7,
             "roofline": {"kernel": "dep_accum_kernel", "bound": "hbm", "achieved": ach, "peak": hbm,
-                         "peak_kind": kind, "unit": "GB/s", "frac": ach / hbm, "traffic": None,
+                         "peak_kind": kind, "unit": "GB/s", "frac": ach / hbm,
+                         "traffic": profile_traffic("dep_accum_kernel_J9"),
                          "algorithmic_bytes": alg, "ms_per_launch": acc_ms}}
+
+
+def run_case(args):
+    """Single-kernel workloads for profiling (`--case contract|deposit`): one
+    JSON line with the CUDA-event time per launch; not the headline metric."""
+    import torch
+
+    from pyhermes_gb300 import _lib, kernels, synthetic
+    from pyhermes_gb300 import multipole as mp
+    from pyhermes_gb300.phi import cal_gamma, sample_scaling_function
+    from pyhermes_gb300.window import phi_power_device, rfft_field
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    phi_np = sample_scaling_function()
+    phi = torch.as_tensor(phi_np, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    if args.case == "deposit":
+        flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+        out = deposit_bench(dev, _lib.load(), kernels, phi, flush, args.steps)
+        print(json.dumps({"case": "deposit", **out}))
+        return 0
+    J = args.J
+    L = 1 << J
+    pos, w = synthetic.lognormal_catalogue(MP_NDATA, box=BOX, ng=min(L, 256), device=dev)
+    pw = torch.as_tensor(w / w.sum(), device=dev)
+    eps, _, _ = kernels.deposit(torch.as_tensor(pos, device=dev), pw, J, BOX, phi)
+    eps = (eps - eps.double().mean().float()).contiguous()
+    P = phi_power_device(phi_np, L, 1, 1024, dev)
+    gam = cal_gamma(phi_np, 3, 1024)
+    grid = [r * L / BOX for r in MP_RADII]
+    f = mp.multipole_fields(rfield := rfft_field(eps), J, 2, 1, grid, P)
+    for _ in range(max(args.warmup, 1)):
+        mp.multipole_contract(eps, f, len(grid), gam, J, conj_sign=-1)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for a, b in ev:
+        a.record(stream)
+        S = mp.multipole_contract(eps, f, len(grid), gam, J, conj_sign=-1)
+        b.record(stream)
+    torch.cuda.synchronize(dev)
+    ms = sum(a.elapsed_time(b) for a, b in ev) / len(ev)
+    del rfield
+    print(json.dumps({"case": "contract", "J": J, "bins": len(grid), "l": 2, "m": 1, "ms_per_launch": ms,
+                      "algorithmic_flops": 8.0 * len(grid) ** 2 * 27 * L ** 3, "S00": [S[0, 0].real, S[0, 0].imag]}))
+    return 0
 
 
 def run_gb300(args, ws, rank, local):
@@ -438,7 +486,7 @@ def run_gb300(args, ws, rank, local):
                   "max_rel_diff_batched_vs_plain": mixed_vs_plain},
         "roofline": {"kernel": "mp_contract_kernel (+ mp_reduce_kernel)", "bound": "tensor",
                      "achieved": achieved, "peak": bf16, "peak_kind": kind, "unit": "TFLOP/s",
-                     "frac": achieved / bf16, "traffic": contract_traffic(),
+                     "frac": achieved / bf16, "traffic": profile_traffic("mp_contract_kernel_J9"),
                      "executes_on": "FP32 paired-FMA pipes (separable pair stencil + 4x2-blocked bin product)",
                      "algorithmic_flops": flops, "ms_per_launch": t_con * 1e3,
                      "fields_ms_per_lm": t_fld * 1e3},
@@ -466,7 +514,12 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--case", default="headline", choices=["headline", "contract", "deposit"],
+                    help="headline = the benchmark line; contract/deposit = one kernel, for profiling")
+    ap.add_argument("--J", type=int, default=7, help="grid level of --case contract")
     args = ap.parse_args()
+    if args.case != "headline":
+        return run_case(args)
     ws, rank, local = dist_setup()
     if args.impl == "reference":
         return run_reference(args, ws, rank)
