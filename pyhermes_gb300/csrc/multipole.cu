@@ -11,17 +11,15 @@
 //   mp_jl_table_kernel   j_l(2 pi sqrt(n2) R_b / L) tabulated over the integer
 //                        |k|^2 grid (float32, double-float phase)
 //   mp_prepass_kernel    eps_hat(k) K_lm^b(k) / L^3 for every bin b, Y_lm
-//                        shared by the bins, written as a batch of spectra
+//                        shared by the bins, written as a batch of spectra;
+//                        one window evaluation serves k and -k
 //   cuFFT (batched C2C)  -> a_lm^b(x) for every bin, one contiguous field per
 //                        bin (cuFFT is far slower on strided batches)
 //   mp_interleave_kernel bin-major -> bin-interleaved [cell][16], so one
 //                        cell's bins are one 128-byte row for the contraction
-//   mp_contract_kernel   persistent: per output tile, for every bin b3,
-//                        G^b3(y) = sum_{l1,l2} Gamma3 eps1(y+l1) a3^b3(y+l1-l2)
-//                        by separable shared-memory passes into a tile of G in
-//                        shared memory, then S[b2,b3] += sum_y a2^{b2}(y) G^b3(y)
-//                        (the bin x bin product over cells), float32 per tile,
-//                        float64 per thread
+//   mp_contract_kernel   S[b2,b3] = sum_y a2^{b2}(y) G^{b3}(y) with
+//                        G(y) = sum_{l1,l2} Gamma3 eps1(y+l1) a3(y+l1-l2), an
+//                        x-marching separable pair stencil (see the kernel)
 //   mp_reduce_kernel     float64 cross-block reduction
 // The identity S = sum_y a2(y) G3(y) is the reference sum with y = x - l1.
 // mp_plain_kernel is the reference-form contraction of one (a2, a3) pair
@@ -172,9 +170,49 @@ __device__ __forceinline__ float2 ylm_at(const YlmConst& Y, int a, int b, int c,
   return make_float2(yr, yi);
 }
 
-// out[b * L^3 + k] = eps_hat(k) * K_lm^b(k) / L^3 on the full FFT grid;
-// eps_hat comes from the half spectrum of a real field (Hermitian expansion).
-// NB4 = number of float4 groups of bins handled (bins padded to 4*NB4).
+// acc[b] = K_lm^b(x, y, z) = sum over the 8 images (a, b', c) (each axis
+// index i in {i - L, i}) of Pphi(|a|) Pphi(|b'|) Pphi(|c|) j_l(|k|) Y_lm(k).
+template <int NB4>
+__device__ __forceinline__ void mp_window_sum(int x, int y, int z, int L, const float* __restrict__ P,
+                                              const float4* __restrict__ T4, const YlmConst& Y,
+                                              float (&accr)[4 * NB4], float (&acci)[4 * NB4]) {
+#pragma unroll
+  for (int b = 0; b < 4 * NB4; ++b) accr[b] = acci[b] = 0.f;
+  const int ia[2] = {x - L, x}, ib[2] = {y - L, y}, ic[2] = {z - L, z};
+  const float pa[2] = {P[L - x], P[x]}, pb[2] = {P[L - y], P[y]}, pc[2] = {P[L - z], P[z]};
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        const int n2 = ia[i] * ia[i] + ib[j] * ib[j] + ic[k] * ic[k];
+        const float pw = pa[i] * pb[j] * pc[k];
+        const float2 yv = ylm_at(Y, ia[i], ib[j], ic[k], n2);
+        const float yr = pw * yv.x, yi = pw * yv.y;
+        const float4* tr = T4 + (long long)n2 * (kBinStride / 4);
+#pragma unroll
+        for (int q = 0; q < NB4; ++q) {
+          const float4 jl = __ldg(tr + q);
+          accr[4 * q + 0] = fmaf(jl.x, yr, accr[4 * q + 0]);
+          acci[4 * q + 0] = fmaf(jl.x, yi, acci[4 * q + 0]);
+          accr[4 * q + 1] = fmaf(jl.y, yr, accr[4 * q + 1]);
+          acci[4 * q + 1] = fmaf(jl.y, yi, acci[4 * q + 1]);
+          accr[4 * q + 2] = fmaf(jl.z, yr, accr[4 * q + 2]);
+          acci[4 * q + 2] = fmaf(jl.z, yi, acci[4 * q + 2]);
+          accr[4 * q + 3] = fmaf(jl.w, yr, accr[4 * q + 3]);
+          acci[4 * q + 3] = fmaf(jl.w, yi, acci[4 * q + 3]);
+        }
+      }
+}
+
+// out[b * L^3 + k] = eps_hat(k) * K_lm^b(k) / L^3 on the full FFT grid, from
+// the half spectrum of a real field.  A thread takes one half-spectrum mode
+// (x, y, z), z in [0, L/2], and also writes its mirror -k when z is not 0 or
+// L/2: eps_hat(-k) = conj(eps_hat(k)), and when x, y != 0 the mirror's image
+// set is the negated image set, so K(-k) = (-1)^l K(k) (Y_lm parity; the
+// float32 recurrences are sign-symmetric).  On the x = 0 or y = 0 lines the
+// image sets differ ({-L, 0} against {0, L}) and the mirror is evaluated.
 template <int NB4>
 __global__ void __launch_bounds__(256)
 mp_prepass_kernel(const float2* __restrict__ half, int J, const float* __restrict__ P,
@@ -182,49 +220,35 @@ mp_prepass_kernel(const float2* __restrict__ half, int J, const float* __restric
   constexpr int NB = 4 * NB4;
   const int L = 1 << J, H = L / 2 + 1, Lm = L - 1;
   const long long N = 1LL << (3 * J);
-  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < N;
-       idx += (long long)gridDim.x * blockDim.x) {
-    const int z = (int)(idx & Lm), y = (int)((idx >> J) & Lm), x = (int)(idx >> (2 * J));
-    float2 e;
-    if (z <= L / 2) {
-      e = half[((long long)x * L + y) * H + z];
-    } else {
-      const float2 t = half[((long long)((L - x) & Lm) * L + ((L - y) & Lm)) * H + (L - z)];
-      e = make_float2(t.x, -t.y);
-    }
+  const long long W = (long long)L * L * H;
+  const float lsign = (Y.l & 1) ? -1.f : 1.f;
+  for (long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x; w < W;
+       w += (long long)gridDim.x * blockDim.x) {
+    const int z = (int)(w % H), y = (int)((w / H) & Lm), x = (int)(w / ((long long)H * L));
+    const float2 e = half[w];
     float accr[NB], acci[NB];
-#pragma unroll
-    for (int b = 0; b < NB; ++b) accr[b] = acci[b] = 0.f;
-    const int ia[2] = {x - L, x}, ib[2] = {y - L, y}, ic[2] = {z - L, z};
-    const float pa[2] = {P[L - x], P[x]}, pb[2] = {P[L - y], P[y]}, pc[2] = {P[L - z], P[z]};
-#pragma unroll
-    for (int i = 0; i < 2; ++i)
-#pragma unroll
-      for (int j = 0; j < 2; ++j)
-#pragma unroll
-        for (int k = 0; k < 2; ++k) {
-          const int n2 = ia[i] * ia[i] + ib[j] * ib[j] + ic[k] * ic[k];
-          const float pw = pa[i] * pb[j] * pc[k];
-          const float2 yv = ylm_at(Y, ia[i], ib[j], ic[k], n2);
-          const float yr = pw * yv.x, yi = pw * yv.y;
-          const float4* tr = T4 + (long long)n2 * (kBinStride / 4);
-#pragma unroll
-          for (int q = 0; q < NB4; ++q) {
-            const float4 jl = __ldg(tr + q);
-            accr[4 * q + 0] = fmaf(jl.x, yr, accr[4 * q + 0]);
-            acci[4 * q + 0] = fmaf(jl.x, yi, acci[4 * q + 0]);
-            accr[4 * q + 1] = fmaf(jl.y, yr, accr[4 * q + 1]);
-            acci[4 * q + 1] = fmaf(jl.y, yi, acci[4 * q + 1]);
-            accr[4 * q + 2] = fmaf(jl.z, yr, accr[4 * q + 2]);
-            acci[4 * q + 2] = fmaf(jl.z, yi, acci[4 * q + 2]);
-            accr[4 * q + 3] = fmaf(jl.w, yr, accr[4 * q + 3]);
-            acci[4 * q + 3] = fmaf(jl.w, yi, acci[4 * q + 3]);
-          }
-        }
+    mp_window_sum<NB4>(x, y, z, L, P, T4, Y, accr, acci);
     const float er = e.x * inv_n, ei = e.y * inv_n;
+    const long long idx = ((long long)x * L + y) * L + z;
 #pragma unroll
     for (int b = 0; b < NB; ++b)
       if (b < nb) out[b * N + idx] = make_float2(er * accr[b] - ei * acci[b], er * acci[b] + ei * accr[b]);
+    if (z == 0 || z == L / 2) continue;
+    const int xm = (L - x) & Lm, ym = (L - y) & Lm, zm = L - z;
+    if (x == 0 || y == 0) {
+      mp_window_sum<NB4>(xm, ym, zm, L, P, T4, Y, accr, acci);
+    } else {
+#pragma unroll
+      for (int b = 0; b < NB; ++b) {
+        accr[b] *= lsign;
+        acci[b] *= lsign;
+      }
+    }
+    const float mr = e.x * inv_n, mi = -(e.y * inv_n);  // conj(eps_hat(k)) / L^3
+    const long long idm = ((long long)xm * L + ym) * L + zm;
+#pragma unroll
+    for (int b = 0; b < NB; ++b)
+      if (b < nb) out[b * N + idm] = make_float2(mr * accr[b] - mi * acci[b], mr * acci[b] + mi * accr[b]);
   }
 }
 
