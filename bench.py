@@ -26,7 +26,9 @@ restructured stencil on FP32 paired-FMA pipes (about 1.2e12 real FLOPs per
 committed ncu summary profiles/mp_contract_kernel_J9.md (the deposit's from
 profiles/dep_accum_kernel_J9.md).
 `deposit` = the 4M-point J=9 deposit (Mparticles/s, HBM roofline of the
-accumulate kernel).  `--impl reference` times the float64 CPU restatement of
+accumulate kernel).  `mc3pcf` = Monte Carlo 3PCF on a J=9 lognormal field:
+uniform-MC triplets/s and the learned importance-sampling proposal against
+uniform sampling (variance per sample, bias, equal-wall-time efficiency).  `--impl reference` times the float64 CPU restatement of
 the reference (oracle/) on a bounded unit and scales it the same way.
 Under torchrun each rank runs its own replica catalogue (replicas only: the
 path has no exchange step); rank 0 prints the aggregate.
@@ -61,6 +63,11 @@ WORKLOAD = ("3PCF multipoles: 1e6 lognormal data + 5e6 uniform randoms deposited
             "products delta_ddd_l + rrr_l (random field) + zeta_l")
 DEP_N = 4_000_000
 DEP_J = 9
+MC_N = 4_000_000          # points of the J=9 lognormal field the MC estimators gather from
+MC_CENTRES = 1_000_000    # throughput: centres x rotations = 1e8 triplets
+MC_ROT = 100
+MC_TRAIN = 10_000_000     # uniform samples the proposal network is trained on
+MC_SAMPLES = 100_000_000  # evaluation samples per estimator, split over the test triangles
 
 
 def load_peaks():
@@ -299,6 +306,89 @@ def deposit_bench(dev, lib, kernels, phi, flush, steps):
                          "algorithmic_bytes": alg, "ms_per_launch": acc_ms}}
 
 
+def mc_bench(dev, phi_np, steps):
+    """Monte Carlo 3PCF on a J=9 lognormal field (4e6 points): uniform-MC
+    triplet throughput of hermes_mc_triplets (1e6 centres x 100 rotations),
+    and the learned importance-sampling proposal (trained on 1e7 uniform
+    samples over r12, r13 in [20, 120] Mpc/h, mu in [-1, 1]) against uniform
+    sampling on three test triangles in the reference estimator's form
+    (centres x 100 rotations, hermes_mc_triplets with centre weights; the
+    learned centres are drawn from the proposal over a fresh uniform pool of
+    4x candidates per replicate), 8 independent replicates of ~4e6 triplets
+    per triangle and estimator: estimator variance from the replicate
+    spread, bias in units of the combined standard error, and variance x
+    time at equal wall time (the learned time includes the proposal)."""
+    import torch
+
+    from pyhermes_gb300 import kernels, mc3pcf, synthetic
+
+    L = 1 << DEP_J
+    sc = L / BOX
+    pos, w = synthetic.lognormal_catalogue(MC_N, box=BOX, seed_field=0, seed_poisson=1, seed_weights=2, device=dev)
+    phi = torch.as_tensor(phi_np, device=dev)
+    eps, _, _ = kernels.deposit(torch.as_tensor(pos, device=dev), torch.as_tensor(w / w.sum(), device=dev), DEP_J,
+                                BOX, phi)
+    rho = 1.0 / L ** 3
+    lp = mc3pcf.LearnedProposal(eps, eps, eps, DEP_J, phi_np, rho, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    rng = np.random.default_rng(7)
+    cen = torch.as_tensor(rng.uniform(0.0, L, (MC_CENTRES, 3)), device=dev)
+    off = mc3pcf.rotation_offsets(50.0 * sc, 80.0 * sc, 0.5, MC_ROT, rng=np.random.RandomState(8))
+    for _ in range(2):
+        mc3pcf.triplet_sum(lp.e1, lp.e2, lp.e3, DEP_J, cen, off, lp.phi_t)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for a, b in ev:
+        a.record(stream)
+        mc3pcf.triplet_sum(lp.e1, lp.e2, lp.e3, DEP_J, cen, off, lp.phi_t)
+        b.record(stream)
+    torch.cuda.synchronize(dev)
+    t_tr = sum(a.elapsed_time(b) for a, b in ev) / len(ev) / 1e3
+    ntr = MC_CENTRES * MC_ROT
+    hbm, _, kind = load_peaks()
+    ach = ntr * 324 / t_tr / 1e9
+
+    grid_r = [20.0, 53.3, 86.7, 120.0]
+    configs = [(r1 * sc, r2 * sc, mu) for r1 in grid_r for r2 in grid_r if r2 >= r1 for mu in (-0.75, -0.25, 0.25, 0.75)]
+    n_rot_train = 8
+    n_cen_train = MC_TRAIN // (len(configs) * n_rot_train)
+    t0 = time.perf_counter()
+    losses = lp.train(configs, n_centers=n_cen_train, n_rot_train=n_rot_train, epochs=3, seed=1)
+    torch.cuda.synchronize(dev)
+    t_train = time.perf_counter() - t0
+    tests = [(30.0, 60.0, 0.8), (60.0, 90.0, -0.3), (100.0, 120.0, 0.0)]
+    n_rot = 100
+    n_cen = MC_SAMPLES // (len(tests) * n_rot * 8)  # per replicate; 8 replicates
+    rows = []
+    for k, (r1, r2, mu) in enumerate(tests):
+        args = (r1 * sc, r2 * sc, mu, n_cen, n_rot)
+        lp.centre_estimate(*args, seed=1, replicates=2)  # warm-up
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        mu_u, se_u = lp.centre_estimate(*args, seed=100 + k, uniform=True)
+        torch.cuda.synchronize(dev)
+        t_u = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        mu_l, se_l = lp.centre_estimate(*args, seed=200 + k)  # includes the proposal on fresh candidate pools
+        torch.cuda.synchronize(dev)
+        t_l = time.perf_counter() - t0
+        se = float(np.sqrt(se_u ** 2 + se_l ** 2))
+        rows.append({"r12": r1, "r13": r2, "mu": mu, "triplets": 8 * n_cen * n_rot, "centres_per_replicate": n_cen,
+                     "rotations": n_rot, "mean_uniform": mu_u, "mean_learned": mu_l, "stderr_uniform": se_u,
+                     "stderr_learned": se_l, "variance_ratio_equal_samples": (se_u / se_l) ** 2,
+                     "bias_sigma": (mu_l - mu_u) / se, "s_uniform": t_u, "s_learned": t_l,
+                     "efficiency_equal_wall_time": (se_u ** 2 * t_u) / (se_l ** 2 * t_l)})
+    return {"metric": "uniform-MC triplet samples/s (J=9 lognormal field from 4e6 points)",
+            "value": ntr / t_tr, "unit": "triplets/s", "ms_per_launch": t_tr * 1e3,
+            "sample": f"{MC_CENTRES} centres x {MC_ROT} rotations, r12=50, r13=80 Mpc/h, mu=0.5",
+            "roofline": {"kernel": "mc_triplet_kernel", "bound": "hbm", "achieved": ach, "peak": hbm,
+                         "peak_kind": kind, "unit": "GB/s", "frac": ach / hbm,
+                         "algorithmic_bytes_per_triplet": 324,
+                         "note": "3 x 27 float32 gathers per triplet; the gathers are served mostly from L2"},
+            "learned_proposal": {"train_samples": len(configs) * n_cen_train * n_rot_train,
+                                 "train_s": t_train, "loss_first_last": [losses[0], losses[-1]],
+                                 "pool_factor": 4, "replicates": 8, "tests": rows}}
+
+
 def run_case(args):
     """Single-kernel workloads for profiling (`--case contract|deposit`): one
     JSON line with the CUDA-event time per launch; not the headline metric."""
@@ -314,6 +404,9 @@ def run_case(args):
     phi_np = sample_scaling_function()
     phi = torch.as_tensor(phi_np, device=dev)
     stream = torch.cuda.current_stream(dev)
+    if args.case == "mc":
+        print(json.dumps({"case": "mc", **mc_bench(dev, phi_np, args.steps)}))
+        return 0
     if args.case == "deposit":
         flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
         out = deposit_bench(dev, _lib.load(), kernels, phi, flush, args.steps)
@@ -465,6 +558,7 @@ def run_gb300(args, ws, rank, local):
 
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
     dep = deposit_bench(dev, lib, kernels, phi, flush, max(args.steps, 5))
+    mc = mc_bench(dev, phi_np, max(args.steps, 3))
 
     if rank != 0:
         if ws > 1:
@@ -491,6 +585,7 @@ def run_gb300(args, ws, rank, local):
                      "algorithmic_flops": flops, "ms_per_launch": t_con * 1e3,
                      "fields_ms_per_lm": t_fld * 1e3},
         "deposit": dep,
+        "mc3pcf": mc,
         "cpu_baseline": {"value": cpu_per_cat, "unit": "s/catalogue", "cores": cores, "kind": "port",
                          "sample": (f"one (r12, r13, l=1, m=1) unit at J=8 ({cpu_unit:.2f} s, float64 oracle "
                                     "restatement: windows, FFT convolutions, 729-term contraction); scaled x8 "
@@ -514,8 +609,8 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--case", default="headline", choices=["headline", "contract", "deposit"],
-                    help="headline = the benchmark line; contract/deposit = one kernel, for profiling")
+    ap.add_argument("--case", default="headline", choices=["headline", "contract", "deposit", "mc"],
+                    help="headline = the benchmark line; contract/deposit/mc = one part, for profiling")
     ap.add_argument("--J", type=int, default=7, help="grid level of --case contract")
     args = ap.parse_args()
     if args.case != "headline":

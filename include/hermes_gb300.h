@@ -256,6 +256,24 @@ int hermes_mc_triplets(const float* eps1, const float* eps2, const float* eps3, 
                        int phi_res, double rho1, double* sum_out, float* samples_out,
                        void* workspace, size_t workspace_bytes, void* stream);
 
+/* hermes_mc_sample: the same triplet product with ONE rotation per sampled
+ * centre, for importance sampling of single triplets (the learned proposal
+ * has no reference counterpart; each value is the reference's per-triplet
+ * product n1 n2 n3 of utils/corr3pcf_kernels.py:66-140).  Sample k's centre
+ * is pool[i] (pool: device [M][3] float64, grid units), i = idx[k] (device
+ * int64, clamped to [0, M)) or uniform in [0, M) when idx is NULL.  Offsets
+ * come from `offsets` [n][6] (device float64, grid units) or, when NULL, the
+ * triangle (R1, R2, mu) (grid units) rotated by three uniforms as
+ * generate_triangle_offsets (corr3pcf_kernels.py:21-63).  Random draws are
+ * SplitMix64 of (seed, k), so results do not depend on the launch shape.
+ * f_k = weights[k] (or 1) * n1 n2 n3; sums_out (host) = {sum f, sum f^2} in
+ * float64.  Workspace: hermes_mc_workspace_size.  Synchronises `stream`. */
+int hermes_mc_sample(const float* eps1, const float* eps2, const float* eps3, int J,
+                     const double* pool, int64_t M, const int64_t* idx, const double* weights,
+                     const double* offsets, int64_t n, double R1, double R2, double mu, uint64_t seed,
+                     const double* phi, int n_phi, int phi_res, double* sums_out,
+                     void* workspace, size_t workspace_bytes, void* stream);
+
 /* ---- learned proposal network (no reference counterpart) ---------------------
  * A tanh MLP with dims[0] inputs, dims[n_layers] outputs, widths <= 128:
  * params = per layer W [in][out] then b [out] (float32).  forward writes

@@ -45,6 +45,9 @@ SIGNATURES = {
     "hermes_multipole_contract_plain": (_c_int, [_p, _p, _p, _p, _c_int, _p, _p, _c_sz, _p]),
     "hermes_mixing_solve": (_c_int, [_p, _p, _p, _c_int, _c_int, _p, _p, _p, _p]),
     "hermes_mc_workspace_size": (_c_int, [ctypes.POINTER(_c_sz)]),
+    "hermes_mc_sample": (_c_int, [_p, _p, _p, _c_int, _p, ctypes.c_int64, _p, _p, _p, ctypes.c_int64, ctypes.c_double,
+                                  ctypes.c_double, ctypes.c_double, ctypes.c_uint64, _p, _c_int, _c_int, _p, _p, _c_sz,
+                                  _p]),
     "hermes_interp": (_c_int, [_p, _c_int, _p, _c_i64, _p, _c_int, _c_int, _dbl, _dbl, _dbl, _p, _p, _c_sz, _p]),
     "hermes_mc_triplets": (_c_int, [_p, _p, _p, _c_int, _p, _p, _c_i64, _p, _c_int, _p, _c_int, _c_int, _dbl,
                                     ctypes.POINTER(_dbl), _p, _p, _c_sz, _p]),

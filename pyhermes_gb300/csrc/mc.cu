@@ -112,6 +112,101 @@ __global__ void mc_sum_kernel(const double* __restrict__ partial, int n, double*
   if (threadIdx.x == 0) *out = sh[0];
 }
 
+// SplitMix64 (Steele, Lea and Flood, 2014): a counter-based generator, so a
+// sample's draws depend only on (seed, sample index) and not on the launch.
+__device__ __forceinline__ unsigned long long mc_splitmix(unsigned long long& s) {
+  unsigned long long z = (s += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+__device__ __forceinline__ double mc_u01(unsigned long long& s) {
+  return (double)(mc_splitmix(s) >> 11) * (1.0 / 9007199254740992.0);
+}
+
+// generate_triangle_offsets (corr3pcf_kernels.py:21-63) in float64 with the
+// angles given as fractions of a turn: phi = 2 pi fp, alpha = 2 pi fa.
+__device__ __forceinline__ void mc_triangle(double R1, double R2, double mu, double fp, double ct1, double fa,
+                                            double o[6]) {
+  const double st1 = sqrt(1.0 - ct1 * ct1);
+  double sp, cp, sa, ca;
+  sincospi(2.0 * fp, &sp, &cp);
+  sincospi(2.0 * fa, &sa, &ca);
+  const double dx1 = st1 * cp, dy1 = st1 * sp, dz1 = ct1;
+  double ox1, oy1, oz1;
+  if (fabs(dx1) > 1e-10 || fabs(dy1) > 1e-10) {
+    ox1 = -dy1; oy1 = dx1; oz1 = 0.0;
+  } else {
+    ox1 = 0.0; oy1 = -dz1; oz1 = dy1;
+  }
+  const double nrm = sqrt(ox1 * ox1 + oy1 * oy1 + oz1 * oz1);
+  ox1 /= nrm; oy1 /= nrm; oz1 /= nrm;
+  const double ox2 = dy1 * oz1 - dz1 * oy1, oy2 = dz1 * ox1 - dx1 * oz1, oz2 = dx1 * oy1 - dy1 * ox1;
+  double st2 = 1.0 - mu * mu;
+  if (st2 < 0.0) st2 = 0.0;
+  const double st = sqrt(st2);
+  o[0] = R1 * dx1; o[1] = R1 * dy1; o[2] = R1 * dz1;
+  o[3] = R2 * (mu * dx1 + st * (ca * ox1 + sa * ox2));
+  o[4] = R2 * (mu * dy1 + st * (ca * oy1 + sa * oy2));
+  o[5] = R2 * (mu * dz1 + st * (ca * oz1 + sa * oz2));
+}
+
+// One triplet per sample k: centre c = pool[i], i = idx[k] (clamped to
+// [0, M)) or uniform in [0, M) when idx == NULL; offsets from `offsets`
+// [n][6] or drawn (phi, cos theta1, alpha uniform, as the reference's three
+// uniforms); value f_k = w_k n1(c) n2(c + o1) n3(c + o2) (w_k = 1 when w is
+// NULL).  Block partial sums of f and f^2.
+__global__ void __launch_bounds__(256)
+mc_sample_kernel(const float* __restrict__ eps1, const float* __restrict__ eps2, const float* __restrict__ eps3,
+                 int J, const double* __restrict__ pool, long long M, const long long* __restrict__ idx,
+                 const double* __restrict__ w, const double* __restrict__ offsets, long long n, double R1, double R2,
+                 double mu,
+                 unsigned long long seed, const float* __restrict__ phis, int res, double* __restrict__ partial) {
+  double acc = 0.0, acc2 = 0.0;
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+    unsigned long long st = seed ^ ((unsigned long long)k * 0xD1B54A32D192ED03ull);
+    long long i;
+    if (idx) {
+      i = idx[k];
+      i = i < 0 ? 0 : (i >= M ? M - 1 : i);  // indices outside the pool are clamped, never read past it
+    } else {
+      i = (long long)(mc_u01(st) * (double)M);
+      if (i >= M) i = M - 1;
+    }
+    double o[6];
+    if (offsets) {
+#pragma unroll
+      for (int q = 0; q < 6; ++q) o[q] = offsets[6 * k + q];
+    } else {
+      const double a = mc_u01(st), bb = mc_u01(st), c = mc_u01(st);
+      mc_triangle(R1, R2, mu, a, 2.0 * bb - 1.0, c, o);
+    }
+    const double x = pool[3 * i], y = pool[3 * i + 1], z = pool[3 * i + 2];
+    const float n1 = mc_interp(eps1, phis, res, J, x, y, z);
+    const float n2 = mc_interp(eps2, phis, res, J, x + o[0], y + o[1], z + o[2]);
+    const float n3 = mc_interp(eps3, phis, res, J, x + o[3], y + o[4], z + o[5]);
+    double f = (double)(n1 * n2 * n3);
+    if (w) f *= w[k];
+    acc += f;
+    acc2 += f * f;
+  }
+  __shared__ double sh[2][256];
+  sh[0][threadIdx.x] = acc;
+  sh[1][threadIdx.x] = acc2;
+  __syncthreads();
+  for (int s2 = blockDim.x / 2; s2 > 0; s2 >>= 1) {
+    if (threadIdx.x < s2) {
+      sh[0][threadIdx.x] += sh[0][threadIdx.x + s2];
+      sh[1][threadIdx.x] += sh[1][threadIdx.x + s2];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    partial[blockIdx.x] = sh[0][0];
+    partial[gridDim.x + blockIdx.x] = sh[1][0];
+  }
+}
+
 int mc_grid() {
   int dev = 0, nsm = 148;
   cudaGetDevice(&dev);
@@ -125,7 +220,7 @@ extern "C" int hermes_mc_workspace_size(size_t* bytes) {
   if (!bytes) return fail(HERMES_ERR_INVALID, "bytes is NULL");
   hermes::Carver c(nullptr, 0);
   c.take<float>(4 * 1024);
-  c.take<double>((size_t)mc_grid() + 1);
+  c.take<double>(2 * ((size_t)mc_grid() + 1));
   *bytes = c.used;
   return HERMES_OK;
 }
@@ -139,7 +234,7 @@ static int mc_prepare(const double* phi, int n_phi, int res, void* workspace, si
   if (!workspace || workspace_bytes < need) return fail(HERMES_ERR_WORKSPACE, "mc: workspace %zu < %zu", workspace_bytes, need);
   hermes::Carver c(workspace, workspace_bytes);
   *phis = c.take<float>(4 * 1024);
-  *partial = c.take<double>((size_t)mc_grid() + 1);
+  *partial = c.take<double>(2 * ((size_t)mc_grid() + 1));
   mc_phi_kernel<<<4, 256, 0, s>>>(phi, n_phi, *phis);
   HERMES_LAUNCH_CHECK("mc_phi_kernel");
   return HERMES_OK;
@@ -182,6 +277,34 @@ extern "C" int hermes_mc_triplets(const float* eps1, const float* eps2, const fl
   mc_sum_kernel<<<1, 256, 0, s>>>(partial, g, partial + g);
   HERMES_LAUNCH_CHECK("mc_sum_kernel");
   HERMES_CUDA_TRY(cudaMemcpyAsync(sum_out, partial + g, sizeof(double), cudaMemcpyDeviceToHost, s));
+  HERMES_CUDA_TRY(cudaStreamSynchronize(s));
+  return HERMES_OK;
+}
+
+extern "C" int hermes_mc_sample(const float* eps1, const float* eps2, const float* eps3, int J, const double* pool,
+                                int64_t M, const int64_t* idx, const double* weights, const double* offsets,
+                                int64_t n, double R1, double R2, double mu, uint64_t seed, const double* phi,
+                                int n_phi, int phi_res, double* sums_out, void* workspace, size_t workspace_bytes,
+                                void* stream) {
+  if (!eps1 || !eps2 || !eps3 || !sums_out) return fail(HERMES_ERR_INVALID, "mc_sample: NULL argument");
+  if (J < 2 || J > 10) return fail(HERMES_ERR_INVALID, "mc_sample: J=%d outside [2,10]", J);
+  if (n < 0 || M < 0) return fail(HERMES_ERR_INVALID, "mc_sample: negative count");
+  if (n > 0 && (!pool || M == 0)) return fail(HERMES_ERR_INVALID, "mc_sample: empty centre pool");
+  cudaStream_t s = hermes::as_stream(stream);
+  float* phis;
+  double* partial;
+  int rc = mc_prepare(phi, n_phi, phi_res, workspace, workspace_bytes, &phis, &partial, s);
+  if (rc) return rc;
+  const int g = mc_grid();
+  mc_sample_kernel<<<g, 256, 0, s>>>(eps1, eps2, eps3, J, pool, (long long)M, reinterpret_cast<const long long*>(idx),
+                                     weights, offsets, (long long)n, R1, R2, mu, (unsigned long long)seed, phis,
+                                     phi_res, partial);
+  HERMES_LAUNCH_CHECK("mc_sample_kernel");
+  mc_sum_kernel<<<1, 256, 0, s>>>(partial, g, partial + 2 * g);
+  HERMES_LAUNCH_CHECK("mc_sum_kernel");
+  mc_sum_kernel<<<1, 256, 0, s>>>(partial + g, g, partial + 2 * g + 1);
+  HERMES_LAUNCH_CHECK("mc_sum_kernel");
+  HERMES_CUDA_TRY(cudaMemcpyAsync(sums_out, partial + 2 * g, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
   HERMES_CUDA_TRY(cudaStreamSynchronize(s));
   return HERMES_OK;
 }

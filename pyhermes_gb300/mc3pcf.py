@@ -123,6 +123,22 @@ def interp(grid, J, scaled_pos, phi_t, offset=(0.0, 0.0, 0.0)):
     return out
 
 
+def mc_sample(eps1, eps2, eps3, J, pool, phi_t, R1, R2, mu, n, seed=0, idx=None, weights=None, offsets=None):
+    """(sum f, sum f^2) in float64 over n one-rotation triplets f = w n1 n2 n3
+    (hermes_mc_sample): centre pool[idx[k]] (uniform from the pool when idx
+    is None), offsets given [n, 6] or drawn on the device for the triangle
+    (R1, R2, mu) in grid units."""
+    dev = eps2.device
+    out = (ctypes.c_double * 2)()
+    ws = _mc_workspace(dev)
+    rc = _lib.load().hermes_mc_sample(_ptr(eps1), _ptr(eps2), _ptr(eps3), J, _ptr(pool), pool.shape[0], _ptr(idx),
+                                      _ptr(weights), _ptr(offsets), int(n), float(R1), float(R2), float(mu),
+                                      int(seed) & ((1 << 64) - 1), _ptr(phi_t), phi_t.numel(), phi_t.numel() // 3,
+                                      out, _ptr(ws), ws.numel(), _stream_ptr(dev))
+    _lib.check(rc, "hermes_mc_sample")
+    return out[0], out[1]
+
+
 PRODUCT_DEPS = {"Q": ["zeta", "zeta_H"], "zeta_H": ["xi12", "xi13", "xi23"], "zeta": ["delta_ddd", "rrr"]}
 ALLOWED = {"ddd", "rrr", "delta_ddd", "xi12", "xi13", "xi23", "zeta", "zeta_H", "Q"}
 
@@ -479,6 +495,67 @@ class LearnedProposal:
             vals[s:e] = self._f_pairs(cen[s:e], off[s:e])
         v = vals * wts
         return float(v.mean()), v
+
+    def draw(self, q, n, generator):
+        """n i.i.d. pool indices from q and their weights (1/M)/q_i."""
+        M = q.shape[0]
+        cdf = torch.cumsum(q, 0)
+        u = torch.rand(n, generator=generator, device=self.device, dtype=torch.float64) * cdf[-1]
+        idx = torch.searchsorted(cdf, u).clamp_max(M - 1)
+        return idx, (1.0 / M) / q[idx]
+
+    def sample_stats(self, pool, r12s, r13s, mu, n_samples, seed=0, uniform=False, bf16=True, q=None,
+                     replicates=8):
+        """Single-triplet estimate of the pool mean of E_rot[f] through
+        hermes_mc_sample (rotations drawn on the GPU), as `replicates`
+        independent runs of n_samples / replicates i.i.d. samples: uniform
+        centres (weight 1) or centres from the proposal q (weight (1/M)/q).
+        Returns (mean, standard error from the replicate spread, variance
+        per sample)."""
+        if not uniform and q is None:
+            q = self.proposal(pool, r12s, r13s, mu, bf16=bf16)
+        gen = torch.Generator(device=self.device).manual_seed(seed)
+        nr = max(n_samples // replicates, 1)
+        means, s1, s2 = [], 0.0, 0.0
+        for r in range(replicates):
+            rseed = (seed * 0x9E3779B97F4A7C15 + r * 0xBF58476D1CE4E5B9) & ((1 << 64) - 1)
+            idx, wts = (None, None) if uniform else self.draw(q, nr, gen)
+            a, b = mc_sample(self.e1, self.e2, self.e3, self.J, pool, self.phi_t, r12s, r13s, mu, nr, rseed,
+                             idx=idx, weights=wts)
+            means.append(a / nr)
+            s1 += a
+            s2 += b
+        nt = nr * replicates
+        mean = float(np.mean(means))
+        var = max(s2 / nt - (s1 / nt) ** 2, 0.0)
+        return mean, float(np.std(means, ddof=1) / np.sqrt(replicates)), var
+
+    def centre_estimate(self, r12s, r13s, mu, n_centres, n_rot, seed=0, uniform=False, pool_factor=4,
+                        replicates=8, bf16=True):
+        """The reference estimator's form (centres x rotations, one rotation
+        set per run from a seeded MT19937 as rotation_offsets) with the
+        centres importance-sampled: each replicate draws a fresh uniform pool
+        of pool_factor * n_centres candidates, evaluates the proposal on it,
+        takes n_centres i.i.d. centres from q and weights them (1/M)/q, so
+        the estimate is unbiased for the box mean of E_rot[f].  Uniform:
+        n_centres uniform centres, weight 1.  Returns (mean, standard error
+        from the replicate spread)."""
+        gen = torch.Generator(device=self.device).manual_seed(seed)
+        means = []
+        for r in range(replicates):
+            off = rotation_offsets(r12s, r13s, mu, n_rot, rng=np.random.RandomState((seed * 1000003 + r) % (1 << 31)))
+            if uniform:
+                cen = torch.rand((n_centres, 3), generator=gen, device=self.device, dtype=torch.float64) * self.L
+                w = None
+            else:
+                pool = torch.rand((pool_factor * n_centres, 3), generator=gen, device=self.device,
+                                  dtype=torch.float64) * self.L
+                q = self.proposal(pool, r12s, r13s, mu, bf16=bf16)
+                idx, w = self.draw(q, n_centres, gen)
+                cen = pool[idx].contiguous()
+            tot, _ = triplet_sum(self.e1, self.e2, self.e3, self.J, cen, off, self.phi_t, center_w=w)
+            means.append(tot / (n_centres * n_rot))
+        return float(np.mean(means)), float(np.std(means, ddof=1) / np.sqrt(replicates))
 
     def _f_pairs(self, centers, offsets):
         o = torch.as_tensor(offsets, device=self.device)
