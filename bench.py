@@ -28,7 +28,9 @@ profiles/dep_accum_kernel_J9.md).
 `deposit` = the 4M-point J=9 deposit (Mparticles/s, HBM roofline of the
 accumulate kernel).  `mc3pcf` = Monte Carlo 3PCF on a J=9 lognormal field:
 uniform-MC triplets/s and the learned importance-sampling proposal against
-uniform sampling (variance per sample, bias, equal-wall-time efficiency).  `--impl reference` times the float64 CPU restatement of
+uniform sampling (variance per sample, bias, equal-wall-time efficiency).
+`c2_window_2pcf` = `field @ W` (gaussian R=10) and the 30x10 (s, mu) ring
+2PCF on the 4M-point J=9 field, with their HBM rooflines.  `--impl reference` times the float64 CPU restatement of
 the reference (oracle/) on a bounded unit and scales it the same way.
 Under torchrun each rank runs its own replica catalogue (replicas only: the
 path has no exchange step); rank 0 prints the aggregate.
@@ -306,6 +308,59 @@ def deposit_bench(dev, lib, kernels, phi, flush, steps):
                          "algorithmic_bytes": alg, "ms_per_launch": acc_ms}}
 
 
+def c2_bench(dev, phi, steps):
+    """4e6 lognormal points at J=9: `field @ W` (gaussian R=10 Mpc/h) and the
+    (s, mu) ring 2PCF 30x10 (s 5-150 Mpc/h, mu 0-1, smu_to_RH) through the
+    public API, CUDA-event timed with the field in HBM."""
+    import torch
+
+    from pyhermes_gb300 import kernels, synthetic
+    from pyhermes_gb300.corr2pcf import Corr_2PCF
+    from pyhermes_gb300.window import WindowFunc
+
+    pos, w = synthetic.lognormal_catalogue(DEP_N, box=BOX, seed_field=0, seed_poisson=1, seed_weights=2, device=dev)
+    f = deposit_field(torch.as_tensor(pos, device=dev), torch.as_tensor(w, device=dev), DEP_J, phi,
+                      kernels.DepositWorkspace(dev))
+    L = 1 << DEP_J
+    stream = torch.cuda.current_stream(dev)
+    win = WindowFunc({"type": "gaussian", "len_args": {"R": 10.0}}, f.sfc_info)
+
+    def timed(fn, n):
+        for _ in range(2):
+            fn()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
+        for a, b in ev:
+            a.record(stream)
+            fn()
+            b.record(stream)
+        torch.cuda.synchronize(dev)
+        return sum(a.elapsed_time(b) for a, b in ev) / n / 1e3
+
+    t_win = timed(lambda: f @ win, steps)
+    s_edges = np.linspace(5.0, 150.0, 31)
+    mu_edges = np.linspace(0.0, 1.0, 11)
+    task = Corr_2PCF({"Corr_2PCF": {
+        "sfc_field": f, "random": "uniform", "binning_window": {"type": "ring"},
+        "sampling": {"s": 0.5 * (s_edges[1:] + s_edges[:-1]), "mu": 0.5 * (mu_edges[1:] + mu_edges[:-1])},
+        "products": ["delta_dd", "xi"]}}, device=dev)
+    t_2pcf = timed(lambda: task.run(save_result=False), steps)
+    hbm, _, kind = load_peaks()
+    real_b, half_b = L ** 3 * 4, L * L * (L // 2 + 1) * 8
+    win_bytes = 2 * (real_b + half_b) + 2 * half_b  # rFFT r+w, irFFT r+w, window pass r+w
+    tp_bytes = real_b + 2 * half_b                  # rFFT of the field + one read of the half spectrum
+    return {"metric": "field @ gaussian(R=10) and 30x10 (s, mu) ring 2PCF, 4e6 lognormal points, J=9",
+            "window_ms": t_win * 1e3, "twopcf_ms": t_2pcf * 1e3, "twopcf_bins": 300,
+            "window_roofline": {"bound": "hbm", "achieved": win_bytes / t_win / 1e9, "peak": hbm, "peak_kind": kind,
+                                "unit": "GB/s", "frac": win_bytes / t_win / 1e9 / hbm,
+                                "algorithmic_bytes": win_bytes,
+                                "note": "cuFFT R2C + on-the-fly window multiply + cuFFT C2R"},
+            "twopcf_roofline": {"bound": "hbm", "achieved": tp_bytes / t_2pcf / 1e9, "peak": hbm,
+                                "peak_kind": kind, "unit": "GB/s", "frac": tp_bytes / t_2pcf / 1e9 / hbm,
+                                "algorithmic_bytes": tp_bytes,
+                                "note": "one forward rFFT and one pass over the half spectrum for all 300 bins; "
+                                        "the pass evaluates 300 ring windows x 8 images per mode (compute-bound)"}}
+
+
 def mc_bench(dev, phi_np, steps):
     """Monte Carlo 3PCF on a J=9 lognormal field (4e6 points): uniform-MC
     triplet throughput of hermes_mc_triplets (1e6 centres x 100 rotations),
@@ -314,7 +369,7 @@ def mc_bench(dev, phi_np, steps):
     sampling on three test triangles in the reference estimator's form
     (centres x 100 rotations, hermes_mc_triplets with centre weights; the
     learned centres are drawn from the proposal over a fresh uniform pool of
-    4x candidates per replicate), 8 independent replicates of ~4e6 triplets
+    2x candidates per replicate), 8 independent replicates of ~4e6 triplets
     per triangle and estimator: estimator variance from the replicate
     spread, bias in units of the combined standard error, and variance x
     time at equal wall time (the learned time includes the proposal)."""
@@ -357,18 +412,20 @@ def mc_bench(dev, phi_np, steps):
     t_train = time.perf_counter() - t0
     tests = [(30.0, 60.0, 0.8), (60.0, 90.0, -0.3), (100.0, 120.0, 0.0)]
     n_rot = 100
+    pool_factor = 2
     n_cen = MC_SAMPLES // (len(tests) * n_rot * 8)  # per replicate; 8 replicates
     rows = []
     for k, (r1, r2, mu) in enumerate(tests):
         args = (r1 * sc, r2 * sc, mu, n_cen, n_rot)
-        lp.centre_estimate(*args, seed=1, replicates=2)  # warm-up
+        lp.centre_estimate(*args, seed=1, replicates=2, pool_factor=pool_factor)  # warm-up
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
         mu_u, se_u = lp.centre_estimate(*args, seed=100 + k, uniform=True)
         torch.cuda.synchronize(dev)
         t_u = time.perf_counter() - t0
         t0 = time.perf_counter()
-        mu_l, se_l = lp.centre_estimate(*args, seed=200 + k)  # includes the proposal on fresh candidate pools
+        # includes the proposal on fresh candidate pools
+        mu_l, se_l = lp.centre_estimate(*args, seed=200 + k, pool_factor=pool_factor)
         torch.cuda.synchronize(dev)
         t_l = time.perf_counter() - t0
         se = float(np.sqrt(se_u ** 2 + se_l ** 2))
@@ -386,7 +443,7 @@ def mc_bench(dev, phi_np, steps):
                          "note": "3 x 27 float32 gathers per triplet; the gathers are served mostly from L2"},
             "learned_proposal": {"train_samples": len(configs) * n_cen_train * n_rot_train,
                                  "train_s": t_train, "loss_first_last": [losses[0], losses[-1]],
-                                 "pool_factor": 4, "replicates": 8, "tests": rows}}
+                                 "pool_factor": pool_factor, "replicates": 8, "tests": rows}}
 
 
 def run_case(args):
@@ -404,6 +461,9 @@ def run_case(args):
     phi_np = sample_scaling_function()
     phi = torch.as_tensor(phi_np, device=dev)
     stream = torch.cuda.current_stream(dev)
+    if args.case == "c2":
+        print(json.dumps({"case": "c2", **c2_bench(dev, phi, args.steps)}))
+        return 0
     if args.case == "mc":
         print(json.dumps({"case": "mc", **mc_bench(dev, phi_np, args.steps)}))
         return 0
@@ -559,6 +619,7 @@ def run_gb300(args, ws, rank, local):
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
     dep = deposit_bench(dev, lib, kernels, phi, flush, max(args.steps, 5))
     mc = mc_bench(dev, phi_np, max(args.steps, 3))
+    c2 = c2_bench(dev, phi, max(args.steps, 3))
 
     if rank != 0:
         if ws > 1:
@@ -586,6 +647,7 @@ def run_gb300(args, ws, rank, local):
                      "fields_ms_per_lm": t_fld * 1e3},
         "deposit": dep,
         "mc3pcf": mc,
+        "c2_window_2pcf": c2,
         "cpu_baseline": {"value": cpu_per_cat, "unit": "s/catalogue", "cores": cores, "kind": "port",
                          "sample": (f"one (r12, r13, l=1, m=1) unit at J=8 ({cpu_unit:.2f} s, float64 oracle "
                                     "restatement: windows, FFT convolutions, 729-term contraction); scaled x8 "
@@ -609,8 +671,8 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--case", default="headline", choices=["headline", "contract", "deposit", "mc"],
-                    help="headline = the benchmark line; contract/deposit/mc = one part, for profiling")
+    ap.add_argument("--case", default="headline", choices=["headline", "contract", "deposit", "mc", "c2"],
+                    help="headline = the benchmark line; contract/deposit/mc/c2 = one part, for profiling")
     ap.add_argument("--J", type=int, default=7, help="grid level of --case contract")
     args = ap.parse_args()
     if args.case != "headline":

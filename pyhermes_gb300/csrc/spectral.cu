@@ -164,12 +164,32 @@ __global__ void phi_power_to_f32(const double* __restrict__ p, int n, float* __r
   if (i < n) out[i] = (float)p[i];
 }
 
-// spec[k] *= K(k) * factor on the half spectrum [L][L][L/2+1].
+// spec[k] *= K(k) * factor on the half spectrum [L][L][L/2+1].  The gaussian
+// exp(-q^2/2) factors over the axes, so its image sum is G(x) G(y) G(z) with
+// G(i) = sum over the axis images u of P(|u|) exp(-(2 pi u R / L)^2 / 2),
+// tabulated per block in shared memory (the other windows are evaluated per
+// mode by kernel_value).
 __global__ void spec_apply_window_kernel(float2* __restrict__ spec, WinDev w, int L,
                                          const double* __restrict__ pd, int np, int bw, float factor) {
   extern __shared__ float P[];
+  float* G = P + np;  // [L], gaussian only
   for (int i = threadIdx.x; i < np; i += blockDim.x) P[i] = (float)pd[i];
   __syncthreads();
+  const bool sep = w.type == HERMES_WIN_GAUSSIAN;
+  if (sep) {
+    for (int i = threadIdx.x; i < L; i += blockDim.x) {
+      float g = 0.f;
+      for (int kk = 0; kk < bw; ++kk) {
+        const int u1 = kk * L + i, u2 = kk * L + (L - i);
+        const float q1 = kTwoPi * ((float)u1 * w.rho_hi[0] + (float)u1 * w.rho_lo[0]);
+        const float q2 = kTwoPi * ((float)u2 * w.rho_hi[0] + (float)u2 * w.rho_lo[0]);
+        g = fmaf(P[u1], expf(-0.5f * q1 * q1), g);
+        g = fmaf(P[u2], expf(-0.5f * q2 * q2), g);
+      }
+      G[i] = g;
+    }
+    __syncthreads();
+  }
   const int H = L / 2 + 1;
   const long long total = (long long)L * L * H;
   const long long stride = (long long)gridDim.x * blockDim.x;
@@ -177,7 +197,13 @@ __global__ void spec_apply_window_kernel(float2* __restrict__ spec, WinDev w, in
     const int z = (int)(m % H);
     const long long r = m / H;
     const int y = (int)(r % L), x = (int)(r / L);
-    const float2 K = kernel_value(w, x, y, z, L, P, bw);
+    float2 K;
+    if (sep) {
+      K = make_float2(G[x] * G[y] * G[z] * w.scale, 0.f);
+      if (w.zero_k0 && m == 0) K.x = 0.f;
+    } else {
+      K = kernel_value(w, x, y, z, L, P, bw);
+    }
     const float2 s = spec[m];
     spec[m] = make_float2((s.x * K.x - s.y * K.y) * factor, (s.x * K.y + s.y * K.x) * factor);
   }
@@ -230,7 +256,7 @@ struct PPArgs {
 // grid.x: mode blocks; grid.y: bin groups.  partial[(blockIdx.x * n_bins + b) * n_pairs + p].
 // NP = number of (i, j) spectrum pairs handled together (compile-time).
 template <int NP>
-__global__ void __launch_bounds__(kPPThreads)
+__global__ void __launch_bounds__(kPPThreads, 2)
 pair_products_kernel(PPArgs a, const WinDev* __restrict__ wins, const double* __restrict__ pd,
                      double* __restrict__ partial, double* __restrict__ k0) {
   extern __shared__ float P[];
@@ -401,7 +427,7 @@ extern "C" int hermes_window_apply(const float* eps, float* out, int J, const he
   const int np = L * bandwidth + 1;
   const long long total = (long long)L * L * (L / 2 + 1);
   const float factor = (float)(1.0 / ((double)L * L * L));
-  spec_apply_window_kernel<<<grid_for(total, 256), 256, np * sizeof(float), as_stream(stream)>>>(
+  spec_apply_window_kernel<<<grid_for(total, 256), 256, (np + L) * sizeof(float), as_stream(stream)>>>(
       spec, w, L, phi_power, np, bandwidth, factor);
   HERMES_LAUNCH_CHECK("spec_apply_window_kernel");
   return hermes_fft_c2r(spec, out, J, stream);
@@ -437,6 +463,152 @@ extern "C" int hermes_spectrum_multiply(void* spec, const float* k_real, const v
       static_cast<float2*>(spec), k_real, static_cast<const float2*>(k_cplx), total, (float)factor);
   HERMES_LAUNCH_CHECK("spec_multiply_kernel");
   return HERMES_OK;
+}
+
+// Cylindrical bins (ring / disk / cylshell / cylinder) with the line of sight
+// on z: the kernel is K(x, y, z) = scale * A(x, y) * B(z) with
+//   A = sum over the (x, y) images of P P f(k_perp R),  B = sum over the z
+//   images of P g(k_par H)   (cyl_image_sum).
+// A block takes kCylBins bins; B is tabulated for them in shared memory
+// (z in [0, L/2]).  A warp takes one (x, y) column at a time: it stages the
+// column's spectrum values in shared memory, each lane computes A for its
+// kCylBins/32 bins and then streams the column's modes, so per mode and bin
+// there is one table load and two FMAs, and the spectra are read once per
+// block group of bins.
+constexpr int kCylBins = 64;
+constexpr int kCylPerLane = kCylBins / 32;
+
+template <int NP>
+__global__ void __launch_bounds__(kPPThreads, 2)
+pair_products_cylz_kernel(PPArgs a, const WinDev* __restrict__ wins, const double* __restrict__ pd,
+                          double* __restrict__ partial, double* __restrict__ k0) {
+  constexpr int kWarps = kPPThreads / 32;
+  extern __shared__ __align__(16) unsigned char cyl_sm[];
+  const int L = a.L, H = L / 2 + 1;
+  float* P = reinterpret_cast<float*>(cyl_sm);
+  float* B = P + ((a.np + 3) & ~3);                          // [kCylBins][H]
+  float* T = B + (size_t)kCylBins * H;                        // [kWarps][NP][H] column products
+  double* red = reinterpret_cast<double*>(T + (size_t)kWarps * NP * H + 2);  // [kWarps][kCylBins][NP]
+  for (int i = threadIdx.x; i < a.np; i += blockDim.x) P[i] = (float)pd[i];
+  const int b0 = blockIdx.y * kCylBins;
+  const int nb = min(kCylBins, a.n_bins - b0);
+  __syncthreads();
+  if (blockIdx.x == 0 && threadIdx.x < nb) k0[b0 + threadIdx.x] = (double)kernel_value(wins[b0 + threadIdx.x], 0, 0, 0, L, P, a.bw).x;
+  const int sgn = wins[b0].mode == HERMES_KMODE_OCTANT ? 1 : -1;
+  for (int i = threadIdx.x; i < kCylBins * H; i += blockDim.x) {
+    const int b = i / H, z = i - b * H;
+    float v = 0.f;
+    if (b < nb) {
+      const WinDev& w = wins[b0 + b];
+      for (int kk = 0; kk < a.bw; ++kk) {
+        const int cp = kk * L + z, cn = kk * L + (L - z);
+        v = fmaf(P[cp], cyl_par(w, cp), v);
+        v = fmaf(P[cn], cyl_par(w, sgn * cn), v);
+      }
+      v *= w.scale;
+    }
+    B[i] = v;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  float* Tw = T + (size_t)wid * NP * H;
+  double acc[kCylPerLane][NP];
+  int zk[kCylPerLane];
+#pragma unroll
+  for (int j = 0; j < kCylPerLane; ++j) {
+    const int b = lane + 32 * j;
+    zk[j] = b < nb ? wins[b0 + b].zero_k0 : 0;
+#pragma unroll
+    for (int p = 0; p < NP; ++p) acc[j][p] = 0.0;
+  }
+  const int n_img = 4 * a.bw * a.bw;
+  for (long long col = (long long)blockIdx.x * kWarps + wid; col < (long long)L * L;
+       col += (long long)gridDim.x * kWarps) {
+    const int x = (int)(col / L), y = (int)(col % L);
+    const long long mbase = col * H;
+    __syncwarp();
+    for (int z = lane; z < H; z += 32) {  // weighted Re(u conj v) of the column's modes
+      const long long m = mbase + z;
+      const float wgt = (z == 0 || z == L / 2) ? 1.f : 2.f;
+#pragma unroll
+      for (int p = 0; p < NP; ++p) {
+        const float2 u = a.si[p][m], v = a.sj[p][m];
+        Tw[p * H + z] = (a.exclude_k0 && m == 0) ? 0.f : wgt * (u.x * v.x + u.y * v.y);
+      }
+    }
+    float A[kCylPerLane];
+#pragma unroll
+    for (int j = 0; j < kCylPerLane; ++j) {
+      const int b = lane + 32 * j;
+      float av = 0.f;
+      if (b < nb) {
+        const WinDev& w = wins[b0 + b];
+        for (int t = 0; t < n_img; ++t) {
+          const int pair = t >> 2, sp = t & 1, sq = (t >> 1) & 1;
+          const int ii = pair / a.bw, jj = pair - ii * a.bw;
+          const int pu = sp ? ii * L + (L - x) : ii * L + x;
+          const int qu = sq ? jj * L + (L - y) : jj * L + y;
+          av = fmaf(P[pu] * P[qu], cyl_perp(w, sp ? sgn * pu : pu, sq ? sgn * qu : qu), av);
+        }
+      }
+      A[j] = av;
+    }
+    __syncwarp();
+    float fac[kCylPerLane][NP];
+#pragma unroll
+    for (int j = 0; j < kCylPerLane; ++j)
+#pragma unroll
+      for (int p = 0; p < NP; ++p) fac[j][p] = 0.f;
+    for (int z = 0; z < H; ++z) {
+      float tr[NP];
+#pragma unroll
+      for (int p = 0; p < NP; ++p) tr[p] = Tw[p * H + z];
+#pragma unroll
+      for (int j = 0; j < kCylPerLane; ++j) {
+        const float bz = B[(lane + 32 * j) * H + z];
+#pragma unroll
+        for (int p = 0; p < NP; ++p) fac[j][p] = fmaf(tr[p], bz, fac[j][p]);
+      }
+    }
+    const bool origin = col == 0;
+#pragma unroll
+    for (int j = 0; j < kCylPerLane; ++j)
+#pragma unroll
+      for (int p = 0; p < NP; ++p) {
+        float f = fac[j][p];
+        if (origin && zk[j]) f -= Tw[p * H] * B[(lane + 32 * j) * H];  // K(0,0,0) forced to 0
+        acc[j][p] += (double)A[j] * (double)f;
+      }
+  }
+  // block reduction over warps (fixed order -> deterministic)
+#pragma unroll
+  for (int j = 0; j < kCylPerLane; ++j)
+#pragma unroll
+    for (int p = 0; p < NP; ++p) red[((size_t)wid * kCylBins + lane + 32 * j) * NP + p] = acc[j][p];
+  __syncthreads();
+  for (int i = threadIdx.x; i < nb * NP; i += blockDim.x) {
+    double v = 0.0;
+    for (int w2 = 0; w2 < kWarps; ++w2) v += red[(size_t)w2 * kCylBins * NP + i];
+    const int b = i / NP, p = i - b * NP;
+    partial[((long long)blockIdx.x * a.n_bins + b0 + b) * a.n_pairs + p] = v;
+  }
+}
+
+static size_t cylz_smem(int np, int L, int n_pairs) {
+  const int H = L / 2 + 1;
+  return sizeof(float) * ((((size_t)np + 3) & ~(size_t)3) + (size_t)kCylBins * H + (size_t)(kPPThreads / 32) * n_pairs * H + 2) +
+         sizeof(double) * (size_t)(kPPThreads / 32) * kCylBins * n_pairs + 16;
+}
+
+// True when every bin is a cylindrical window with the line of sight on z
+// and all bins use the same image mode (the column kernel's precondition).
+static bool all_cyl_z(const std::vector<WinDev>& hw) {
+  for (const WinDev& w : hw) {
+    const bool cyl = w.type == HERMES_WIN_RING || w.type == HERMES_WIN_DISK || w.type == HERMES_WIN_CYLSHELL ||
+                     w.type == HERMES_WIN_CYLINDER;
+    if (!cyl || w.los_axis != 2 || w.mode != hw[0].mode) return false;
+  }
+  return !hw.empty();
 }
 
 static long long pp_mode_blocks(int J) {
@@ -503,6 +675,47 @@ extern "C" int hermes_pair_products(const void* const* spectra, int n_spec, cons
   double* dk0 = c.take<double>((size_t)n_bins);
   cudaStream_t s = as_stream(stream);
   HERMES_CUDA_TRY(cudaMemcpyAsync(dwin, hw.data(), sizeof(WinDev) * n_bins, cudaMemcpyHostToDevice, s));
+  if (all_cyl_z(hw) && n_pairs <= 4 && cylz_smem(a.np, L, n_pairs) <= 200 * 1024) {
+    // about 2 resident blocks per SM over all bin groups, so each block's
+    // table of B(z) is reused over many columns
+    int dev = 0, nsm = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const int groups = (n_bins + kCylBins - 1) / kCylBins;
+    long long cblk = (2LL * nsm + groups - 1) / groups;
+    const long long max_cols = (long long)L * L / (kPPThreads / 32);
+    if (cblk > max_cols) cblk = max_cols;
+    if (cblk > nblk) cblk = nblk;  // partial sums sized for nblk blocks
+    if (cblk < 1) cblk = 1;
+    dim3 cgrid((unsigned)cblk, (unsigned)groups);
+    const size_t csm = cylz_smem(a.np, L, n_pairs);
+    switch (n_pairs) {
+      case 1:
+        HERMES_CUDA_TRY(cudaFuncSetAttribute(pair_products_cylz_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm));
+        pair_products_cylz_kernel<1><<<cgrid, kPPThreads, csm, s>>>(a, dwin, phi_power, partial, dk0);
+        break;
+      case 2:
+        HERMES_CUDA_TRY(cudaFuncSetAttribute(pair_products_cylz_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm));
+        pair_products_cylz_kernel<2><<<cgrid, kPPThreads, csm, s>>>(a, dwin, phi_power, partial, dk0);
+        break;
+      case 3:
+        HERMES_CUDA_TRY(cudaFuncSetAttribute(pair_products_cylz_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm));
+        pair_products_cylz_kernel<3><<<cgrid, kPPThreads, csm, s>>>(a, dwin, phi_power, partial, dk0);
+        break;
+      default:
+        HERMES_CUDA_TRY(cudaFuncSetAttribute(pair_products_cylz_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm));
+        pair_products_cylz_kernel<4><<<cgrid, kPPThreads, csm, s>>>(a, dwin, phi_power, partial, dk0);
+        break;
+    }
+    HERMES_LAUNCH_CHECK("pair_products_cylz_kernel");
+    const double cscale = 1.0 / ((double)L * L * L * (double)L * L * L);
+    reduce_partials_kernel<<<n_bins * n_pairs, 256, 0, s>>>(partial, (int)cblk, n_bins * n_pairs, cscale, dout);
+    HERMES_LAUNCH_CHECK("reduce_partials_kernel");
+    HERMES_CUDA_TRY(cudaMemcpyAsync(out, dout, sizeof(double) * n_bins * n_pairs, cudaMemcpyDeviceToHost, s));
+    if (k0_out) HERMES_CUDA_TRY(cudaMemcpyAsync(k0_out, dk0, sizeof(double) * n_bins, cudaMemcpyDeviceToHost, s));
+    HERMES_CUDA_TRY(cudaStreamSynchronize(s));
+    return HERMES_OK;
+  }
   dim3 grid((unsigned)nblk, (unsigned)((n_bins + kBinsPerGroup - 1) / kBinsPerGroup));
   const size_t sm = a.np * sizeof(float);
   switch (n_pairs) {
