@@ -217,6 +217,19 @@ int hermes_multipole_contract(const float* eps1, const void* fields2, int nb2,
                               const void* fields3, int nb3, int conj_sign,
                               const double* gamma, int J, double* out,
                               void* workspace, size_t workspace_bytes, void* stream);
+/* hermes_multipole_contract_async: the same S[b2][b3] (times 4 pi / L^3) into
+ * the DEVICE array dev_out [16][16][2] float64 (slots b >= nb are zero or
+ * unspecified), with no host synchronisation and no host-device copy, so a
+ * sequence of fields/contract calls can be captured into a CUDA graph once
+ * cuFFT plans and kernel attributes exist (make one uncaptured call per J
+ * first).  chunk_x: x planes per work item (power of two <= L; 0 = min(64, L));
+ * ctas_per_sm: 1 or 2 (0 = 2) -- the tile choices an autotuner varies.  Same
+ * reference sum as hermes_multipole_contract (corr3pcf_multipoles.py:33-58). */
+int hermes_multipole_contract_async(const float* eps1, const void* fields2, int nb2,
+                                    const void* fields3, int nb3, int conj_sign,
+                                    const double* gamma, int J, int chunk_x, int ctas_per_sm,
+                                    double* dev_out, void* workspace, size_t workspace_bytes,
+                                    void* stream);
 int hermes_multipole_contract_plain(const float* eps1, const void* a2, const void* a3,
                                     const double* gamma, int J, double* out,
                                     void* workspace, size_t workspace_bytes, void* stream);

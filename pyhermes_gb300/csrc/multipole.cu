@@ -104,7 +104,13 @@ __device__ float sph_jl_f32(int l, float xh, float xl) {
 
 // T[n2 * kBinStride + b] = j_l(2 pi sqrt(n2) R_b / L), n2 = 0 .. n2max (rows
 // padded to 16 floats so one image's bins are four float4 loads).
-__global__ void mp_jl_table_kernel(float* __restrict__ T, int n2max, const float* __restrict__ rho,
+struct RhoArgs {
+  float v[2 * kMaxBins];  // R_b / L as double-float (hi, lo) pairs
+};
+
+// Radii travel as a kernel argument (no host-to-device copy), so the fields
+// call can be captured into a CUDA graph.
+__global__ void mp_jl_table_kernel(float* __restrict__ T, int n2max, RhoArgs rho,
                                    int nb, int l) {
   const long long total = (long long)(n2max + 1) * kBinStride;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
@@ -116,7 +122,7 @@ __global__ void mp_jl_table_kernel(float* __restrict__ T, int n2max, const float
     }
     float nh, nl, xh, xl;
     df_sqrt_int(n2, nh, nl);
-    df_mul(nh, nl, rho[2 * b], rho[2 * b + 1], xh, xl);
+    df_mul(nh, nl, rho.v[2 * b], rho.v[2 * b + 1], xh, xl);
     T[i] = sph_jl_f32(l, xh, xl);
   }
 }
@@ -303,7 +309,7 @@ constexpr int kA3Plane = HY * HZ * kBinStride;  // float2
 constexpr int kA2Stride = kBinStride + 2;       // float2 per cell (pad: no bank conflicts)
 constexpr int kA2Plane = kCols * kA2Stride;
 constexpr int kEpsPlane = EY * EZ;
-constexpr int kMaxCX = 64;
+constexpr int kMaxCX = 64;  // default x-chunk below L = 256
 // a3 planes x2, a2 planes x3, V ring x3, eps planes x2, one G plane, float64 S
 constexpr size_t kSmem = sizeof(float2) * (2 * kA3Plane + 3 * kA2Plane + kA2Plane) +
                          sizeof(float) * (3 * kVPlane + 2 * kEpsPlane) + sizeof(double) * 2 * kMaxBins * kMaxBins;
@@ -610,7 +616,8 @@ __global__ void __launch_bounds__(ct::kThreads, 2) mp_contract_kernel(ContractAr
 }
 
 // out[o] = sum over blocks of partial[blk * nout + o]
-__global__ void mp_reduce_kernel(const double* __restrict__ partial, int nblocks, int nout, double* __restrict__ out) {
+__global__ void mp_reduce_kernel(const double* __restrict__ partial, int nblocks, int nout, double* __restrict__ out,
+                                 double scale = 1.0) {
   const int o = blockIdx.x;
   double s = 0.0;
   for (int b = threadIdx.x; b < nblocks; b += blockDim.x) s += partial[(long long)b * nout + o];
@@ -621,7 +628,7 @@ __global__ void mp_reduce_kernel(const double* __restrict__ partial, int nblocks
     if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
     __syncthreads();
   }
-  if (threadIdx.x == 0) out[o] = sh[0];
+  if (threadIdx.x == 0) out[o] = sh[0] * scale;
 }
 
 // ---- plain reference-form contraction of one (a2, a3) pair -----------------
@@ -768,25 +775,25 @@ extern "C" int hermes_multipole_fields(const void* half_spec, int J, int l, int 
   const long long N = 1LL << (3 * J);
   cudaStream_t s = hermes::as_stream(stream);
   hermes::Carver c(workspace, workspace_bytes);
-  float* rho = c.take<float>(2 * kMaxBins);
+  c.take<float>(2 * kMaxBins);
   float* T = c.take<float>(table_floats(J));
   float* Pf = c.take<float>(L + 1);
   c.take<double>((size_t)1024 * kMaxBins * kMaxBins * 2);
   c.take<double>((size_t)kMaxBins * kMaxBins * 2);
   float2* binmajor = nb > 1 ? c.take<float2>((size_t)nb * N) : static_cast<float2*>(fields_out);
-  float hrho[2 * kMaxBins];
+  RhoArgs hrho;
   for (int b = 0; b < nb; ++b) {
     if (!(radii[b] >= 0.0)) return fail(HERMES_ERR_INVALID, "multipole_fields: radius %d must be >= 0", b);
     const double v = radii[b] / (double)L;
-    hrho[2 * b] = (float)v;
-    hrho[2 * b + 1] = (float)(v - (double)hrho[2 * b]);
+    hrho.v[2 * b] = (float)v;
+    hrho.v[2 * b + 1] = (float)(v - (double)hrho.v[2 * b]);
   }
-  HERMES_CUDA_TRY(cudaMemcpyAsync(rho, hrho, sizeof(float) * 2 * nb, cudaMemcpyHostToDevice, s));
   mp_power_to_f32<<<(L + 1 + 255) / 256, 256, 0, s>>>(phi_power, L + 1, Pf);
   HERMES_LAUNCH_CHECK("mp_power_to_f32");
   const int n2max = 3 * L * L;
   const int nsm = sm_count();
-  mp_jl_table_kernel<<<nsm * 8, 256, 0, s>>>(T, n2max, rho, nb, l);
+  for (int b = nb; b < kMaxBins; ++b) hrho.v[2 * b] = hrho.v[2 * b + 1] = 0.f;
+  mp_jl_table_kernel<<<nsm * 8, 256, 0, s>>>(T, n2max, hrho, nb, l);
   HERMES_LAUNCH_CHECK("mp_jl_table_kernel");
   const YlmConst Y = make_ylm(l, m);
   const float inv_n = (float)(1.0 / (double)N);
@@ -815,10 +822,12 @@ extern "C" int hermes_multipole_fields(const void* half_spec, int J, int l, int 
   return HERMES_OK;
 }
 
-extern "C" int hermes_multipole_contract(const float* eps1, const void* fields2, int nb2, const void* fields3,
-                                         int nb3, int conj_sign, const double* gamma, int J, double* out,
-                                         void* workspace, size_t workspace_bytes, void* stream) {
-  if (!eps1 || !fields2 || !gamma || !out) return fail(HERMES_ERR_INVALID, "multipole_contract: NULL argument");
+// Launches the contraction and the float64 reduction into dout [16][16][2]
+// (already multiplied by `scale`), with no host synchronisation.
+static int mp_contract_launch(const float* eps1, const void* fields2, int nb2, const void* fields3, int nb3,
+                              int conj_sign, const double* gamma, int J, int chunk_x, int ctas_per_sm, double scale,
+                              double* dout, void* workspace, size_t workspace_bytes, cudaStream_t s) {
+  if (!eps1 || !fields2 || !gamma || !dout) return fail(HERMES_ERR_INVALID, "multipole_contract: NULL argument");
   if (nb2 < 1 || nb2 > kMaxBins) return fail(HERMES_ERR_INVALID, "multipole_contract: nb2=%d", nb2);
   const int conj_src = fields3 == nullptr;
   if (conj_src) {
@@ -826,21 +835,34 @@ extern "C" int hermes_multipole_contract(const float* eps1, const void* fields2,
     if (conj_sign != 1 && conj_sign != -1) return fail(HERMES_ERR_INVALID, "multipole_contract: conj_sign must be +-1");
   }
   if (nb3 < 1 || nb3 > kMaxBins) return fail(HERMES_ERR_INVALID, "multipole_contract: nb3=%d", nb3);
-  size_t need = 0;
-  int rc = hermes_multipole_workspace_size(J, nb2 > nb3 ? nb2 : nb3, &need);
-  if (rc) return rc;
-  if (!workspace || workspace_bytes < need) return fail(HERMES_ERR_WORKSPACE, "multipole_contract: workspace %zu < %zu", workspace_bytes, need);
+  if (J < 4 || J > 10) return fail(HERMES_ERR_INVALID, "multipole_contract: J=%d outside [4,10]", J);
   const int L = 1 << J;
-  const long long N = 1LL << (3 * J);
-  cudaStream_t s = hermes::as_stream(stream);
+  // default x-chunk: 128 planes from L = 256 up (what the tile autotuner picks
+  // there: the 4-plane halo costs 3% and work items still outnumber the CTAs),
+  // else min(64, L)
+  if (chunk_x == 0) chunk_x = L >= 256 ? 128 : (L < ct::kMaxCX ? L : ct::kMaxCX);
+  if (chunk_x < 1 || chunk_x > L || (chunk_x & (chunk_x - 1)) != 0)
+    return fail(HERMES_ERR_INVALID, "multipole_contract: chunk_x=%d must be a power of two in [1, L=%d]", chunk_x, L);
+  if (ctas_per_sm == 0) ctas_per_sm = 2;
+  if (ctas_per_sm < 1 || ctas_per_sm > 2) return fail(HERMES_ERR_INVALID, "multipole_contract: ctas_per_sm=%d", ctas_per_sm);
+  size_t need = 0;
+  int rc = hermes_multipole_workspace_size(J, 1, &need);
+  if (rc) return rc;
+  if (!workspace || workspace_bytes < need)
+    return fail(HERMES_ERR_WORKSPACE, "multipole_contract: workspace %zu < %zu", workspace_bytes, need);
   hermes::Carver c(workspace, workspace_bytes);
   c.take<float>(2 * kMaxBins);
   c.take<float>(table_floats(J));
   c.take<float>(L + 1);
   double* partial = c.take<double>((size_t)1024 * kMaxBins * kMaxBins * 2);
-  double* dout = c.take<double>((size_t)kMaxBins * kMaxBins * 2);
-  HERMES_CUDA_TRY(cudaFuncSetAttribute(mp_contract_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)ct::kSmem));
+  static bool smem_set[64] = {false};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64 || !smem_set[dev]) {  // once per device, before any stream capture
+    HERMES_CUDA_TRY(cudaFuncSetAttribute(mp_contract_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)ct::kSmem));
+    if (dev >= 0 && dev < 64) smem_set[dev] = true;
+  }
   // field layout follows hermes_multipole_fields: [cell][16] for nb > 1, [cell] for nb == 1
   ContractArgs A;
   A.eps1 = eps1;
@@ -851,27 +873,60 @@ extern "C" int hermes_multipole_contract(const float* eps1, const void* fields2,
   A.conj_src = conj_src;
   A.sign = (float)conj_sign;
   A.J = J;
-  A.CX = L < ct::kMaxCX ? L : ct::kMaxCX;
+  A.CX = chunk_x;
   A.gm = make_gamma(gamma);
   A.partial = partial;
   const int n_items = (L / A.CX) * (L / ct::TY) * (L / ct::TZ);
-  int nblk = 2 * sm_count();  // two resident CTAs per SM
+  int nblk = ctas_per_sm * sm_count();
   if (nblk > n_items) nblk = n_items;
   if (nblk > 1024) nblk = 1024;
   mp_contract_kernel<<<nblk, ct::kThreads, ct::kSmem, s>>>(A);
   HERMES_LAUNCH_CHECK("mp_contract_kernel");
-  mp_reduce_kernel<<<kMaxBins * kMaxBins * 2, 256, 0, s>>>(partial, nblk, kMaxBins * kMaxBins * 2, dout);
+  mp_reduce_kernel<<<kMaxBins * kMaxBins * 2, 256, 0, s>>>(partial, nblk, kMaxBins * kMaxBins * 2, dout, scale);
   HERMES_LAUNCH_CHECK("mp_reduce_kernel");
+  return HERMES_OK;
+}
+
+extern "C" int hermes_multipole_contract(const float* eps1, const void* fields2, int nb2, const void* fields3,
+                                         int nb3, int conj_sign, const double* gamma, int J, double* out,
+                                         void* workspace, size_t workspace_bytes, void* stream) {
+  if (!out) return fail(HERMES_ERR_INVALID, "multipole_contract: NULL argument");
+  if (J < 4 || J > 10) return fail(HERMES_ERR_INVALID, "multipole_contract: J=%d outside [4,10]", J);
+  size_t need = 0;
+  int rc = hermes_multipole_workspace_size(J, 1, &need);
+  if (rc) return rc;
+  if (!workspace || workspace_bytes < need)
+    return fail(HERMES_ERR_WORKSPACE, "multipole_contract: workspace %zu < %zu", workspace_bytes, need);
+  hermes::Carver c(workspace, workspace_bytes);
+  c.take<float>(2 * kMaxBins);
+  c.take<float>(table_floats(J));
+  c.take<float>((1 << J) + 1);
+  c.take<double>((size_t)1024 * kMaxBins * kMaxBins * 2);
+  double* dout = c.take<double>((size_t)kMaxBins * kMaxBins * 2);
+  cudaStream_t s = hermes::as_stream(stream);
+  const double scale = 4.0 * 3.141592653589793 / (double)(1LL << (3 * J));
+  rc = mp_contract_launch(eps1, fields2, nb2, fields3, nb3, conj_sign, gamma, J, 0, 0, scale, dout, workspace,
+                          workspace_bytes, s);
+  if (rc) return rc;
+  if (fields3 == nullptr) nb3 = nb2;
   std::vector<double> h((size_t)kMaxBins * kMaxBins * 2);
   HERMES_CUDA_TRY(cudaMemcpyAsync(h.data(), dout, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, s));
   HERMES_CUDA_TRY(cudaStreamSynchronize(s));
-  const double scale = 4.0 * 3.141592653589793 / (double)N;
   for (int a = 0; a < nb2; ++a)
     for (int b = 0; b < nb3; ++b) {
-      out[(a * nb3 + b) * 2] = h[(a * kMaxBins + b) * 2] * scale;
-      out[(a * nb3 + b) * 2 + 1] = h[(a * kMaxBins + b) * 2 + 1] * scale;
+      out[(a * nb3 + b) * 2] = h[(a * kMaxBins + b) * 2];
+      out[(a * nb3 + b) * 2 + 1] = h[(a * kMaxBins + b) * 2 + 1];
     }
   return HERMES_OK;
+}
+
+extern "C" int hermes_multipole_contract_async(const float* eps1, const void* fields2, int nb2, const void* fields3,
+                                               int nb3, int conj_sign, const double* gamma, int J, int chunk_x,
+                                               int ctas_per_sm, double* dev_out, void* workspace,
+                                               size_t workspace_bytes, void* stream) {
+  const double scale = 4.0 * 3.141592653589793 / (double)(1LL << (3 * (J < 0 ? 0 : (J > 10 ? 10 : J))));
+  return mp_contract_launch(eps1, fields2, nb2, fields3, nb3, conj_sign, gamma, J, chunk_x, ctas_per_sm, scale,
+                            dev_out, workspace, workspace_bytes, hermes::as_stream(stream));
 }
 
 extern "C" int hermes_multipole_contract_plain(const float* eps1, const void* a2, const void* a3,

@@ -62,7 +62,7 @@ def _ws_bytes(J, nb):
 BIN_STRIDE = 16
 
 
-def multipole_fields(half_spec, J, l, m, radii_grid, phi_power, out=None):
+def multipole_fields(half_spec, J, l, m, radii_grid, phi_power, out=None, ws=None):
     """a_lm^b = ifftn(fftn(eps) K_lm^b) for thin-shell radii (grid units).
 
     Returns complex64 [L^3, 16] (bin-interleaved; bins >= nb unused) for
@@ -73,7 +73,8 @@ def multipole_fields(half_spec, J, l, m, radii_grid, phi_power, out=None):
     if out is None:
         shape = (N,) if nb == 1 else (N, BIN_STRIDE)
         out = torch.empty(shape, dtype=torch.complex64, device=dev)
-    ws = _workspace(_ws_bytes(J, nb), dev)
+    if ws is None:
+        ws = _workspace(_ws_bytes(J, nb), dev)
     radii = (ctypes.c_double * nb)(*[float(r) for r in radii_grid])
     _lib.check(_lib.load().hermes_multipole_fields(_ptr(half_spec), J, int(l), int(m), radii, nb, _ptr(phi_power),
                                                    _ptr(out), _ptr(ws), ws.numel(), _stream_ptr(dev)),
@@ -95,6 +96,23 @@ def multipole_contract(eps1, fields2, nb2, gamma, J, fields3=None, nb3=None, con
     return out[..., 0] + 1j * out[..., 1]
 
 
+def multipole_contract_async(eps1, fields2, nb2, gamma_c, J, dev_out, fields3=None, nb3=None, conj_sign=1,
+                             chunk_x=0, ctas_per_sm=0, ws=None):
+    """hermes_multipole_contract_async: S (times 4 pi / L^3) into the device
+    float64 tensor dev_out [16, 16, 2] on the current stream, no host sync.
+    gamma_c: a ctypes double[9] (kept alive by the caller during capture)."""
+    nb3 = nb2 if fields3 is None else nb3
+    dev = eps1.device
+    if ws is None:
+        ws = _workspace(_ws_bytes(J, max(nb2, nb3)), dev)
+    _lib.check(_lib.load().hermes_multipole_contract_async(_ptr(eps1), _ptr(fields2), nb2, _ptr(fields3), nb3,
+                                                           int(conj_sign), gamma_c, J, int(chunk_x),
+                                                           int(ctas_per_sm), _ptr(dev_out), _ptr(ws), ws.numel(),
+                                                           _stream_ptr(dev)),
+               "hermes_multipole_contract_async")
+    return dev_out
+
+
 def multipole_contract_plain(eps1, a2, a3, gamma, J):
     dev = eps1.device
     ws = _workspace(_ws_bytes(J, 1), dev)
@@ -105,6 +123,81 @@ def multipole_contract_plain(eps1, a2, a3, gamma, J):
                                                            ws.numel(), _stream_ptr(dev)),
                "hermes_multipole_contract_plain")
     return complex(out[0], out[1])
+
+
+class GraphedMultipole:
+    """The (l, m) loop of MultipoleEngine.ddd for one (J, radii, l_max) with
+    vertices 2 and 3 sharing the field and radii, as ONE CUDA graph: the rFFT
+    of the field and, for every (l, m >= 0), hermes_multipole_fields +
+    hermes_multipole_contract_async into a device array of S matrices.  The
+    graph works on fixed buffers, including its own workspace: run(delta)
+    copies the field into them and replays.  The first run does one uncaptured pass (cuFFT plans, workspace,
+    kernel attributes) and then captures.  chunk_x / ctas_per_sm are the
+    contraction tile choices (see autotune.tune_contract)."""
+
+    def __init__(self, J, box_size, radii_phys, l_max, phi_array, device, phi_resolution=1024, chunk_x=0,
+                 ctas_per_sm=0, use_graph=True):
+        self.J, self.L, self.box = int(J), 1 << int(J), float(box_size)
+        self.dev = torch.device(device)
+        self.radii = [float(r) for r in radii_phys]
+        if not 1 < len(self.radii) <= MAX_BINS:
+            raise ValueError(f"GraphedMultipole needs 2..{MAX_BINS} radii.")
+        self.grid = [r * self.L / self.box for r in self.radii]
+        self.l_max = int(l_max)
+        self.lm = [(l, m) for l in range(self.l_max + 1) for m in range(l + 1)]
+        phi = np.asarray(phi_array, dtype=np.float64)
+        self.gamma = (ctypes.c_double * 9)(*cal_gamma(phi, phi.shape[0] // phi_resolution, phi_resolution).ravel())
+        self.P = phi_power_device(phi, self.L, 1, phi_resolution, self.dev)
+        L = self.L
+        self.eps = torch.empty((L, L, L), dtype=torch.float32, device=self.dev)
+        self.spec = torch.empty((L, L, L // 2 + 1), dtype=torch.complex64, device=self.dev)
+        self.fields = torch.empty((L ** 3, BIN_STRIDE), dtype=torch.complex64, device=self.dev)
+        self.out = torch.zeros((len(self.lm), MAX_BINS, MAX_BINS, 2), dtype=torch.float64, device=self.dev)
+        # own workspace: a captured graph must never see the shared one reallocated
+        self.ws = torch.empty(max(_ws_bytes(self.J, len(self.grid)), 256), dtype=torch.uint8, device=self.dev)
+        self.chunk_x, self.ctas = int(chunk_x), int(ctas_per_sm)
+        self.use_graph = bool(use_graph)
+        self.graph = None
+
+    def _body(self):
+        lib = _lib.load()
+        _lib.check(lib.hermes_fft_r2c(_ptr(self.eps), _ptr(self.spec), self.J, _stream_ptr(self.dev)), "hermes_fft_r2c")
+        nb = len(self.grid)
+        for k, (l, m) in enumerate(self.lm):
+            multipole_fields(self.spec, self.J, l, m, self.grid, self.P, out=self.fields, ws=self.ws)
+            multipole_contract_async(self.eps, self.fields, nb, self.gamma, self.J, self.out[k],
+                                     conj_sign=(-1) ** ((l + m) % 2), chunk_x=self.chunk_x,
+                                     ctas_per_sm=self.ctas, ws=self.ws)
+
+    def summands(self, delta):
+        """S_lm[i, j] (complex128 [n_lm, nb, nb]) for the field delta."""
+        self.eps.copy_(delta.to(torch.float32))
+        if not self.use_graph:
+            self._body()
+        else:
+            if self.graph is None:
+                self._body()  # uncaptured pass: plans, workspace and attributes exist before capture
+                torch.cuda.synchronize(self.dev)
+                g = torch.cuda.CUDAGraph()
+                with torch.cuda.graph(g):
+                    self._body()
+                self.graph = g
+            self.graph.replay()
+        nb = len(self.grid)
+        o = self.out[:, :nb, :nb].cpu().numpy()
+        return o[..., 0] + 1j * o[..., 1]
+
+    def ddd(self, delta, pairs, l_min=0):
+        """DDD_l [n_samples, n_l] for (r12, r13) samples drawn from the radii
+        (the same combination as MultipoleEngine.ddd)."""
+        S = self.summands(delta)
+        idx = {r: i for i, r in enumerate(self.radii)}
+        k_of = {lm: k for k, lm in enumerate(self.lm)}
+        res = np.zeros((len(pairs), self.l_max - l_min + 1))
+        for li, l in enumerate(range(l_min, self.l_max + 1)):
+            for s, (a, b) in enumerate(pairs):
+                res[s, li] = combine_multipole_m_terms([S[k_of[(l, m)]][idx[a], idx[b]] for m in range(l + 1)], l)
+        return res
 
 
 def combine_multipole_m_terms(m_values, l):
