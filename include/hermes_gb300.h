@@ -217,6 +217,28 @@ int hermes_multipole_contract(const float* eps1, const void* fields2, int nb2,
                               const void* fields3, int nb3, int conj_sign,
                               const double* gamma, int J, double* out,
                               void* workspace, size_t workspace_bytes, void* stream);
+/* hermes_multipole_fields_window / _table: the same fields for radial
+ * profiles other than the thin shell (radial_multipole_windows.py:186-313),
+ * the Y_lm, image sum, FFT and output layout unchanged.  _window: isotropic
+ * analytic transfers of `bins` (host, nb; types SPHERE, GAUSSIAN, SHELL,
+ * THICK_SHELL, GAUSSIAN_SHELL, lengths in grid units) -- the l = 0 monopole
+ * path of the reference.  _table: U_l(k) from uniform tables over
+ * [0, k_max[b]] (tables: device float64, bin b at offsets[b], sizes[b] >= 4
+ * points; offsets, sizes, k_max on the host), evaluated at physical
+ * k = |k_grid| * grid_to_physical (grid_to_physical = L / box) with the
+ * reference's local cubic (utils/radial_multipole_windows.py:186-210); the
+ * tables come from the host restatement of build_radial_multipole_table
+ * (utils/radial_profiles.py:651-709). */
+int hermes_multipole_fields_window(const void* half_spec, int J, int l, int m,
+                                   const hermes_window_t* bins, int nb, const double* phi_power,
+                                   void* fields_out, void* workspace, size_t workspace_bytes,
+                                   void* stream);
+int hermes_multipole_fields_table(const void* half_spec, int J, int l, int m, const double* tables,
+                                  const int64_t* offsets, const int32_t* sizes, const double* k_max,
+                                  double grid_to_physical, int nb, const double* phi_power,
+                                  void* fields_out, void* workspace, size_t workspace_bytes,
+                                  void* stream);
+
 /* hermes_multipole_contract_async: the same S[b2][b3] (times 4 pi / L^3) into
  * the DEVICE array dev_out [16][16][2] float64 (slots b >= nb are zero or
  * unspecified), with no host synchronisation and no host-device copy, so a

@@ -42,6 +42,9 @@ SIGNATURES = {
     "hermes_multipole_workspace_size": (_c_int, [_c_int, _c_int, ctypes.POINTER(_c_sz)]),
     "hermes_multipole_fields": (_c_int, [_p, _c_int, _c_int, _c_int, _p, _c_int, _p, _p, _p, _c_sz, _p]),
     "hermes_multipole_contract": (_c_int, [_p, _p, _c_int, _p, _c_int, _c_int, _p, _c_int, _p, _p, _c_sz, _p]),
+    "hermes_multipole_fields_window": (_c_int, [_p, _c_int, _c_int, _c_int, _p, _c_int, _p, _p, _p, _c_sz, _p]),
+    "hermes_multipole_fields_table": (_c_int, [_p, _c_int, _c_int, _c_int, _p, _p, _p, _p, _dbl, _c_int, _p, _p, _p,
+                                               _c_sz, _p]),
     "hermes_multipole_contract_async": (_c_int, [_p, _p, _c_int, _p, _c_int, _c_int, _p, _c_int, _c_int, _c_int, _p, _p,
                                                  _c_sz, _p]),
     "hermes_multipole_contract_plain": (_c_int, [_p, _p, _p, _p, _c_int, _p, _p, _c_sz, _p]),

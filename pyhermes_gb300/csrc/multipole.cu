@@ -36,6 +36,7 @@
 
 namespace hermes {
 int get_plan_c2c_batch(int J, int batch, cufftHandle* out);
+int prepare_window(const hermes_window_t& in, int L, WinDev* out);
 }
 
 namespace {
@@ -124,6 +125,84 @@ __global__ void mp_jl_table_kernel(float* __restrict__ T, int n2max, RhoArgs rho
     df_sqrt_int(n2, nh, nl);
     df_mul(nh, nl, rho.v[2 * b], rho.v[2 * b + 1], xh, xl);
     T[i] = sph_jl_f32(l, xh, xl);
+  }
+}
+
+// T[n2 * 16 + b] = U_b(|k|) for isotropic window transfers (sphere, gaussian,
+// shell, thick_shell, gaussian_shell; the analytic monopole profiles of
+// radial_multipole_windows.py:60-128), k = sqrt(n2) / L.  The window
+// descriptors are staged in shared memory.
+struct IsoWins {
+  hermes::WinDev w[kMaxBins];
+};
+__global__ void mp_iso_table_kernel(float* __restrict__ T, int n2max, IsoWins wins, int nb) {
+  __shared__ hermes::WinDev sw[kMaxBins];
+  if (threadIdx.x < kMaxBins) sw[threadIdx.x] = wins.w[threadIdx.x];
+  __syncthreads();
+  const long long total = (long long)(n2max + 1) * kBinStride;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int n2 = (int)(i / kBinStride), b = (int)(i % kBinStride);
+    float v = 0.f;
+    if (b < nb) {
+      bool ok;
+      v = hermes::window_iso_n2(sw[b], n2, &ok).x * sw[b].scale;
+      if (!ok) v = __int_as_float(0x7fc00000);
+    }
+    T[i] = v;
+  }
+}
+
+// T[n2 * 16 + b] = U_b(k) from uniform tables over k in [0, kmax_b] (n_b
+// points; physical k = sqrt(n2) * k_scale), with the local cubic of
+// radial_multipole_windows.py:186-210 (linear in the first and last
+// interval, clamped outside), float64.
+struct TabArgs {
+  long long off[kMaxBins];
+  int n[kMaxBins];
+  double kmax[kMaxBins];
+  double k_scale;  // grid_to_physical / L
+};
+__global__ void mp_tab_table_kernel(float* __restrict__ T, int n2max, const double* __restrict__ tables, TabArgs ta,
+                                    int nb) {
+  __shared__ long long soff[kMaxBins];
+  __shared__ int sn[kMaxBins];
+  __shared__ double skm[kMaxBins];
+  if (threadIdx.x < kMaxBins) {
+    soff[threadIdx.x] = ta.off[threadIdx.x];
+    sn[threadIdx.x] = ta.n[threadIdx.x];
+    skm[threadIdx.x] = ta.kmax[threadIdx.x];
+  }
+  __syncthreads();
+  const long long total = (long long)(n2max + 1) * kBinStride;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int n2 = (int)(i / kBinStride), b = (int)(i % kBinStride);
+    double v = 0.0;
+    if (b < nb) {
+      const double* t = tables + soff[b];
+      const int n = sn[b];
+      const double km = skm[b];
+      const double k = sqrt((double)n2) * ta.k_scale;
+      if (k <= 0.0) {
+        v = t[0];
+      } else if (k >= km) {
+        v = t[n - 1];
+      } else {
+        const double idx = k * (double)(n - 1) / km;
+        const int lo = (int)idx;
+        const double f = idx - (double)lo;
+        if (lo == 0 || lo >= n - 2) {
+          v = t[lo] * (1.0 - f) + t[lo + 1] * f;
+        } else {
+          const double p0 = t[lo - 1], p1 = t[lo], p2 = t[lo + 1], p3 = t[lo + 2];
+          const double f2 = f * f, f3 = f2 * f;
+          v = 0.5 * (2.0 * p1 + (-p0 + p2) * f + (2.0 * p0 - 5.0 * p1 + 4.0 * p2 - p3) * f2 +
+                     (-p0 + 3.0 * p1 - 3.0 * p2 + p3) * f3);
+        }
+      }
+    }
+    T[i] = (float)v;
   }
 }
 
@@ -301,7 +380,6 @@ constexpr int EY = TY + 2, EZ = TZ + 2;    // eps plane region (halo +2)
 constexpr int kCols = TY * TZ;
 constexpr int kGroups = kCols / 4;         // 2x2 column groups
 constexpr int kThreads = kGroups * 16;     // 256
-constexpr int kWarps = kThreads / 32;
 constexpr int kVRow = 8;                   // floats per (column, uy) row of V; 5 used
 constexpr int kVCol = 5 * kVRow + 4;       // floats per column (pad: conflict-free V stores)
 constexpr int kVPlane = kCols * kVCol;
@@ -762,64 +840,142 @@ __global__ void mp_power_to_f32(const double* __restrict__ p, int n, float* __re
   if (i < n) out[i] = (float)p[i];
 }
 
-extern "C" int hermes_multipole_fields(const void* half_spec, int J, int l, int m, const double* radii,
-                                       int nb, const double* phi_power, void* fields_out, void* workspace,
-                                       size_t workspace_bytes, void* stream) {
-  if (!half_spec || !radii || !phi_power || !fields_out) return fail(HERMES_ERR_INVALID, "multipole_fields: NULL argument");
+namespace {
+// Shared tail of the fields entry points: validation, workspace carving and,
+// after the caller has filled the radial table T, the Y_lm prepass, the
+// batched inverse FFT and the interleave.
+struct FieldsCtx {
+  float* T;
+  float* Pf;
+  float2* binmajor;
+  float2* out;
+  int L, nsm;
+  long long N;
+  cudaStream_t s;
+};
+
+int fields_setup(const void* half_spec, int J, int l, int m, int nb, const double* phi_power, void* fields_out,
+                 void* workspace, size_t workspace_bytes, void* stream, FieldsCtx* ctx) {
+  if (!half_spec || !phi_power || !fields_out) return fail(HERMES_ERR_INVALID, "multipole_fields: NULL argument");
   if (l < 0 || l > 40 || m < -l || m > l) return fail(HERMES_ERR_INVALID, "multipole_fields: bad (l=%d, m=%d)", l, m);
   size_t need = 0;
   int rc = hermes_multipole_workspace_size(J, nb, &need);
   if (rc) return rc;
   if (!workspace || workspace_bytes < need) return fail(HERMES_ERR_WORKSPACE, "multipole_fields: workspace %zu < %zu", workspace_bytes, need);
-  const int L = 1 << J;
-  const long long N = 1LL << (3 * J);
-  cudaStream_t s = hermes::as_stream(stream);
+  ctx->L = 1 << J;
+  ctx->N = 1LL << (3 * J);
+  ctx->s = hermes::as_stream(stream);
+  ctx->nsm = sm_count();
   hermes::Carver c(workspace, workspace_bytes);
   c.take<float>(2 * kMaxBins);
-  float* T = c.take<float>(table_floats(J));
-  float* Pf = c.take<float>(L + 1);
+  ctx->T = c.take<float>(table_floats(J));
+  ctx->Pf = c.take<float>(ctx->L + 1);
   c.take<double>((size_t)1024 * kMaxBins * kMaxBins * 2);
   c.take<double>((size_t)kMaxBins * kMaxBins * 2);
-  float2* binmajor = nb > 1 ? c.take<float2>((size_t)nb * N) : static_cast<float2*>(fields_out);
-  RhoArgs hrho;
-  for (int b = 0; b < nb; ++b) {
-    if (!(radii[b] >= 0.0)) return fail(HERMES_ERR_INVALID, "multipole_fields: radius %d must be >= 0", b);
-    const double v = radii[b] / (double)L;
-    hrho.v[2 * b] = (float)v;
-    hrho.v[2 * b + 1] = (float)(v - (double)hrho.v[2 * b]);
-  }
-  mp_power_to_f32<<<(L + 1 + 255) / 256, 256, 0, s>>>(phi_power, L + 1, Pf);
+  ctx->out = static_cast<float2*>(fields_out);
+  ctx->binmajor = nb > 1 ? c.take<float2>((size_t)nb * ctx->N) : ctx->out;
+  mp_power_to_f32<<<(ctx->L + 1 + 255) / 256, 256, 0, ctx->s>>>(phi_power, ctx->L + 1, ctx->Pf);
   HERMES_LAUNCH_CHECK("mp_power_to_f32");
-  const int n2max = 3 * L * L;
-  const int nsm = sm_count();
-  for (int b = nb; b < kMaxBins; ++b) hrho.v[2 * b] = hrho.v[2 * b + 1] = 0.f;
-  mp_jl_table_kernel<<<nsm * 8, 256, 0, s>>>(T, n2max, hrho, nb, l);
-  HERMES_LAUNCH_CHECK("mp_jl_table_kernel");
+  return HERMES_OK;
+}
+
+int fields_run(const FieldsCtx& ctx, const void* half_spec, int J, int l, int m, int nb) {
+  cudaStream_t s = ctx.s;
   const YlmConst Y = make_ylm(l, m);
-  const float inv_n = (float)(1.0 / (double)N);
-  float2* out = static_cast<float2*>(fields_out);
-  const int grid = nsm * 8;
+  const float inv_n = (float)(1.0 / (double)ctx.N);
+  const int grid = ctx.nsm * 8;
   const float2* half = static_cast<const float2*>(half_spec);
-  const float4* T4 = reinterpret_cast<const float4*>(T);
-  if (nb <= 4) mp_prepass_kernel<1><<<grid, 256, 0, s>>>(half, J, Pf, T4, Y, nb, binmajor, inv_n);
-  else if (nb <= 8) mp_prepass_kernel<2><<<grid, 256, 0, s>>>(half, J, Pf, T4, Y, nb, binmajor, inv_n);
-  else mp_prepass_kernel<4><<<grid, 256, 0, s>>>(half, J, Pf, T4, Y, nb, binmajor, inv_n);
+  const float4* T4 = reinterpret_cast<const float4*>(ctx.T);
+  if (nb <= 4) mp_prepass_kernel<1><<<grid, 256, 0, s>>>(half, J, ctx.Pf, T4, Y, nb, ctx.binmajor, inv_n);
+  else if (nb <= 8) mp_prepass_kernel<2><<<grid, 256, 0, s>>>(half, J, ctx.Pf, T4, Y, nb, ctx.binmajor, inv_n);
+  else mp_prepass_kernel<4><<<grid, 256, 0, s>>>(half, J, ctx.Pf, T4, Y, nb, ctx.binmajor, inv_n);
   HERMES_LAUNCH_CHECK("mp_prepass_kernel");
   cufftHandle h;
-  rc = hermes::get_plan_c2c_batch(J, nb, &h);
+  int rc = hermes::get_plan_c2c_batch(J, nb, &h);
   if (rc) return rc;
   cufftResult r = cufftSetStream(h, s);
   if (r != CUFFT_SUCCESS) return fail(HERMES_ERR_CUFFT, "cufftSetStream failed: %d", (int)r);
-  r = cufftExecC2C(h, reinterpret_cast<cufftComplex*>(binmajor), reinterpret_cast<cufftComplex*>(binmajor),
+  r = cufftExecC2C(h, reinterpret_cast<cufftComplex*>(ctx.binmajor), reinterpret_cast<cufftComplex*>(ctx.binmajor),
                    CUFFT_INVERSE);
   if (r != CUFFT_SUCCESS) return fail(HERMES_ERR_CUFFT, "cufftExecC2C failed: %d", (int)r);
   if (nb > 1) {
-    long long nblk = N / kIlCells;
-    if (nblk > (long long)nsm * 16) nblk = (long long)nsm * 16;
-    mp_interleave_kernel<<<(int)nblk, 256, 0, s>>>(binmajor, nb, N, out);
+    long long nblk = ctx.N / kIlCells;
+    if (nblk > (long long)ctx.nsm * 16) nblk = (long long)ctx.nsm * 16;
+    mp_interleave_kernel<<<(int)nblk, 256, 0, s>>>(ctx.binmajor, nb, ctx.N, ctx.out);
     HERMES_LAUNCH_CHECK("mp_interleave_kernel");
   }
   return HERMES_OK;
+}
+}  // namespace
+
+extern "C" int hermes_multipole_fields(const void* half_spec, int J, int l, int m, const double* radii,
+                                       int nb, const double* phi_power, void* fields_out, void* workspace,
+                                       size_t workspace_bytes, void* stream) {
+  if (!radii) return fail(HERMES_ERR_INVALID, "multipole_fields: NULL argument");
+  FieldsCtx ctx;
+  int rc = fields_setup(half_spec, J, l, m, nb, phi_power, fields_out, workspace, workspace_bytes, stream, &ctx);
+  if (rc) return rc;
+  RhoArgs hrho;
+  for (int b = 0; b < kMaxBins; ++b) hrho.v[2 * b] = hrho.v[2 * b + 1] = 0.f;
+  for (int b = 0; b < nb; ++b) {
+    if (!(radii[b] >= 0.0)) return fail(HERMES_ERR_INVALID, "multipole_fields: radius %d must be >= 0", b);
+    const double v = radii[b] / (double)ctx.L;
+    hrho.v[2 * b] = (float)v;
+    hrho.v[2 * b + 1] = (float)(v - (double)hrho.v[2 * b]);
+  }
+  mp_jl_table_kernel<<<ctx.nsm * 8, 256, 0, ctx.s>>>(ctx.T, 3 * ctx.L * ctx.L, hrho, nb, l);
+  HERMES_LAUNCH_CHECK("mp_jl_table_kernel");
+  return fields_run(ctx, half_spec, J, l, m, nb);
+}
+
+extern "C" int hermes_multipole_fields_window(const void* half_spec, int J, int l, int m,
+                                              const hermes_window_t* bins, int nb, const double* phi_power,
+                                              void* fields_out, void* workspace, size_t workspace_bytes,
+                                              void* stream) {
+  if (!bins) return fail(HERMES_ERR_INVALID, "multipole_fields_window: NULL argument");
+  if (nb < 1 || nb > kMaxBins) return fail(HERMES_ERR_INVALID, "multipole_fields_window: nb=%d", nb);
+  FieldsCtx ctx;
+  int rc = fields_setup(half_spec, J, l, m, nb, phi_power, fields_out, workspace, workspace_bytes, stream, &ctx);
+  if (rc) return rc;
+  IsoWins wins;
+  memset(&wins, 0, sizeof(wins));
+  for (int b = 0; b < nb; ++b) {
+    const int t = bins[b].type;
+    if (t != HERMES_WIN_SPHERE && t != HERMES_WIN_GAUSSIAN && t != HERMES_WIN_SHELL && t != HERMES_WIN_THICK_SHELL &&
+        t != HERMES_WIN_GAUSSIAN_SHELL)
+      return fail(HERMES_ERR_UNSUPPORTED, "multipole_fields_window: bin %d type %d is not an isotropic profile", b, t);
+    rc = hermes::prepare_window(bins[b], ctx.L, &wins.w[b]);
+    if (rc) return rc;
+  }
+  mp_iso_table_kernel<<<ctx.nsm * 8, 256, 0, ctx.s>>>(ctx.T, 3 * ctx.L * ctx.L, wins, nb);
+  HERMES_LAUNCH_CHECK("mp_iso_table_kernel");
+  return fields_run(ctx, half_spec, J, l, m, nb);
+}
+
+extern "C" int hermes_multipole_fields_table(const void* half_spec, int J, int l, int m, const double* tables,
+                                             const int64_t* offsets, const int32_t* sizes, const double* k_max,
+                                             double grid_to_physical, int nb, const double* phi_power,
+                                             void* fields_out, void* workspace, size_t workspace_bytes,
+                                             void* stream) {
+  if (!tables || !offsets || !sizes || !k_max) return fail(HERMES_ERR_INVALID, "multipole_fields_table: NULL argument");
+  if (nb < 1 || nb > kMaxBins) return fail(HERMES_ERR_INVALID, "multipole_fields_table: nb=%d", nb);
+  if (!(grid_to_physical > 0.0)) return fail(HERMES_ERR_INVALID, "multipole_fields_table: grid_to_physical must be > 0");
+  FieldsCtx ctx;
+  int rc = fields_setup(half_spec, J, l, m, nb, phi_power, fields_out, workspace, workspace_bytes, stream, &ctx);
+  if (rc) return rc;
+  TabArgs ta;
+  memset(&ta, 0, sizeof(ta));
+  for (int b = 0; b < nb; ++b) {
+    if (sizes[b] < 4 || offsets[b] < 0 || !(k_max[b] > 0.0))
+      return fail(HERMES_ERR_INVALID, "multipole_fields_table: bin %d needs >= 4 points, offset >= 0, k_max > 0", b);
+    ta.off[b] = offsets[b];
+    ta.n[b] = sizes[b];
+    ta.kmax[b] = k_max[b];
+  }
+  ta.k_scale = grid_to_physical / (double)ctx.L;
+  mp_tab_table_kernel<<<ctx.nsm * 8, 256, 0, ctx.s>>>(ctx.T, 3 * ctx.L * ctx.L, tables, ta, nb);
+  HERMES_LAUNCH_CHECK("mp_tab_table_kernel");
+  return fields_run(ctx, half_spec, J, l, m, nb);
 }
 
 // Launches the contraction and the float64 reduction into dout [16][16][2]

@@ -144,11 +144,12 @@ __device__ __forceinline__ float cosine_wavelet_g(float q) {
   return 0.5f * q * ((q - 1.f) * expf(q - 0.5f * q2) + (q + 1.f) * expf(-q - 0.5f * q2));
 }
 
-// One window at integer frequency indices (a, b, c) = k * L (signed), for
-// the given magnitude n2 = a^2+b^2+c^2.  Returns (re, im).
-__device__ __forceinline__ float2 window_at(const WinDev& w, int a, int b, int c) {
-  const int n2 = a * a + b * b + c * c;
+// Isotropic windows (sphere, gaussian, shell, thick_shell, gaussian_shell)
+// as functions of the integer squared frequency n2 = |k L|^2 alone.  Sets
+// *ok = false for the other types.
+__device__ __forceinline__ float2 window_iso_n2(const WinDev& w, int n2, bool* ok) {
   float nh, nl;
+  *ok = true;
   switch (w.type) {
     case HERMES_WIN_SPHERE: {
       df_sqrt_int(n2, nh, nl);
@@ -190,6 +191,23 @@ __device__ __forceinline__ float2 window_at(const WinDev& w, int a, int b, int c
       float qsm = kTwoPi * (nh + nl) * (w.rho_hi[1] + w.rho_lo[1]);
       return make_float2((w.c0 * c + w.c1 * sinc) * expf(-0.5f * qsm * qsm), 0.f);
     }
+    default:
+      *ok = false;
+      return make_float2(0.f, 0.f);
+  }
+}
+
+// One window at integer frequency indices (a, b, c) = k * L (signed), for
+// the given magnitude n2 = a^2+b^2+c^2.  Returns (re, im).
+__device__ __forceinline__ float2 window_at(const WinDev& w, int a, int b, int c) {
+  const int n2 = a * a + b * b + c * c;
+  {
+    bool ok;
+    const float2 v = window_iso_n2(w, n2, &ok);
+    if (ok) return v;
+  }
+  float nh, nl;
+  switch (w.type) {
     case HERMES_WIN_CUBIC: {
       // sin(pi k_i L_i)/(pi k_i L_i) per axis; rho[i] = L_i / L (double-float)
       float r = 1.f;

@@ -21,6 +21,7 @@ form on the GPU (the baseline the batched engine is measured against).
 import copy
 import ctypes
 import itertools
+import math
 import logging
 import time
 
@@ -80,6 +81,89 @@ def multipole_fields(half_spec, J, l, m, radii_grid, phi_power, out=None, ws=Non
                                                    _ptr(out), _ptr(ws), ws.numel(), _stream_ptr(dev)),
                "hermes_multipole_fields")
     return out
+
+
+class BinSpec:
+    """One radial bin of a multipole window: radial profile type, physical
+    len_args and the binning window's other_args (profile configuration)."""
+
+    __slots__ = ("type", "len_args", "profile")
+
+    def __init__(self, radial_type, len_args, profile=None):
+        self.type = str(radial_type).strip().lower()
+        self.len_args = {k: float(v) for k, v in dict(len_args).items()}
+        self.profile = profile if profile else None
+
+    def key(self):
+        return (self.type, tuple(sorted(self.len_args.items())), id(self.profile) if self.profile is not None else None)
+
+    def __eq__(self, other):
+        return isinstance(other, BinSpec) and self.key() == other.key()
+
+    def __hash__(self):
+        return hash(self.key())
+
+    def __repr__(self):
+        return f"BinSpec({self.type!r}, {self.len_args!r})"
+
+
+def as_bin(b):
+    """A thin-shell radius (float, physical) or a BinSpec."""
+    return b if isinstance(b, BinSpec) else BinSpec("shell", {"R": float(b)})
+
+
+def multipole_fields_bins(half_spec, J, l, m, bins, box_size, phi_power, out=None, ws=None):
+    """a_lm^b for radial bins of any supported profile (shell, sphere,
+    thick_shell, gaussian, gaussian_shell, custom_real, custom_kspace), in the
+    layout of multipole_fields.  The GPU path per bin follows
+    radial_multipole_windows.py:269-313: j_l for shells, the analytic
+    monopole transfer for l = 0, else a host table of U_l(k)."""
+    from . import radial_profiles as rp
+
+    bins = [as_bin(b) for b in bins]
+    nb = len(bins)
+    L = 1 << J
+    g2p = L / float(box_size)
+    modes = {rp.profile_mode(b.type, b.len_args, l) for b in bins}
+    if len(modes) != 1:
+        raise NotImplementedError("All bins of one multipole call must use the same radial profile path.")
+    mode = modes.pop()
+    if mode == "shell":
+        radii = [(b.len_args["R_shell"] if b.type == "gaussian_shell" else b.len_args["R"]) * g2p for b in bins]
+        return multipole_fields(half_spec, J, l, m, radii, phi_power, out=out, ws=ws)
+    dev = half_spec.device
+    if out is None:
+        out = torch.empty((L ** 3,) if nb == 1 else (L ** 3, BIN_STRIDE), dtype=torch.complex64, device=dev)
+    if ws is None:
+        ws = _workspace(_ws_bytes(J, nb), dev)
+    lib = _lib.load()
+    if mode == "analytic":
+        from .window import WIN_ARGS, WIN_CODES, HermesWindow
+
+        arr = (HermesWindow * nb)()
+        for k, b in enumerate(bins):
+            arr[k].type = WIN_CODES[b.type]
+            for i, nm in enumerate(WIN_ARGS[b.type]):
+                arr[k].len[i] = float(b.len_args[nm]) * g2p
+            arr[k].los[2] = 1.0
+            arr[k].scale = 1.0
+        _lib.check(lib.hermes_multipole_fields_window(_ptr(half_spec), J, int(l), int(m), arr, nb, _ptr(phi_power),
+                                                      _ptr(out), _ptr(ws), ws.numel(), _stream_ptr(dev)),
+                   "hermes_multipole_fields_window")
+        return out
+    k_max = math.sqrt(3.0) * g2p
+    tabs = [rp.build_radial_multipole_table(b.type, b.len_args, l, k_max, b.profile) for b in bins]
+    sizes = np.array([t.size for _, t in tabs], dtype=np.int32)
+    offs = np.concatenate([[0], np.cumsum(sizes[:-1])]).astype(np.int64)
+    kms = np.array([km for km, _ in tabs], dtype=np.float64)
+    dt = torch.as_tensor(np.concatenate([t for _, t in tabs]), dtype=torch.float64, device=dev)
+    _lib.check(lib.hermes_multipole_fields_table(_ptr(half_spec), J, int(l), int(m), _ptr(dt),
+                                                 offs.ctypes.data_as(ctypes.c_void_p),
+                                                 sizes.ctypes.data_as(ctypes.c_void_p),
+                                                 kms.ctypes.data_as(ctypes.c_void_p), g2p, nb, _ptr(phi_power),
+                                                 _ptr(out), _ptr(ws), ws.numel(), _stream_ptr(dev)),
+               "hermes_multipole_fields_table")
+    return out  # dt is released in stream order after the table kernel
 
 
 def multipole_contract(eps1, fields2, nb2, gamma, J, fields3=None, nb3=None, conj_sign=1):
@@ -231,25 +315,29 @@ class MultipoleEngine:
         self.P = phi_power_device(self.phi, self.L, 1, phi_resolution, self.dev)
         self.timing = {"fields_s": 0.0, "contract_s": 0.0}
 
+    def _fields(self, spec, l, m, bins):
+        return multipole_fields_bins(spec, self.J, l, m, bins, self.box, self.P)
+
     def summands(self, l, m, r12_phys, r13_phys):
-        """S_m[i, j] for radius lists (physical units), complex128 [n12, n13]."""
-        g12 = [r * self.L / self.box for r in r12_phys]
-        g13 = [r * self.L / self.box for r in r13_phys]
-        out = np.zeros((len(g12), len(g13)), dtype=np.complex128)
-        shared = self.same23 and list(g12) == list(g13)
-        for i0 in range(0, len(g12), MAX_BINS):
-            c12 = g12[i0:i0 + MAX_BINS]
+        """S_m[i, j] for two lists of radial bins (thin-shell radii in physical
+        units, or BinSpec), complex128 [n12, n13]."""
+        b12 = [as_bin(r) for r in r12_phys]
+        b13 = [as_bin(r) for r in r13_phys]
+        out = np.zeros((len(b12), len(b13)), dtype=np.complex128)
+        shared = self.same23 and b12 == b13
+        for i0 in range(0, len(b12), MAX_BINS):
+            c12 = b12[i0:i0 + MAX_BINS]
             t0 = time.perf_counter()
-            f2 = multipole_fields(self.spec2, self.J, l, m, c12, self.P)
-            for j0 in range(0, len(g13), MAX_BINS):
-                c13 = g13[j0:j0 + MAX_BINS]
+            f2 = self._fields(self.spec2, l, m, c12)
+            for j0 in range(0, len(b13), MAX_BINS):
+                c13 = b13[j0:j0 + MAX_BINS]
                 if shared and i0 == j0:
                     t1 = time.perf_counter()
                     self.timing["fields_s"] += t1 - t0
                     S = multipole_contract(self.eps1, f2, len(c12), self.gamma, self.J,
                                            conj_sign=(-1) ** ((l + m) % 2))
                 else:
-                    f3 = multipole_fields(self.spec3, self.J, l, -m, c13, self.P)
+                    f3 = self._fields(self.spec3, l, -m, c13)
                     t1 = time.perf_counter()
                     self.timing["fields_s"] += t1 - t0
                     S = multipole_contract(self.eps1, f2, len(c12), self.gamma, self.J, fields3=f3, nb3=len(c13))
@@ -262,12 +350,17 @@ class MultipoleEngine:
 
     def ddd(self, pairs, l_min, l_max):
         """DDD_l for samples given as (r12, r13) physical radii -> [n_samples, n_l]."""
-        r12 = sorted({p[0] for p in pairs})
-        r13 = sorted({p[1] for p in pairs})
+        pairs = [(as_bin(a), as_bin(b)) for a, b in pairs]
+
+        def order(bins):
+            return sorted(set(bins), key=lambda b: (b.type, sorted(b.len_args.items()), str(b.key()[2])))
+
+        r12 = order(p[0] for p in pairs)
+        r13 = order(p[1] for p in pairs)
         i12 = {r: i for i, r in enumerate(r12)}
         i13 = {r: i for i, r in enumerate(r13)}
         if self.same23 and r12 != r13:
-            both = sorted(set(r12) | set(r13))
+            both = order(list(r12) + list(r13))
             r12 = r13 = both
             i12 = i13 = {r: i for i, r in enumerate(both)}
         res = np.zeros((len(pairs), l_max - l_min + 1))
@@ -282,12 +375,12 @@ class MultipoleEngine:
         and (l, m), reference-order contraction of one pair."""
         res = np.zeros((len(pairs), l_max - l_min + 1))
         for s, (a, b) in enumerate(pairs):
-            ga, gb = a * self.L / self.box, b * self.L / self.box
+            a, b = as_bin(a), as_bin(b)
             for li, l in enumerate(range(l_min, l_max + 1)):
                 vals = []
                 for m in range(0, l + 1):
-                    f2 = multipole_fields(self.spec2, self.J, l, m, [ga], self.P)
-                    f3 = multipole_fields(self.spec3, self.J, l, -m, [gb], self.P)
+                    f2 = self._fields(self.spec2, l, m, [a])
+                    f3 = self._fields(self.spec3, l, -m, [b])
                     vals.append(multipole_contract_plain(self.eps1, f2, f3, self.gamma, self.J))
                     del f2, f3
                 res[s, li] = combine_multipole_m_terms(vals, l)
@@ -543,12 +636,21 @@ class Corr_3PCF_Multipole:
         return r.epsilon_device.to(torch.float32)
 
     def _pairs(self):
+        """(bin12, bin13) per sample: thin-shell radii as floats, other radial
+        profiles as BinSpec (type, physical len_args, other_args)."""
+        from .radial_profiles import SUPPORTED
+
         pairs = []
         for w12, w13 in zip(self.binning_window12, self.binning_window13):
+            sides = []
             for w in (w12, w13):
-                if str(w.get("type", "shell")).strip().lower() != "shell":
-                    raise NotImplementedError("Only thin-shell radial multipole windows run on the GPU.")
-            pairs.append((float(w12["len_args"]["R"]), float(w13["len_args"]["R"])))
+                kind = str(w.get("type", "shell")).strip().lower()
+                if kind not in SUPPORTED:
+                    raise ValueError(f"Unsupported radial profile '{kind}'.")
+                la = w.get("len_args", {}) or {}
+                sides.append(float(la["R"]) if kind == "shell" else
+                             BinSpec(kind, la, (w.get("other_args") or None)))
+            pairs.append(tuple(sides))
         return pairs
 
     def run(self, save_result=True, overwrite=False):

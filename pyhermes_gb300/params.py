@@ -22,6 +22,15 @@ REPLACE_KEYS = {
 _EMPTY_WINDOW = {"type": "", "len_args": {}, "los_args": {}, "other_args": {}}
 
 DEFAULTS = {
+    "Counting": {
+        "sfc_field": "",
+        "random_count": 1000000,
+        "seed": 42,
+        "weight_normalization": "catalog",
+        "window": dict(_EMPTY_WINDOW),
+        "threads": 1,
+        "fout_path": "",
+    },
     "SFCProjection": {
         "fin": {"path": "", "format": "bin", "download": {}, "reader_params": {},
                 "catalog_weight_key": None, "field_value_key": None},

@@ -12,6 +12,7 @@ on first access (the reference's dtype), so reference tools that read
 """
 
 import copy
+import math
 import os
 import pickle
 from io import BytesIO
@@ -310,6 +311,45 @@ class SFCField:
         if value_unit == "auto":
             value_unit = "physical" if getattr(field, "field_kind", None) == "catalog_field" else "grid"
         return value_unit
+
+    def field_density_at_pos(self, pos, epsilon=None, filter=None, normalization=None, value_unit="auto"):
+        """pyhermes/io/sfc_field.py:487-530: the field's density at positions
+        (box coordinates), by the 27-point scaling-function interpolation of
+        utils/wavelet_grid.py:143-186 on the GPU (hermes_interp; float32
+        gathers and products, float64 indices and output).  filter: a
+        WindowFunc applied first; epsilon: an explicit coefficient grid."""
+        import torch
+
+        from .mc3pcf import interp
+
+        if epsilon is not None and normalization is not None:
+            raise ValueError("normalization cannot be applied when an explicit epsilon array is provided.")
+        sample_field = self.with_normalization(normalization)
+        value_unit = self._resolve_value_unit(value_unit, sample_field=sample_field)
+        if epsilon is None:
+            grid = (sample_field @ filter).epsilon_device if filter is not None else sample_field.epsilon_device
+        else:
+            grid = torch.as_tensor(np.asarray(epsilon) if not isinstance(epsilon, torch.Tensor) else epsilon,
+                                   device=self.device)
+        grid = grid.to(torch.float32).contiguous()
+        L = int(sample_field.L)
+        if tuple(grid.shape) != (L, L, L):
+            raise ValueError(f"epsilon must have shape {(L, L, L)}, got {tuple(grid.shape)}.")
+        phi = getattr(sample_field, "phi_array", None)
+        if phi is None:
+            from .phi import sample_scaling_function
+
+            phi = sample_scaling_function()
+        phi_t = torch.as_tensor(np.asarray(phi, dtype=np.float64), device=grid.device)
+        p = torch.as_tensor(np.asarray(pos, dtype=np.float64) if not isinstance(pos, torch.Tensor) else pos,
+                            dtype=torch.float64, device=grid.device)
+        if p.ndim != 2 or p.shape[1] != 3:
+            raise ValueError("pos must have shape (n, 3).")
+        scaled = (p * float(sample_field.scale_factor)).contiguous()
+        nx = interp(grid, int(round(math.log2(L))), scaled, phi_t).cpu().numpy()
+        if value_unit == "physical":
+            return nx * float(sample_field.scale_factor) ** 3
+        return nx
 
     def field_mean_density(self, normalization=None, value_unit="auto"):
         """pyhermes/io/sfc_field.py:416-423."""

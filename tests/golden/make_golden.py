@@ -233,7 +233,66 @@ def gen_mc3pcf():
     _save("mc3pcf_J4", **out)
 
 
-SECTIONS = {"mc3pcf": gen_mc3pcf, "phi": gen_phi, "deposit": gen_deposit, "windows": gen_windows,
+def gen_counting():
+    from pyhermes.io.window import WindowFunc
+    from pyhermes.theory.counting import Counting
+
+    rng = np.random.default_rng(17)
+    pos = rng.uniform(0.0, 1000.0, (3000, 3))
+    pos[:1000] = pos[:1000] * 0.25 + 400.0
+    w = rng.lognormal(0.0, 0.3, 3000)
+    f = _projection(pos, 4, weights=w)
+    q = rng.uniform(0.0, 1000.0, (500, 3))
+    win = WindowFunc({"type": "gaussian", "len_args": {"R": 80.0}}, f.sfc_info)
+    d = Counting({"Counting": {"sfc_field": f, "random_count": 700, "seed": 5,
+                               "window": {"type": "gaussian", "len_args": {"R": 80.0}}}}).run(save_result=False)
+    _save("counting_J4", pos=pos, weights=w, query=q,
+          nx_physical=f.field_density_at_pos(q, value_unit="physical"),
+          nx_grid=f.field_density_at_pos(q, value_unit="grid"),
+          nx_filter=f.field_density_at_pos(q, filter=win),
+          nx_unit=f.field_density_at_pos(q, normalization="unit"),
+          counting_nx=np.asarray(d.nx))
+
+
+def gen_tabulated():
+    from pyhermes.theory.corr3pcf_multipole import Corr_3PCF_Multipole
+    from pyhermes.utils.radial_multipole_windows import calculate_radial_multipole_window_array
+    from pyhermes.utils.radial_profiles import build_radial_multipole_table
+    from pyhermes.utils.wavelet_grid import fourier_power_spectrum, sample_scaling_function
+
+    J, L, box = 4, 16, 1000.0
+    phi = sample_scaling_function("db2", 10)
+    P = fourier_power_spectrum(phi, 0, 1, L, 1024)
+    kmax = np.sqrt(3.0) * L / box
+    cases = {"thick_shell": {"R": 150.0, "delta_R": 60.0}, "gaussian": {"R": 80.0},
+             "gaussian_shell": {"R_shell": 150.0, "R_smooth": 40.0}, "sphere": {"R": 120.0}}
+    out = {}
+    for name, la in cases.items():
+        for (l, m) in ((0, 0), (2, 1), (3, -2)):
+            out[f"win_{name}_{l}_{m}"] = calculate_radial_multipole_window_array(L, P, la, name, l, m, box_size=box)
+        for l in (1, 2, 3):
+            km, tab = build_radial_multipole_table(name, la, l, kmax)
+            out[f"tab_{name}_{l}"] = tab
+            out[f"tabkmax_{name}_{l}"] = np.array(km)
+    # the task with thick-shell bins (R from the mapping, delta_R fixed)
+    rng = np.random.default_rng(23)
+    pos = rng.uniform(0.0, 1000.0, (4000, 3))
+    pos[:1500] = pos[:1500] * 0.3 + 350.0
+    w = np.full(4000, 1.0)
+    f = _projection(pos, J, weights=w)
+    params = {"sfc_field": f, "random": "uniform",
+              "binning_window12": {"type": "thick_shell", "len_args": {"delta_R": 50.0}, "other_args": {},
+                                   "mapping": {"R": "r12"}},
+              "binning_window13": {"type": "thick_shell", "len_args": {"delta_R": 50.0}, "other_args": {},
+                                   "mapping": {"R": "r13"}},
+              "sampling": {"mode": "paired", "r12": [150.0, 200.0], "r13": [250.0, 300.0]},
+              "l_min": 0, "l_max": 2, "products": ["ddd_l", "zeta_l"], "summation_backend": "cpu"}
+    d = Corr_3PCF_Multipole({"Corr_3PCF_Multipole": params}).run(save_result=False)
+    _save("tabulated_J4", P=P, pos=pos, weights=w, ddd_l=d.ddd_l, delta_ddd_l=d.delta_ddd_l, zeta_l=d.zeta_l,
+          rrr_l=d.rrr_l, **out)
+
+
+SECTIONS = {"tabulated": gen_tabulated, "counting": gen_counting, "mc3pcf": gen_mc3pcf, "phi": gen_phi, "deposit": gen_deposit, "windows": gen_windows,
             "convolution": gen_convolution, "corr2pcf": gen_corr2pcf, "multipole": gen_multipole}
 
 
