@@ -13,6 +13,7 @@ NumPy copy, like the reference) for users and for composite algebra.
 """
 
 import copy
+import os
 import ctypes
 
 import numpy as np
@@ -279,6 +280,38 @@ class WindowFunc(SFCField):
             t = self.kernel_device()
             self.w_kernel = (t.to(torch.complex128) if t.is_complex() else t.to(torch.float64)).cpu().numpy()
         return self.w_kernel
+
+    # ---- persistence (io/window.py:518-548, io/base.py:24-121) ---------------
+    def save(self, f_out, single=True, overwrite=False):
+        """Framed pickle {**input_params, 'window_kernal': kernel} as the
+        reference writes it (the key's spelling is the reference's)."""
+        from .sfc_field import write_numpy_pickle
+
+        if os.path.exists(f_out) and not overwrite:
+            raise FileExistsError(f"{f_out} exists; pass overwrite=True")
+        if not self.input_params:
+            raise ValueError('The dict_argv "win_params" is empty.')
+        d = os.path.dirname(f_out)
+        if d:
+            os.makedirs(d, exist_ok=True)
+        with open(f_out, "wb") as f:
+            write_numpy_pickle(f, {**self.input_params, "window_kernal": self.as_array()})
+
+    def load(self, f_in, single=True):
+        """Reads a saved window: input_params from the file and its kernel,
+        used from then on as a materialised kernel."""
+        from .sfc_field import read_numpy_pickle
+
+        with open(f_in, "rb") as f:
+            dataset = read_numpy_pickle(f)
+        if "window_kernal" not in dataset:
+            raise ValueError("Failed to load the dataset. The file is missing the 'window_kernal' key.")
+        self.input_params = {k: v for k, v in dataset.items() if k != "window_kernal"}
+        k = np.asarray(dataset["window_kernal"])
+        self.w_kernel = k
+        self._kernel_dev = torch.as_tensor(k.astype(np.complex64) if np.iscomplexobj(k) else k.astype(np.float32),
+                                           device=self.device)
+        self.is_composite_window = True
 
     # ---- composite algebra (io/window.py:364-485) ----------------------------
     def _spawn_composite(self, kernel, operation):

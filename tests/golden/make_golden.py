@@ -292,7 +292,16 @@ def gen_tabulated():
           rrr_l=d.rrr_l, **out)
 
 
-SECTIONS = {"tabulated": gen_tabulated, "counting": gen_counting, "mc3pcf": gen_mc3pcf, "phi": gen_phi, "deposit": gen_deposit, "windows": gen_windows,
+def gen_window_file():
+    from pyhermes.io.window import WindowFunc
+
+    w = WindowFunc({"type": "gaussian", "len_args": {"R": 90.0}}, _sfc_params(4))
+    kernel = w.as_array()  # the reference builds its kernel lazily; save() writes it once built
+    w.save(os.path.join(HERE, "window_gaussian_J4.pkl"), overwrite=True)
+    _save("window_file_J4", kernel=kernel)
+
+
+SECTIONS = {"window_file": gen_window_file, "tabulated": gen_tabulated, "counting": gen_counting, "mc3pcf": gen_mc3pcf, "phi": gen_phi, "deposit": gen_deposit, "windows": gen_windows,
             "convolution": gen_convolution, "corr2pcf": gen_corr2pcf, "multipole": gen_multipole}
 
 
