@@ -92,13 +92,34 @@ def rotation_offsets(R1, R2, mu, n_rot, seed_base_rot=-1, mu_index=-1, rng=None)
     return out
 
 
-def triplet_sum(eps1, eps2, eps3, J, centers, offsets, phi_t, center_w=None, rho1=0.0, samples=False):
-    """sum_i w_i n1_i sum_r n2 n3 (float64) and optionally the per-triplet products."""
+def morton_order(centers, L):
+    """Permutation putting centres (grid units) in Morton (Z-curve) order of
+    their cells, so threads that run together gather nearby cells."""
+    c = torch.floor(centers).to(torch.int64) & (L - 1)
+    key = torch.zeros(c.shape[0], dtype=torch.int64, device=c.device)
+    for bit in range(int(L).bit_length() - 1):
+        for ax in range(3):
+            key |= ((c[:, ax] >> bit) & 1) << (3 * bit + ax)
+    return torch.argsort(key)
+
+
+def triplet_sum(eps1, eps2, eps3, J, centers, offsets, phi_t, center_w=None, rho1=0.0, samples=False,
+                locality=True):
+    """sum_i w_i n1_i sum_r n2 n3 (float64) and optionally the per-triplet
+    products.  With locality (and no per-triplet output) the centres are put
+    in Morton order first: every centre uses the same rotation offsets, so
+    neighbouring threads then gather neighbouring cells from L2 (the sum is
+    over all centres, so only its rounding order changes)."""
     dev = eps2.device
     c = torch.as_tensor(np.ascontiguousarray(centers), dtype=torch.float64, device=dev) \
         if not isinstance(centers, torch.Tensor) else centers
     o = torch.as_tensor(np.ascontiguousarray(offsets), dtype=torch.float64, device=dev)
     w = None if center_w is None else torch.as_tensor(center_w, dtype=torch.float64, device=dev)
+    if locality and not samples and c.shape[0] > 4096:
+        perm = morton_order(c, 1 << J)
+        c = c[perm].contiguous()
+        if w is not None:
+            w = w[perm].contiguous()
     nc, nr = c.shape[0], o.shape[0]
     smp = torch.empty((nc, nr), dtype=torch.float32, device=dev) if samples else None
     ws = _mc_workspace(dev)
