@@ -424,8 +424,9 @@ def c2_bench(dev, phi, steps):
             "twopcf_roofline": {"bound": "hbm", "achieved": tp_bytes / t_2pcf / 1e9, "peak": hbm,
                                 "peak_kind": kind, "unit": "GB/s", "frac": tp_bytes / t_2pcf / 1e9 / hbm,
                                 "algorithmic_bytes": tp_bytes,
-                                "note": "one forward rFFT and one pass over the half spectrum for all 300 bins; "
-                                        "the pass evaluates 300 ring windows x 8 images per mode (compute-bound)"}}
+                                "traffic": profile_traffic("pair_products_cylz_kernel_J9"),
+                                "note": "one forward rFFT and one pass over the half spectrum for all 300 bins "
+                                        "(separable ring windows, column kernel); issue-bound"}}
 
 
 def mc_bench(dev, phi_np, steps):
@@ -507,7 +508,8 @@ def mc_bench(dev, phi_np, steps):
             "roofline": {"kernel": "mc_triplet_kernel", "bound": "hbm", "achieved": ach, "peak": hbm,
                          "peak_kind": kind, "unit": "GB/s", "frac": ach / hbm,
                          "algorithmic_bytes_per_triplet": 324,
-                         "note": "3 x 27 float32 gathers per triplet; the gathers are served mostly from L2"},
+                         "traffic": profile_traffic("mc_triplet_kernel_J9"),
+                         "note": "3 x 27 float32 gathers per triplet over Morton-ordered centres"},
             "learned_proposal": {"train_samples": len(configs) * n_cen_train * n_rot_train,
                                  "train_s": t_train, "loss_first_last": [losses[0], losses[-1]],
                                  "pool_factor": pool_factor, "replicates": 8, "tests": rows}}
