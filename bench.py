@@ -621,11 +621,9 @@ def run_gb300(args, ws, rank, local):
     clk = clocks.stop()
     t_total = sum(a.elapsed_time(b) for a, b in ev) / 1e3
     if ws > 1:
-        import torch.distributed as dist
+        from pyhermes_gb300.replicas import max_over_ranks
 
-        t = torch.tensor([t_total], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_total = float(t.item())
+        t_total = max_over_ranks(t_total, device=dev)
     # whole-job: catalogues per second over all ranks -> seconds per catalogue
     value = t_total / (args.steps * ws)
     zeta = np.asarray(res.zeta_l)

@@ -344,6 +344,13 @@ dep_accum_kernel(const DepRec* __restrict__ sorted, const unsigned* __restrict__
   const int x0 = hx * g.tx, y0 = hy * g.ty, z0 = hz * g.tz;
   const int tzl = g.tz_log2, tyzl = g.ty_log2 + g.tz_log2;
 
+  // Zero the accumulators in every thread while warp 0 builds the range
+  // table below (both before the first barrier; an empty tile then skips
+  // shared memory when it writes).
+  for (int i = 2 * threadIdx.x; i < ncell; i += 2 * blockDim.x) {
+    *reinterpret_cast<longlong2*>(acc + i) = make_longlong2(0, 0);
+    if (counts_out) *reinterpret_cast<uint2*>(cnt + i) = make_uint2(0u, 0u);
+  }
   // Range table: warp 0 handles the 64 (neighbour d, region r) combinations,
   // two per lane, with independent loads, then compacts them with a ballot.
   if (threadIdx.x < 32) {
@@ -413,12 +420,6 @@ dep_accum_kernel(const DepRec* __restrict__ sorted, const unsigned* __restrict__
     }
     return;
   }
-
-  for (int i = 2 * threadIdx.x; i < ncell; i += 2 * blockDim.x) {
-    *reinterpret_cast<longlong2*>(acc + i) = make_longlong2(0, 0);
-    if (counts_out) *reinterpret_cast<uint2*>(cnt + i) = make_uint2(0u, 0u);
-  }
-  __syncthreads();
 
   const float scale_f = st->scale_f;
   const int Lm = g.L - 1;
