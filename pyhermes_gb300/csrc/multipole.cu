@@ -206,12 +206,16 @@ __global__ void mp_tab_table_kernel(float* __restrict__ T, int n2max, const doub
   }
 }
 
+constexpr int kMaxEll = 40;
 struct YlmConst {
   int l, m;          // m >= 0 here; negative m handled by the caller's flag
   float norm;        // sqrt((2l+1)/(4pi) (l-m)!/(l+m)!)
   float pmm;         // (-1)^m (2m-1)!!
   int neg_m;         // requested m < 0
   float neg_sign;    // (-1)^|m|
+  // upward recurrence P_e = ca[e] ct P_{e-1} - cb[e] P_{e-2}, e = m+2 .. l:
+  // ca = (2e-1)/(e-m), cb = (e+m-1)/(e-m) (float64 on the host, then float)
+  float ca[kMaxEll + 1], cb[kMaxEll + 1];
 };
 
 // Y_lm(k) for integer frequency indices (a, b, c) != 0: with
@@ -240,7 +244,7 @@ __device__ __forceinline__ float2 ylm_at(const YlmConst& Y, int a, int b, int c,
     } else {
       float p2 = pmm, p1 = pmmp1, pl = 0.f;
       for (int e = Y.m + 2; e <= Y.l; ++e) {
-        pl = ((2.f * e - 1.f) * ct * p1 - (e + Y.m - 1.f) * p2) / (float)(e - Y.m);
+        pl = Y.ca[e] * ct * p1 - Y.cb[e] * p2;
         p2 = p1;
         p1 = pl;
       }
@@ -808,6 +812,13 @@ YlmConst make_ylm(int l, int m) {
   Y.pmm = (float)pmm;
   Y.neg_m = m < 0 ? 1 : 0;
   Y.neg_sign = (mp % 2 == 1) ? -1.f : 1.f;
+  for (int e = 0; e <= kMaxEll; ++e) {
+    Y.ca[e] = Y.cb[e] = 0.f;
+    if (e >= mp + 2 && e <= l) {
+      Y.ca[e] = (float)((2.0 * e - 1.0) / (double)(e - mp));
+      Y.cb[e] = (float)((double)(e + mp - 1) / (double)(e - mp));
+    }
+  }
   return Y;
 }
 
@@ -857,7 +868,7 @@ struct FieldsCtx {
 int fields_setup(const void* half_spec, int J, int l, int m, int nb, const double* phi_power, void* fields_out,
                  void* workspace, size_t workspace_bytes, void* stream, FieldsCtx* ctx) {
   if (!half_spec || !phi_power || !fields_out) return fail(HERMES_ERR_INVALID, "multipole_fields: NULL argument");
-  if (l < 0 || l > 40 || m < -l || m > l) return fail(HERMES_ERR_INVALID, "multipole_fields: bad (l=%d, m=%d)", l, m);
+  if (l < 0 || l > kMaxEll || m < -l || m > l) return fail(HERMES_ERR_INVALID, "multipole_fields: bad (l=%d, m=%d)", l, m);
   size_t need = 0;
   int rc = hermes_multipole_workspace_size(J, nb, &need);
   if (rc) return rc;

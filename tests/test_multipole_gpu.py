@@ -149,3 +149,25 @@ def test_mixing_solve_matches_oracle():
         np.testing.assert_allclose(M[s], m_ref, rtol=1e-13, atol=1e-15)
         assert _rel(C[s], c_ref) < 1e-10
         assert abs(cond[s] - cond_ref) < 1e-10 * cond_ref
+
+
+@pytest.mark.parametrize("J,l,m", [(7, 5, -2), (8, 10, 7), (9, 4, 2)])
+def test_multi_bin_fields_match_single_bin(J, l, m):
+    """Several bins at once (bin-major batched inverse FFT, then the
+    interleave into [cell][16]) against one bin at a time ([cell] layout),
+    up to J=9: the same fields within float32 rounding, 5e-6 * max|a| per
+    bin, and the unused slots zero."""
+    L = 1 << J
+    g = torch.Generator(device="cuda").manual_seed(J)
+    et = torch.randn((L, L, L), generator=g, device="cuda", dtype=torch.float32)
+    spec = rfft_field(et)
+    P = phi_power_device(PHI, L, 1, 1024, "cuda")
+    radii = [0.0, 1.5, 3.0, 7.25, 11.0, 0.4 * L]
+    f = mp.multipole_fields(spec, J, l, m, radii, P)
+    assert f.shape == (L ** 3, 16)
+    assert torch.count_nonzero(f[:, len(radii):]) == 0
+    for b in (0, 2, 5):
+        one = mp.multipole_fields(spec, J, l, m, [radii[b]], P)
+        err = (f[:, b] - one).abs().max().item()
+        scale = one.abs().max().item()
+        assert err <= 5e-6 * max(scale, 1e-30), (J, l, m, b, err, scale)
