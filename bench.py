@@ -516,8 +516,10 @@ def mc_bench(dev, phi_np, steps):
 
 
 def run_case(args):
-    """Single-kernel workloads for profiling (`--case contract|deposit`): one
-    JSON line with the CUDA-event time per launch; not the headline metric."""
+    """Single-part workloads for profiling (`--case contract|fields|deposit|
+    mc|c2|c4`): one JSON line with CUDA-event times; not the headline metric.
+    `fields` is one radial multipole fields call (l=4, m=2, the 15 headline
+    radii) on the deposited lognormal field at level --J."""
     import torch
 
     from pyhermes_gb300 import _lib, kernels, synthetic
@@ -553,6 +555,22 @@ def run_case(args):
     P = phi_power_device(phi_np, L, 1, 1024, dev)
     gam = cal_gamma(phi_np, 3, 1024)
     grid = [r * L / BOX for r in MP_RADII]
+    if args.case == "fields":
+        spec = rfft_field(eps)
+        out = torch.empty((L ** 3, mp.BIN_STRIDE), dtype=torch.complex64, device=dev)
+        wsf = mp._workspace(mp._ws_bytes(J, len(grid)), dev)
+        for _ in range(max(args.warmup, 1)):
+            mp.multipole_fields(spec, J, 4, 2, grid, P, out=out, ws=wsf)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        for a, b in ev:
+            a.record(stream)
+            mp.multipole_fields(spec, J, 4, 2, grid, P, out=out, ws=wsf)
+            b.record(stream)
+        torch.cuda.synchronize(dev)
+        ms = sum(a.elapsed_time(b) for a, b in ev) / len(ev)
+        print(json.dumps({"case": "fields", "J": J, "bins": len(grid), "l": 4, "m": 2, "ms_per_call": ms,
+                          "prepass_bytes_written": len(grid) * L ** 3 * 8}))
+        return 0
     f = mp.multipole_fields(rfield := rfft_field(eps), J, 2, 1, grid, P)
     for _ in range(max(args.warmup, 1)):
         mp.multipole_contract(eps, f, len(grid), gam, J, conj_sign=-1)
@@ -743,9 +761,9 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--case", default="headline", choices=["headline", "contract", "deposit", "mc", "c2", "c4"],
-                    help="headline = the benchmark line; contract/deposit/mc/c2/c4 = one part, for profiling")
-    ap.add_argument("--J", type=int, default=7, help="grid level of --case contract")
+    ap.add_argument("--case", default="headline", choices=["headline", "contract", "fields", "deposit", "mc", "c2", "c4"],
+                    help="headline = the benchmark line; contract/fields/deposit/mc/c2/c4 = one part, for profiling")
+    ap.add_argument("--J", type=int, default=7, help="grid level of --case contract and --case fields")
     args = ap.parse_args()
     if args.case != "headline":
         return run_case(args)

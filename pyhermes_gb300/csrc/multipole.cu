@@ -10,9 +10,10 @@
 // Here, per (l, m), for all radial bins at once:
 //   mp_jl_table_kernel   j_l(2 pi sqrt(n2) R_b / L) tabulated over the integer
 //                        |k|^2 grid (float32, double-float phase)
-//   mp_prepass_kernel    eps_hat(k) K_lm^b(k) / L^3 for every bin b, Y_lm
+//   mp_prepass_*_kernel  eps_hat(k) K_lm^b(k) / L^3 for every bin b, Y_lm
 //                        shared by the bins, written as a batch of spectra;
-//                        one window evaluation serves k and -k
+//                        one window evaluation serves k, its x- and
+//                        y-reflections and their inversions
 //   cuFFT (batched C2C)  -> a_lm^b(x) for every bin, one contiguous field per
 //                        bin (cuFFT is far slower on strided batches)
 //   mp_interleave_kernel bin-major -> bin-interleaved [cell][16], so one
@@ -26,6 +27,7 @@
 // (the per-sample path the batched engine is measured against).
 #include <cufft.h>
 
+#include <algorithm>
 #include <map>
 #include <mutex>
 #include <tuple>
@@ -296,25 +298,95 @@ __device__ __forceinline__ void mp_window_sum(int x, int y, int z, int L, const 
 }
 
 // out[b * L^3 + k] = eps_hat(k) * K_lm^b(k) / L^3 on the full FFT grid, from
-// the half spectrum of a real field.  A thread takes one half-spectrum mode
-// (x, y, z), z in [0, L/2], and also writes its mirror -k when z is not 0 or
-// L/2: eps_hat(-k) = conj(eps_hat(k)), and when x, y != 0 the mirror's image
-// set is the negated image set, so K(-k) = (-1)^l K(k) (Y_lm parity; the
-// float32 recurrences are sign-symmetric).  On the x = 0 or y = 0 lines the
-// image sets differ ({-L, 0} against {0, L}) and the mirror is evaluated.
+// the half spectrum of a real field, in two kernels that together write
+// every mode once.  Symmetries used (the float32 recurrences are
+// sign-symmetric, so each holds exactly in the computed values):
+//   inversion   eps_hat(-k) = conj eps_hat(k); K(-k) = (-1)^l K(k) when the
+//               image set of -k is the negated image set of k, i.e. off the
+//               x = 0 and y = 0 lines and for z != 0 (z = 0 has images
+//               {-L, 0} against {0, L});
+//   x-reflection (x, y, z) -> (L - x, y, z): K -> (-1)^m conj K
+//               (Y_lm(-a, b, c) = (-1)^m conj Y_lm(a, b, c));
+//   y-reflection (x, y, z) -> (x, L - y, z): K -> conj K
+// for x, y not in {0, L/2} (where a reflected line is itself or its image
+// set is not reflected).
+
+// Interior: one thread per (x, y, z), 1 <= x, y < L/2, z in [0, L/2]; one
+// window evaluation serves the four reflected lines (x, y), (L-x, y),
+// (x, L-y), (L-x, L-y) at z and, for z not 0 or L/2, their inversions at
+// L - z (the inversion of line a is line 3 - a).
 template <int NB4>
 __global__ void __launch_bounds__(256)
-mp_prepass_kernel(const float2* __restrict__ half, int J, const float* __restrict__ P,
-                  const float4* __restrict__ T4, YlmConst Y, int nb, float2* __restrict__ out, float inv_n) {
+mp_prepass_quad_kernel(const float2* __restrict__ half, int J, const float* __restrict__ P,
+                       const float4* __restrict__ T4, YlmConst Y, int nb, float2* __restrict__ out, float inv_n) {
+  constexpr int NB = 4 * NB4;
+  const int L = 1 << J, H = L / 2 + 1, Q1 = L / 2 - 1;
+  const long long N = 1LL << (3 * J);
+  const long long W = (long long)Q1 * Q1 * H;
+  const float lsign = (Y.l & 1) ? -1.f : 1.f, msign = (Y.m & 1) ? -1.f : 1.f;
+  for (long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x; w < W;
+       w += (long long)gridDim.x * blockDim.x) {
+    const int z = (int)(w % H), li = (int)(w / H);
+    const int x = 1 + li / Q1, y = 1 + li % Q1;
+    float accr[NB], acci[NB];
+    mp_window_sum<NB4>(x, y, z, L, P, T4, Y, accr, acci);
+    const bool mirror = z != 0 && z != L / 2;
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+      const int xa = (a & 1) ? L - x : x, ya = (a & 2) ? L - y : y;
+      const float cr = (a & 1) ? msign : 1.f;                           // K_a = cr Re K + i ci Im K
+      const float ci = (a == 1) ? -msign : (a == 2 ? -1.f : ((a == 3) ? msign : 1.f));
+      const float2 e = half[((long long)xa * L + ya) * H + z];
+      const float er = e.x * inv_n, ei = e.y * inv_n;
+      const long long idx = ((long long)xa * L + ya) * L + z;
+#pragma unroll
+      for (int b = 0; b < NB; ++b) {
+        if (b < nb) {
+          const float kr = cr * accr[b], ki = ci * acci[b];
+          out[b * N + idx] = make_float2(er * kr - ei * ki, er * ki + ei * kr);
+        }
+      }
+      if (mirror) {
+        const long long idm = ((long long)(L - xa) * L + (L - ya)) * L + (L - z);
+        const float mr = er, mi = -ei;  // conj(eps_hat(k)) / L^3
+#pragma unroll
+        for (int b = 0; b < NB; ++b) {
+          if (b < nb) {
+            const float kr = lsign * cr * accr[b], ki = lsign * ci * acci[b];
+            out[b * N + idm] = make_float2(mr * kr - mi * ki, mr * ki + mi * kr);
+          }
+        }
+      }
+    }
+  }
+}
+
+// Edge lines, x in {0, L/2} or y in {0, L/2} (4L - 4 lines): one thread per
+// half-spectrum mode, which also writes its inversion when z is not 0 or
+// L/2, evaluating it on the x = 0 and y = 0 lines.
+template <int NB4>
+__global__ void __launch_bounds__(256)
+mp_prepass_edge_kernel(const float2* __restrict__ half, int J, const float* __restrict__ P,
+                       const float4* __restrict__ T4, YlmConst Y, int nb, float2* __restrict__ out, float inv_n) {
   constexpr int NB = 4 * NB4;
   const int L = 1 << J, H = L / 2 + 1, Lm = L - 1;
   const long long N = 1LL << (3 * J);
-  const long long W = (long long)L * L * H;
+  const long long W = (long long)(4 * L - 4) * H;
   const float lsign = (Y.l & 1) ? -1.f : 1.f;
   for (long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x; w < W;
        w += (long long)gridDim.x * blockDim.x) {
-    const int z = (int)(w % H), y = (int)((w / H) & Lm), x = (int)(w / ((long long)H * L));
-    const float2 e = half[w];
+    const int z = (int)(w % H), bi = (int)(w / H);
+    int x, y;
+    if (bi < 2 * L) {  // x in {0, L/2}, any y
+      x = bi < L ? 0 : L / 2;
+      y = bi & Lm;
+    } else {           // y in {0, L/2}, x not in {0, L/2}
+      const int t = bi - 2 * L;
+      y = t < L - 2 ? 0 : L / 2;
+      x = (t < L - 2 ? t : t - (L - 2)) + 1;
+      if (x >= L / 2) ++x;
+    }
+    const float2 e = half[((long long)x * L + y) * H + z];
     float accr[NB], acci[NB];
     mp_window_sum<NB4>(x, y, z, L, P, T4, Y, accr, acci);
     const float er = e.x * inv_n, ei = e.y * inv_n;
@@ -897,9 +969,18 @@ int fields_run(const FieldsCtx& ctx, const void* half_spec, int J, int l, int m,
   const int grid = ctx.nsm * 8;
   const float2* half = static_cast<const float2*>(half_spec);
   const float4* T4 = reinterpret_cast<const float4*>(ctx.T);
-  if (nb <= 4) mp_prepass_kernel<1><<<grid, 256, 0, s>>>(half, J, ctx.Pf, T4, Y, nb, ctx.binmajor, inv_n);
-  else if (nb <= 8) mp_prepass_kernel<2><<<grid, 256, 0, s>>>(half, J, ctx.Pf, T4, Y, nb, ctx.binmajor, inv_n);
-  else mp_prepass_kernel<4><<<grid, 256, 0, s>>>(half, J, ctx.Pf, T4, Y, nb, ctx.binmajor, inv_n);
+  const long long we = (long long)(4 * ctx.L - 4) * (ctx.L / 2 + 1);
+  const int grid_e = (int)std::min<long long>(grid, (we + 255) / 256);
+  if (nb <= 4) {
+    mp_prepass_quad_kernel<1><<<grid, 256, 0, s>>>(half, J, ctx.Pf, T4, Y, nb, ctx.binmajor, inv_n);
+    mp_prepass_edge_kernel<1><<<grid_e, 256, 0, s>>>(half, J, ctx.Pf, T4, Y, nb, ctx.binmajor, inv_n);
+  } else if (nb <= 8) {
+    mp_prepass_quad_kernel<2><<<grid, 256, 0, s>>>(half, J, ctx.Pf, T4, Y, nb, ctx.binmajor, inv_n);
+    mp_prepass_edge_kernel<2><<<grid_e, 256, 0, s>>>(half, J, ctx.Pf, T4, Y, nb, ctx.binmajor, inv_n);
+  } else {
+    mp_prepass_quad_kernel<4><<<grid, 256, 0, s>>>(half, J, ctx.Pf, T4, Y, nb, ctx.binmajor, inv_n);
+    mp_prepass_edge_kernel<4><<<grid_e, 256, 0, s>>>(half, J, ctx.Pf, T4, Y, nb, ctx.binmajor, inv_n);
+  }
   HERMES_LAUNCH_CHECK("mp_prepass_kernel");
   cufftHandle h;
   int rc = hermes::get_plan_c2c_batch(J, nb, &h);
