@@ -25,7 +25,7 @@ import time
 import numpy as np
 import torch
 
-from .params import task_params
+from .params import plain_copy, task_params
 from .sfc_field import SFCField, normalize_task_weight_normalization, write_numpy_pickle
 from .window import (
     ANISOTROPIC_AUTO_WINDOW_TYPES, LOS_AWARE_WINDOW_TYPES, WindowFunc, normalize_los_args, pair_products,
@@ -88,7 +88,7 @@ def normalize_sampling_spec(name, spec):
 
 
 def mapping_s_to_R(sample, bw):
-    p = copy.deepcopy(bw)
+    p = plain_copy(bw)
     p.setdefault("len_args", {})
     if p["len_args"].get("R") is None:
         p["len_args"]["R"] = sample["s"]
@@ -96,7 +96,7 @@ def mapping_s_to_R(sample, bw):
 
 
 def mapping_smu_to_RH(sample, bw):
-    p = copy.deepcopy(bw)
+    p = plain_copy(bw)
     p.setdefault("len_args", {})
     if p["len_args"].get("R") is None:
         p["len_args"]["R"] = sample["s"] * np.sqrt(max(0.0, 1.0 - sample["mu"] * sample["mu"]))
@@ -106,7 +106,7 @@ def mapping_smu_to_RH(sample, bw):
 
 
 def mapping_rppi_to_RH(sample, bw):
-    p = copy.deepcopy(bw)
+    p = plain_copy(bw)
     p.setdefault("len_args", {})
     if p["len_args"].get("R") is None:
         p["len_args"]["R"] = sample["rp"]
@@ -178,7 +178,9 @@ def normalize_binning_window(bw):
 def build_binning_window_params_for_sample(sample, bw):
     mapping = bw.get("mapping")
     mapper = BINNING_WINDOW_MAPPING_SPECS[mapping]["func"] if isinstance(mapping, str) else mapping
-    params = copy.deepcopy(mapper(sample, bw))
+    params = mapper(sample, bw)
+    if not isinstance(mapping, str):  # the built-in mappings already return a fresh copy
+        params = plain_copy(params)
     params.pop("mapping", None)
     params.setdefault("len_args", {})
     params.setdefault("los_args", {})

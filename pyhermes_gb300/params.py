@@ -10,6 +10,30 @@ default_params.json files for the keys this package reads.
 
 import copy
 
+import numpy as np
+
+_ATOMIC = (str, int, float, bool, complex, type(None), np.generic)
+
+
+def plain_copy(obj):
+    """``copy.deepcopy`` for parameter structures, without its memo
+    bookkeeping: plain dict / list / tuple containers are rebuilt, numpy
+    arrays copied, immutable scalars shared; anything else goes through
+    ``copy.deepcopy`` (which shares functions, as before)."""
+    if isinstance(obj, _ATOMIC):
+        return obj
+    t = type(obj)
+    if t is dict:
+        return {k: plain_copy(v) for k, v in obj.items()}
+    if t is list:
+        return [plain_copy(v) for v in obj]
+    if t is tuple:
+        return tuple(plain_copy(v) for v in obj)
+    if t is np.ndarray:
+        return obj.copy()
+    return copy.deepcopy(obj)
+
+
 REPLACE_KEYS = {
     "Corr_2PCF.binning_window",
     "Corr_2PCF.sampling",

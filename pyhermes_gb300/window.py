@@ -21,6 +21,7 @@ import torch
 
 from . import _lib
 from .kernels import _ptr, _stream_ptr
+from .params import plain_copy
 from .phi import fourier_power_spectrum, sample_scaling_function
 from .sfc_field import SFCField
 
@@ -68,11 +69,11 @@ def normalize_los_args(los_args, window_type=None):
             raise ValueError("los_args array must contain exactly three values: [nx, ny, nz].")
         los_args = {k: float(v) for k, v in zip(LOS_ARG_KEYS, arr)}
     elif isinstance(los_args, dict):
-        los_args = copy.deepcopy(los_args)
+        los_args = plain_copy(los_args)
     else:
         raise TypeError("los_args must be a dict, length-3 array, or None.")
     if not los_args and window_type in LOS_AWARE_WINDOW_TYPES:
-        los_args = copy.deepcopy(DEFAULT_LOS_ARGS)
+        los_args = plain_copy(DEFAULT_LOS_ARGS)
     if los_args:
         if not all(k in los_args for k in LOS_ARG_KEYS):
             raise ValueError("los_args must define nx, ny, and nz together.")
@@ -165,9 +166,9 @@ class WindowFunc(SFCField):
         self.kernel_mode = normalize_kernel_mode(km)
         self.input_params["kernel_mode"] = self.kernel_mode
         self.window_params["kernel_mode"] = self.kernel_mode
-        self.len_args = copy.deepcopy(win_params.get("len_args", {})) or {}
-        self.input_params["len_args"] = copy.deepcopy(self.len_args)
-        self.window_params["len_args"] = copy.deepcopy(self.len_args)
+        self.len_args = plain_copy(win_params.get("len_args", {})) or {}
+        self.input_params["len_args"] = plain_copy(self.len_args)
+        self.window_params["len_args"] = plain_copy(self.len_args)
         self.rescale_len_args = {k: v * self.L / self.box_size for k, v in self.len_args.items()
                                  if v is not None}
         self.los_args = normalize_los_args(win_params.get("los_args", {}), self.type)
@@ -176,7 +177,7 @@ class WindowFunc(SFCField):
         self.window_params["los_args"] = self.los_args
         self.window_args = dict(self.rescale_len_args)
         self.window_args.update(self.los_args)
-        self.window_args.update(copy.deepcopy(self.other_args))
+        self.window_args.update(plain_copy(self.other_args))
         if self.type == "thick_shell":
             try:
                 r = float(self.rescale_len_args["R"])

@@ -1,0 +1,40 @@
+"""Host-side parameter handling (no GPU): the parameter copy used on the
+per-bin window paths behaves as copy.deepcopy, and the (s, mu) -> (R, H)
+binning windows carry the reference mapping (corr2pcf.py mapping_smu_to_RH)."""
+import copy
+
+import numpy as np
+
+from pyhermes_gb300.corr2pcf import build_binning_window_params_for_sample, normalize_binning_window
+from pyhermes_gb300.params import plain_copy
+
+
+def test_plain_copy_matches_deepcopy():
+    def f(k):
+        return k
+
+    src = {"type": "ring", "len_args": {"R": None, "H": 2.5}, "los_args": {"nx": 0.0, "ny": 0.0, "nz": 1.0},
+           "other_args": {"table": np.arange(4.0), "func": f, "nested": [1, (2, {"a": 3})]}, "mapping": "smu_to_RH"}
+    a, b = plain_copy(src), copy.deepcopy(src)
+    assert a.keys() == b.keys()
+    assert a["len_args"] == b["len_args"] and a["los_args"] == b["los_args"]
+    assert a["other_args"]["nested"] == b["other_args"]["nested"]
+    np.testing.assert_array_equal(a["other_args"]["table"], src["other_args"]["table"])
+    # no aliasing of containers or arrays; functions are shared, as deepcopy does
+    assert a["len_args"] is not src["len_args"] and a["other_args"]["nested"][1][1] is not src["other_args"]["nested"][1][1]
+    assert a["other_args"]["table"] is not src["other_args"]["table"]
+    assert a["other_args"]["func"] is f and b["other_args"]["func"] is f
+    a["len_args"]["R"] = 1.0
+    a["other_args"]["table"][0] = 9.0
+    assert src["len_args"]["R"] is None and src["other_args"]["table"][0] == 0.0
+
+
+def test_ring_binning_params_per_sample_are_independent():
+    bw = normalize_binning_window({"type": "ring"})
+    before = copy.deepcopy(bw)
+    p1 = build_binning_window_params_for_sample({"s": 50.0, "mu": 0.6}, bw)
+    p2 = build_binning_window_params_for_sample({"s": 20.0, "mu": 0.0}, bw)
+    assert np.isclose(p1["len_args"]["R"], 50.0 * np.sqrt(1 - 0.36)) and np.isclose(p1["len_args"]["H"], 30.0)
+    assert p2["len_args"]["R"] == 20.0 and p2["len_args"]["H"] == 0.0
+    assert "mapping" not in p1 and p1["len_args"] is not p2["len_args"]
+    assert bw == before  # the task's template is untouched
