@@ -160,8 +160,31 @@ def mc_sample(eps1, eps2, eps3, J, pool, phi_t, R1, R2, mu, n, seed=0, idx=None,
     return out[0], out[1]
 
 
+# product rules per centre mode (theory/corr3pcf.py:30-48)
 PRODUCT_DEPS = {"Q": ["zeta", "zeta_H"], "zeta_H": ["xi12", "xi13", "xi23"], "zeta": ["delta_ddd", "rrr"]}
 ALLOWED = {"ddd", "rrr", "delta_ddd", "xi12", "xi13", "xi23", "zeta", "zeta_H", "Q"}
+PRODUCT_DEPS_PARTICLE = dict(PRODUCT_DEPS, delta_ddd=["d_delta_dd", "r_delta_dd"])
+ALLOWED_PARTICLE = ALLOWED | {"d_delta_dd", "r_delta_dd"}
+
+
+def _centre_arrays(pos, weight, pos_name, weight_name):
+    """Explicit particle centres and weights (theory/corr3pcf.py:550-599):
+    given together, (N, 3) float64 positions, 1-D weights of length N with a
+    positive sum."""
+    if (pos is None) != (weight is None):
+        raise ValueError(f"{pos_name} and {weight_name} must be provided together for center='particle'. "
+                         "This avoids mixing explicit center coordinates with field-derived weights.")
+    if pos is None:
+        return None, None
+    p = np.ascontiguousarray(np.asarray(pos, dtype=np.float64))
+    if p.ndim != 2 or p.shape[1] != 3:
+        raise ValueError(f"{pos_name} must be an array-like with shape (N, 3), got shape {p.shape}.")
+    w = np.ascontiguousarray(np.asarray(weight, dtype=np.float64))
+    if w.ndim != 1 or w.shape[0] != p.shape[0]:
+        raise ValueError(f"{weight_name} must be a 1D array with length {p.shape[0]}, got shape {w.shape}.")
+    if float(np.sum(w)) <= 0.0:
+        raise ValueError(f"{weight_name} must have a positive sum.")
+    return p, w
 
 
 class Corr3PCFData:
@@ -194,18 +217,22 @@ class Corr_3PCF:
         self.base_seed = int(tp["base_seed"])
         self.particle_pos1 = tp.get("particle_pos1")
         self.particle_weight1 = tp.get("particle_weight1")
+        self.random_pos1 = tp.get("random_pos1")
+        self.random_weight1 = tp.get("random_weight1")
+        allowed, deps = (ALLOWED_PARTICLE, PRODUCT_DEPS_PARTICLE) if self.center == "particle" else (ALLOWED,
+                                                                                                    PRODUCT_DEPS)
         prods = tp.get("products", "Q")
         prods = [prods] if isinstance(prods, str) else list(prods)
         out = []
         for p in prods:
             p = str(p).strip()
-            if p not in ALLOWED:
-                raise ValueError(f"Unsupported product '{p}'.")
+            if p not in allowed:
+                raise ValueError(f"Unsupported product '{p}' for center='{self.center}'.")
             if p not in out:
                 out.append(p)
         i = 0
         while i < len(out):
-            for d in PRODUCT_DEPS.get(out[i], []):
+            for d in deps.get(out[i], []):
                 if d not in out:
                     out.append(d)
             i += 1
@@ -290,57 +317,89 @@ class Corr_3PCF:
                 return (data[i].epsilon_device.double() - r).float().contiguous()
             return (data[i].epsilon_device.double() - r.epsilon_device.double()).float().contiguous()
 
+        seed_base_rot = self.base_seed + 1
+        n = self.mu_arr.size
+
+        def mc(prod_fields, c_t, w_c, norm):
+            """sum over rotations and centres for every mu, divided by norm."""
+            e1, e2, e3 = prod_fields
+            vals = np.zeros(n)
+            for it, mu in enumerate(self.mu_arr):
+                off = rotation_offsets(r12s, r13s, float(mu), self.n_rot, seed_base_rot, it)
+                s, _ = triplet_sum(e1, e2, e3, J, c_t, off, phi_t, center_w=w_c, rho1=1.0)
+                vals[it] = s / norm
+            return vals
+
+        res = {}
         if self.center == "box_random":
             rng = np.random.default_rng(self.base_seed + 1000003 * 1)
             centers = rng.uniform(0.0, float(L), size=(self.n_box_centers, 3))
-            weights, wsum, rho1 = None, float(self.n_box_centers), 0.0
+            c_t = torch.as_tensor(centers, dtype=torch.float64, device=self.device)
+            norm = float(self.n_rot * centers.shape[0])
+            if "ddd" in self.expanded:
+                res["ddd"] = mc((eps[1], eps[2], eps[3]), c_t, None, norm)
+            if "delta_ddd" in self.expanded:
+                res["delta_ddd"] = mc((delta(1), delta(2), delta(3)), c_t, None, norm)
+            rho1_rrr = None
         else:
-            if self.particle_pos1 is None:
-                raise ValueError("center='particle' needs particle_pos1 (catalogue re-reading is not part of this package).")
-            centers = np.asarray(self.particle_pos1, dtype=np.float64) * sf
-            weights = np.ones(centers.shape[0]) if self.particle_weight1 is None else \
-                np.asarray(self.particle_weight1, dtype=np.float64)
-            wsum = float(weights.sum())
-            rho1 = wsum / float(L) ** 3
-        c_t = torch.as_tensor(centers, dtype=torch.float64, device=self.device)
-        res = {}
-        seed_base_rot = self.base_seed + 1
-        loop = [p for p in ("ddd", "delta_ddd") if p in self.expanded]
-        for prod in loop:
-            vals = np.zeros(self.mu_arr.size)
-            if prod == "ddd":
-                e1, e2, e3 = eps[1], eps[2], eps[3]
-            else:
-                e1, e2, e3 = delta(1), delta(2), delta(3)
-            for it, mu in enumerate(self.mu_arr):
-                off = rotation_offsets(r12s, r13s, float(mu), self.n_rot, seed_base_rot, it)
-                if self.center == "box_random":
-                    s, _ = triplet_sum(e1, e2, e3, J, c_t, off, phi_t)
-                    vals[it] = s / (self.n_rot * centers.shape[0])
+            # particle centres (theory/corr3pcf.py:1134-1180, 1425-1450): n1 is
+            # rho1 = (sum of the centre weights) / V, so each estimate is
+            # rho1 sum_r sum_i w_i n2 n3 / (n_rot sum_i w_i); r_delta_dd uses
+            # the random centres (or the data centres when none are given)
+            cpos, cw = _centre_arrays(self.particle_pos1, self.particle_weight1, "particle_pos1", "particle_weight1")
+            rpos, rw = _centre_arrays(self.random_pos1, self.random_weight1, "random_pos1", "random_weight1")
+            V = float(L) ** 3
+            rho1_rrr = None
+            if cpos is not None:
+                wsum = float(cw.sum())
+                rho1_p = wsum / V
+                c_t = torch.as_tensor(cpos * sf, dtype=torch.float64, device=self.device)
+                rho1_rrr = rho1_p
+            if rpos is not None:
+                rwsum = float(rw.sum())
+                rho1_rrr = rwsum / V
+                r_t = torch.as_tensor(rpos * sf, dtype=torch.float64, device=self.device)
+            needs_data_centres = any(p in self.expanded for p in ("ddd", "d_delta_dd")) or \
+                ("r_delta_dd" in self.expanded and rpos is None and not isinstance(rand[1], float))
+            if needs_data_centres and cpos is None:
+                raise ValueError("center='particle' needs particle_pos1 and particle_weight1 "
+                                 "(catalogue re-reading is not part of this package).")
+            if "ddd" in self.expanded:
+                res["ddd"] = rho1_p * mc((None, eps[2], eps[3]), c_t, cw, self.n_rot * wsum)
+            if "d_delta_dd" in self.expanded:
+                res["d_delta_dd"] = rho1_p * mc((None, delta(2), delta(3)), c_t, cw, self.n_rot * wsum)
+            if "r_delta_dd" in self.expanded and not (rpos is None and isinstance(rand[1], float)):
+                if rpos is not None:
+                    res["r_delta_dd"] = rho1_rrr * mc((None, delta(2), delta(3)), r_t, rw, self.n_rot * rwsum)
                 else:
-                    s, _ = triplet_sum(None, e2, e3, J, c_t, off, phi_t, center_w=weights, rho1=rho1)
-                    vals[it] = rho1 * s / (self.n_rot * wsum)
-            res[prod] = vals
-        if "rrr" in self.expanded:
+                    res["r_delta_dd"] = rho1_p * mc((None, delta(2), delta(3)), c_t, cw, self.n_rot * wsum)
+        shortcut_r = (self.center == "particle" and "r_delta_dd" in self.expanded and "r_delta_dd" not in res)
+        if "rrr" in self.expanded or shortcut_r:
             n_uniform = sum(isinstance(rand[i], float) for i in (1, 2, 3))
             if n_uniform >= 2:
-                res["rrr"] = np.full(self.mu_arr.size, self._density(rand[1]) * self._density(rand[2])
-                                     * self._density(rand[3]))
+                r1 = self._density(rand[1]) if rho1_rrr is None else rho1_rrr
+                res["rrr"] = np.full(n, r1 * self._density(rand[2]) * self._density(rand[3]))
             else:
                 raise NotImplementedError("rrr with fewer than two uniform random vertices")
         scale = float(getattr(self, "_density_physical_scale", 1.0)) ** 3
-        for p in ("ddd", "rrr", "delta_ddd"):
+        for p in ("ddd", "rrr", "d_delta_dd", "r_delta_dd", "delta_ddd"):
             if p in res:
                 res[p] = res[p] * scale
         out = Corr3PCFData()
         out.mu, out.theta = self.mu_arr, self.theta_arr
         out.r23 = np.sqrt(np.clip(self.r12 ** 2 + self.r13 ** 2 - 2 * self.r12 * self.r13 * self.mu_arr, 0, None))
-        for p in ("ddd", "rrr", "delta_ddd"):
+        for p in ("ddd", "rrr", "d_delta_dd", "r_delta_dd", "delta_ddd"):
             setattr(out, p, res.get(p))
-        if any(p in self.expanded for p in ("xi12", "xi13", "xi23")):
+        if "xi12" in self.expanded:
             out.xi12 = self._xi(self.r12, data[1], data[2], rand[1], rand[2])
+        if "xi13" in self.expanded:
             out.xi13 = self._xi(self.r13, data[1], data[3], rand[1], rand[3])
+        if "xi23" in self.expanded or shortcut_r:
             out.xi23 = self._xi(out.r23, data[2], data[3], rand[2], rand[3])
+        if shortcut_r:  # uniform random vertex 1 without random centres: r_delta_dd = rrr xi23
+            out.r_delta_dd = out.rrr * out.xi23
+        if self.center == "particle" and "delta_ddd" in self.expanded:
+            out.delta_ddd = out.d_delta_dd - out.r_delta_dd
         if "zeta" in self.expanded:
             out.zeta = out.delta_ddd / out.rrr
         if "zeta_H" in self.expanded:

@@ -115,7 +115,7 @@ DEFAULTS = {
     },
     "Corr_3PCF": {
         "sfc_field": "", "sfc_field1": "", "sfc_field2": "", "sfc_field3": "",
-        "particle_pos1": None, "particle_weight1": None,
+        "particle_pos1": None, "particle_weight1": None, "random_pos1": None, "random_weight1": None,
         "random": None, "random1": "", "random2": "", "random3": "",
         "weight_normalization": "catalog",
         "r12": 20.0, "r13": 40.0,

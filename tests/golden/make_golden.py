@@ -233,6 +233,38 @@ def gen_mc3pcf():
     _save("mc3pcf_J4", **out)
 
 
+def gen_mc3pcf_particle():
+    """center='particle': data-particle centres for ddd / d_delta_dd, explicit
+    random centres (random_pos1) or the uniform-random shortcut for
+    r_delta_dd, delta_ddd = d_delta_dd - r_delta_dd (corr3pcf.py:1134-1180,
+    1590-1614)."""
+    from pyhermes.theory.corr3pcf import Corr_3PCF
+
+    rng = np.random.default_rng(41)
+    pos = rng.uniform(0.0, 1000.0, (3000, 3))
+    pos[:1000] = pos[:1000] * 0.3 + 300.0
+    w = rng.lognormal(0.0, 0.3, 3000)
+    f = _projection(pos, 4, weights=w)
+    cpos = pos[::5].copy()
+    cw = w[::5].copy()
+    rpos = rng.uniform(0.0, 1000.0, (500, 3))
+    rw = rng.uniform(0.5, 1.5, 500)
+    out = {"pos": pos, "weights": w, "cpos": cpos, "cw": cw, "rpos": rpos, "rw": rw,
+           "epsilon": np.asarray(f.epsilon), "field_integral": float(f.sfc_info["field_integral"])}
+    common = {"sfc_field": f, "random": "uniform", "r12": 150.0, "r13": 250.0, "angle_param": "mu",
+              "mu": {"mu_min": -0.8, "mu_max": 0.8, "n_mu": 3}, "n_rot": 3, "center": "particle",
+              "base_seed": 7, "particle_pos1": cpos, "particle_weight1": cw}
+    d = Corr_3PCF({"Corr_3PCF": dict(common, random_pos1=rpos, random_weight1=rw,
+                                     products=["ddd", "rrr", "d_delta_dd", "r_delta_dd", "delta_ddd"])}).run(
+        save_result=False)
+    for k in ("mu", "ddd", "rrr", "d_delta_dd", "r_delta_dd", "delta_ddd"):
+        out["rpos_" + k] = np.asarray(getattr(d, k))
+    d = Corr_3PCF({"Corr_3PCF": dict(common, products=["zeta", "ddd"])}).run(save_result=False)
+    for k in ("ddd", "rrr", "d_delta_dd", "r_delta_dd", "delta_ddd", "xi23", "zeta"):
+        out["uni_" + k] = np.asarray(getattr(d, k))
+    _save("mc3pcf_particle_J4", **out)
+
+
 def gen_counting():
     from pyhermes.io.window import WindowFunc
     from pyhermes.theory.counting import Counting
@@ -301,7 +333,7 @@ def gen_window_file():
     _save("window_file_J4", kernel=kernel)
 
 
-SECTIONS = {"window_file": gen_window_file, "tabulated": gen_tabulated, "counting": gen_counting, "mc3pcf": gen_mc3pcf, "phi": gen_phi, "deposit": gen_deposit, "windows": gen_windows,
+SECTIONS = {"mc3pcf_particle": gen_mc3pcf_particle, "window_file": gen_window_file, "tabulated": gen_tabulated, "counting": gen_counting, "mc3pcf": gen_mc3pcf, "phi": gen_phi, "deposit": gen_deposit, "windows": gen_windows,
             "convolution": gen_convolution, "corr2pcf": gen_corr2pcf, "multipole": gen_multipole}
 
 

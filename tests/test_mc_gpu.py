@@ -53,6 +53,27 @@ def test_corr3pcf_box_random_matches_reference(golden_dir):
         assert _rel(getattr(d, k), g["box_" + k]) < 1e-5, (k, getattr(d, k), g["box_" + k])
 
 
+def test_corr3pcf_particle_centres_match_reference(golden_dir):
+    """center='particle' against the reference: explicit random centres
+    (ddd, rrr, d_delta_dd, r_delta_dd, delta_ddd) and the uniform-random
+    shortcut r_delta_dd = rrr xi23 (with xi23 and zeta)."""
+    from pyhermes_gb300.projection import SFCProjection
+
+    g = np.load(os.path.join(golden_dir, "mc3pcf_particle_J4.npz"))
+    f = SFCProjection({"SFCProjection": {"particle_pos": g["pos"], "catalog_weight": g["weights"], "J": 4,
+                                         "box_size": 1000.0}}).run(save_result=False)
+    common = {"sfc_field": f, "random": "uniform", "r12": 150.0, "r13": 250.0, "angle_param": "mu",
+              "mu": {"mu_min": -0.8, "mu_max": 0.8, "n_mu": 3}, "n_rot": 3, "center": "particle", "base_seed": 7,
+              "particle_pos1": g["cpos"], "particle_weight1": g["cw"]}
+    d = mc3pcf.Corr_3PCF({"Corr_3PCF": dict(common, random_pos1=g["rpos"], random_weight1=g["rw"],
+                                            products=["ddd", "rrr", "d_delta_dd", "r_delta_dd", "delta_ddd"])}).run()
+    for k in ("ddd", "rrr", "d_delta_dd", "r_delta_dd", "delta_ddd"):
+        assert _rel(getattr(d, k), g["rpos_" + k]) < 1e-5, (k, getattr(d, k), g["rpos_" + k])
+    d = mc3pcf.Corr_3PCF({"Corr_3PCF": dict(common, products=["zeta", "ddd"])}).run()
+    for k in ("ddd", "rrr", "d_delta_dd", "r_delta_dd", "delta_ddd", "xi23", "zeta"):
+        assert _rel(getattr(d, k), g["uni_" + k]) < 1e-5, (k, getattr(d, k), g["uni_" + k])
+
+
 def test_mlp_gradients_match_oracle():
     dims = [4, 128, 128, 128, 1]
     net = mc3pcf.MLP(dims, seed=3)
