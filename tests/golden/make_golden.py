@@ -265,6 +265,40 @@ def gen_mc3pcf_particle():
     _save("mc3pcf_particle_J4", **out)
 
 
+def gen_random_catalogue():
+    """Data and random catalogues (random = a projected field, not
+    'uniform'): Corr_2PCF dd/dr/rd/rr/delta_dd/xi with thick shells and
+    Corr_3PCF_Multipole ddd_l/delta_ddd_l/rrr_l/zeta_l with delta = D - R."""
+    from pyhermes.theory.corr2pcf import Corr_2PCF
+    from pyhermes.theory.corr3pcf_multipole import Corr_3PCF_Multipole
+
+    rng = np.random.default_rng(51)
+    pos = rng.uniform(0.0, 1000.0, (3000, 3))
+    pos[:1200] = pos[:1200] * 0.3 + 350.0
+    w = rng.lognormal(0.0, 0.3, 3000)
+    rpos = rng.uniform(0.0, 1000.0, (9000, 3))
+    f = _projection(pos, 4, weights=w)
+    r = _projection(rpos, 4)
+    out = {"pos": pos, "weights": w, "rpos": rpos}
+    d = Corr_2PCF({"Corr_2PCF": {
+        "sfc_field": f, "random": r,
+        "binning_window": {"type": "thick_shell", "len_args": {"R": None, "delta_R": 60.0}, "mapping": "s_to_R"},
+        "sampling": {"s": {"min": 100.0, "max": 300.0, "n": 3}},
+        "products": ["dd", "dr", "rd", "rr", "delta_dd", "xi"]}}).run(save_result=False)
+    for k in ("dd", "dr", "rd", "rr", "delta_dd", "xi"):
+        out["r2_" + k] = np.asarray(getattr(d, k))
+    d = Corr_3PCF_Multipole({"Corr_3PCF_Multipole": {
+        "sfc_field": f, "random": r,
+        "binning_window12": {"type": "shell", "len_args": {}, "other_args": {}, "mapping": {"R": "r12"}},
+        "binning_window13": {"type": "shell", "len_args": {}, "other_args": {}, "mapping": {"R": "r13"}},
+        "sampling": {"mode": "paired", "r12": [150.0, 200.0], "r13": [250.0, 300.0]},
+        "l_min": 0, "l_max": 2, "summation_backend": "cpu",
+        "products": ["ddd_l", "delta_ddd_l", "rrr_l", "zeta_l"]}}).run(save_result=False)
+    for k in ("ddd_l", "delta_ddd_l", "rrr_l", "zeta_l"):
+        out["r3_" + k] = np.asarray(getattr(d, k))
+    _save("random_catalogue_J4", **out)
+
+
 def gen_counting():
     from pyhermes.io.window import WindowFunc
     from pyhermes.theory.counting import Counting
@@ -333,7 +367,7 @@ def gen_window_file():
     _save("window_file_J4", kernel=kernel)
 
 
-SECTIONS = {"mc3pcf_particle": gen_mc3pcf_particle, "window_file": gen_window_file, "tabulated": gen_tabulated, "counting": gen_counting, "mc3pcf": gen_mc3pcf, "phi": gen_phi, "deposit": gen_deposit, "windows": gen_windows,
+SECTIONS = {"random_catalogue": gen_random_catalogue, "mc3pcf_particle": gen_mc3pcf_particle, "window_file": gen_window_file, "tabulated": gen_tabulated, "counting": gen_counting, "mc3pcf": gen_mc3pcf, "phi": gen_phi, "deposit": gen_deposit, "windows": gen_windows,
             "convolution": gen_convolution, "corr2pcf": gen_corr2pcf, "multipole": gen_multipole}
 
 

@@ -171,3 +171,23 @@ def test_multi_bin_fields_match_single_bin(J, l, m):
         err = (f[:, b] - one).abs().max().item()
         scale = one.abs().max().item()
         assert err <= 5e-6 * max(scale, 1e-30), (J, l, m, b, err, scale)
+
+
+def test_corr3pcf_multipole_random_field_matches_reference(golden_dir):
+    """random = a projected random catalogue: delta = D - R, rrr_l from the
+    random field's own multipoles, zeta_l from the mixing solve."""
+    from pyhermes_gb300.projection import SFCProjection
+
+    g = np.load(os.path.join(golden_dir, "random_catalogue_J4.npz"))
+    f = SFCProjection({"SFCProjection": {"particle_pos": g["pos"], "catalog_weight": g["weights"], "J": 4,
+                                         "box_size": 1000.0}}).run(save_result=False)
+    r = SFCProjection({"SFCProjection": {"particle_pos": g["rpos"], "J": 4, "box_size": 1000.0}}).run(
+        save_result=False)
+    d = mp.Corr_3PCF_Multipole({"Corr_3PCF_Multipole": {
+        "sfc_field": f, "random": r,
+        "binning_window12": {"type": "shell", "len_args": {}, "other_args": {}, "mapping": {"R": "r12"}},
+        "binning_window13": {"type": "shell", "len_args": {}, "other_args": {}, "mapping": {"R": "r13"}},
+        "sampling": {"mode": "paired", "r12": [150.0, 200.0], "r13": [250.0, 300.0]},
+        "l_min": 0, "l_max": 2, "products": ["ddd_l", "delta_ddd_l", "rrr_l", "zeta_l"]}}).run(save_result=False)
+    for k in ("ddd_l", "delta_ddd_l", "rrr_l", "zeta_l"):
+        assert _rel(getattr(d, k), g["r3_" + k]) < 1e-4, (k, _rel(getattr(d, k), g["r3_" + k]))

@@ -142,3 +142,23 @@ def test_corr2pcf_cpu_config_200k_J7():
     assert _rel(r.dd, ref_dd) <= 1e-5
     assert _rel(r.delta_dd, ref_ddd) <= 1e-5, _rel(r.delta_dd, ref_ddd)
     assert _rel(r.xi, ref_xi) <= 1e-5, _rel(r.xi, ref_xi)
+
+
+def test_corr2pcf_random_field_matches_reference(golden_dir):
+    """random = a projected random catalogue (dr, rd, rr and delta = D - R
+    on the field paths): all products against the reference golden."""
+    from pyhermes_gb300.corr2pcf import Corr_2PCF
+    from pyhermes_gb300.projection import SFCProjection
+
+    g = np.load(os.path.join(golden_dir, "random_catalogue_J4.npz"))
+    f = SFCProjection({"SFCProjection": {"particle_pos": g["pos"], "catalog_weight": g["weights"], "J": 4,
+                                         "box_size": 1000.0}}).run(save_result=False)
+    r = SFCProjection({"SFCProjection": {"particle_pos": g["rpos"], "J": 4, "box_size": 1000.0}}).run(
+        save_result=False)
+    d = Corr_2PCF({"Corr_2PCF": {
+        "sfc_field": f, "random": r,
+        "binning_window": {"type": "thick_shell", "len_args": {"R": None, "delta_R": 60.0}, "mapping": "s_to_R"},
+        "sampling": {"s": {"min": 100.0, "max": 300.0, "n": 3}},
+        "products": ["dd", "dr", "rd", "rr", "delta_dd", "xi"]}}).run(save_result=False)
+    for k in ("dd", "dr", "rd", "rr", "delta_dd", "xi"):
+        assert _rel(getattr(d, k), g["r2_" + k]) <= 1e-5, (k, getattr(d, k), g["r2_" + k])

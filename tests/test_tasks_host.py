@@ -1,0 +1,106 @@
+"""Host-side task logic on the CPU: the public task classes run end to end
+(SFCProjection -> Corr_2PCF / Corr_3PCF_Multipole) with their GPU kernels
+replaced by the float64 oracle (deposit, Parseval pair products, DDD_l,
+mixing solve), against reference goldens made with a random catalogue
+(random = a projected field, so dr / rd / rr and delta = D - R take the
+field paths).  Relative 1e-5 of the largest |value| (the fields are float32,
+as on the GPU)."""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from pyhermes_gb300 import corr2pcf, kernels
+from pyhermes_gb300 import multipole as mp
+from pyhermes_gb300.phi import sample_scaling_function
+from pyhermes_gb300.projection import SFCProjection
+
+PHI = sample_scaling_function()
+
+
+def _rel(a, b):
+    a, b = np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64)
+    return np.abs(a - b).max() / np.abs(b).max()
+
+
+@pytest.fixture
+def oracle_kernels(monkeypatch):
+    def deposit(pos, w, J, box, phi, phi_res=1024, out_dtype=torch.float32, counts=False, workspace=None, out=None):
+        eps = oracle.deposit(pos.cpu().numpy(), w.cpu().numpy(), phi.cpu().numpy(), J, box, phi_res)
+        return torch.as_tensor(eps, dtype=out_dtype), None, None
+
+    def rfft_field(eps):  # the "spectrum" handed to pair_products is the real field itself
+        return eps.detach().double().cpu().clone()
+
+    def pair_products(spectra, pairs, windows, exclude_k0=True):
+        L = windows[0].L
+        P = oracle.fourier_power(PHI, windows[0].bandwidth, L)
+        vals, k0 = np.zeros((len(windows), len(pairs))), np.zeros(len(windows))
+        for b, w in enumerate(windows):
+            K = oracle.window_kernel(w.type, w.len_args, L, P, mode=w.resolved_mode(), box=w.box_size)
+            k0[b] = K[0, 0, 0]
+            for c, (i, j) in enumerate(pairs):
+                ei, ej = spectra[i].numpy(), spectra[j].numpy()
+                vals[b, c] = oracle.pair_product(ei, ej, K)
+                if exclude_k0:
+                    vals[b, c] -= K[0, 0, 0] * ei.sum() * ej.sum() / float(L) ** 6
+        return vals, k0
+
+    class Engine:
+        def __init__(self, eps1, eps2, eps3, phi_array, J, box_size, phi_resolution=1024, share23=None):
+            self.e = [e.double().cpu().numpy() for e in (eps1, eps2, eps3)]
+            self.phi, self.box, self.res = phi_array, box_size, phi_resolution
+            self.timing = {"fields_s": 0.0, "contract_s": 0.0}
+
+        def ddd(self, pairs, l_min, l_max):
+            return np.array([oracle.calc_ddd_multipole(*self.e, a, b, l_min, l_max, self.phi, self.res, self.box)[1]
+                             for a, b in pairs])
+
+        ddd_plain = ddd
+
+    def mixing_solve(A, B, lmax, device="cuda"):
+        sol = [oracle.solve_multipoles_from_ratio(a, b, lmax) for a, b in zip(np.atleast_2d(A), np.atleast_2d(B))]
+        return tuple(np.array([s[k] for s in sol]) for k in range(3))
+
+    monkeypatch.setattr(kernels, "deposit", deposit)
+    monkeypatch.setattr(kernels, "deposit_rejected", lambda ws, device=None: 0)
+    monkeypatch.setattr(corr2pcf, "rfft_field", rfft_field)
+    monkeypatch.setattr(corr2pcf, "pair_products", pair_products)
+    monkeypatch.setattr(mp, "MultipoleEngine", Engine)
+    monkeypatch.setattr(mp, "mixing_solve", mixing_solve)
+
+
+def _fields(g):
+    f = SFCProjection({"SFCProjection": {"particle_pos": g["pos"], "catalog_weight": g["weights"], "J": 4,
+                                         "box_size": 1000.0}}, device="cpu").run(save_result=False)
+    r = SFCProjection({"SFCProjection": {"particle_pos": g["rpos"], "J": 4, "box_size": 1000.0}},
+                      device="cpu").run(save_result=False)
+    return f, r
+
+
+def test_corr2pcf_random_field_matches_reference(golden_dir, oracle_kernels):
+    g = np.load(os.path.join(golden_dir, "random_catalogue_J4.npz"))
+    f, r = _fields(g)
+    d = corr2pcf.Corr_2PCF({"Corr_2PCF": {
+        "sfc_field": f, "random": r,
+        "binning_window": {"type": "thick_shell", "len_args": {"R": None, "delta_R": 60.0}, "mapping": "s_to_R"},
+        "sampling": {"s": {"min": 100.0, "max": 300.0, "n": 3}},
+        "products": ["dd", "dr", "rd", "rr", "delta_dd", "xi"]}}, device="cpu").run(save_result=False)
+    for k in ("dd", "dr", "rd", "rr", "delta_dd", "xi"):
+        assert _rel(getattr(d, k), g["r2_" + k]) < 1e-5, (k, getattr(d, k), g["r2_" + k])
+
+
+def test_multipole_random_field_matches_reference(golden_dir, oracle_kernels):
+    g = np.load(os.path.join(golden_dir, "random_catalogue_J4.npz"))
+    f, r = _fields(g)
+    d = mp.Corr_3PCF_Multipole({"Corr_3PCF_Multipole": {
+        "sfc_field": f, "random": r,
+        "binning_window12": {"type": "shell", "len_args": {}, "other_args": {}, "mapping": {"R": "r12"}},
+        "binning_window13": {"type": "shell", "len_args": {}, "other_args": {}, "mapping": {"R": "r13"}},
+        "sampling": {"mode": "paired", "r12": [150.0, 200.0], "r13": [250.0, 300.0]},
+        "l_min": 0, "l_max": 2, "summation_backend": "gb300",
+        "products": ["ddd_l", "delta_ddd_l", "rrr_l", "zeta_l"]}}, device="cpu").run(save_result=False)
+    for k in ("ddd_l", "delta_ddd_l", "rrr_l", "zeta_l"):
+        assert _rel(getattr(d, k), g["r3_" + k]) < 1e-5, (k, getattr(d, k), g["r3_" + k])
