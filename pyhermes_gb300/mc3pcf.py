@@ -374,13 +374,35 @@ class Corr_3PCF:
                 else:
                     res["r_delta_dd"] = rho1_p * mc((None, delta(2), delta(3)), c_t, cw, self.n_rot * wsum)
         shortcut_r = (self.center == "particle" and "r_delta_dd" in self.expanded and "r_delta_dd" not in res)
+        r23 = np.sqrt(np.clip(self.r12 ** 2 + self.r13 ** 2 - 2 * self.r12 * self.r13 * self.mu_arr, 0, None))
         if "rrr" in self.expanded or shortcut_r:
-            n_uniform = sum(isinstance(rand[i], float) for i in (1, 2, 3))
-            if n_uniform >= 2:
-                r1 = self._density(rand[1]) if rho1_rrr is None else rho1_rrr
-                res["rrr"] = np.full(n, r1 * self._density(rand[2]) * self._density(rand[3]))
-            else:
-                raise NotImplementedError("rrr with fewer than two uniform random vertices")
+            # theory/corr3pcf.py:736-772 (_compute_rrr_value) and 1346-1351,
+            # 1597-1602 (rrr deferred to rho1 RR23 when xi23 is requested with a
+            # uniform random vertex 1 and no random centres)
+            uniform = [isinstance(rand[i], float) for i in (1, 2, 3)]
+            deferred = "xi23" in self.expanded and uniform[0] and self.random_pos1 is None
+            r1 = rho1_rrr if (self.center == "particle" and not deferred and rho1_rrr is not None) else None
+            if sum(uniform) >= 2 or uniform[0]:
+                r1 = self._density(rand[1]) if r1 is None else r1
+            if sum(uniform) >= 2:
+                rrr = np.full(n, r1 * self._density(rand[2]) * self._density(rand[3]))
+            elif uniform[0]:
+                rrr = r1 * np.asarray(self._pair(r23, rand[2], rand[3]), dtype=np.float64).reshape(n)
+            elif uniform[1]:
+                rrr = np.full(n, self._density(rand[2]) * float(np.asarray(self._pair(self.r13, rand[1], rand[3]))[0]))
+            elif uniform[2]:
+                rrr = np.full(n, self._density(rand[3]) * float(np.asarray(self._pair(self.r12, rand[1], rand[2]))[0]))
+            else:  # three random fields: Monte Carlo over the same centres and rotations
+                if any(rand[i] is None for i in (1, 2, 3)):
+                    raise ValueError("rrr needs random1, random2 and random3 (or 'uniform').")
+                reps = {i: rand[i].epsilon_device.to(torch.float32).contiguous() for i in (1, 2, 3)}
+                if self.center == "box_random":
+                    rrr = mc((reps[1], reps[2], reps[3]), c_t, None, norm)
+                else:
+                    rt, rwt, rws = (r_t, rw, rwsum) if rpos is not None else (c_t, cw, wsum)
+                    r1 = rho1_rrr if rho1_rrr is not None else self._density(rand[1])
+                    rrr = r1 * mc((None, reps[2], reps[3]), rt, rwt, self.n_rot * rws)
+            res["rrr"] = rrr
         scale = float(getattr(self, "_density_physical_scale", 1.0)) ** 3
         for p in ("ddd", "rrr", "d_delta_dd", "r_delta_dd", "delta_ddd"):
             if p in res:

@@ -299,6 +299,33 @@ def gen_random_catalogue():
     _save("random_catalogue_J4", **out)
 
 
+def gen_mc3pcf_randoms():
+    """Box-random MC 3PCF with random catalogues as fields: three random
+    fields (rrr by Monte Carlo) and a uniform random vertex 1 with random
+    fields 2 and 3 (rrr = rho1 RR23(r23))."""
+    from pyhermes.theory.corr3pcf import Corr_3PCF
+
+    rng = np.random.default_rng(61)
+    pos = rng.uniform(0.0, 1000.0, (3000, 3))
+    pos[:1200] = pos[:1200] * 0.3 + 350.0
+    w = rng.lognormal(0.0, 0.3, 3000)
+    rpos = rng.uniform(0.0, 1000.0, (9000, 3))
+    f = _projection(pos, 4, weights=w)
+    r = _projection(rpos, 4)
+    out = {"pos": pos, "weights": w, "rpos": rpos}
+    common = {"sfc_field": f, "r12": 150.0, "r13": 250.0, "angle_param": "mu",
+              "mu": {"mu_min": -0.8, "mu_max": 0.8, "n_mu": 3}, "n_rot": 3, "center": "box_random",
+              "n_box_centers": 600, "base_seed": 42}
+    d = Corr_3PCF({"Corr_3PCF": dict(common, random=r, products=["zeta", "ddd"])}).run(save_result=False)
+    for k in ("ddd", "delta_ddd", "rrr", "zeta"):
+        out["fields_" + k] = np.asarray(getattr(d, k))
+    d = Corr_3PCF({"Corr_3PCF": dict(common, random1="uniform", random2=r, random3=r, products=["zeta"])}).run(
+        save_result=False)
+    for k in ("delta_ddd", "rrr", "zeta"):
+        out["uni1_" + k] = np.asarray(getattr(d, k))
+    _save("mc3pcf_randoms_J4", **out)
+
+
 def gen_counting():
     from pyhermes.io.window import WindowFunc
     from pyhermes.theory.counting import Counting
@@ -367,7 +394,7 @@ def gen_window_file():
     _save("window_file_J4", kernel=kernel)
 
 
-SECTIONS = {"random_catalogue": gen_random_catalogue, "mc3pcf_particle": gen_mc3pcf_particle, "window_file": gen_window_file, "tabulated": gen_tabulated, "counting": gen_counting, "mc3pcf": gen_mc3pcf, "phi": gen_phi, "deposit": gen_deposit, "windows": gen_windows,
+SECTIONS = {"mc3pcf_randoms": gen_mc3pcf_randoms, "random_catalogue": gen_random_catalogue, "mc3pcf_particle": gen_mc3pcf_particle, "window_file": gen_window_file, "tabulated": gen_tabulated, "counting": gen_counting, "mc3pcf": gen_mc3pcf, "phi": gen_phi, "deposit": gen_deposit, "windows": gen_windows,
             "convolution": gen_convolution, "corr2pcf": gen_corr2pcf, "multipole": gen_multipole}
 
 

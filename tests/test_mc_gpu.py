@@ -74,6 +74,31 @@ def test_corr3pcf_particle_centres_match_reference(golden_dir):
         assert _rel(getattr(d, k), g["uni_" + k]) < 1e-5, (k, getattr(d, k), g["uni_" + k])
 
 
+@pytest.mark.parametrize("case", ["fields", "uni1"])
+def test_corr3pcf_random_fields_match_reference(golden_dir, case):
+    """Random catalogues as fields: rrr by Monte Carlo over three random
+    fields, or rho1 RR23(r23) with a uniform vertex 1."""
+    from pyhermes_gb300.projection import SFCProjection
+
+    g = np.load(os.path.join(golden_dir, "mc3pcf_randoms_J4.npz"))
+    f = SFCProjection({"SFCProjection": {"particle_pos": g["pos"], "catalog_weight": g["weights"], "J": 4,
+                                         "box_size": 1000.0}}).run(save_result=False)
+    r = SFCProjection({"SFCProjection": {"particle_pos": g["rpos"], "J": 4, "box_size": 1000.0}}).run(
+        save_result=False)
+    params = {"sfc_field": f, "r12": 150.0, "r13": 250.0, "angle_param": "mu",
+              "mu": {"mu_min": -0.8, "mu_max": 0.8, "n_mu": 3}, "n_rot": 3, "center": "box_random",
+              "n_box_centers": 600, "base_seed": 42}
+    if case == "fields":
+        params.update(random=r, products=["zeta", "ddd"])
+        keys = ("ddd", "delta_ddd", "rrr", "zeta")
+    else:
+        params.update(random1="uniform", random2=r, random3=r, products=["zeta"])
+        keys = ("delta_ddd", "rrr", "zeta")
+    d = mc3pcf.Corr_3PCF({"Corr_3PCF": params}).run()
+    for k in keys:
+        assert _rel(getattr(d, k), g[f"{case}_{k}"]) < 1e-5, (k, getattr(d, k), g[f"{case}_{k}"])
+
+
 def test_mlp_gradients_match_oracle():
     dims = [4, 128, 128, 128, 1]
     net = mc3pcf.MLP(dims, seed=3)

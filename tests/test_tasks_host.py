@@ -104,3 +104,42 @@ def test_multipole_random_field_matches_reference(golden_dir, oracle_kernels):
         "products": ["ddd_l", "delta_ddd_l", "rrr_l", "zeta_l"]}}, device="cpu").run(save_result=False)
     for k in ("ddd_l", "delta_ddd_l", "rrr_l", "zeta_l"):
         assert _rel(getattr(d, k), g["r3_" + k]) < 1e-5, (k, getattr(d, k), g["r3_" + k])
+
+
+def _cpu_triplet_sum(eps1, eps2, eps3, J, centers, offsets, phi_t, center_w=None, rho1=0.0, samples=False,
+                     locality=True):
+    """sum_i w_i n1_i sum_r n2 n3 with the oracle's float64 interpolation."""
+    c = centers.double().cpu().numpy()
+    phi = phi_t.double().cpu().numpy()
+    e2, e3 = (e.double().cpu().numpy() for e in (eps2, eps3))
+    n1 = oracle.interp(c, eps1.double().cpu().numpy(), phi, J) if eps1 is not None else rho1
+    w = np.ones(c.shape[0]) if center_w is None else np.asarray(center_w, dtype=np.float64)
+    total = 0.0
+    for o in np.asarray(offsets, dtype=np.float64):
+        total += float(np.sum(w * n1 * oracle.interp(c, e2, phi, J, offset=o[0:3])
+                              * oracle.interp(c, e3, phi, J, offset=o[3:6])))
+    return total, None
+
+
+@pytest.mark.parametrize("case", ["fields", "uni1"])
+def test_mc3pcf_random_fields_match_reference(golden_dir, oracle_kernels, monkeypatch, case):
+    """Box-random MC 3PCF with random catalogues as fields: three random
+    fields (rrr by Monte Carlo over the same centres and rotations), and a
+    uniform vertex 1 with random fields 2 and 3 (rrr = rho1 RR23(r23))."""
+    from pyhermes_gb300 import mc3pcf
+
+    monkeypatch.setattr(mc3pcf, "triplet_sum", _cpu_triplet_sum)
+    g = np.load(os.path.join(golden_dir, "mc3pcf_randoms_J4.npz"))
+    f, r = _fields(g)
+    params = {"sfc_field": f, "r12": 150.0, "r13": 250.0, "angle_param": "mu",
+              "mu": {"mu_min": -0.8, "mu_max": 0.8, "n_mu": 3}, "n_rot": 3, "center": "box_random",
+              "n_box_centers": 600, "base_seed": 42}
+    if case == "fields":
+        params.update(random=r, products=["zeta", "ddd"])
+        keys = ("ddd", "delta_ddd", "rrr", "zeta")
+    else:
+        params.update(random1="uniform", random2=r, random3=r, products=["zeta"])
+        keys = ("delta_ddd", "rrr", "zeta")
+    d = mc3pcf.Corr_3PCF({"Corr_3PCF": params}, device="cpu").run()
+    for k in keys:
+        assert _rel(getattr(d, k), g[f"{case}_{k}"]) < 1e-5, (k, getattr(d, k), g[f"{case}_{k}"])
