@@ -326,6 +326,46 @@ def gen_mc3pcf_randoms():
     _save("mc3pcf_randoms_J4", **out)
 
 
+def gen_normalization():
+    """Task-level weight_normalization on a catalogue field with field values
+    (io/sfc_field.py:32-38 modes; each task switches the field before use):
+    Corr_2PCF and Counting for raw / field / unit, Corr_3PCF_Multipole for
+    field."""
+    from pyhermes.theory.corr2pcf import Corr_2PCF
+    from pyhermes.theory.corr3pcf_multipole import Corr_3PCF_Multipole
+    from pyhermes.theory.counting import Counting
+
+    rng = np.random.default_rng(71)
+    pos = rng.uniform(0.0, 1000.0, (3000, 3))
+    pos[:1200] = pos[:1200] * 0.3 + 350.0
+    w = rng.lognormal(0.0, 0.3, 3000)
+    fv = rng.uniform(0.5, 2.0, 3000)
+    f = _projection(pos, 4, weights=w, field_value=fv)
+    out = {"pos": pos, "weights": w, "field_value": fv, "epsilon": np.asarray(f.epsilon),
+           "field_integral": float(f.sfc_info["field_integral"])}
+    for mode in ("raw", "field", "unit"):
+        d = Corr_2PCF({"Corr_2PCF": {
+            "sfc_field": f, "random": "uniform", "weight_normalization": mode,
+            "binning_window": {"type": "thick_shell", "len_args": {"R": None, "delta_R": 60.0}, "mapping": "s_to_R"},
+            "sampling": {"s": {"min": 100.0, "max": 300.0, "n": 3}},
+            "products": ["dd", "rr", "delta_dd", "xi"]}}).run(save_result=False)
+        for k in ("dd", "rr", "delta_dd", "xi"):
+            out[f"n2_{mode}_{k}"] = np.asarray(getattr(d, k))
+        c = Counting({"Counting": {"sfc_field": f, "random_count": 400, "seed": 5,
+                                   "weight_normalization": mode}}).run(save_result=False)
+        out[f"count_{mode}_nx"] = np.asarray(c.nx)
+    d = Corr_3PCF_Multipole({"Corr_3PCF_Multipole": {
+        "sfc_field": f, "random": "uniform", "weight_normalization": "field",
+        "binning_window12": {"type": "shell", "len_args": {}, "other_args": {}, "mapping": {"R": "r12"}},
+        "binning_window13": {"type": "shell", "len_args": {}, "other_args": {}, "mapping": {"R": "r13"}},
+        "sampling": {"mode": "paired", "r12": [150.0], "r13": [250.0]},
+        "l_min": 0, "l_max": 1, "summation_backend": "cpu",
+        "products": ["ddd_l", "delta_ddd_l", "rrr_l", "zeta_l"]}}).run(save_result=False)
+    for k in ("ddd_l", "delta_ddd_l", "rrr_l", "zeta_l"):
+        out["n3_field_" + k] = np.asarray(getattr(d, k))
+    _save("normalization_J4", **out)
+
+
 def gen_counting():
     from pyhermes.io.window import WindowFunc
     from pyhermes.theory.counting import Counting
@@ -394,7 +434,7 @@ def gen_window_file():
     _save("window_file_J4", kernel=kernel)
 
 
-SECTIONS = {"mc3pcf_randoms": gen_mc3pcf_randoms, "random_catalogue": gen_random_catalogue, "mc3pcf_particle": gen_mc3pcf_particle, "window_file": gen_window_file, "tabulated": gen_tabulated, "counting": gen_counting, "mc3pcf": gen_mc3pcf, "phi": gen_phi, "deposit": gen_deposit, "windows": gen_windows,
+SECTIONS = {"normalization": gen_normalization, "mc3pcf_randoms": gen_mc3pcf_randoms, "random_catalogue": gen_random_catalogue, "mc3pcf_particle": gen_mc3pcf_particle, "window_file": gen_window_file, "tabulated": gen_tabulated, "counting": gen_counting, "mc3pcf": gen_mc3pcf, "phi": gen_phi, "deposit": gen_deposit, "windows": gen_windows,
             "convolution": gen_convolution, "corr2pcf": gen_corr2pcf, "multipole": gen_multipole}
 
 

@@ -162,3 +162,27 @@ def test_corr2pcf_random_field_matches_reference(golden_dir):
         "products": ["dd", "dr", "rd", "rr", "delta_dd", "xi"]}}).run(save_result=False)
     for k in ("dd", "dr", "rd", "rr", "delta_dd", "xi"):
         assert _rel(getattr(d, k), g["r2_" + k]) <= 1e-5, (k, getattr(d, k), g["r2_" + k])
+
+
+@pytest.mark.parametrize("mode", ["raw", "field", "unit"])
+def test_task_weight_normalization_matches_reference(golden_dir, mode):
+    """Corr_2PCF products and Counting densities with the task-level
+    weight_normalization on a catalogue field with field values."""
+    from pyhermes_gb300.corr2pcf import Corr_2PCF
+    from pyhermes_gb300.counting import Counting
+    from pyhermes_gb300.projection import SFCProjection
+
+    g = np.load(os.path.join(golden_dir, "normalization_J4.npz"))
+    f = SFCProjection({"SFCProjection": {"particle_pos": g["pos"], "catalog_weight": g["weights"],
+                                         "field_value": g["field_value"], "J": 4, "box_size": 1000.0}}).run(
+        save_result=False)
+    d = Corr_2PCF({"Corr_2PCF": {
+        "sfc_field": f, "random": "uniform", "weight_normalization": mode,
+        "binning_window": {"type": "thick_shell", "len_args": {"R": None, "delta_R": 60.0}, "mapping": "s_to_R"},
+        "sampling": {"s": {"min": 100.0, "max": 300.0, "n": 3}},
+        "products": ["dd", "rr", "delta_dd", "xi"]}}).run(save_result=False)
+    for k in ("dd", "rr", "delta_dd", "xi"):
+        assert _rel(getattr(d, k), g[f"n2_{mode}_{k}"]) <= 1e-5, (mode, k)
+    c = Counting({"Counting": {"sfc_field": f, "random_count": 400, "seed": 5,
+                               "weight_normalization": mode}}).run(save_result=False)
+    assert _rel(c.nx, g[f"count_{mode}_nx"]) <= 1e-5, mode

@@ -143,3 +143,43 @@ def test_mc3pcf_random_fields_match_reference(golden_dir, oracle_kernels, monkey
     d = mc3pcf.Corr_3PCF({"Corr_3PCF": params}, device="cpu").run()
     for k in keys:
         assert _rel(getattr(d, k), g[f"{case}_{k}"]) < 1e-5, (k, getattr(d, k), g[f"{case}_{k}"])
+
+
+@pytest.mark.parametrize("mode", ["raw", "field", "unit"])
+def test_task_weight_normalization_matches_reference(golden_dir, oracle_kernels, monkeypatch, mode):
+    """Task-level weight_normalization on a catalogue field with field
+    values: Corr_2PCF products and Counting densities for each mode, and the
+    multipole task for 'field', against the reference golden."""
+    from pyhermes_gb300 import mc3pcf
+    from pyhermes_gb300.counting import Counting
+
+    def interp(grid, J, scaled_pos, phi_t, offset=(0.0, 0.0, 0.0)):
+        p = scaled_pos.cpu().numpy() if isinstance(scaled_pos, torch.Tensor) else np.asarray(scaled_pos)
+        return torch.as_tensor(oracle.interp(p, grid.double().cpu().numpy(), phi_t.double().cpu().numpy(), J,
+                                             offset=offset))
+
+    monkeypatch.setattr(mc3pcf, "interp", interp)
+    g = np.load(os.path.join(golden_dir, "normalization_J4.npz"))
+    f = SFCProjection({"SFCProjection": {"particle_pos": g["pos"], "catalog_weight": g["weights"],
+                                         "field_value": g["field_value"], "J": 4, "box_size": 1000.0}},
+                      device="cpu").run(save_result=False)
+    d = corr2pcf.Corr_2PCF({"Corr_2PCF": {
+        "sfc_field": f, "random": "uniform", "weight_normalization": mode,
+        "binning_window": {"type": "thick_shell", "len_args": {"R": None, "delta_R": 60.0}, "mapping": "s_to_R"},
+        "sampling": {"s": {"min": 100.0, "max": 300.0, "n": 3}},
+        "products": ["dd", "rr", "delta_dd", "xi"]}}, device="cpu").run(save_result=False)
+    for k in ("dd", "rr", "delta_dd", "xi"):
+        assert _rel(getattr(d, k), g[f"n2_{mode}_{k}"]) < 1e-5, (mode, k, getattr(d, k), g[f"n2_{mode}_{k}"])
+    c = Counting({"Counting": {"sfc_field": f, "random_count": 400, "seed": 5, "weight_normalization": mode}},
+                 device="cpu").run(save_result=False)
+    assert _rel(c.nx, g[f"count_{mode}_nx"]) < 1e-5, (mode, c.nx[:4], g[f"count_{mode}_nx"][:4])
+    if mode == "field":
+        d = mp.Corr_3PCF_Multipole({"Corr_3PCF_Multipole": {
+            "sfc_field": f, "random": "uniform", "weight_normalization": "field",
+            "binning_window12": {"type": "shell", "len_args": {}, "other_args": {}, "mapping": {"R": "r12"}},
+            "binning_window13": {"type": "shell", "len_args": {}, "other_args": {}, "mapping": {"R": "r13"}},
+            "sampling": {"mode": "paired", "r12": [150.0], "r13": [250.0]},
+            "l_min": 0, "l_max": 1, "products": ["ddd_l", "delta_ddd_l", "rrr_l", "zeta_l"]}},
+            device="cpu").run(save_result=False)
+        for k in ("ddd_l", "delta_ddd_l", "rrr_l", "zeta_l"):
+            assert _rel(getattr(d, k), g["n3_field_" + k]) < 1e-5, (k, getattr(d, k), g["n3_field_" + k])
