@@ -366,6 +366,43 @@ def gen_normalization():
     _save("normalization_J4", **out)
 
 
+def gen_cross():
+    """Distinct fields per vertex and per-vertex smoothing windows:
+    Corr_2PCF (sfc_field1 != sfc_field2, window1) and Corr_3PCF_Multipole
+    (fields A, B, A, window2, grid sampling, l_min = 1)."""
+    from pyhermes.theory.corr2pcf import Corr_2PCF
+    from pyhermes.theory.corr3pcf_multipole import Corr_3PCF_Multipole
+
+    rng = np.random.default_rng(81)
+    pa = rng.uniform(0.0, 1000.0, (3000, 3))
+    pa[:1200] = pa[:1200] * 0.3 + 350.0
+    wa = rng.lognormal(0.0, 0.3, 3000)
+    pb = rng.uniform(0.0, 1000.0, (2500, 3))
+    pb[:800] = pb[:800] * 0.25 + 420.0
+    a = _projection(pa, 4, weights=wa)
+    b = _projection(pb, 4)
+    out = {"pa": pa, "wa": wa, "pb": pb}
+    d = Corr_2PCF({"Corr_2PCF": {
+        "sfc_field1": a, "sfc_field2": b, "random": "uniform",
+        "window1": {"type": "gaussian", "len_args": {"R": 30.0}},
+        "binning_window": {"type": "thick_shell", "len_args": {"R": None, "delta_R": 60.0}, "mapping": "s_to_R"},
+        "sampling": {"s": {"min": 100.0, "max": 300.0, "n": 3}},
+        "products": ["dd", "delta_dd", "xi"]}}).run(save_result=False)
+    for k in ("dd", "delta_dd", "rr", "xi"):
+        out["c2_" + k] = np.asarray(getattr(d, k))
+    d = Corr_3PCF_Multipole({"Corr_3PCF_Multipole": {
+        "sfc_field1": a, "sfc_field2": b, "sfc_field3": a, "random": "uniform",
+        "window2": {"type": "gaussian", "len_args": {"R": 40.0}},
+        "binning_window12": {"type": "shell", "len_args": {}, "other_args": {}, "mapping": {"R": "r12"}},
+        "binning_window13": {"type": "shell", "len_args": {}, "other_args": {}, "mapping": {"R": "r13"}},
+        "sampling": {"mode": "grid", "r12": [150.0, 200.0], "r13": [250.0]},
+        "l_min": 1, "l_max": 2, "summation_backend": "cpu", "products": ["ddd_l", "delta_ddd_l"]}}).run(
+        save_result=False)
+    for k in ("ddd_l", "delta_ddd_l"):
+        out["c3_" + k] = np.asarray(getattr(d, k))
+    _save("cross_J4", **out)
+
+
 def gen_counting():
     from pyhermes.io.window import WindowFunc
     from pyhermes.theory.counting import Counting
@@ -434,7 +471,7 @@ def gen_window_file():
     _save("window_file_J4", kernel=kernel)
 
 
-SECTIONS = {"normalization": gen_normalization, "mc3pcf_randoms": gen_mc3pcf_randoms, "random_catalogue": gen_random_catalogue, "mc3pcf_particle": gen_mc3pcf_particle, "window_file": gen_window_file, "tabulated": gen_tabulated, "counting": gen_counting, "mc3pcf": gen_mc3pcf, "phi": gen_phi, "deposit": gen_deposit, "windows": gen_windows,
+SECTIONS = {"cross": gen_cross, "normalization": gen_normalization, "mc3pcf_randoms": gen_mc3pcf_randoms, "random_catalogue": gen_random_catalogue, "mc3pcf_particle": gen_mc3pcf_particle, "window_file": gen_window_file, "tabulated": gen_tabulated, "counting": gen_counting, "mc3pcf": gen_mc3pcf, "phi": gen_phi, "deposit": gen_deposit, "windows": gen_windows,
             "convolution": gen_convolution, "corr2pcf": gen_corr2pcf, "multipole": gen_multipole}
 
 

@@ -191,3 +191,24 @@ def test_corr3pcf_multipole_random_field_matches_reference(golden_dir):
         "l_min": 0, "l_max": 2, "products": ["ddd_l", "delta_ddd_l", "rrr_l", "zeta_l"]}}).run(save_result=False)
     for k in ("ddd_l", "delta_ddd_l", "rrr_l", "zeta_l"):
         assert _rel(getattr(d, k), g["r3_" + k]) < 1e-4, (k, _rel(getattr(d, k), g["r3_" + k]))
+
+
+def test_cross_fields_and_vertex_windows_match_reference(golden_dir):
+    """Fields A, B, A on the three vertices, a smoothing window on vertex 2,
+    grid sampling and l_min = 1 (the conjugate shortcut does not apply)."""
+    from pyhermes_gb300.projection import SFCProjection
+
+    g = np.load(os.path.join(golden_dir, "cross_J4.npz"))
+    a = SFCProjection({"SFCProjection": {"particle_pos": g["pa"], "catalog_weight": g["wa"], "J": 4,
+                                         "box_size": 1000.0}}).run(save_result=False)
+    b = SFCProjection({"SFCProjection": {"particle_pos": g["pb"], "J": 4, "box_size": 1000.0}}).run(
+        save_result=False)
+    d = mp.Corr_3PCF_Multipole({"Corr_3PCF_Multipole": {
+        "sfc_field1": a, "sfc_field2": b, "sfc_field3": a, "random": "uniform",
+        "window2": {"type": "gaussian", "len_args": {"R": 40.0}},
+        "binning_window12": {"type": "shell", "len_args": {}, "other_args": {}, "mapping": {"R": "r12"}},
+        "binning_window13": {"type": "shell", "len_args": {}, "other_args": {}, "mapping": {"R": "r13"}},
+        "sampling": {"mode": "grid", "r12": [150.0, 200.0], "r13": [250.0]},
+        "l_min": 1, "l_max": 2, "products": ["ddd_l", "delta_ddd_l"]}}).run(save_result=False)
+    for k in ("ddd_l", "delta_ddd_l"):
+        assert _rel(getattr(d, k), g["c3_" + k]) < 1e-4, (k, _rel(getattr(d, k), g["c3_" + k]))

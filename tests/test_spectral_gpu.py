@@ -186,3 +186,22 @@ def test_task_weight_normalization_matches_reference(golden_dir, mode):
     c = Counting({"Counting": {"sfc_field": f, "random_count": 400, "seed": 5,
                                "weight_normalization": mode}}).run(save_result=False)
     assert _rel(c.nx, g[f"count_{mode}_nx"]) <= 1e-5, mode
+
+
+def test_corr2pcf_cross_fields_with_vertex_window_matches_reference(golden_dir):
+    from pyhermes_gb300.corr2pcf import Corr_2PCF
+    from pyhermes_gb300.projection import SFCProjection
+
+    g = np.load(os.path.join(golden_dir, "cross_J4.npz"))
+    a = SFCProjection({"SFCProjection": {"particle_pos": g["pa"], "catalog_weight": g["wa"], "J": 4,
+                                         "box_size": 1000.0}}).run(save_result=False)
+    b = SFCProjection({"SFCProjection": {"particle_pos": g["pb"], "J": 4, "box_size": 1000.0}}).run(
+        save_result=False)
+    d = Corr_2PCF({"Corr_2PCF": {
+        "sfc_field1": a, "sfc_field2": b, "random": "uniform",
+        "window1": {"type": "gaussian", "len_args": {"R": 30.0}},
+        "binning_window": {"type": "thick_shell", "len_args": {"R": None, "delta_R": 60.0}, "mapping": "s_to_R"},
+        "sampling": {"s": {"min": 100.0, "max": 300.0, "n": 3}},
+        "products": ["dd", "delta_dd", "xi"]}}).run(save_result=False)
+    for k in ("dd", "delta_dd", "rr", "xi"):
+        assert _rel(getattr(d, k), g["c2_" + k]) <= 1e-5, k

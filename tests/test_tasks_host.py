@@ -183,3 +183,46 @@ def test_task_weight_normalization_matches_reference(golden_dir, oracle_kernels,
             device="cpu").run(save_result=False)
         for k in ("ddd_l", "delta_ddd_l", "rrr_l", "zeta_l"):
             assert _rel(getattr(d, k), g["n3_field_" + k]) < 1e-5, (k, getattr(d, k), g["n3_field_" + k])
+
+
+def test_cross_fields_and_vertex_windows_match_reference(golden_dir, oracle_kernels, monkeypatch):
+    """Distinct fields per vertex and per-vertex smoothing windows (field @ W
+    by the oracle's kernel and FFT convolution): Corr_2PCF with
+    sfc_field1 != sfc_field2 and window1, Corr_3PCF_Multipole with fields
+    A, B, A, window2, grid sampling and l_min = 1."""
+    from pyhermes_gb300 import window as win_mod
+
+    def apply_window(eps, w, out=None):
+        L = w.L
+        K = oracle.window_kernel(w.type, w.len_args, L, oracle.fourier_power(PHI, w.bandwidth, L),
+                                 mode=w.resolved_mode(), box=w.box_size)
+        return torch.as_tensor(oracle.convolve(eps.double().cpu().numpy(), K), dtype=torch.float32)
+
+    def as_array(w):
+        return oracle.window_kernel(w.type, w.len_args, w.L, oracle.fourier_power(PHI, w.bandwidth, w.L),
+                                    mode=w.resolved_mode(), box=w.box_size)
+
+    monkeypatch.setattr(win_mod, "apply_window", apply_window)
+    monkeypatch.setattr(win_mod.WindowFunc, "as_array", as_array)
+    g = np.load(os.path.join(golden_dir, "cross_J4.npz"))
+    a = SFCProjection({"SFCProjection": {"particle_pos": g["pa"], "catalog_weight": g["wa"], "J": 4,
+                                         "box_size": 1000.0}}, device="cpu").run(save_result=False)
+    b = SFCProjection({"SFCProjection": {"particle_pos": g["pb"], "J": 4, "box_size": 1000.0}},
+                      device="cpu").run(save_result=False)
+    d = corr2pcf.Corr_2PCF({"Corr_2PCF": {
+        "sfc_field1": a, "sfc_field2": b, "random": "uniform",
+        "window1": {"type": "gaussian", "len_args": {"R": 30.0}},
+        "binning_window": {"type": "thick_shell", "len_args": {"R": None, "delta_R": 60.0}, "mapping": "s_to_R"},
+        "sampling": {"s": {"min": 100.0, "max": 300.0, "n": 3}},
+        "products": ["dd", "delta_dd", "xi"]}}, device="cpu").run(save_result=False)
+    for k in ("dd", "delta_dd", "rr", "xi"):
+        assert _rel(getattr(d, k), g["c2_" + k]) < 1e-5, (k, getattr(d, k), g["c2_" + k])
+    d = mp.Corr_3PCF_Multipole({"Corr_3PCF_Multipole": {
+        "sfc_field1": a, "sfc_field2": b, "sfc_field3": a, "random": "uniform",
+        "window2": {"type": "gaussian", "len_args": {"R": 40.0}},
+        "binning_window12": {"type": "shell", "len_args": {}, "other_args": {}, "mapping": {"R": "r12"}},
+        "binning_window13": {"type": "shell", "len_args": {}, "other_args": {}, "mapping": {"R": "r13"}},
+        "sampling": {"mode": "grid", "r12": [150.0, 200.0], "r13": [250.0]},
+        "l_min": 1, "l_max": 2, "products": ["ddd_l", "delta_ddd_l"]}}, device="cpu").run(save_result=False)
+    for k in ("ddd_l", "delta_ddd_l"):
+        assert _rel(getattr(d, k), g["c3_" + k]) < 1e-5, (k, getattr(d, k), g["c3_" + k])
