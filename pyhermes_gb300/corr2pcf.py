@@ -26,7 +26,8 @@ import numpy as np
 import torch
 
 from .params import plain_copy, task_params
-from .sfc_field import SFCField, normalize_task_weight_normalization, write_numpy_pickle
+from .sfc_field import (SFCField, describe_input, normalize_task_weight_normalization, read_numpy_pickle,
+                        write_numpy_pickle)
 from .window import (
     ANISOTROPIC_AUTO_WINDOW_TYPES, LOS_AWARE_WINDOW_TYPES, WindowFunc, normalize_los_args, pair_products,
     rfft_field,
@@ -189,9 +190,14 @@ def build_binning_window_params_for_sample(sample, bw):
 
 
 class Corr2PCFData:
-    """Result container (pyhermes/io/corr2pcf.py): sampling + products."""
+    """Result container (pyhermes/io/corr2pcf.py): sampling + products.
 
-    def __init__(self):
+    The file written by ``save_corr2pcf`` / read by ``load_corr2pcf`` is the
+    reference's NumPy-framed pickle with the same top-level keys and order:
+    sfc_info1, sfc_info2, corr2pcf_info, sampling_names, the products
+    dd .. xi, then one array per sampling name."""
+
+    def __init__(self, data_path=None):
         self.sampling_names = ()
         self.sampling = {}
         for p in PRODUCT_NAMES:
@@ -199,6 +205,8 @@ class Corr2PCFData:
         self.corr2pcf_info = {}
         self.sfc_info1 = None
         self.sfc_info2 = None
+        if data_path:
+            self.load_corr2pcf(data_path)
 
     def set_sampling(self, names, arrays):
         self.sampling_names = tuple(names)
@@ -212,11 +220,23 @@ class Corr2PCFData:
         d = os.path.dirname(f_out)
         if d:
             os.makedirs(d, exist_ok=True)
-        data = {p: getattr(self, p) for p in PRODUCT_NAMES}
-        data.update({"sampling_names": self.sampling_names, "sampling": self.sampling,
-                     "corr2pcf_info": self.corr2pcf_info})
+        data = {"sfc_info1": self.sfc_info1, "sfc_info2": self.sfc_info2, "corr2pcf_info": self.corr2pcf_info,
+                "sampling_names": tuple(self.sampling_names)}
+        data.update({p: getattr(self, p) for p in PRODUCT_NAMES})
+        data.update({n: self.sampling[n] for n in self.sampling_names})
         with open(f_out, "wb") as f:
             write_numpy_pickle(f, data)
+
+    def load_corr2pcf(self, f_in):
+        with open(f_in, "rb") as f:
+            d = read_numpy_pickle(f)
+        names = tuple(d.get("sampling_names") or ())
+        self.set_sampling(names, {n: d[n] for n in names if n in d})
+        for p in PRODUCT_NAMES:
+            setattr(self, p, d.get(p))
+        self.corr2pcf_info = d.get("corr2pcf_info") or {}
+        self.sfc_info1 = d.get("sfc_info1")
+        self.sfc_info2 = d.get("sfc_info2")
 
 
 def _is_scalar(v):
@@ -261,6 +281,25 @@ class Corr_2PCF:
         self.threads = int(tp.get("threads", 1))
         self.fout_path = tp.get("fout_path", "")
         self._fields_prepared = False
+
+    def _info_snapshot(self):
+        """corr2pcf_info with the reference's keys (theory/corr2pcf.py:919-1112,
+        _current_task_params_snapshot): inputs summarised, randoms resolved."""
+        rand = getattr(self, "rand", {}) or {}
+        info = {"sfc_field": describe_input(self.sfc_field), "sfc_field1": describe_input(self.sfc_field1),
+                "sfc_field2": describe_input(self.sfc_field2), "random": describe_input(self.random)}
+        for i in (1, 2):
+            info[f"random{i}"] = describe_input(rand.get(i, getattr(self, f"random{i}")))
+        info.update({"window": describe_input(self.window), "window1": describe_input(self.window1),
+                     "window2": describe_input(self.window2),
+                     "binning_window": {k: v for k, v in self.binning_window.items()
+                                        if k != "mapping" or isinstance(v, str)},
+                     "sampling_spec": plain_copy(self.sampling), "sampling_names": list(self.sampling_names),
+                     "sampling": {n: [float(v) for v in self.sampling_arrays[n]] for n in self.sampling_names},
+                     "threads": self.threads, "products": list(self.products), "memory_strategy": "speed",
+                     "binning_window_cache": False, "binning_window_cache_dir": "",
+                     "weight_normalization": self.weight_normalization, "fout_path": self.fout_path})
+        return info
 
     # ---- sampling ----------------------------------------------------------
     def _resolve_sampling(self):
@@ -445,9 +484,7 @@ class Corr_2PCF:
             setattr(data, p, results.get(p) if p in expanded else None)
         if "xi" in expanded:
             data.xi = data.delta_dd / data.rr
-        data.corr2pcf_info = {"products": self.products, "sampling_names": list(self.sampling_names),
-                              "binning_window": {k: v for k, v in self.binning_window.items() if k != "mapping"
-                                                 or isinstance(v, str)}}
+        data.corr2pcf_info = self._info_snapshot()
         if 1 in self.data:
             data.sfc_info1 = self.data[1].sfc_info
         if 2 in self.data:

@@ -17,7 +17,8 @@ import time
 import numpy as np
 
 from .params import task_params
-from .sfc_field import SFCField, normalize_task_weight_normalization, read_numpy_pickle, write_numpy_pickle
+from .sfc_field import (SFCField, describe_input, normalize_task_weight_normalization, read_numpy_pickle,
+                        write_numpy_pickle)
 from .window import WindowFunc
 
 logger = logging.getLogger("pyhermes_gb300.Counting")
@@ -68,6 +69,7 @@ class Counting:
         p = task_params("Counting", param_task or {"Counting": {}})
         self.device = device
         self.sfc_field = p.get("sfc_field", "")
+        self._sfc_input = self.sfc_field
         self.random_count = int(p["random_count"])
         self.seed = int(p["seed"])
         self.weight_normalization = normalize_task_weight_normalization(p.get("weight_normalization", "catalog"))
@@ -82,7 +84,7 @@ class Counting:
         win = self.window
         if isinstance(win, WindowFunc):
             win = dict(getattr(win, "input_params", {}) or {})
-        return {"random_count": self.random_count, "seed": self.seed,
+        return {"sfc_field": describe_input(self._sfc_input), "random_count": self.random_count, "seed": self.seed,
                 "weight_normalization": self.weight_normalization, "window": win, "threads": self.threads,
                 "fout_path": self.fout_path}
 

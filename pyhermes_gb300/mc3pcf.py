@@ -32,7 +32,7 @@ from . import _lib
 from .kernels import _ptr, _stream_ptr
 from .params import task_params
 from .phi import sample_scaling_function
-from .sfc_field import SFCField, normalize_task_weight_normalization
+from .sfc_field import SFCField, describe_input, normalize_task_weight_normalization, read_numpy_pickle, write_numpy_pickle
 
 _WS = {}
 
@@ -188,11 +188,37 @@ def _centre_arrays(pos, weight, pos_name, weight_name):
 
 
 class Corr3PCFData:
-    def __init__(self):
-        for k in ("mu", "theta", "r23", "ddd", "rrr", "d_delta_dd", "r_delta_dd", "delta_ddd", "xi12", "xi13",
-                  "xi23", "zeta", "zeta_H", "Q"):
+    """Result container (pyhermes/io/corr3pcf.py).  ``save_corr3pcf`` /
+    ``load_corr3pcf`` use the reference's NumPy-framed pickle with the same
+    top-level keys and order."""
+
+    FILE_KEYS = ("sfc_info1", "sfc_info2", "sfc_info3", "corr3pcf_info", "mu", "theta", "r23", "ddd", "rrr",
+                 "d_delta_dd", "r_delta_dd", "delta_ddd", "xi12", "xi13", "xi23", "zeta", "zeta_H", "Q")
+
+    def __init__(self, data_path=None):
+        for k in self.FILE_KEYS:
             setattr(self, k, None)
         self.corr3pcf_info = {}
+        if data_path:
+            self.load_corr3pcf(data_path)
+
+    def save_corr3pcf(self, f_out, overwrite=False):
+        import os
+
+        if os.path.exists(f_out) and not overwrite:
+            raise FileExistsError(f_out)
+        d = os.path.dirname(f_out)
+        if d:
+            os.makedirs(d, exist_ok=True)
+        with open(f_out, "wb") as f:
+            write_numpy_pickle(f, {k: getattr(self, k) for k in self.FILE_KEYS})
+
+    def load_corr3pcf(self, f_in):
+        with open(f_in, "rb") as f:
+            d = read_numpy_pickle(f)
+        for k in self.FILE_KEYS:
+            setattr(self, k, d.get(k))
+        self.corr3pcf_info = d.get("corr3pcf_info") or {}
 
 
 class Corr_3PCF:
@@ -219,10 +245,12 @@ class Corr_3PCF:
         self.particle_weight1 = tp.get("particle_weight1")
         self.random_pos1 = tp.get("random_pos1")
         self.random_weight1 = tp.get("random_weight1")
+        self.fout_path = tp.get("fout_path", "")
         allowed, deps = (ALLOWED_PARTICLE, PRODUCT_DEPS_PARTICLE) if self.center == "particle" else (ALLOWED,
                                                                                                     PRODUCT_DEPS)
         prods = tp.get("products", "Q")
         prods = [prods] if isinstance(prods, str) else list(prods)
+        self._given_products = list(prods)
         out = []
         for p in prods:
             p = str(p).strip()
@@ -298,7 +326,7 @@ class Corr_3PCF:
         t._density_physical_scale = 1.0
         return np.asarray(t.run(save_result=False).dd)
 
-    def run(self, save_result=False, overwrite=False):
+    def run(self, save_result=True, overwrite=False):
         data = {i: self._field(getattr(self, f"sfc_field{i}"), f"field vertex {i}") for i in (1, 2, 3)}
         ref = data[1]
         rand = {i: self._rand(i, data[i]) for i in (1, 2, 3)}
@@ -416,7 +444,7 @@ class Corr_3PCF:
             out.xi12 = self._xi(self.r12, data[1], data[2], rand[1], rand[2])
         if "xi13" in self.expanded:
             out.xi13 = self._xi(self.r13, data[1], data[3], rand[1], rand[3])
-        if "xi23" in self.expanded or shortcut_r:
+        if "xi23" in self.expanded or "rrr" in self.expanded or shortcut_r:  # corr3pcf.py:1207 pair cache
             out.xi23 = self._xi(out.r23, data[2], data[3], rand[2], rand[3])
         if shortcut_r:  # uniform random vertex 1 without random centres: r_delta_dd = rrr xi23
             out.r_delta_dd = out.rrr * out.xi23
@@ -428,8 +456,42 @@ class Corr_3PCF:
             out.zeta_H = out.xi12 * out.xi13 + out.xi12 * out.xi23 + out.xi13 * out.xi23
         if "Q" in self.expanded:
             out.Q = out.zeta / out.zeta_H
+        for i in (1, 2, 3):
+            setattr(out, f"sfc_info{i}", data[i].sfc_info)
+        out.corr3pcf_info = self._info_snapshot(rand)
         self.corr3pcf_data = out
+        if save_result and self.fout_path:
+            out.save_corr3pcf(self.fout_path, overwrite=overwrite)
         return out
+
+    def _info_snapshot(self, rand):
+        """corr3pcf_info with the reference's keys (theory/corr3pcf.py:330-380)."""
+        def arr(name):
+            v = getattr(self, name)
+            return None if v is None else {"kind": name, "shape": tuple(np.asarray(v).shape)}
+
+        tp = self.task_params
+        info = {"sfc_field": describe_input(self.sfc_field)}
+        for i in (1, 2, 3):
+            info[f"sfc_field{i}"] = describe_input(getattr(self, f"sfc_field{i}"))
+        info.update({"particle_pos1": arr("particle_pos1"), "particle_weight1": arr("particle_weight1"),
+                     "random": describe_input(tp.get("random"))})
+        for i in (1, 2, 3):
+            info[f"random{i}"] = describe_input(rand.get(i))
+        info.update({"random_pos1": arr("random_pos1"), "random_weight1": arr("random_weight1"),
+                     "weight_normalization": self.weight_normalization, "window": describe_input(tp.get("window"))})
+        for i in (1, 2, 3):
+            info[f"window{i}"] = describe_input(tp.get(f"window{i}"))
+        theta, mu = tp.get("theta"), tp.get("mu")
+        info.update({"r12": self.r12, "r13": self.r13, "angle_param": str(tp["angle_param"]).strip().lower(),
+                     "theta_spec": describe_input(theta), "mu_spec": describe_input(mu),
+                     "n_theta": int(self.theta_arr.size), "n_mu": int(self.mu_arr.size),
+                     "theta_min": float(self.theta_arr.min()), "theta_max": float(self.theta_arr.max()),
+                     "mu_min": float(self.mu_arr.min()), "mu_max": float(self.mu_arr.max()), "n_rot": self.n_rot,
+                     "center": self.center, "n_box_centers": self.n_box_centers, "base_seed": self.base_seed,
+                     "threads": int(tp.get("threads", 1)), "products": self._given_products,
+                     "fout_path": self.fout_path})
+        return info
 
     def _xi(self, radius, fa, fb, ra, rb):
         """corr3pcf.py:1011-1036: xi = delta_dd / rr with shell pair products."""

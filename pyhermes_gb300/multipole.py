@@ -32,7 +32,8 @@ from . import _lib
 from .kernels import _ptr, _stream_ptr
 from .params import task_params
 from .phi import cal_gamma, sample_scaling_function
-from .sfc_field import SFCField, normalize_task_weight_normalization, write_numpy_pickle
+from .sfc_field import (SFCField, describe_input, normalize_task_weight_normalization, read_numpy_pickle,
+                        write_numpy_pickle)
 from .window import WindowFunc, phi_power_device, rfft_field
 
 logger = logging.getLogger("pyhermes_gb300.Corr_3PCF_Multipole")
@@ -442,22 +443,40 @@ def mixing_solve(A, B, lmax, device="cuda"):
 
 
 class Corr3PCFMultipoleData:
-    """Result container (pyhermes/io/corr3pcf_multipole.py:9-30)."""
+    """Result container (pyhermes/io/corr3pcf_multipole.py:9-30).  The file
+    written by ``save_corr3pcf_multipole`` / read by
+    ``load_corr3pcf_multipole`` is the reference's NumPy-framed pickle with
+    the same top-level keys and order (``timing`` stays in memory)."""
 
-    def __init__(self):
-        for k in ("sfc_info1", "sfc_info2", "sfc_info3", "sample_params", "binning_window12", "binning_window13",
-                  "r12", "r13", "l", "ddd_l", "rrr_l", "delta_ddd_l", "zeta_l", "zeta_condition"):
+    FILE_KEYS = ("sfc_info1", "sfc_info2", "sfc_info3", "corr3pcf_multipole_info", "sample_params",
+                 "binning_window12", "binning_window13", "r12", "r13", "l", "ddd_l", "rrr_l", "delta_ddd_l",
+                 "zeta_l", "zeta_condition")
+
+    def __init__(self, data_path=None):
+        for k in self.FILE_KEYS:
             setattr(self, k, None)
         self.corr3pcf_multipole_info = {}
         self.timing = {}
+        if data_path:
+            self.load_corr3pcf_multipole(data_path)
 
     def save_corr3pcf_multipole(self, f_out, overwrite=False):
         import os
 
         if os.path.exists(f_out) and not overwrite:
             raise FileExistsError(f_out)
+        d = os.path.dirname(f_out)
+        if d:
+            os.makedirs(d, exist_ok=True)
         with open(f_out, "wb") as f:
-            write_numpy_pickle(f, {k: v for k, v in self.__dict__.items()})
+            write_numpy_pickle(f, {k: getattr(self, k) for k in self.FILE_KEYS})
+
+    def load_corr3pcf_multipole(self, f_in):
+        with open(f_in, "rb") as f:
+            d = read_numpy_pickle(f)
+        for k in self.FILE_KEYS:
+            setattr(self, k, d.get(k))
+        self.corr3pcf_multipole_info = d.get("corr3pcf_multipole_info") or {}
 
 
 PRODUCTS = ("ddd_l", "rrr_l", "delta_ddd_l", "zeta_l")
@@ -493,6 +512,7 @@ class Corr_3PCF_Multipole:
         if self.l_min < 0 or self.l_max < 0 or self.l_min > self.l_max:
             raise ValueError("Corr_3PCF_Multipole requires 0 <= l_min <= l_max.")
         backend = str(tp.get("summation_backend", "gb300")).strip().lower()
+        self._backend_given = backend
         if backend not in {"gb300", "gpu", "plain", "cpu"}:
             raise ValueError("summation_backend must be 'gb300', 'gpu', 'plain' or 'cpu'.")
         self.summation_backend = "plain" if backend == "plain" else "gb300"
@@ -507,6 +527,69 @@ class Corr_3PCF_Multipole:
                 self.products.append(p)
         self.fout_path = tp.get("fout_path", "")
         self._fields_prepared = False
+
+    def _resolution_diagnostics(self):
+        """theory/corr3pcf_multipole.py:621-665: per binning edge, the smallest
+        radial scale against l_max (pi R / dx; a warning when
+        l_max / (pi R / dx) >= 0.7)."""
+        out = []
+        if self.l_max == 0:
+            return out
+        keys = {"shell": "R", "thick_shell": "R", "sphere": "R", "gaussian": "R", "gaussian_shell": "R_shell"}
+        ref = self.reference
+        for name, windows in (("binning_window12", self.binning_window12), ("binning_window13", self.binning_window13)):
+            kind = str(windows[0]["type"]).strip().lower()
+            if kind not in keys:
+                continue
+            radii = np.asarray([float(w["len_args"][keys[kind]]) for w in windows], dtype=np.float64)
+            pos = radii[radii > 0.0]
+            if pos.size == 0:
+                continue
+            q = float(np.pi * pos.min() * ref.L / ref.box_size)
+            ratio = float(self.l_max / q)
+            out.append({"edge": name, "radial_type": kind, "min_radius": float(pos.min()),
+                        "max_radius": float(pos.max()), "q_grid_min": q, "l_max_over_q_grid_min": ratio})
+            if ratio >= 0.7:
+                logger.warning("Multipole resolution diagnostic | %s: l_max=%d, min radial scale=%.6g, pi R / dx=%.3f, "
+                               "l_max/(pi R/dx)=%.3f. The highest multipoles are close to the grid high-k range; "
+                               "check J convergence.", name, self.l_max, pos.min(), q, ratio)
+        return out
+
+    def _info_snapshot(self, expanded):
+        """corr3pcf_multipole_info with the reference's keys
+        (theory/corr3pcf_multipole.py:767 and the task parameters)."""
+        tp = self.task_params
+        info = {"sfc_field": describe_input(self.sfc_field)}
+        for i in (1, 2, 3):
+            info[f"sfc_field{i}"] = describe_input(getattr(self, f"sfc_field{i}"))
+        info["random"] = describe_input(tp.get("random"))
+        for i in (1, 2, 3):
+            info[f"random{i}"] = describe_input(self.rand.get(i, getattr(self, f"random{i}", None)))
+        info.update({"weight_normalization": self.weight_normalization, "window": describe_input(self.window)})
+        for i in (1, 2, 3):
+            info[f"window{i}"] = describe_input(getattr(self, f"window{i}"))
+        sampling = {"mode": self.sampling["mode"],
+                    "values": {k: [float(x) for x in v] for k, v in self.sampling["values"].items()}}
+        info.update({"binning_window12_template": describe_input(tp.get("binning_window12")),
+                     "binning_window13_template": describe_input(tp.get("binning_window13")),
+                     "sampling": sampling, "n_samples": len(self.samples), "l_min": self.l_min, "l_max": self.l_max,
+                     "gpu_device_id": int(tp.get("gpu_device_id", 0) or 0),
+                     "gpu_threads_per_block": list(tp.get("gpu_threads_per_block") or [8, 8, 8]),
+                     "summation_backend": self._backend_given, "execution_mode": "serial",
+                     "sample_mpi": {"ranks_per_sample": 1, "gpu_device_ids": []},
+                     "cache_multipole_fields": False, "cache_dir": "", "verbose_m_progress": False,
+                     "verbose_profile": False, "zeta_condition_warning": 1e12,
+                     "threads": int(tp.get("threads", 1) or 1), "products": list(self.products),
+                     "radial_profile_diagnostics": bool(tp.get("radial_profile_diagnostics", True)),
+                     "radial_profile_diagnostic_tolerance": float(tp.get("radial_profile_diagnostic_tolerance", 1e-5)),
+                     "radial_profile_diagnostic_probes": int(tp.get("radial_profile_diagnostic_probes", 33)),
+                     "expanded_products": list(expanded),
+                     "resolution_diagnostics": self._resolution_diagnostics(),
+                     "radial_profile_diagnostics_result": [],
+                     "rho_vertices": [self.data[i].field_mean_density(value_unit="grid") if i in self.data else None
+                                      for i in (1, 2, 3)],
+                     "fout_path": self.fout_path})
+        return info
 
     # ---- sampling (corr3pcf_multipole.py:229-322) ----------------------------
     def _normalize_sampling(self, sampling):
@@ -701,6 +784,7 @@ class Corr_3PCF_Multipole:
         for i in (1, 2, 3):
             if i in self.data:
                 setattr(data, f"sfc_info{i}", self.data[i].sfc_info)
+        data.corr3pcf_multipole_info = self._info_snapshot(exp)
         self.corr3pcf_multipole_data = data
         if save_result and self.fout_path:
             data.save_corr3pcf_multipole(self.fout_path, overwrite=overwrite)

@@ -80,6 +80,29 @@ def _normalize_pathlike(value):
     return value
 
 
+def describe_input(value):
+    """A task input as the reference records it in result files
+    (theory/corr2pcf.py:174-208): strings and 'uniform' as given, numbers as
+    float, a field or window object as a short summary, dicts copied."""
+    if value is None or isinstance(value, str):
+        return value
+    if isinstance(value, (float, int, np.floating)):
+        return float(value)
+    if getattr(value, "is_window", False):
+        return {"kind": "WindowFunc", "type": getattr(value, "type", "custom"),
+                "len_args": dict(getattr(value, "len_args", {}) or {}),
+                "los_args": dict(getattr(value, "los_args", {}) or {}),
+                "other_args": dict(getattr(value, "other_args", {}) or {})}
+    if isinstance(value, SFCField):
+        return {"kind": "SFCField", "L": value.L, "box_size": value.box_size, "wavelet_mode": value.wavelet_mode,
+                "wavelet_level": value.wavelet_level}
+    if isinstance(value, dict):
+        from .params import plain_copy
+
+        return plain_copy(value)
+    return value
+
+
 class SFCField:
     _REQUIRED_ARGV = REQUIRED_ARGV
 

@@ -403,6 +403,51 @@ def gen_cross():
     _save("cross_J4", **out)
 
 
+def gen_io():
+    """Files written by the reference's own save methods (NumPy-framed
+    pickles, io/pickle_compat.py): a projected field (io/sfc_field.py:546)
+    and the results of Corr_2PCF, Counting, Corr_3PCF and
+    Corr_3PCF_Multipole (io/corr2pcf.py:90, io/counting.py:29,
+    io/corr3pcf.py:55, io/corr3pcf_multipole.py:39)."""
+    from pyhermes.theory.corr2pcf import Corr_2PCF
+    from pyhermes.theory.corr3pcf import Corr_3PCF
+    from pyhermes.theory.corr3pcf_multipole import Corr_3PCF_Multipole
+    from pyhermes.theory.counting import Counting
+
+    d_io = os.path.join(HERE, "io")
+    os.makedirs(d_io, exist_ok=True)
+    cwd = os.getcwd()
+    os.chdir(d_io)  # the result files record fout_path; keep it relative
+    rng = np.random.default_rng(91)
+    pos = rng.uniform(0.0, 1000.0, (2000, 3))
+    pos[:800] = pos[:800] * 0.3 + 350.0
+    w = rng.lognormal(0.0, 0.3, 2000)
+    np.savez_compressed("catalogue.npz", pos=pos, weights=w)
+    f = _projection(pos, 4, weights=w)
+    f.save_sfc_field("./field_J4.pkl", overwrite=True)
+    Corr_2PCF({"Corr_2PCF": {
+        "sfc_field": f, "random": "uniform", "fout_path": "./corr2pcf_J4.pkl",
+        "binning_window": {"type": "thick_shell", "len_args": {"R": None, "delta_R": 60.0}, "mapping": "s_to_R"},
+        "sampling": {"s": {"min": 100.0, "max": 300.0, "n": 3}}, "products": ["dd", "xi"]}}).run(
+        save_result=True, overwrite=True)
+    Counting({"Counting": {"sfc_field": f, "random_count": 50, "seed": 3,
+                           "fout_path": "./counting_J4.pkl"}}).run(save_result=True, overwrite=True)
+    Corr_3PCF({"Corr_3PCF": {
+        "sfc_field": f, "random": "uniform", "r12": 150.0, "r13": 250.0, "angle_param": "mu",
+        "mu": {"mu_min": -0.5, "mu_max": 0.5, "n_mu": 2}, "n_rot": 2, "center": "box_random",
+        "n_box_centers": 100, "base_seed": 42, "products": ["zeta", "ddd"],
+        "fout_path": "./corr3pcf_J4.pkl"}}).run(save_result=True, overwrite=True)
+    Corr_3PCF_Multipole({"Corr_3PCF_Multipole": {
+        "sfc_field": f, "random": "uniform", "fout_path": "./corr3pcf_multipole_J4.pkl",
+        "binning_window12": {"type": "shell", "len_args": {}, "other_args": {}, "mapping": {"R": "r12"}},
+        "binning_window13": {"type": "shell", "len_args": {}, "other_args": {}, "mapping": {"R": "r13"}},
+        "sampling": {"mode": "paired", "r12": [150.0], "r13": [250.0]},
+        "l_min": 0, "l_max": 1, "summation_backend": "cpu", "products": ["ddd_l", "zeta_l"]}}).run(
+        save_result=True, overwrite=True)
+    os.chdir(cwd)
+    print("wrote", sorted(os.listdir(d_io)))
+
+
 def gen_counting():
     from pyhermes.io.window import WindowFunc
     from pyhermes.theory.counting import Counting
@@ -471,7 +516,7 @@ def gen_window_file():
     _save("window_file_J4", kernel=kernel)
 
 
-SECTIONS = {"cross": gen_cross, "normalization": gen_normalization, "mc3pcf_randoms": gen_mc3pcf_randoms, "random_catalogue": gen_random_catalogue, "mc3pcf_particle": gen_mc3pcf_particle, "window_file": gen_window_file, "tabulated": gen_tabulated, "counting": gen_counting, "mc3pcf": gen_mc3pcf, "phi": gen_phi, "deposit": gen_deposit, "windows": gen_windows,
+SECTIONS = {"io": gen_io, "cross": gen_cross, "normalization": gen_normalization, "mc3pcf_randoms": gen_mc3pcf_randoms, "random_catalogue": gen_random_catalogue, "mc3pcf_particle": gen_mc3pcf_particle, "window_file": gen_window_file, "tabulated": gen_tabulated, "counting": gen_counting, "mc3pcf": gen_mc3pcf, "phi": gen_phi, "deposit": gen_deposit, "windows": gen_windows,
             "convolution": gen_convolution, "corr2pcf": gen_corr2pcf, "multipole": gen_multipole}
 
 

@@ -14,6 +14,7 @@ import oracle
 from pyhermes_gb300 import mc3pcf
 from pyhermes_gb300.phi import sample_scaling_function
 from pyhermes_gb300.sfc_field import SFCField
+from test_tasks_host import oracle_kernels  # noqa: F401  (fixture: oracle pair products for xi23)
 
 PHI = sample_scaling_function()
 
@@ -49,7 +50,7 @@ def _rel(a, b):
     return np.abs(a - b).max() / np.abs(b).max()
 
 
-def test_particle_centre_products_match_reference(golden_dir, monkeypatch):
+def test_particle_centre_products_match_reference(golden_dir, oracle_kernels, monkeypatch):
     g = np.load(os.path.join(golden_dir, "mc3pcf_particle_J4.npz"))
     monkeypatch.setattr(mc3pcf, "triplet_sum", _cpu_triplet_sum)
     task = mc3pcf.Corr_3PCF({"Corr_3PCF": {
@@ -77,7 +78,7 @@ def test_particle_centre_argument_rules():
         mc3pcf._centre_arrays(np.zeros((3, 2)), np.ones(3), "particle_pos1", "particle_weight1")
 
 
-def test_box_random_products_match_reference(golden_dir, monkeypatch):
+def test_box_random_products_match_reference(golden_dir, oracle_kernels, monkeypatch):
     """center='box_random' (seeded box centres, n1 interpolated): ddd, rrr
     and delta_ddd against the reference golden, with the field deposited by
     the oracle from the same catalogue (catalog weight normalisation)."""
