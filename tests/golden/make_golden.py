@@ -448,6 +448,28 @@ def gen_io():
     print("wrote", sorted(os.listdir(d_io)))
 
 
+def gen_rppi():
+    """Corr_2PCF with (r_p, pi) sampling: ring and cylinder-shell bins
+    through the rppi_to_RH mapping (theory/corr2pcf.py:287-296)."""
+    from pyhermes.theory.corr2pcf import Corr_2PCF
+
+    rng = np.random.default_rng(101)
+    pos = rng.uniform(0.0, 1000.0, (3000, 3))
+    pos[:1200] = pos[:1200] * 0.3 + 350.0
+    w = rng.lognormal(0.0, 0.3, 3000)
+    f = _projection(pos, 4, weights=w)
+    out = {"pos": pos, "weights": w}
+    for kind in ("ring", "cylshell"):
+        d = Corr_2PCF({"Corr_2PCF": {
+            "sfc_field": f, "random": "uniform",
+            "binning_window": {"type": kind, "mapping": "rppi_to_RH"},
+            "sampling": {"rp": {"min": 60.0, "max": 180.0, "n": 3}, "pi": {"min": 30.0, "max": 90.0, "n": 2}},
+            "products": ["delta_dd", "xi"]}}).run(save_result=False)
+        out[f"{kind}_delta_dd"] = np.asarray(d.delta_dd)
+        out[f"{kind}_xi"] = np.asarray(d.xi)
+    _save("rppi_J4", **out)
+
+
 def gen_counting():
     from pyhermes.io.window import WindowFunc
     from pyhermes.theory.counting import Counting
@@ -516,7 +538,7 @@ def gen_window_file():
     _save("window_file_J4", kernel=kernel)
 
 
-SECTIONS = {"io": gen_io, "cross": gen_cross, "normalization": gen_normalization, "mc3pcf_randoms": gen_mc3pcf_randoms, "random_catalogue": gen_random_catalogue, "mc3pcf_particle": gen_mc3pcf_particle, "window_file": gen_window_file, "tabulated": gen_tabulated, "counting": gen_counting, "mc3pcf": gen_mc3pcf, "phi": gen_phi, "deposit": gen_deposit, "windows": gen_windows,
+SECTIONS = {"rppi": gen_rppi, "io": gen_io, "cross": gen_cross, "normalization": gen_normalization, "mc3pcf_randoms": gen_mc3pcf_randoms, "random_catalogue": gen_random_catalogue, "mc3pcf_particle": gen_mc3pcf_particle, "window_file": gen_window_file, "tabulated": gen_tabulated, "counting": gen_counting, "mc3pcf": gen_mc3pcf, "phi": gen_phi, "deposit": gen_deposit, "windows": gen_windows,
             "convolution": gen_convolution, "corr2pcf": gen_corr2pcf, "multipole": gen_multipole}
 
 

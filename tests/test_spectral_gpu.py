@@ -205,3 +205,19 @@ def test_corr2pcf_cross_fields_with_vertex_window_matches_reference(golden_dir):
         "products": ["dd", "delta_dd", "xi"]}}).run(save_result=False)
     for k in ("dd", "delta_dd", "rr", "xi"):
         assert _rel(getattr(d, k), g["c2_" + k]) <= 1e-5, k
+
+
+@pytest.mark.parametrize("kind", ["ring", "cylshell"])
+def test_corr2pcf_rppi_sampling_matches_reference(golden_dir, kind):
+    from pyhermes_gb300.corr2pcf import Corr_2PCF
+    from pyhermes_gb300.projection import SFCProjection
+
+    g = np.load(os.path.join(golden_dir, "rppi_J4.npz"))
+    f = SFCProjection({"SFCProjection": {"particle_pos": g["pos"], "catalog_weight": g["weights"], "J": 4,
+                                         "box_size": 1000.0}}).run(save_result=False)
+    d = Corr_2PCF({"Corr_2PCF": {
+        "sfc_field": f, "random": "uniform", "binning_window": {"type": kind, "mapping": "rppi_to_RH"},
+        "sampling": {"rp": {"min": 60.0, "max": 180.0, "n": 3}, "pi": {"min": 30.0, "max": 90.0, "n": 2}},
+        "products": ["delta_dd", "xi"]}}).run(save_result=False)
+    for k in ("delta_dd", "xi"):
+        assert _rel(getattr(d, k), g[f"{kind}_{k}"]) <= 1e-5, (kind, k)

@@ -226,3 +226,18 @@ def test_cross_fields_and_vertex_windows_match_reference(golden_dir, oracle_kern
         "l_min": 1, "l_max": 2, "products": ["ddd_l", "delta_ddd_l"]}}, device="cpu").run(save_result=False)
     for k in ("ddd_l", "delta_ddd_l"):
         assert _rel(getattr(d, k), g["c3_" + k]) < 1e-5, (k, getattr(d, k), g["c3_" + k])
+
+
+@pytest.mark.parametrize("kind", ["ring", "cylshell"])
+def test_corr2pcf_rppi_sampling_matches_reference(golden_dir, oracle_kernels, kind):
+    """(r_p, pi) sampling through the rppi_to_RH mapping (R = r_p, H = pi)."""
+    g = np.load(os.path.join(golden_dir, "rppi_J4.npz"))
+    f = SFCProjection({"SFCProjection": {"particle_pos": g["pos"], "catalog_weight": g["weights"], "J": 4,
+                                         "box_size": 1000.0}}, device="cpu").run(save_result=False)
+    d = corr2pcf.Corr_2PCF({"Corr_2PCF": {
+        "sfc_field": f, "random": "uniform", "binning_window": {"type": kind, "mapping": "rppi_to_RH"},
+        "sampling": {"rp": {"min": 60.0, "max": 180.0, "n": 3}, "pi": {"min": 30.0, "max": 90.0, "n": 2}},
+        "products": ["delta_dd", "xi"]}}, device="cpu").run(save_result=False)
+    assert d.xi.shape == (3, 2)
+    for k in ("delta_dd", "xi"):
+        assert _rel(getattr(d, k), g[f"{kind}_{k}"]) < 1e-5, (k, getattr(d, k), g[f"{kind}_{k}"])
