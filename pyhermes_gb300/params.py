@@ -56,7 +56,9 @@ DEFAULTS = {
         "fout_path": "",
     },
     "SFCProjection": {
-        "fin": {"path": "", "format": "bin", "download": {}, "reader_params": {},
+        "fin": {"path": "", "format": "bin",
+                "download": {"cache_path": "", "cache_dir": "", "sha256": "", "timeout": 60},
+                "reader_params": {"dtype": "float32", "ncols": 3, "pos_cols": [0, 1, 2], "fields": {}},
                 "catalog_weight_key": None, "field_value_key": None},
         "particle_pos": None,
         "catalog_weight": None,

@@ -470,6 +470,54 @@ def gen_rppi():
     _save("rppi_J4", **out)
 
 
+def _info_json(info):
+    import json
+
+    def clean(v):
+        if isinstance(v, dict):
+            return {k: clean(x) for k, x in v.items() if k not in ("phi_array",)}
+        if isinstance(v, (list, tuple)):
+            return [clean(x) for x in v]
+        if isinstance(v, (np.floating, np.integer)):
+            return v.item()
+        if isinstance(v, np.ndarray):
+            return v.tolist()
+        return v
+
+    return json.dumps(clean(info), sort_keys=True)
+
+
+def gen_field_algebra():
+    """SFCField algebra and normalisation (io/sfc_field.py:152-423, 484-530):
+    the epsilon and sfc_info (without phi_array, as JSON) of each result,
+    mean densities and field_density_at_pos options."""
+    rng = np.random.default_rng(111)
+    pa = rng.uniform(0.0, 1000.0, (2000, 3))
+    pa[:800] = pa[:800] * 0.3 + 350.0
+    wa = rng.lognormal(0.0, 0.3, 2000)
+    fva = rng.uniform(0.5, 2.0, 2000)
+    pb = rng.uniform(0.0, 1000.0, (1500, 3))
+    a = _projection(pa, 4, weights=wa, field_value=fva)
+    b = _projection(pb, 4)
+    q = rng.uniform(0.0, 1000.0, (200, 3))
+    out = {"pa": pa, "wa": wa, "fva": fva, "pb": pb, "query": q}
+    results = {"add": a + b, "sub": a - b, "mul": a * b, "adds": a + 0.5, "subs": a - 0.25, "rsubs": 1.0 - a,
+               "muls": 3.0 * a, "divs": a / 4.0, "switch_raw": a.switch_weight_normalization("raw"),
+               "switch_field": a.switch_weight_normalization("field"), "unit": a.to_unit_weight(),
+               "with_raw": a.with_normalization("raw")}
+    for name, r in results.items():
+        out[name + "_eps"] = np.asarray(r.epsilon)
+        out[name + "_info"] = np.array(_info_json(r.sfc_info))
+    dens = {}
+    for norm in (None, "raw", "field", "unit"):
+        for unit in ("grid", "physical"):
+            key = f"{norm}_{unit}"
+            dens["mean_" + key] = a.field_mean_density(normalization=norm, value_unit=unit)
+            out["at_" + key] = np.asarray(a.field_density_at_pos(q, normalization=norm, value_unit=unit))
+    out["means"] = np.array(_info_json(dens))
+    _save("field_algebra_J4", **out)
+
+
 def gen_counting():
     from pyhermes.io.window import WindowFunc
     from pyhermes.theory.counting import Counting
@@ -538,7 +586,7 @@ def gen_window_file():
     _save("window_file_J4", kernel=kernel)
 
 
-SECTIONS = {"rppi": gen_rppi, "io": gen_io, "cross": gen_cross, "normalization": gen_normalization, "mc3pcf_randoms": gen_mc3pcf_randoms, "random_catalogue": gen_random_catalogue, "mc3pcf_particle": gen_mc3pcf_particle, "window_file": gen_window_file, "tabulated": gen_tabulated, "counting": gen_counting, "mc3pcf": gen_mc3pcf, "phi": gen_phi, "deposit": gen_deposit, "windows": gen_windows,
+SECTIONS = {"field_algebra": gen_field_algebra, "rppi": gen_rppi, "io": gen_io, "cross": gen_cross, "normalization": gen_normalization, "mc3pcf_randoms": gen_mc3pcf_randoms, "random_catalogue": gen_random_catalogue, "mc3pcf_particle": gen_mc3pcf_particle, "window_file": gen_window_file, "tabulated": gen_tabulated, "counting": gen_counting, "mc3pcf": gen_mc3pcf, "phi": gen_phi, "deposit": gen_deposit, "windows": gen_windows,
             "convolution": gen_convolution, "corr2pcf": gen_corr2pcf, "multipole": gen_multipole}
 
 
