@@ -52,28 +52,45 @@ class SFCProjection:
         self.threads = int(tp["threads"])
         self.fout_path = tp["fout_path"]
 
+    def _read_catalogue(self):
+        """Positions and per-particle values from ``fin`` (a catalogue file,
+        pyhermes/base/sfc_projection.py:145-167): the reader for fin.format
+        (or the file name), then catalog_weight_key / field_value_key
+        resolved to named fields or unit values."""
+        from .readers import read_particle_data, resolve_particle_value
+
+        if not self.fin.get("path"):
+            raise ValueError("SFCProjection needs particle_pos or fin.path.")
+        data = read_particle_data(self.fin["path"], self.fin.get("format"), download=self.fin.get("download", {}),
+                                  **dict(self.fin.get("reader_params") or {}))
+        cw, ck = resolve_particle_value(data, self.fin.get("catalog_weight_key"), label="Catalogue weight")
+        fv, fk = resolve_particle_value(data, self.fin.get("field_value_key"), label="Field value")
+        self.fin["catalog_weight_key"], self.fin["field_value_key"] = ck, fk
+        return np.asarray(data["pos"], dtype=np.float64), cw, fv
+
     def _load_particle_input(self):
-        """pyhermes/base/sfc_projection.py:125-193 (array input)."""
+        """pyhermes/base/sfc_projection.py:125-193: array input, or a
+        catalogue file named by fin.path."""
         if self.particle_pos is None:
-            raise NotImplementedError(
-                "File catalogue readers are not part of this package; pass particle_pos (N,3)."
-            )
-        p_pos = self.particle_pos
-        if isinstance(p_pos, torch.Tensor):
+            p_pos, cw, fv = self._read_catalogue()
             n = p_pos.shape[0]
         else:
-            p_pos = np.asarray(p_pos)
-            n = p_pos.shape[0]
+            p_pos = self.particle_pos
+            if isinstance(p_pos, torch.Tensor):
+                n = p_pos.shape[0]
+            else:
+                p_pos = np.asarray(p_pos)
+                n = p_pos.shape[0]
+            cw = self.catalog_weight
+            fv = self.field_value
+            self.fin["catalog_weight_key"] = None if cw is None else "custom"
+            self.fin["field_value_key"] = None if fv is None else "custom"
         if p_pos.ndim != 2 or p_pos.shape[1] != 3:
             raise ValueError(
                 "Wrong input of particle data! 'particle_pos' must be a 2D array of shape (N, 3), "
                 f"but got shape={tuple(p_pos.shape)}."
             )
         self.particle_count = n
-        cw = self.catalog_weight
-        fv = self.field_value
-        self.fin["catalog_weight_key"] = None if cw is None else "custom"
-        self.fin["field_value_key"] = None if fv is None else "custom"
         if cw is None:
             cw = np.ones(n, dtype=np.float32)
         if fv is None:
