@@ -376,6 +376,17 @@ class Corr_3PCF:
             # the random centres (or the data centres when none are given)
             cpos, cw = _centre_arrays(self.particle_pos1, self.particle_weight1, "particle_pos1", "particle_weight1")
             rpos, rw = _centre_arrays(self.random_pos1, self.random_weight1, "random_pos1", "random_weight1")
+            # without explicit centres: the catalogues behind vertex 1's data
+            # and random fields, weighted by their projection weights
+            # (theory/corr3pcf.py:578-613, 815-833)
+            if cpos is None and any(p in self.expanded for p in ("ddd", "d_delta_dd")):
+                pd = data[1].get_particle_data()
+                cpos, cw = _centre_arrays(pd["pos"], pd["projection_weight"], "sfc_field1 particle positions",
+                                          "sfc_field1 particle weight")
+            if rpos is None and "r_delta_dd" in self.expanded and isinstance(rand[1], SFCField):
+                pd = rand[1].get_particle_data()
+                rpos, rw = _centre_arrays(pd["pos"], pd["projection_weight"], "random1 particle positions",
+                                          "random1 particle weight")
             V = float(L) ** 3
             rho1_rrr = None
             if cpos is not None:
@@ -390,8 +401,8 @@ class Corr_3PCF:
             needs_data_centres = any(p in self.expanded for p in ("ddd", "d_delta_dd")) or \
                 ("r_delta_dd" in self.expanded and rpos is None and not isinstance(rand[1], float))
             if needs_data_centres and cpos is None:
-                raise ValueError("center='particle' needs particle_pos1 and particle_weight1 "
-                                 "(catalogue re-reading is not part of this package).")
+                raise ValueError("center='particle' needs particle_pos1 and particle_weight1, or a catalog "
+                                 "sfc_field1 whose particles can be re-read.")
             if "ddd" in self.expanded:
                 res["ddd"] = rho1_p * mc((None, eps[2], eps[3]), c_t, cw, self.n_rot * wsum)
             if "d_delta_dd" in self.expanded:

@@ -8,6 +8,7 @@ The MPI x-slab path (:325-379) has no counterpart: one process owns the GPU.
 """
 
 import copy
+import os
 import logging
 import time
 
@@ -141,7 +142,28 @@ class SFCProjection:
                 raise ValueError("weight_normalization='field' requires a finite, non-zero raw_field_weighted_sum.")
         self.projection_weight = cw * fv / den
         self.field_integral = self.raw_field_weighted_sum / den
+        if self.save_particle_data:
+            self._save_particle_dataset()
         self._fields_prepared = True
+
+    def _save_particle_dataset(self):
+        """pyhermes/base/sfc_projection.py:195-219: positions (float32),
+        catalogue weights and field values (float64) as an npz at
+        particle_data_path, or next to fout_path as <name>_particles.npz."""
+        path = self.particle_data_path
+        if not path:
+            if not self.fout_path:
+                raise ValueError("save_particle_data=True requires either 'particle_data_path' or 'fout_path' "
+                                 "so the particle dataset has a place to go.")
+            path = f"{os.path.splitext(self.fout_path)[0]}_particles.npz"
+        d = os.path.dirname(path)
+        if d:
+            os.makedirs(d, exist_ok=True)
+        pos = self.particle_pos.cpu().numpy() if isinstance(self.particle_pos, torch.Tensor) else self.particle_pos
+        np.savez(path, pos=np.ascontiguousarray(pos, dtype=np.float32),
+                 catalog_weight=np.ascontiguousarray(self.catalog_weight, dtype=np.float64),
+                 field_value=np.ascontiguousarray(self.field_value, dtype=np.float64))
+        self.particle_data_path = path
 
     def run(self, save_result=True, overwrite=False, out_dtype=torch.float32):
         t0 = time.perf_counter()

@@ -282,6 +282,43 @@ class SFCField:
             return None
         return float(raw_sum / self._normalization_denominator(weight_normalization))
 
+    def get_particle_data(self):
+        """pyhermes/io/sfc_field.py:425-482: the catalogue behind a catalog
+        field -- from the saved particle dataset (particle_data_path) or by
+        re-reading fin -- with catalogue weights, normalised weights, field
+        values and the projection weights of the field's normalisation."""
+        if getattr(self, "field_kind", None) != "catalog_field":
+            raise ValueError("Only catalog fields can provide particle data. Derived fields do not retain a unique "
+                             "particle catalogue.")
+        if not bool(getattr(self, "particle_data_retrievable", True)):
+            raise ValueError("This field no longer maps to one retrievable particle catalogue. Provide particle_pos1 "
+                             "and particle_weight1 explicitly for particle-centred statistics.")
+        den = self._normalization_denominator(getattr(self, "weight_normalization", "raw"))
+        path = self.sfc_info.get("particle_data_path", "")
+        if path:
+            with np.load(path) as z:
+                if not {"pos", "catalog_weight", "field_value"}.issubset(z.files):
+                    raise ValueError(f"Particle dataset '{path}' must contain ['catalog_weight', 'field_value', 'pos'] "
+                                     "arrays.")
+                pos = z["pos"]
+                cw = np.asarray(z["catalog_weight"], dtype=np.float64)
+                fv = np.asarray(z["field_value"], dtype=np.float64)
+        else:
+            from .readers import read_particle_data, resolve_particle_value
+
+            fin = self.sfc_info.get("fin") or {}
+            if not fin.get("path", ""):
+                raise ValueError("Input particle path is not specified.")
+            data = read_particle_data(fin["path"], fin.get("format"), download=fin.get("download", {}),
+                                      **dict(fin.get("reader_params") or {}))
+            pos = data["pos"]
+            cw = np.asarray(resolve_particle_value(data, fin.get("catalog_weight_key"), "Catalogue weight")[0],
+                            dtype=np.float64)
+            fv = np.asarray(resolve_particle_value(data, fin.get("field_value_key"), "Field value")[0],
+                            dtype=np.float64)
+        return {"pos": pos, "catalog_weight": cw, "normalized_catalog_weight": cw / float(self.catalog_weight_sum),
+                "field_value": fv, "projection_weight": cw * fv / den}
+
     def switch_weight_normalization(self, weight_normalization):
         """pyhermes/io/sfc_field.py:360-378 (rescale by old_den/new_den)."""
         mode = normalize_weight_normalization(weight_normalization)

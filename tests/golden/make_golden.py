@@ -641,6 +641,55 @@ def gen_catalogues():
     _save("catalogues_J4", **out)
 
 
+def gen_particle_data():
+    """SFCField.get_particle_data (io/sfc_field.py:425-482) from a fin-read
+    catalogue and from a saved particle dataset (base/sfc_projection.py:
+    195-219), and Corr_3PCF particle centres taken from sfc_field1's
+    catalogue (theory/corr3pcf.py:578-613)."""
+    import tempfile
+
+    from pyhermes.base.sfc_projection import SFCProjection
+    from pyhermes.io.readers import read_particle_data
+    from pyhermes.theory.corr3pcf import Corr_3PCF
+
+    d = os.path.join(HERE, "catalogues")
+    fin = {"path": os.path.join(d, "cat.bin"), "format": "bin",
+           "reader_params": {"ncols": 5, "fields": {"weight": 3, "value": 4}},
+           "catalog_weight_key": "weight", "field_value_key": "value"}
+    out = {}
+    f = SFCProjection({"SFCProjection": {"fin": fin, "J": 4, "box_size": 1000.0,
+                                         "weight_normalization": "field"}}).run(save_result=False)
+    data = read_particle_data(fin["path"], "bin", ncols=5, fields={"weight": 3, "value": 4})
+    f64 = SFCProjection({"SFCProjection": {"particle_pos": np.asarray(data["pos"], dtype=np.float64),
+                                           "catalog_weight": np.asarray(data["weight"], dtype=np.float64),
+                                           "field_value": np.asarray(data["value"], dtype=np.float64), "J": 4,
+                                           "box_size": 1000.0, "weight_normalization": "field"}}).run(
+        save_result=False)
+    f.epsilon = f64.epsilon  # numba's float64 arithmetic (see gen_catalogues); fin stays for re-reading
+    for k, v in f.get_particle_data().items():
+        out["fin__" + k] = np.asarray(v)
+    with tempfile.TemporaryDirectory() as tmp:
+        rng = np.random.default_rng(131)
+        pos = rng.uniform(0.0, 1000.0, (400, 3))
+        g = SFCProjection({"SFCProjection": {"particle_pos": pos, "catalog_weight": rng.lognormal(0.0, 0.3, 400),
+                                             "J": 4, "box_size": 1000.0, "save_particle_data": True,
+                                             "particle_data_path": os.path.join(tmp, "p.npz")}}).run(
+            save_result=False)
+        out["saved_pos_in"] = pos
+        for k, v in g.get_particle_data().items():
+            out["saved__" + k] = np.asarray(v)
+        with np.load(os.path.join(tmp, "p.npz")) as z:
+            for k in z.files:
+                out["savedfile__" + k] = z[k]
+    d3 = Corr_3PCF({"Corr_3PCF": {
+        "sfc_field": f, "random": "uniform", "r12": 150.0, "r13": 250.0, "angle_param": "mu",
+        "mu": {"mu_min": -0.8, "mu_max": 0.8, "n_mu": 3}, "n_rot": 3, "center": "particle", "base_seed": 9,
+        "weight_normalization": "field", "products": ["zeta", "ddd"]}}).run(save_result=False)
+    for k in ("ddd", "d_delta_dd", "rrr", "xi23", "r_delta_dd", "delta_ddd", "zeta"):
+        out["p3_" + k] = np.asarray(getattr(d3, k))
+    _save("particle_data_J4", **out)
+
+
 def gen_counting():
     from pyhermes.io.window import WindowFunc
     from pyhermes.theory.counting import Counting
@@ -709,7 +758,7 @@ def gen_window_file():
     _save("window_file_J4", kernel=kernel)
 
 
-SECTIONS = {"catalogues": gen_catalogues, "field_algebra": gen_field_algebra, "rppi": gen_rppi, "io": gen_io, "cross": gen_cross, "normalization": gen_normalization, "mc3pcf_randoms": gen_mc3pcf_randoms, "random_catalogue": gen_random_catalogue, "mc3pcf_particle": gen_mc3pcf_particle, "window_file": gen_window_file, "tabulated": gen_tabulated, "counting": gen_counting, "mc3pcf": gen_mc3pcf, "phi": gen_phi, "deposit": gen_deposit, "windows": gen_windows,
+SECTIONS = {"particle_data": gen_particle_data, "catalogues": gen_catalogues, "field_algebra": gen_field_algebra, "rppi": gen_rppi, "io": gen_io, "cross": gen_cross, "normalization": gen_normalization, "mc3pcf_randoms": gen_mc3pcf_randoms, "random_catalogue": gen_random_catalogue, "mc3pcf_particle": gen_mc3pcf_particle, "window_file": gen_window_file, "tabulated": gen_tabulated, "counting": gen_counting, "mc3pcf": gen_mc3pcf, "phi": gen_phi, "deposit": gen_deposit, "windows": gen_windows,
             "convolution": gen_convolution, "corr2pcf": gen_corr2pcf, "multipole": gen_multipole}
 
 

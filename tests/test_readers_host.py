@@ -70,3 +70,52 @@ def test_projection_from_catalogue_file_matches_reference(golden_dir, oracle_ker
     _close(_clean({k: v for k, v in f.sfc_info.items() if k != "fin"}), json.loads(str(g[name + "__info"])), name)
     _close(_clean({k: v for k, v in f.sfc_info["fin"].items() if k != "path"}), json.loads(str(g[name + "__fin"])),
            name + ".fin")
+
+
+def _bin_fin(golden_dir):
+    return {"path": os.path.join(golden_dir, "catalogues", "cat.bin"), "format": "bin",
+            "reader_params": {"ncols": 5, "fields": {"weight": 3, "value": 4}},
+            "catalog_weight_key": "weight", "field_value_key": "value"}
+
+
+def test_get_particle_data_matches_reference(golden_dir, oracle_kernels, tmp_path):
+    """From the fin catalogue (field normalisation) and from a saved
+    particle dataset (save_particle_data)."""
+    g = np.load(os.path.join(golden_dir, "particle_data_J4.npz"))
+    f = SFCProjection({"SFCProjection": {"fin": _bin_fin(golden_dir), "J": 4, "box_size": 1000.0,
+                                         "weight_normalization": "field"}}, device="cpu").run(save_result=False)
+    for k, v in f.get_particle_data().items():
+        np.testing.assert_allclose(v, g["fin__" + k], rtol=1e-15, atol=0, err_msg=k)
+    rng = np.random.default_rng(131)
+    pos = rng.uniform(0.0, 1000.0, (400, 3))
+    np.testing.assert_array_equal(pos, g["saved_pos_in"])
+    s = SFCProjection({"SFCProjection": {"particle_pos": pos, "catalog_weight": rng.lognormal(0.0, 0.3, 400), "J": 4,
+                                         "box_size": 1000.0, "save_particle_data": True,
+                                         "particle_data_path": str(tmp_path / "p.npz")}}, device="cpu").run(
+        save_result=False)
+    with np.load(tmp_path / "p.npz") as z:
+        assert sorted(z.files) == sorted(k.split("__")[1] for k in g.files if k.startswith("savedfile__"))
+        for k in z.files:
+            assert z[k].dtype == g["savedfile__" + k].dtype
+            np.testing.assert_array_equal(z[k], g["savedfile__" + k])
+    for k, v in s.get_particle_data().items():
+        np.testing.assert_allclose(v, g["saved__" + k], rtol=1e-15, atol=0, err_msg=k)
+
+
+def test_corr3pcf_particle_centres_from_field_catalogue(golden_dir, oracle_kernels, monkeypatch):
+    """center='particle' without particle_pos1: the centres and projection
+    weights come from sfc_field1's catalogue (re-read through fin)."""
+    from pyhermes_gb300 import mc3pcf
+    from test_tasks_host import _cpu_triplet_sum
+
+    monkeypatch.setattr(mc3pcf, "triplet_sum", _cpu_triplet_sum)
+    g = np.load(os.path.join(golden_dir, "particle_data_J4.npz"))
+    f = SFCProjection({"SFCProjection": {"fin": _bin_fin(golden_dir), "J": 4, "box_size": 1000.0,
+                                         "weight_normalization": "field"}}, device="cpu").run(save_result=False)
+    d = mc3pcf.Corr_3PCF({"Corr_3PCF": {
+        "sfc_field": f, "random": "uniform", "r12": 150.0, "r13": 250.0, "angle_param": "mu",
+        "mu": {"mu_min": -0.8, "mu_max": 0.8, "n_mu": 3}, "n_rot": 3, "center": "particle", "base_seed": 9,
+        "weight_normalization": "field", "products": ["zeta", "ddd"]}}, device="cpu").run()
+    for k in ("ddd", "d_delta_dd", "rrr", "xi23", "r_delta_dd", "delta_ddd", "zeta"):
+        ref = g["p3_" + k]
+        assert np.abs(getattr(d, k) - ref).max() <= 1e-5 * np.abs(ref).max(), (k, getattr(d, k), ref)
