@@ -324,6 +324,9 @@ class WindowFunc(SFCField):
         new.other_args = {"operation": copy.deepcopy(operation)}
         new.window_params = {"type": new.type, "len_args": {}, "los_args": {}, "other_args": new.other_args,
                              "kernel_mode": new.kernel_mode}
+        new.input_params = {**copy.deepcopy(new.window_params), "J": self.J, "box_size": self.box_size,
+                            "phi_resolution": self.phi_resolution, "wavelet_mode": self.wavelet_mode,
+                            "wavelet_level": self.wavelet_level, "bandwidth": self.bandwidth}
         new.w_kernel = None
         new._kernel_dev = kernel
         new.is_composite_window = True

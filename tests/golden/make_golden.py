@@ -690,6 +690,32 @@ def gen_particle_data():
     _save("particle_data_J4", **out)
 
 
+def gen_composite_windows():
+    """WindowFunc composite algebra (io/window.py:345-485): kernels of
+    window +, -, x with windows and scalars, and the file a composite saves."""
+    import tempfile
+
+    from pyhermes.io.sfc_field import read_numpy_pickle
+    from pyhermes.io.window import WindowFunc
+
+    sfc = _sfc_params(4)
+    a = WindowFunc({"type": "gaussian", "len_args": {"R": 30.0}}, sfc)
+    b = WindowFunc({"type": "sphere", "len_args": {"R": 50.0}}, sfc)
+    out = {}
+    for name, w in {"add": a + b, "sub": a - 0.5 * b, "neg": -a, "prod": a * b, "div": a / 4.0,
+                    "nested": (a + b) * 2.0 - a}.items():
+        out[name + "_kernel"] = np.asarray(w.as_array())
+    with tempfile.TemporaryDirectory() as tmp:
+        fn = os.path.join(tmp, "w.pkl")
+        (a + b).save(fn)
+        with open(fn, "rb") as f:
+            d = read_numpy_pickle(f)
+    out["saved_keys"] = np.array(list(d.keys()))
+    out["saved_info"] = np.array(_info_json({k: v for k, v in d.items() if k != "window_kernal"}))
+    out["saved_kernel"] = np.asarray(d["window_kernal"])
+    _save("composite_windows_J4", **out)
+
+
 def gen_counting():
     from pyhermes.io.window import WindowFunc
     from pyhermes.theory.counting import Counting
@@ -758,7 +784,7 @@ def gen_window_file():
     _save("window_file_J4", kernel=kernel)
 
 
-SECTIONS = {"particle_data": gen_particle_data, "catalogues": gen_catalogues, "field_algebra": gen_field_algebra, "rppi": gen_rppi, "io": gen_io, "cross": gen_cross, "normalization": gen_normalization, "mc3pcf_randoms": gen_mc3pcf_randoms, "random_catalogue": gen_random_catalogue, "mc3pcf_particle": gen_mc3pcf_particle, "window_file": gen_window_file, "tabulated": gen_tabulated, "counting": gen_counting, "mc3pcf": gen_mc3pcf, "phi": gen_phi, "deposit": gen_deposit, "windows": gen_windows,
+SECTIONS = {"composite_windows": gen_composite_windows, "particle_data": gen_particle_data, "catalogues": gen_catalogues, "field_algebra": gen_field_algebra, "rppi": gen_rppi, "io": gen_io, "cross": gen_cross, "normalization": gen_normalization, "mc3pcf_randoms": gen_mc3pcf_randoms, "random_catalogue": gen_random_catalogue, "mc3pcf_particle": gen_mc3pcf_particle, "window_file": gen_window_file, "tabulated": gen_tabulated, "counting": gen_counting, "mc3pcf": gen_mc3pcf, "phi": gen_phi, "deposit": gen_deposit, "windows": gen_windows,
             "convolution": gen_convolution, "corr2pcf": gen_corr2pcf, "multipole": gen_multipole}
 
 
