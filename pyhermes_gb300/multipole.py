@@ -526,6 +526,9 @@ class Corr_3PCF_Multipole:
             if p not in self.products:
                 self.products.append(p)
         self.fout_path = tp.get("fout_path", "")
+        self.zeta_condition_warning = float(tp.get("zeta_condition_warning", 1.0e12))
+        if not np.isfinite(self.zeta_condition_warning) or self.zeta_condition_warning <= 0.0:
+            raise ValueError("zeta_condition_warning must be a finite positive number.")
         self._fields_prepared = False
 
     def _resolution_diagnostics(self):
@@ -578,7 +581,7 @@ class Corr_3PCF_Multipole:
                      "summation_backend": self._backend_given, "execution_mode": "serial",
                      "sample_mpi": {"ranks_per_sample": 1, "gpu_device_ids": []},
                      "cache_multipole_fields": False, "cache_dir": "", "verbose_m_progress": False,
-                     "verbose_profile": False, "zeta_condition_warning": 1e12,
+                     "verbose_profile": False, "zeta_condition_warning": self.zeta_condition_warning,
                      "threads": int(tp.get("threads", 1) or 1), "products": list(self.products),
                      "radial_profile_diagnostics": bool(tp.get("radial_profile_diagnostics", True)),
                      "radial_profile_diagnostic_tolerance": float(tp.get("radial_profile_diagnostic_tolerance", 1e-5)),
@@ -781,6 +784,13 @@ class Corr_3PCF_Multipole:
             z, _, cond = mixing_solve(data.delta_ddd_l, data.rrr_l, self.l_max, device=self.device)
             data.zeta_l = z
             data.zeta_condition = cond
+            # theory/corr3pcf_multipole.py:1580-1589
+            bad = np.where(cond > self.zeta_condition_warning)[0]
+            if bad.size:
+                logger.warning("zeta_l mixing matrices exceed zeta_condition_warning=%.3e for samples %s.",
+                               self.zeta_condition_warning, bad.tolist())
+            logger.info("zeta_l solved from multipole ratio | mixing matrix cond range=[%.3e, %.3e]",
+                        float(np.min(cond)), float(np.max(cond)))
         for i in (1, 2, 3):
             if i in self.data:
                 setattr(data, f"sfc_info{i}", self.data[i].sfc_info)
