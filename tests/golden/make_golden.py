@@ -716,6 +716,25 @@ def gen_composite_windows():
     _save("composite_windows_J4", **out)
 
 
+def gen_mc_theta():
+    """Corr_3PCF with angle_param='theta' (a min/max/n spec and a list)."""
+    from pyhermes.theory.corr3pcf import Corr_3PCF
+
+    rng = np.random.default_rng(141)
+    pos = rng.uniform(0.0, 1000.0, (3000, 3))
+    pos[:1200] = pos[:1200] * 0.3 + 350.0
+    f = _projection(pos, 4)
+    out = {"pos": pos}
+    for name, theta in {"spec": {"theta_min": 0.3, "theta_max": 2.5, "n_theta": 3}, "list": [0.5, 1.5]}.items():
+        d = Corr_3PCF({"Corr_3PCF": {
+            "sfc_field": f, "random": "uniform", "r12": 150.0, "r13": 250.0, "angle_param": "theta",
+            "theta": theta, "n_rot": 3, "center": "box_random", "n_box_centers": 400, "base_seed": 11,
+            "products": ["ddd", "rrr", "delta_ddd"]}}).run(save_result=False)
+        for k in ("theta", "mu", "r23", "ddd", "rrr", "delta_ddd", "xi23"):
+            out[f"{name}_{k}"] = np.asarray(getattr(d, k))
+    _save("mc_theta_J4", **out)
+
+
 def gen_counting():
     from pyhermes.io.window import WindowFunc
     from pyhermes.theory.counting import Counting
@@ -784,7 +803,7 @@ def gen_window_file():
     _save("window_file_J4", kernel=kernel)
 
 
-SECTIONS = {"composite_windows": gen_composite_windows, "particle_data": gen_particle_data, "catalogues": gen_catalogues, "field_algebra": gen_field_algebra, "rppi": gen_rppi, "io": gen_io, "cross": gen_cross, "normalization": gen_normalization, "mc3pcf_randoms": gen_mc3pcf_randoms, "random_catalogue": gen_random_catalogue, "mc3pcf_particle": gen_mc3pcf_particle, "window_file": gen_window_file, "tabulated": gen_tabulated, "counting": gen_counting, "mc3pcf": gen_mc3pcf, "phi": gen_phi, "deposit": gen_deposit, "windows": gen_windows,
+SECTIONS = {"mc_theta": gen_mc_theta, "composite_windows": gen_composite_windows, "particle_data": gen_particle_data, "catalogues": gen_catalogues, "field_algebra": gen_field_algebra, "rppi": gen_rppi, "io": gen_io, "cross": gen_cross, "normalization": gen_normalization, "mc3pcf_randoms": gen_mc3pcf_randoms, "random_catalogue": gen_random_catalogue, "mc3pcf_particle": gen_mc3pcf_particle, "window_file": gen_window_file, "tabulated": gen_tabulated, "counting": gen_counting, "mc3pcf": gen_mc3pcf, "phi": gen_phi, "deposit": gen_deposit, "windows": gen_windows,
             "convolution": gen_convolution, "corr2pcf": gen_corr2pcf, "multipole": gen_multipole}
 
 

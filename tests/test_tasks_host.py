@@ -241,3 +241,22 @@ def test_corr2pcf_rppi_sampling_matches_reference(golden_dir, oracle_kernels, ki
     assert d.xi.shape == (3, 2)
     for k in ("delta_dd", "xi"):
         assert _rel(getattr(d, k), g[f"{kind}_{k}"]) < 1e-5, (k, getattr(d, k), g[f"{kind}_{k}"])
+
+
+@pytest.mark.parametrize("case", ["spec", "list"])
+def test_mc3pcf_theta_sampling_matches_reference(golden_dir, oracle_kernels, monkeypatch, case):
+    from pyhermes_gb300 import mc3pcf
+
+    monkeypatch.setattr(mc3pcf, "triplet_sum", _cpu_triplet_sum)
+    g = np.load(os.path.join(golden_dir, "mc_theta_J4.npz"))
+    f = SFCProjection({"SFCProjection": {"particle_pos": g["pos"], "J": 4, "box_size": 1000.0}},
+                      device="cpu").run(save_result=False)
+    theta = {"spec": {"theta_min": 0.3, "theta_max": 2.5, "n_theta": 3}, "list": [0.5, 1.5]}[case]
+    d = mc3pcf.Corr_3PCF({"Corr_3PCF": {
+        "sfc_field": f, "random": "uniform", "r12": 150.0, "r13": 250.0, "angle_param": "theta", "theta": theta,
+        "n_rot": 3, "center": "box_random", "n_box_centers": 400, "base_seed": 11,
+        "products": ["ddd", "rrr", "delta_ddd"]}}, device="cpu").run()
+    for k in ("theta", "mu", "r23"):
+        np.testing.assert_allclose(getattr(d, k), g[f"{case}_{k}"], rtol=1e-14, atol=1e-14)
+    for k in ("ddd", "rrr", "delta_ddd", "xi23"):
+        assert _rel(getattr(d, k), g[f"{case}_{k}"]) < 1e-5, (k, getattr(d, k), g[f"{case}_{k}"])
