@@ -25,6 +25,7 @@ theory/corr2pcf.py:366-372 ``pair_product_with_window``          ``hermes_fft_r2
                                                                  ``hermes_pair_products``
 utils/corr3pcf_multipoles.py:460-579 ``calc_DDD_multipole``      the batched multipole engine
 utils/special_functions.py:392-409 ``solve_multipoles_from_ratio``  ``hermes_mixing_solve``
+theory/corr3pcf.py:68-122 ``estimate_triplet_product_with_sampled_centers``  ``hermes_mc_triplets``
 ==============================================================  =====================================
 
 Fields go to the device as float32 (the arithmetic type of this package);
@@ -43,7 +44,8 @@ from . import _lib, kernels
 from .kernels import _ptr, _stream_ptr
 
 __all__ = ["project_scaling_grid_numba", "interpolate_grid_at_pos_numba", "specialized_convolution_3d",
-           "pair_product_with_window", "calc_DDD_multipole", "solve_multipoles_from_ratio"]
+           "pair_product_with_window", "calc_DDD_multipole", "solve_multipoles_from_ratio",
+           "estimate_triplet_product_with_sampled_centers"]
 
 
 def _device():
@@ -307,3 +309,45 @@ def solve_multipoles_from_ratio(A, B, lmax, rcond_warning=1e12):
     if condM > rcond_warning:
         print(f"[warning] mixing matrix is ill-conditioned: cond(M) = {condM:.3e}")
     return C[0], M[0], condM
+
+
+def estimate_triplet_product_with_sampled_centers(r12_scaled, r13_scaled, mu, center_scaled, n_rot, sfc_meta,
+                                                  sfc_field2, sfc_field3, center="box_random", center_weight=None,
+                                                  center_weight_sum=None, seed_base_rot=-1, mu_index=-1, eps1=None,
+                                                  rho1=None):
+    """Monte Carlo triple product for one mu: the rotated triangles of
+    utils/corr3pcf_kernels.py:21-63 (seeded per rotation as the reference)
+    around each centre.  box_random: mean of n1 n2 n3 with n1 interpolated
+    from eps1; particle: rho1 sum_r sum_i w_i n2 n3 / (n_rot sum_i w_i)
+    (rho1 defaults to 1 / L^3)."""
+    from .mc3pcf import rotation_offsets, triplet_sum
+
+    L = int(getattr(sfc_meta, "L"))
+    J = _level(L)
+    phi = torch.as_tensor(np.ascontiguousarray(getattr(sfc_meta, "phi_array"), dtype=np.float64), device=_device())
+    if int(getattr(sfc_meta, "phi_support", 3)) != 3:
+        raise ValueError("the GPU stencil is 3 points per axis (phi_support=3)")
+    centres = np.ascontiguousarray(center_scaled, dtype=np.float64)
+    offsets = rotation_offsets(float(r12_scaled), float(r13_scaled), float(mu), int(n_rot), seed_base_rot, mu_index)
+    e2, e3 = _field_eps(sfc_field2), _field_eps(sfc_field3)
+    if center == "box_random":
+        if eps1 is None:
+            raise ValueError("eps1 must be provided when center='box_random'.")
+        c_t = torch.as_tensor(centres, device=_device())
+        s, _ = triplet_sum(_field_eps(eps1), e2, e3, J, c_t, offsets, phi)
+        return s / (int(n_rot) * centres.shape[0])
+    if center == "particle":
+        if rho1 is None:
+            rho1 = 1.0 / L ** 3
+        if centres.shape[0] == 0:
+            return 0.0
+        w = np.ones(centres.shape[0]) if center_weight is None else np.asarray(center_weight, dtype=np.float64)
+        if w.shape[0] != centres.shape[0]:
+            raise ValueError("center_weight must have the same length as center_scaled.")
+        wsum = float(np.sum(w)) if center_weight_sum is None else float(center_weight_sum)
+        if wsum <= 0.0:
+            raise ValueError("Particle-center weights must have a positive sum.")
+        c_t = torch.as_tensor(centres, device=_device())
+        s, _ = triplet_sum(None, e2, e3, J, c_t, offsets, phi, center_w=w, rho1=1.0)
+        return float(rho1) * s / (int(n_rot) * wsum)
+    raise ValueError(f"Unknown center='{center}'. Use 'box_random' or 'particle'.")

@@ -160,3 +160,16 @@ def test_solve_multipoles_from_ratio_matches_oracle(capsys):
     assert abs(cond - cond_ref) <= 1e-10 * cond_ref
     seams.solve_multipoles_from_ratio(A, B, lmax, rcond_warning=0.5)
     assert "ill-conditioned" in capsys.readouterr().out
+
+
+def test_mc_seam_matches_oracle():
+    from types import SimpleNamespace
+
+    J, L = 5, 32
+    e1, e2, e3 = (_uniform_field(s, J, 8000) for s in (31, 32, 33))
+    centres = np.random.default_rng(34).uniform(0.0, L, (300, 3))
+    meta = SimpleNamespace(L=L, phi_array=PHI, phi_resolution=1024, phi_support=3)
+    got = seams.estimate_triplet_product_with_sampled_centers(4.8, 8.0, 0.3, centres, 4, meta, e2, e3,
+                                                              seed_base_rot=5, mu_index=2, eps1=e1)
+    ref = oracle.mc_box_random(e1, e2, e3, J, centres, 4.8, 8.0, 0.3, 4, 5, 2, PHI)
+    assert abs(got - ref) <= 1e-5 * abs(ref), (got, ref)
