@@ -26,6 +26,7 @@ theory/corr2pcf.py:366-372 ``pair_product_with_window``          ``hermes_fft_r2
 utils/corr3pcf_multipoles.py:460-579 ``calc_DDD_multipole``      the batched multipole engine
 utils/special_functions.py:392-409 ``solve_multipoles_from_ratio``  ``hermes_mixing_solve``
 theory/corr3pcf.py:68-122 ``estimate_triplet_product_with_sampled_centers``  ``hermes_mc_triplets``
+utils/corr3pcf_multipoles.py:393-457 ``compute_multipole_m_summand``  ``hermes_multipole_contract_plain``
 ==============================================================  =====================================
 
 Fields go to the device as float32 (the arithmetic type of this package);
@@ -45,7 +46,7 @@ from .kernels import _ptr, _stream_ptr
 
 __all__ = ["project_scaling_grid_numba", "interpolate_grid_at_pos_numba", "specialized_convolution_3d",
            "pair_product_with_window", "calc_DDD_multipole", "solve_multipoles_from_ratio",
-           "estimate_triplet_product_with_sampled_centers"]
+           "estimate_triplet_product_with_sampled_centers", "compute_multipole_m_summand"]
 
 
 def _device():
@@ -351,3 +352,41 @@ def estimate_triplet_product_with_sampled_centers(r12_scaled, r13_scaled, mu, ce
         s, _ = triplet_sum(None, e2, e3, J, c_t, offsets, phi, center_w=w, rho1=1.0)
         return float(rho1) * s / (int(n_rot) * wsum)
     raise ValueError(f"Unknown center='{center}'. Use 'box_random' or 'particle'.")
+
+
+def _context_array(ctx, host_key, device_key):
+    """A context entry as a device tensor: the host array, or the device
+    array through __cuda_array_interface__."""
+    if ctx.get(host_key) is not None:
+        return torch.as_tensor(np.ascontiguousarray(ctx[host_key]), device=_device())
+    v = ctx.get(device_key)
+    if v is None:
+        raise KeyError(f"sum_context has neither '{host_key}' nor '{device_key}'")
+    return torch.as_tensor(v, device=_device())
+
+
+def compute_multipole_m_summand(field_r1_m, field_r2_m, sum_context):
+    """One m summand S_m = 4 pi / L^3 sum_x eps1(x) sum_{l1,l2} Gamma3(l1, l2)
+    a2(x - l1) a3(x - l2) for the two radial multipole fields of one
+    (l, m), by the reference-form GPU contraction; ``sum_context`` is the
+    reference's (utils/corr3pcf_multipoles.py:324-390: eps1 as 'data' or
+    'data_gpu', Gamma as 'gamma' or 'gamma_gpu', 'L', 'phi_support').
+    Returns (complex value, timing dict with the reference's keys)."""
+    from .multipole import multipole_contract_plain
+
+    if int(sum_context.get("phi_support", 3)) != 3:
+        raise ValueError("the GPU contraction is specialised for a support-3 scaling function")
+    t0 = time.perf_counter()
+    L = int(sum_context["L"])
+    J = _level(L)
+    eps1 = _context_array(sum_context, "data", "data_gpu").to(torch.float32).reshape(-1).contiguous()
+    gamma = _context_array(sum_context, "gamma", "gamma_gpu").double().cpu().numpy()
+    a2 = torch.as_tensor(np.asarray(field_r1_m), device=_device()).to(torch.complex64).reshape(-1).contiguous()
+    a3 = torch.as_tensor(np.asarray(field_r2_m), device=_device()).to(torch.complex64).reshape(-1).contiguous()
+    if eps1.numel() != L ** 3 or a2.numel() != L ** 3 or a3.numel() != L ** 3:
+        raise ValueError("fields and sum_context disagree on the grid size")
+    t1 = time.perf_counter()
+    value = multipole_contract_plain(eps1, a2, a3, gamma, J)
+    t2 = time.perf_counter()
+    return value, {"h2d_elapsed_sec": t1 - t0, "kernel_elapsed_sec": t2 - t1, "reduce_elapsed_sec": 0.0,
+                   "d2h_elapsed_sec": 0.0}

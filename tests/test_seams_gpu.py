@@ -173,3 +173,23 @@ def test_mc_seam_matches_oracle():
                                                               seed_base_rot=5, mu_index=2, eps1=e1)
     ref = oracle.mc_box_random(e1, e2, e3, J, centres, 4.8, 8.0, 0.3, 4, 5, 2, PHI)
     assert abs(got - ref) <= 1e-5 * abs(ref), (got, ref)
+
+
+def test_m_summand_seam_matches_oracle():
+    """compute_multipole_m_summand with the reference's cpu-style context
+    against the oracle's 729-term contraction of the same fields."""
+    from scipy.fft import fftn, ifftn
+
+    J, L = 5, 32
+    eps = _uniform_field(35, J)
+    eps = eps - eps.mean()
+    P = oracle.fourier_power(PHI, 1, L)
+    s = fftn(eps)
+    a2 = ifftn(s * oracle.radial_multipole_window(L, P, 5.0, 3, 1))
+    a3 = ifftn(s * oracle.radial_multipole_window(L, P, 7.5, 3, -1))
+    gamma = oracle.cal_gamma(PHI)
+    ctx = {"backend": "cpu", "gamma": gamma, "data": eps, "n_result": eps.size, "L": L, "phi_support": 3}
+    val, timing = seams.compute_multipole_m_summand(a2, a3, ctx)
+    ref = 4 * np.pi * oracle.contract(eps, a2, a3, gamma) / L ** 3
+    assert abs(val - ref) <= 1e-4 * abs(ref), (val, ref)
+    assert set(timing) == {"h2d_elapsed_sec", "kernel_elapsed_sec", "reduce_elapsed_sec", "d2h_elapsed_sec"}

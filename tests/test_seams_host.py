@@ -26,6 +26,8 @@ REFERENCE_SIGNATURES = {
                            "cache_dir", "cache_namespace", "threads", "progress_callback", "m_progress_callback"],
     # pyhermes/utils/special_functions.py:392
     "solve_multipoles_from_ratio": ["A", "B", "lmax", "rcond_warning"],
+    # pyhermes/utils/corr3pcf_multipoles.py:393
+    "compute_multipole_m_summand": ["field_r1_m", "field_r2_m", "sum_context"],
     # pyhermes/theory/corr3pcf.py:68-78
     "estimate_triplet_product_with_sampled_centers": ["r12_scaled", "r13_scaled", "mu", "center_scaled", "n_rot",
                                                       "sfc_meta", "sfc_field2", "sfc_field3", "center",
