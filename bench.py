@@ -647,9 +647,9 @@ def run_gb300(args, ws, rank, local):
     zeta = np.asarray(res.zeta_l)
 
     # our kernels per step: 2 deposits x 7; per product per (l, m): fields (power, j_l table,
-    # prepass, interleave; the inverse FFT is cuFFT) + contract (contraction, reduce); the
-    # mixing solve
-    kernel_launches = args.steps * (14 + 2 * N_LM * 6 + 1)
+    # interior and edge prepass, interleave; the inverse FFT is cuFFT) + contract
+    # (contraction, reduce); the mixing solve
+    kernel_launches = args.steps * (14 + 2 * N_LM * 7 + 1)
 
     # end to end: catalogues in pinned host memory, copies inside the timed region
     h = [torch.as_tensor(a).pin_memory() for a in (dpos_np, dw_np, rpos_np, rw_np)]
