@@ -209,7 +209,7 @@ def pair_product_with_window(field1, field2, binning_window_obj, threads):
     e1 = _field_eps(field1)
     e2 = e1 if field2 is field1 else _field_eps(field2)
     L = e1.shape[0]
-    if win is None or win.is_composite_window or win.is_complex or win.resolved_mode() == "complex_full_fft":
+    if win is None or win.materialized or win.is_complex or win.resolved_mode() == "complex_full_fft":
         # any other window: its materialised rFFT-grid kernel
         conv = specialized_convolution_3d(e1, binning_window_obj.as_array(), threads)
         return float(np.einsum("ijk,ijk->", conv, e2.double().cpu().numpy(), optimize=True) / conv.size)

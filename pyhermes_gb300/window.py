@@ -13,8 +13,9 @@ NumPy copy, like the reference) for users and for composite algebra.
 """
 
 import copy
-import os
 import ctypes
+import inspect
+import os
 
 import numpy as np
 import torch
@@ -104,6 +105,96 @@ def normalize_kernel_mode(kernel_mode):
     return mode
 
 
+def ordered_window_args(func, kwargs):
+    """Values of ``func``'s parameters after (kx, ky, kz), taken from
+    ``kwargs`` or the parameter's default (utils/convolution.py:41-62)."""
+    params = inspect.signature(func).parameters
+    names = list(params)[3:]
+    missing = [n for n in names if n not in kwargs and params[n].default is inspect.Parameter.empty]
+    if missing:
+        raise ValueError(f"Missing keyword arguments: {missing} for custom window function "
+                         f"'{getattr(func, '__name__', func)}'.")
+    return [kwargs[n] if n in kwargs else params[n].default for n in names]
+
+
+def _window_values(func, kx, ky, kz, args, shape, dtype):
+    """func on the broadcast grid kx x ky x kz: one call on arrays when the
+    function is elementwise NumPy code, else one call per point."""
+    try:
+        with np.errstate(all="ignore"):
+            v = np.asarray(func(kx, ky, kz, *args))
+        if v.dtype != object:
+            return np.broadcast_to(v, shape)
+    except Exception:  # scalar-only code (math.*, branches on the arguments)
+        pass
+    one = np.vectorize(lambda a, b, c: func(float(a), float(b), float(c), *args), otypes=[dtype])
+    return one(*np.broadcast_arrays(kx, ky, kz))
+
+
+_SIGNS = ((1, 1, 1), (-1, 1, 1), (1, -1, 1), (1, 1, -1), (-1, -1, 1), (-1, 1, -1), (1, -1, -1), (-1, -1, -1))
+
+
+def custom_window_kernel(func, args, L, bandwidth, power, mode, rows=8):
+    """rFFT-grid kernel [L, L, L/2+1] of a user window W(kx, ky, kz, *args)
+    (k in cycles per cell), built on the host in float64 like the reference:
+
+    * ``full_rfft`` / ``complex_rfft`` (utils/convolution.py:74-252): for
+      each image (ii, jj, kk) < bandwidth, eight terms P P P W at
+      +(n L + x)/L and -(n L + L - x)/L per axis, summed in the reference's
+      order; complex accumulation for ``complex_rfft``;
+    * ``octant`` (:14-38, :264-283): W at (n L + i)/L for i in [0, L] on
+      every axis, folded over the eight reflections i -> L - i.
+
+    ``power`` holds |phi_hat(n/L)|^2 for n = 0..L*bandwidth."""
+    P = np.asarray(power, dtype=np.float64)
+    inv = 1.0 / L
+    H = L // 2 + 1
+    cplx = mode == "complex_rfft"
+    dt = np.complex128 if cplx else np.float64
+    y, z = np.arange(L), np.arange(H)
+    if mode == "octant":
+        n = np.arange(L + 1)
+        arr = np.zeros((L + 1, L + 1, L + 1))
+        for x0 in range(0, L + 1, rows):
+            xs = n[x0:x0 + rows]
+            acc = np.zeros((xs.size, L + 1, L + 1))
+            for ii in range(bandwidth):
+                ix = ii * L + xs
+                for jj in range(bandwidth):
+                    iy = jj * L + n
+                    for kk in range(bandwidth):
+                        iz = kk * L + n
+                        w = _window_values(func, (ix * inv)[:, None, None], (iy * inv)[None, :, None],
+                                           (iz * inv)[None, None, :], args, acc.shape, np.float64)
+                        acc += P[ix][:, None, None] * P[iy][None, :, None] * P[iz][None, None, :] * w
+            arr[x0:x0 + xs.size] = acc
+        X, Xm = np.arange(L), L - np.arange(L)
+        Y, Ym, Z, Zm = y, L - y, z, L - z
+        return (arr[np.ix_(X, Y, Z)] + arr[np.ix_(Xm, Y, Z)] + arr[np.ix_(X, Ym, Z)] + arr[np.ix_(X, Y, Zm)]
+                + arr[np.ix_(Xm, Ym, Z)] + arr[np.ix_(Xm, Y, Zm)] + arr[np.ix_(X, Ym, Zm)]
+                + arr[np.ix_(Xm, Ym, Zm)])
+    if mode not in ("full_rfft", "complex_rfft"):
+        raise ValueError(f"Custom window functions do not support kernel_mode='{mode}'. "
+                         "Use a real or complex RFFT kernel mode.")
+    out = np.zeros((L, L, H), dtype=dt)
+    for x0 in range(0, L, rows):
+        xs = np.arange(x0, min(x0 + rows, L))
+        acc = np.zeros((xs.size, L, H), dtype=dt)
+        for ii in range(bandwidth):
+            xi = (ii * L + xs, ii * L + L - xs)
+            for jj in range(bandwidth):
+                yi = (jj * L + y, jj * L + L - y)
+                for kk in range(bandwidth):
+                    zi = (kk * L + z, kk * L + L - z)
+                    for sx, sy, sz in _SIGNS:
+                        a, b, c = xi[sx < 0], yi[sy < 0], zi[sz < 0]
+                        w = _window_values(func, (sx * a * inv)[:, None, None], (sy * b * inv)[None, :, None],
+                                           (sz * c * inv)[None, None, :], args, acc.shape, dt)
+                        acc += P[a][:, None, None] * P[b][None, :, None] * P[c][None, None, :] * w
+        out[x0:x0 + xs.size] = acc
+    return out
+
+
 _POWER_CACHE = {}
 
 
@@ -147,22 +238,24 @@ class WindowFunc(SFCField):
         self.phi_array = np.asarray(phi_array, dtype=np.float64)
         self.phi_fourier_power = phi_fourier_power
         self.window_params = dict(win_params)
+        # an explicit callable wins over a built-in type (io/window.py:88-96)
         custom = win_params.get("func")
         self.has_custom_func = custom is not None
         if self.has_custom_func:
             if not callable(custom):
                 raise TypeError("Custom window parameter 'func' must be callable.")
-            raise NotImplementedError(
-                "Custom Python window callables cannot run inside the CUDA kernels; use a built-in type.")
-        if win_params.get("type") in COMPLEX_FULL_FFT_WINDOW_TYPES:
+            self.type = win_params.get("type") or "custom"
+            self.func = custom
+        elif win_params.get("type") in COMPLEX_FULL_FFT_WINDOW_TYPES:
             self.type = win_params["type"]
+            self.func = None
         else:
             if "type" not in win_params or win_params["type"] not in WIN_CODES:
                 raise ValueError(f"Unsupported input window function type: {win_params.get('type')}. "
                                  f"Supported types: {', '.join(WIN_CODES)}")
             self.type = win_params["type"]
-        self.func = None
-        km = win_params.get("kernel_mode") or default_kernel_mode(self.type)
+            self.func = None
+        km = win_params.get("kernel_mode") or default_kernel_mode(self.type, self.has_custom_func)
         self.kernel_mode = normalize_kernel_mode(km)
         self.input_params["kernel_mode"] = self.kernel_mode
         self.window_params["kernel_mode"] = self.kernel_mode
@@ -171,14 +264,15 @@ class WindowFunc(SFCField):
         self.window_params["len_args"] = plain_copy(self.len_args)
         self.rescale_len_args = {k: v * self.L / self.box_size for k, v in self.len_args.items()
                                  if v is not None}
-        self.los_args = normalize_los_args(win_params.get("los_args", {}), self.type)
+        self.los_args = normalize_los_args(win_params.get("los_args", {}),
+                                           None if self.has_custom_func else self.type)
         self.other_args = win_params.get("other_args", {}) or {}
         self.input_params["los_args"] = self.los_args
         self.window_params["los_args"] = self.los_args
         self.window_args = dict(self.rescale_len_args)
         self.window_args.update(self.los_args)
         self.window_args.update(plain_copy(self.other_args))
-        if self.type == "thick_shell":
+        if self.type == "thick_shell" and not self.has_custom_func:
             try:
                 r = float(self.rescale_len_args["R"])
                 d = float(self.rescale_len_args["delta_R"])
@@ -196,7 +290,10 @@ class WindowFunc(SFCField):
     # ---- mode resolution (io/window.py:150-195) ---------------------------
     def _los_is_axis_aligned(self):
         has_complete = all(k in self.los_args for k in LOS_ARG_KEYS)
-        if self.type not in ANISOTROPIC_AUTO_WINDOW_TYPES and not has_complete:
+        if self.has_custom_func:
+            if not has_complete:
+                return False
+        elif self.type not in ANISOTROPIC_AUTO_WINDOW_TYPES and not has_complete:
             return True
         los = np.array([float(self.los_args.get("nx", 0.0)), float(self.los_args.get("ny", 0.0)),
                         float(self.los_args.get("nz", 1.0))])
@@ -211,6 +308,13 @@ class WindowFunc(SFCField):
         """The kernel builder the reference would use: octant / full_rfft /
         complex_rfft / complex_full_fft (io/window.py:274-332)."""
         t, m = self.type, self.kernel_mode
+        if self.has_custom_func:
+            if m == "complex_full_fft":
+                raise ValueError("Custom window functions do not support kernel_mode='complex_full_fft'. "
+                                 "Use a real or complex RFFT kernel mode.")
+            if m in ("octant", "full_rfft", "complex_rfft"):
+                return m
+            return "octant" if self._los_is_axis_aligned() else "full_rfft"
         if t in COMPLEX_RFFT_WINDOW_TYPES and m == "octant":
             raise ValueError(f"Window type '{t}' is complex and directional; use kernel_mode='complex_rfft' or 'auto'.")
         if t in COMPLEX_FULL_FFT_WINDOW_TYPES and m not in ("auto", "complex_full_fft"):
@@ -226,7 +330,15 @@ class WindowFunc(SFCField):
         return "octant" if self._los_is_axis_aligned() else "full_rfft"
 
     # ---- device descriptor --------------------------------------------------
+    @property
+    def materialized(self):
+        """True when the kernel is a stored array (composite, loaded or
+        custom-function windows) rather than evaluated on the fly."""
+        return self.is_composite_window or self.has_custom_func
+
     def descriptor(self):
+        if self.has_custom_func:
+            raise ValueError("A custom window function has no built-in descriptor; use its materialised kernel.")
         mode = self.resolved_mode()
         if mode == "complex_full_fft":
             raise ValueError("complex_full_fft windows are handled by the multipole engine.")
@@ -254,11 +366,23 @@ class WindowFunc(SFCField):
     def is_complex(self):
         if self.is_composite_window:
             return self._kernel_dev.is_complex()
+        if self.has_custom_func:
+            return self.resolved_mode() == "complex_rfft"
         return self.resolved_mode() in ("complex_rfft", "complex_full_fft")
 
     def kernel_device(self):
         """Materialised rFFT-grid kernel as a device tensor (float32 or complex64)."""
         if self._kernel_dev is not None:
+            return self._kernel_dev
+        if self.has_custom_func:
+            # io/window.py:274-332 with utils/convolution.py: built on the host
+            # (a Python callable), kept on the device for the convolutions
+            args = ordered_window_args(self.func, self.window_args)
+            pw = self.phi_power().double().cpu().numpy()
+            k = custom_window_kernel(self.func, args, self.L, self.bandwidth, pw, self.resolved_mode())
+            self.w_kernel = k
+            self._kernel_dev = torch.as_tensor(k.astype(np.complex64) if np.iscomplexobj(k)
+                                               else k.astype(np.float32), device=self.device)
             return self._kernel_dev
         L, H = self.L, self.L // 2 + 1
         d = self.descriptor()
@@ -279,7 +403,8 @@ class WindowFunc(SFCField):
     def as_array(self):
         if self.w_kernel is None:
             t = self.kernel_device()
-            self.w_kernel = (t.to(torch.complex128) if t.is_complex() else t.to(torch.float64)).cpu().numpy()
+            if self.w_kernel is None:  # custom windows keep their float64 host kernel
+                self.w_kernel = (t.to(torch.complex128) if t.is_complex() else t.to(torch.float64)).cpu().numpy()
         return self.w_kernel
 
     # ---- persistence (io/window.py:518-548, io/base.py:24-121) ---------------
@@ -319,6 +444,7 @@ class WindowFunc(SFCField):
         new = self.__class__.__new__(self.__class__)
         new.__dict__.update({k: copy.copy(v) for k, v in self.__dict__.items()})
         new.type = "composite"
+        new.has_custom_func, new.func = False, None
         new.kernel_mode = "materialized"
         new.len_args, new.rescale_len_args, new.los_args, new.window_args = {}, {}, {}, {}
         new.other_args = {"operation": copy.deepcopy(operation)}
@@ -396,7 +522,7 @@ def apply_window(eps, window, out=None):
     need = ctypes.c_size_t(0)
     _lib.check(lib.hermes_window_workspace_size(J, ctypes.byref(need)), "window_workspace_size")
     ws = _workspace("spectrum", need.value, dev)
-    if window.is_composite_window:
+    if window.materialized:
         k = window.kernel_device()
         _lib.check(lib.hermes_fft_r2c(_ptr(eps), _ptr(ws), J, sptr), "hermes_fft_r2c")
         kr = k if not k.is_complex() else None
@@ -421,7 +547,7 @@ def convolve_field(field, window):
         raise ValueError("Convolution expects a 3D field.")
     if eps.shape[0] != window.L:
         raise ValueError(f"Convolution requires same shape; field L={eps.shape[0]}, window L={window.L}.")
-    mode = "materialized" if window.is_composite_window else window.resolved_mode()
+    mode = "materialized" if window.materialized else window.resolved_mode()
     if mode == "complex_full_fft":
         from .multipole import convolve_complex_full
 

@@ -716,6 +716,42 @@ def gen_composite_windows():
     _save("composite_windows_J4", **out)
 
 
+def gen_custom_windows():
+    """WindowFunc with a user callable (io/window.py:88-96, :274-332;
+    utils/convolution.py): kernels in full_rfft (default), octant,
+    complex_rfft and bandwidth 2, a scalar-only function, a callable named
+    with a built-in type, and a field convolved with one of them."""
+    from custom_window_funcs import aniso_gauss, odd_los, skewed_gauss, stepped_tophat
+    from pyhermes.io.window import WindowFunc
+
+    sfc = _sfc_params(4)
+    cases = {
+        "gauss_full": ({"func": aniso_gauss, "len_args": {"R": 60.0}}, 1),
+        "gauss_octant": ({"func": aniso_gauss, "len_args": {"R": 60.0}, "other_args": {"q": 0.7},
+                          "kernel_mode": "octant"}, 1),
+        "gauss_bw2": ({"func": aniso_gauss, "len_args": {"R": 40.0}}, 2),
+        "skew_full": ({"func": skewed_gauss, "len_args": {"R": 50.0}}, 1),
+        "skew_octant": ({"func": skewed_gauss, "len_args": {"R": 50.0}, "kernel_mode": "octant"}, 1),
+        "skew_auto_axis": ({"func": skewed_gauss, "len_args": {"R": 50.0}, "kernel_mode": "auto",
+                            "los_args": [0.0, 0.0, 1.0]}, 1),
+        "step_full": ({"func": stepped_tophat, "len_args": {"R": 80.0}}, 1),
+        "odd_complex": ({"func": odd_los, "len_args": {"R": 50.0}, "los_args": {"nx": 0.0, "ny": 1.0, "nz": 1.0},
+                         "kernel_mode": "complex_rfft"}, 1),
+        "named_gaussian": ({"type": "gaussian", "func": aniso_gauss, "len_args": {"R": 60.0}}, 1),
+    }
+    out = {}
+    for name, (wp, bw) in cases.items():
+        w = WindowFunc(dict(wp), sfc, bandwidth=bw)
+        out[name] = np.asarray(w.as_array())
+        out[name + "_meta"] = np.array([w.type, w.kernel_mode])
+    rng = np.random.default_rng(21)
+    pos = rng.uniform(0.0, 1000.0, (3000, 3))
+    f = _projection(pos, 4, weights=rng.lognormal(0.0, 0.3, 3000))
+    out["epsilon"] = f.epsilon
+    out["conv_skew"] = (f @ WindowFunc(dict(cases["skew_full"][0]), f.sfc_info)).epsilon
+    _save("custom_windows_J4", **out)
+
+
 def gen_mc_theta():
     """Corr_3PCF with angle_param='theta' (a min/max/n spec and a list)."""
     from pyhermes.theory.corr3pcf import Corr_3PCF
@@ -803,7 +839,7 @@ def gen_window_file():
     _save("window_file_J4", kernel=kernel)
 
 
-SECTIONS = {"mc_theta": gen_mc_theta, "composite_windows": gen_composite_windows, "particle_data": gen_particle_data, "catalogues": gen_catalogues, "field_algebra": gen_field_algebra, "rppi": gen_rppi, "io": gen_io, "cross": gen_cross, "normalization": gen_normalization, "mc3pcf_randoms": gen_mc3pcf_randoms, "random_catalogue": gen_random_catalogue, "mc3pcf_particle": gen_mc3pcf_particle, "window_file": gen_window_file, "tabulated": gen_tabulated, "counting": gen_counting, "mc3pcf": gen_mc3pcf, "phi": gen_phi, "deposit": gen_deposit, "windows": gen_windows,
+SECTIONS = {"custom_windows": gen_custom_windows, "mc_theta": gen_mc_theta, "composite_windows": gen_composite_windows, "particle_data": gen_particle_data, "catalogues": gen_catalogues, "field_algebra": gen_field_algebra, "rppi": gen_rppi, "io": gen_io, "cross": gen_cross, "normalization": gen_normalization, "mc3pcf_randoms": gen_mc3pcf_randoms, "random_catalogue": gen_random_catalogue, "mc3pcf_particle": gen_mc3pcf_particle, "window_file": gen_window_file, "tabulated": gen_tabulated, "counting": gen_counting, "mc3pcf": gen_mc3pcf, "phi": gen_phi, "deposit": gen_deposit, "windows": gen_windows,
             "convolution": gen_convolution, "corr2pcf": gen_corr2pcf, "multipole": gen_multipole}
 
 
