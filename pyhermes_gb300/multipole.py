@@ -125,10 +125,18 @@ def multipole_fields_bins(half_spec, J, l, m, bins, box_size, phi_power, out=Non
     nb = len(bins)
     L = 1 << J
     g2p = L / float(box_size)
-    modes = {rp.profile_mode(b.type, b.len_args, l) for b in bins}
-    if len(modes) != 1:
-        raise NotImplementedError("All bins of one multipole call must use the same radial profile path.")
-    mode = modes.pop()
+    per_bin = [rp.profile_mode(b.type, b.len_args, l) for b in bins]
+    if len(set(per_bin)) > 1:
+        # bins on different profile paths: one call per path, its columns
+        # gathered into the shared [cell][BIN_STRIDE] layout
+        if out is None:
+            out = torch.zeros((L ** 3, BIN_STRIDE), dtype=torch.complex64, device=half_spec.device)
+        for path in dict.fromkeys(per_bin):
+            idx = [i for i, p in enumerate(per_bin) if p == path]
+            part = multipole_fields_bins(half_spec, J, l, m, [bins[i] for i in idx], box_size, phi_power, ws=ws)
+            out[:, idx] = part.view(L ** 3, 1) if part.dim() == 1 else part[:, :len(idx)]
+        return out
+    mode = per_bin[0]
     if mode == "shell":
         radii = [(b.len_args["R_shell"] if b.type == "gaussian_shell" else b.len_args["R"]) * g2p for b in bins]
         return multipole_fields(half_spec, J, l, m, radii, phi_power, out=out, ws=ws)
@@ -694,18 +702,34 @@ class Corr_3PCF_Multipole:
                 if r == "uniform":
                     base = self.data.get(i) or ref
                     rho_i = base.field_mean_density(value_unit="grid") if i in self.data else self.rho
-                    w = getattr(self, f"window{i}")
-                    if w:
-                        win = WindowFunc(w, base.sfc_info, device=self.device)
-                        k0 = float(np.asarray(win.as_array())[0, 0, 0].real)
-                        if not np.isclose(k0, 1.0, rtol=1e-10, atol=1e-12):
-                            raise NotImplementedError("uniform randoms with a window whose W(0) != 1")
-                    self.rand[i] = float(rho_i)
+                    self.rand[i] = self._uniform_random_after_window(base, rho_i, getattr(self, f"window{i}"), i)
                 else:
                     base = self._normalized(self._resolve(r, f"random vertex {i}"))
                     w = getattr(self, f"window{i}")
                     self.rand[i] = base @ WindowFunc(w, base.sfc_info, device=self.device) if w else base.copy()
         self._fields_prepared = True
+
+    def _uniform_random_after_window(self, base, rho, w, vertex):
+        """A uniform random vertex after the vertex's window
+        (theory/corr3pcf_multipole.py:587-619): the density itself when
+        there is no window or W(0) = 1, else a uniform field of that density
+        convolved with the window."""
+        if not w:
+            return float(rho)
+        win = WindowFunc(w, base.sfc_info, device=self.device)
+        z = complex(np.asarray(win.as_array())[0, 0, 0])
+        if abs(z.imag) <= 1e-12 * max(1.0, abs(z.real)) and np.isclose(z.real, 1.0, rtol=1e-10, atol=1e-12):
+            return float(rho)
+        field = base._spawn_like()
+        field.epsilon = torch.full((base.L,) * 3, float(rho), dtype=torch.float32, device=self.device)
+        field.sfc_info.update({
+            "catalog_weight_sum": None, "catalog_weight_sq_sum": None, "raw_field_weighted_sum": None,
+            "field_integral": float(rho) * float(base.V), "weight_normalization": None, "particle_count": None,
+            "particle_data_retrievable": False, "particle_data_path": "", "particle_data_format": "",
+            "field_kind": "derived_field", "uniform_random_materialized": True, "uniform_random_vertex": int(vertex),
+        })
+        field.format_sfc_params()
+        return field @ win
 
     def _eps(self, product, i):
         if product == "ddd_l":

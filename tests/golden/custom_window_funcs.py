@@ -32,3 +32,9 @@ def odd_los(kx, ky, kz, R, nx, ny, nz):
     """i (n . k) 2 pi R times a Gaussian: an odd, complex directional window."""
     proj = (nx * kx + ny * ky + nz * kz) / math.sqrt(nx * nx + ny * ny + nz * nz)
     return 1j * 2.0 * np.pi * R * proj * np.exp(-0.5 * (2.0 * np.pi * R) ** 2 * (kx * kx + ky * ky + kz * kz))
+
+
+def doubled_gauss(kx, ky, kz, R):
+    """Twice a Gaussian: W(0) = 2, so a uniform random vertex behind it is a
+    uniform field convolved with the window, not the bare density."""
+    return 2.0 * np.exp(-0.5 * (2.0 * np.pi * R) ** 2 * (kx * kx + ky * ky + kz * kz))

@@ -746,9 +746,24 @@ def gen_custom_windows():
         out[name + "_meta"] = np.array([w.type, w.kernel_mode])
     rng = np.random.default_rng(21)
     pos = rng.uniform(0.0, 1000.0, (3000, 3))
-    f = _projection(pos, 4, weights=rng.lognormal(0.0, 0.3, 3000))
-    out["epsilon"] = f.epsilon
+    wts = rng.lognormal(0.0, 0.3, 3000)
+    f = _projection(pos, 4, weights=wts)
+    out.update({"pos": pos, "weights": wts, "epsilon": f.epsilon})
     out["conv_skew"] = (f @ WindowFunc(dict(cases["skew_full"][0]), f.sfc_info)).epsilon
+    # a uniform random behind windows with W(0) = 2 (theory/corr3pcf_multipole.py:607-619)
+    from custom_window_funcs import doubled_gauss
+    from pyhermes.theory.corr3pcf_multipole import Corr_3PCF_Multipole
+
+    win = {"func": doubled_gauss, "len_args": {"R": 40.0}}
+    d = Corr_3PCF_Multipole({"Corr_3PCF_Multipole": {
+        "sfc_field": f, "random": "uniform", "window1": dict(win), "window2": dict(win), "window3": dict(win),
+        "binning_window12": {"type": "shell", "len_args": {}, "other_args": {}, "mapping": {"R": "r12"}},
+        "binning_window13": {"type": "shell", "len_args": {}, "other_args": {}, "mapping": {"R": "r13"}},
+        "sampling": {"mode": "paired", "r12": [150.0, 200.0], "r13": [250.0, 300.0]},
+        "l_min": 0, "l_max": 2, "summation_backend": "cpu",
+        "products": ["ddd_l", "delta_ddd_l", "rrr_l", "zeta_l"]}}).run(save_result=False)
+    for k in ("ddd_l", "delta_ddd_l", "rrr_l", "zeta_l"):
+        out["mp_" + k] = np.asarray(getattr(d, k))
     _save("custom_windows_J4", **out)
 
 

@@ -118,3 +118,26 @@ def test_custom_window_convolution_matches_reference(golden_dir):
     ref = d["conv_skew"]
     assert np.abs(out - ref).max() <= 1e-5 * np.abs(ref).max()
     assert np.linalg.norm(out - ref) <= 2e-6 * np.linalg.norm(ref)
+
+
+@pytest.mark.gpu
+def test_uniform_random_behind_window_with_nonunit_zero_mode(golden_dir):
+    """random = 'uniform' behind vertex windows with W(0) = 2: the random
+    vertex is the uniform field convolved with the window
+    (theory/corr3pcf_multipole.py:607-619), so rrr_l = (2 rho)^3 at l = 0."""
+    from pyhermes_gb300.multipole import Corr_3PCF_Multipole
+    from pyhermes_gb300.projection import SFCProjection
+
+    g = np.load(os.path.join(golden_dir, "custom_windows_J4.npz"))
+    f = SFCProjection({"SFCProjection": {"particle_pos": g["pos"], "catalog_weight": g["weights"], "J": 4,
+                                         "box_size": 1000.0}}).run(save_result=False)
+    win = {"func": cwf.doubled_gauss, "len_args": {"R": 40.0}}
+    d = Corr_3PCF_Multipole({"Corr_3PCF_Multipole": {
+        "sfc_field": f, "random": "uniform", "window1": dict(win), "window2": dict(win), "window3": dict(win),
+        "binning_window12": {"type": "shell", "len_args": {}, "other_args": {}, "mapping": {"R": "r12"}},
+        "binning_window13": {"type": "shell", "len_args": {}, "other_args": {}, "mapping": {"R": "r13"}},
+        "sampling": {"mode": "paired", "r12": [150.0, 200.0], "r13": [250.0, 300.0]},
+        "l_min": 0, "l_max": 2, "products": ["ddd_l", "delta_ddd_l", "rrr_l", "zeta_l"]}}).run(save_result=False)
+    for k in ("ddd_l", "delta_ddd_l", "rrr_l", "zeta_l"):
+        got, ref = np.asarray(getattr(d, k)), g["mp_" + k]
+        assert np.abs(got - ref).max() <= 1e-4 * np.abs(ref).max(), k

@@ -173,6 +173,31 @@ def test_multi_bin_fields_match_single_bin(J, l, m):
         assert err <= 5e-6 * max(scale, 1e-30), (J, l, m, b, err, scale)
 
 
+def test_mixed_profile_bins_match_single_bins():
+    """Bins on different radial profile paths in one call (thin shells, an
+    analytic sphere, a tabulated thick shell at l > 0) equal one call per
+    bin, and the engine's DDD with shells on r12 and spheres on r13 over a
+    shared field equals its per-sample reference form."""
+    J, L = 5, 32
+    eps = _field(J)
+    et = torch.as_tensor(eps, dtype=torch.float32, device="cuda")
+    spec = rfft_field(et)
+    P = phi_power_device(PHI, L, 1, 1024, "cuda")
+    bins = [mp.BinSpec("shell", {"R": 150.0}), mp.BinSpec("sphere", {"R": 200.0}),
+            mp.BinSpec("thick_shell", {"R": 180.0, "delta_R": 60.0}), 240.0]
+    for l, m in ((0, 0), (2, 1)):
+        f = mp.multipole_fields_bins(spec, J, l, m, bins, 1000.0, P)
+        assert f.shape == (L ** 3, 16) and torch.count_nonzero(f[:, len(bins):]) == 0
+        for b, spec_b in enumerate(bins):
+            one = mp.multipole_fields_bins(spec, J, l, m, [spec_b], 1000.0, P)
+            assert (f[:, b] - one).abs().max().item() <= 1e-6 * max(one.abs().max().item(), 1e-30), (l, m, b)
+    eng = mp.MultipoleEngine(et, et, et, PHI, J, 1000.0)
+    pairs = [(150.0, mp.BinSpec("sphere", {"R": 200.0})), (240.0, mp.BinSpec("sphere", {"R": 120.0}))]
+    got = eng.ddd(pairs, 0, 2)
+    ref = eng.ddd_plain(pairs, 0, 2)
+    assert _rel(got, ref) < 1e-4
+
+
 def test_corr3pcf_multipole_random_field_matches_reference(golden_dir):
     """random = a projected random catalogue: delta = D - R, rrr_l from the
     random field's own multipoles, zeta_l from the mixing solve."""
