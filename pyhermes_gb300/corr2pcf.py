@@ -29,8 +29,8 @@ from .params import plain_copy, task_params
 from .sfc_field import (SFCField, describe_input, normalize_task_weight_normalization, read_numpy_pickle,
                         write_numpy_pickle)
 from .window import (
-    ANISOTROPIC_AUTO_WINDOW_TYPES, LOS_AWARE_WINDOW_TYPES, WindowFunc, normalize_los_args, pair_products,
-    rfft_field,
+    ANISOTROPIC_AUTO_WINDOW_TYPES, LOS_AWARE_WINDOW_TYPES, WindowFunc, materialized_pair_products, normalize_los_args,
+    pair_products, rfft_field,
 )
 
 logger = logging.getLogger("pyhermes_gb300.Corr_2PCF")
@@ -415,7 +415,7 @@ class Corr_2PCF:
                 return self.rand[side]
             return ("delta", side)
 
-        field_keys, spectra, dcs = {}, [], {}
+        field_keys, spectra, reals, dcs = {}, [], [], {}
         pairs, pair_products_of = [], {}
         scalar_results = {}
         for prod in computed:
@@ -443,6 +443,7 @@ class Corr_2PCF:
                 if spec_key not in field_keys:
                     field_keys[spec_key] = len(spectra)
                     spectra.append(rfft_field(fld_t.contiguous()))
+                    reals.append(fld_t.contiguous())
                     dcs[spec_key] = float(fld_t.double().sum().item())
                 keys.append(field_keys[spec_key])
             pair_products_of[prod] = len(pairs)
@@ -451,10 +452,20 @@ class Corr_2PCF:
             windows = self._binning_windows(ref)
             # split into groups of <= 4 pairs per pass
             vals = np.zeros((len(windows), len(pairs)))
-            k0 = None
+            k0 = np.zeros(len(windows))
+            # built-in bins evaluate their kernels on the fly; bins with a
+            # stored kernel (custom callables) go through the convolution
+            on_fly = [b for b, w in enumerate(windows) if not w.materialized]
+            stored = [b for b, w in enumerate(windows) if w.materialized]
             for s in range(0, len(pairs), 4):
-                v, k0 = pair_products(spectra, pairs[s:s + 4], windows, exclude_k0=True)
-                vals[:, s:s + 4] = v
+                if on_fly:
+                    v, kb = pair_products(spectra, pairs[s:s + 4], [windows[b] for b in on_fly], exclude_k0=True)
+                    vals[on_fly, s:s + 4] = v
+                    k0[on_fly] = kb
+            if stored:
+                v, kb = materialized_pair_products(reals, pairs, [windows[b] for b in stored], exclude_k0=True)
+                vals[stored, :] = v
+                k0[stored] = kb
             L = windows[0].L
             N2 = float(L) ** 6
             for prod, col in pair_products_of.items():

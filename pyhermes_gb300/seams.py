@@ -179,14 +179,14 @@ def _gb300_window(obj, field):
     if isinstance(obj, WindowFunc):
         return obj
     params = getattr(obj, "window_params", None) or getattr(obj, "input_params", None)
-    if not params or params.get("func") is not None or getattr(obj, "is_composite_window", False):
+    if not params or getattr(obj, "is_composite_window", False):
         return None
     J, box, phi, res = _field_meta(field)
     if getattr(obj, "phi_array", None) is not None:
         phi = np.asarray(obj.phi_array, dtype=np.float64)
     sfc = {"J": J, "box_size": box, "phi_resolution": res, "phi_array": phi,
            "wavelet_mode": getattr(obj, "wavelet_mode", "db2"), "wavelet_level": getattr(obj, "wavelet_level", 10)}
-    keep = ("type", "len_args", "los_args", "other_args", "kernel_mode")
+    keep = ("type", "func", "len_args", "los_args", "other_args", "kernel_mode")
     try:
         return WindowFunc({k: params[k] for k in keep if k in params}, sfc,
                           bandwidth=int(getattr(obj, "bandwidth", 1)))
@@ -199,7 +199,7 @@ def pair_product_with_window(field1, field2, binning_window_obj, threads):
     sum_k eps1_hat K conj(eps2_hat) / L^6 (Parseval), with the k = 0 term in
     float64.  Scalar vertices give the product of mean densities."""
     from .corr2pcf import _is_scalar, field_mean_density
-    from .window import pair_products, rfft_field
+    from .window import materialized_pair_products, pair_products, rfft_field
 
     if field2 is None:
         field2 = field1
@@ -209,7 +209,10 @@ def pair_product_with_window(field1, field2, binning_window_obj, threads):
     e1 = _field_eps(field1)
     e2 = e1 if field2 is field1 else _field_eps(field2)
     L = e1.shape[0]
-    if win is None or win.materialized or win.is_complex or win.resolved_mode() == "complex_full_fft":
+    if win is not None and win.materialized:
+        v, _ = materialized_pair_products([e1, e2], [(0, 1)], [win], exclude_k0=False)
+        return float(v[0, 0])
+    if win is None or win.is_complex or win.resolved_mode() == "complex_full_fft":
         # any other window: its materialised rFFT-grid kernel
         conv = specialized_convolution_3d(e1, binning_window_obj.as_array(), threads)
         return float(np.einsum("ijk,ijk->", conv, e2.double().cpu().numpy(), optimize=True) / conv.size)

@@ -572,6 +572,34 @@ def rfft_field(eps):
     return spec
 
 
+def materialized_pair_products(fields, pairs, windows, exclude_k0=True):
+    """pair_products for windows with a stored kernel (custom callables,
+    composites): mean over cells of (f_i convolved with K) * f_j, the
+    reference's own form of the product (theory/corr2pcf.py:366-382), with
+    the convolution on hermes_fft_r2c / hermes_spectrum_multiply /
+    hermes_fft_c2r and the cell sum in float64.  fields: float32 [L,L,L]
+    device tensors.  Same return as pair_products."""
+    n_bins, n_pairs = len(windows), len(pairs)
+    out = np.zeros((n_bins, n_pairs), dtype=np.float64)
+    k0 = np.zeros(n_bins, dtype=np.float64)
+    dcs = [float(f.double().sum().item()) for f in fields]
+    # mean-free copies carry every k != 0 mode: the k = 0 term is added in
+    # float64 below instead of surviving a float32 cancellation
+    cen = [(f.double() - dc / f.numel()).to(torch.float32).contiguous() for f, dc in zip(fields, dcs)]
+    for b, w in enumerate(windows):
+        if not w.materialized:
+            raise ValueError("materialized_pair_products takes windows with a stored kernel.")
+        L3 = float(w.L) ** 3
+        k0[b] = float(w.kernel_device()[0, 0, 0].real.item())
+        convs = {}
+        for c, (i, j) in enumerate(pairs):
+            if i not in convs:
+                convs[i] = apply_window(cen[i], w)
+            v = float((convs[i].double() * cen[j].double()).sum().item()) / L3
+            out[b, c] = v + (0.0 if exclude_k0 else k0[b] * dcs[i] * dcs[j] / L3 ** 2)
+    return out, k0
+
+
 def pair_products(spectra, pairs, windows, exclude_k0=True):
     """sum_k F_i K_b conj(F_j) / L^6 for every window b and pair (i, j).
 

@@ -38,3 +38,8 @@ def doubled_gauss(kx, ky, kz, R):
     """Twice a Gaussian: W(0) = 2, so a uniform random vertex behind it is a
     uniform field convolved with the window, not the bare density."""
     return 2.0 * np.exp(-0.5 * (2.0 * np.pi * R) ** 2 * (kx * kx + ky * ky + kz * kz))
+
+
+def j0_shell(kx, ky, kz, R):
+    """Thin spherical shell of radius R: j0(2 pi R |k|)."""
+    return np.sinc(2.0 * R * np.sqrt(kx * kx + ky * ky + kz * kz))

@@ -764,6 +764,17 @@ def gen_custom_windows():
         "products": ["ddd_l", "delta_ddd_l", "rrr_l", "zeta_l"]}}).run(save_result=False)
     for k in ("ddd_l", "delta_ddd_l", "rrr_l", "zeta_l"):
         out["mp_" + k] = np.asarray(getattr(d, k))
+    # Corr_2PCF with a user-callable binning window (theory/corr2pcf.py:366-382)
+    from custom_window_funcs import j0_shell
+    from pyhermes.theory.corr2pcf import Corr_2PCF
+
+    d = Corr_2PCF({"Corr_2PCF": {
+        "sfc_field": f, "random": "uniform",
+        "binning_window": {"func": j0_shell, "len_args": {"R": None}, "mapping": "s_to_R"},
+        "sampling": {"s": {"min": 100.0, "max": 300.0, "n": 3}},
+        "products": ["dd", "delta_dd", "xi"]}}).run(save_result=False)
+    for k in ("dd", "delta_dd", "rr", "xi"):
+        out["c2_" + k] = np.asarray(getattr(d, k))
     _save("custom_windows_J4", **out)
 
 

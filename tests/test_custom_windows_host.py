@@ -2,8 +2,10 @@
 utils/convolution.py:14-283) against the reference (golden
 custom_windows_J4.npz): the host-built kernel in full_rfft (the default),
 octant, complex_rfft, auto and bandwidth 2, a function that only works on
-scalars, a callable named with a built-in type; and, on the GPU, a field
-convolved with a custom window.
+scalars, a callable named with a built-in type; Corr_2PCF with a callable
+binning window and a multipole task whose uniform random sits behind
+windows with W(0) = 2 (on the host with the oracle's convolution, and on
+the GPU); and, on the GPU, a field convolved with a custom window.
 
 Tolerances: kernels are float64 on both sides, |dK| <= 1e-12 max|K|; the GPU
 convolution is float32, |d| <= 1e-5 max|ref| and relative L2 <= 2e-6.
@@ -15,7 +17,9 @@ import numpy as np
 import pytest
 import torch
 
+import oracle
 from pyhermes_gb300.window import WindowFunc, custom_window_kernel, ordered_window_args
+from test_tasks_host import oracle_kernels  # noqa: F401  (fixture)
 
 _spec = importlib.util.spec_from_file_location(
     "custom_window_funcs", os.path.join(os.path.dirname(__file__), "golden", "custom_window_funcs.py"))
@@ -125,19 +129,76 @@ def test_uniform_random_behind_window_with_nonunit_zero_mode(golden_dir):
     """random = 'uniform' behind vertex windows with W(0) = 2: the random
     vertex is the uniform field convolved with the window
     (theory/corr3pcf_multipole.py:607-619), so rrr_l = (2 rho)^3 at l = 0."""
-    from pyhermes_gb300.multipole import Corr_3PCF_Multipole
+    g = np.load(os.path.join(golden_dir, "custom_windows_J4.npz"))
+    d = _multipole_uniform_behind_w2(g, "cuda")
+    for k in ("ddd_l", "delta_ddd_l", "rrr_l", "zeta_l"):
+        assert _rel(getattr(d, k), g["mp_" + k]) < 1e-4, k
+
+@pytest.fixture
+def numpy_convolution(monkeypatch):
+    """field @ window on the host: the oracle's rFFT convolution with the
+    window's own float64 kernel."""
+    from pyhermes_gb300 import window as win_mod
+
+    def apply_window(eps, w, out=None):
+        K = np.asarray(w.as_array())
+        return torch.as_tensor(oracle.convolve(eps.double().cpu().numpy(), K), dtype=torch.float32)
+
+    monkeypatch.setattr(win_mod, "apply_window", apply_window)
+
+
+def _rel(a, b):
+    return np.abs(np.asarray(a) - b).max() / np.abs(b).max()
+
+
+def _projected(g, device):
     from pyhermes_gb300.projection import SFCProjection
 
-    g = np.load(os.path.join(golden_dir, "custom_windows_J4.npz"))
-    f = SFCProjection({"SFCProjection": {"particle_pos": g["pos"], "catalog_weight": g["weights"], "J": 4,
-                                         "box_size": 1000.0}}).run(save_result=False)
+    return SFCProjection({"SFCProjection": {"particle_pos": g["pos"], "catalog_weight": g["weights"], "J": 4,
+                                            "box_size": 1000.0}}, device=device).run(save_result=False)
+
+
+def _corr2pcf_custom_bins(g, device):
+    from pyhermes_gb300.corr2pcf import Corr_2PCF
+
+    return Corr_2PCF({"Corr_2PCF": {
+        "sfc_field": _projected(g, device), "random": "uniform",
+        "binning_window": {"func": cwf.j0_shell, "len_args": {"R": None}, "mapping": "s_to_R"},
+        "sampling": {"s": {"min": 100.0, "max": 300.0, "n": 3}},
+        "products": ["dd", "delta_dd", "xi"]}}, device=device).run(save_result=False)
+
+
+def _multipole_uniform_behind_w2(g, device):
+    from pyhermes_gb300.multipole import Corr_3PCF_Multipole
+
     win = {"func": cwf.doubled_gauss, "len_args": {"R": 40.0}}
-    d = Corr_3PCF_Multipole({"Corr_3PCF_Multipole": {
-        "sfc_field": f, "random": "uniform", "window1": dict(win), "window2": dict(win), "window3": dict(win),
+    return Corr_3PCF_Multipole({"Corr_3PCF_Multipole": {
+        "sfc_field": _projected(g, device), "random": "uniform",
+        "window1": dict(win), "window2": dict(win), "window3": dict(win),
         "binning_window12": {"type": "shell", "len_args": {}, "other_args": {}, "mapping": {"R": "r12"}},
         "binning_window13": {"type": "shell", "len_args": {}, "other_args": {}, "mapping": {"R": "r13"}},
         "sampling": {"mode": "paired", "r12": [150.0, 200.0], "r13": [250.0, 300.0]},
-        "l_min": 0, "l_max": 2, "products": ["ddd_l", "delta_ddd_l", "rrr_l", "zeta_l"]}}).run(save_result=False)
+        "l_min": 0, "l_max": 2, "products": ["ddd_l", "delta_ddd_l", "rrr_l", "zeta_l"]}},
+        device=device).run(save_result=False)
+
+
+def test_corr2pcf_custom_binning_window_on_host(golden_dir, oracle_kernels, numpy_convolution):
+    g = np.load(os.path.join(golden_dir, "custom_windows_J4.npz"))
+    d = _corr2pcf_custom_bins(g, "cpu")
+    for k in ("dd", "delta_dd", "rr", "xi"):
+        assert _rel(getattr(d, k), g["c2_" + k]) < 1e-5, (k, getattr(d, k), g["c2_" + k])
+
+
+def test_uniform_random_behind_nonunit_window_on_host(golden_dir, oracle_kernels, numpy_convolution):
+    g = np.load(os.path.join(golden_dir, "custom_windows_J4.npz"))
+    d = _multipole_uniform_behind_w2(g, "cpu")
     for k in ("ddd_l", "delta_ddd_l", "rrr_l", "zeta_l"):
-        got, ref = np.asarray(getattr(d, k)), g["mp_" + k]
-        assert np.abs(got - ref).max() <= 1e-4 * np.abs(ref).max(), k
+        assert _rel(getattr(d, k), g["mp_" + k]) < 1e-5, (k, getattr(d, k), g["mp_" + k])
+
+
+@pytest.mark.gpu
+def test_corr2pcf_custom_binning_window_gpu(golden_dir):
+    g = np.load(os.path.join(golden_dir, "custom_windows_J4.npz"))
+    d = _corr2pcf_custom_bins(g, "cuda")
+    for k in ("dd", "delta_dd", "rr", "xi"):
+        assert _rel(getattr(d, k), g["c2_" + k]) < 1e-4, k
