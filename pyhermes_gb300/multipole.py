@@ -175,6 +175,48 @@ def multipole_fields_bins(half_spec, J, l, m, bins, box_size, phi_power, out=Non
     return out  # dt is released in stream order after the table kernel
 
 
+def complex_full_window_bin(window):
+    """(l, m, bin) of a complex full-FFT WindowFunc (io/window.py:198-264):
+    legendre_multipole is the thin shell j_l(2 pi k R) Y_lm
+    (utils/legendre_windows.py:41-119), radial_multipole any radial profile
+    (utils/radial_multipole_windows.py:267-316); both bandwidth 1."""
+    if window.bandwidth != 1:
+        raise ValueError(f"{window.type} currently supports only bandwidth=1.")
+    oa = window.other_args or {}
+    try:
+        l, m = int(oa["l"]), int(oa["m"])
+        if window.type == "radial_multipole":
+            return l, m, BinSpec(str(oa["radial_type"]), window.len_args, oa.get("profile_config") or None)
+    except KeyError as exc:
+        raise ValueError(f"{window.type} missing required other_args key: {exc}") from None
+    if window.type != "legendre_multipole":
+        raise ValueError(f"Unsupported complex full-FFT window type: {window.type}")
+    if window.len_args.get("R") is None:
+        raise ValueError("legendre_multipole requires len_args={'R': ...}.")
+    return l, m, BinSpec("shell", {"R": float(window.len_args["R"])})
+
+
+def convolve_complex_full(field, window):
+    """SFCField @ a complex full-FFT window: ifftn(fftn(eps) K_lm) as a
+    complex64 [L, L, L] device tensor (utils/convolution.py:291-295), from
+    the multipole field kernels."""
+    l, m, b = complex_full_window_bin(window)
+    spec = rfft_field(field.epsilon_device.to(torch.float32).contiguous())
+    a = multipole_fields_bins(spec, window.J, l, m, [b], window.box_size, window.phi_power())
+    return a.view(window.L, window.L, window.L)
+
+
+def complex_full_kernel(window):
+    """K_lm of a complex full-FFT window as complex64 [L, L, L]: the field
+    kernels applied to the half spectrum of a unit impulse (all ones) give
+    ifftn(K), and one forward FFT returns K."""
+    l, m, b = complex_full_window_bin(window)
+    L = window.L
+    ones = torch.ones((L, L, L // 2 + 1), dtype=torch.complex64, device=window.device)
+    a = multipole_fields_bins(ones, window.J, l, m, [b], window.box_size, window.phi_power())
+    return torch.fft.fftn(a.view(L, L, L).to(torch.complex128)).to(torch.complex64)
+
+
 def multipole_contract(eps1, fields2, nb2, gamma, J, fields3=None, nb3=None, conj_sign=1):
     """S[b2, b3] complex128 (see include/hermes_gb300.h)."""
     nb3 = nb2 if fields3 is None else nb3

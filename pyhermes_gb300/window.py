@@ -384,6 +384,11 @@ class WindowFunc(SFCField):
             self._kernel_dev = torch.as_tensor(k.astype(np.complex64) if np.iscomplexobj(k)
                                                else k.astype(np.float32), device=self.device)
             return self._kernel_dev
+        if self.resolved_mode() == "complex_full_fft":
+            from .multipole import complex_full_kernel
+
+            self._kernel_dev = complex_full_kernel(self)
+            return self._kernel_dev
         L, H = self.L, self.L // 2 + 1
         d = self.descriptor()
         pw = self.phi_power()

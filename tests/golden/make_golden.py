@@ -778,6 +778,36 @@ def gen_custom_windows():
     _save("custom_windows_J4", **out)
 
 
+def gen_full_fft_windows():
+    """Complex full-FFT windows (io/window.py:198-264): legendre_multipole
+    (utils/legendre_windows.py) and radial_multipole
+    (utils/radial_multipole_windows.py:267-316) kernels, and a field
+    convolved with them (utils/convolution.py:291-295)."""
+    from pyhermes.io.window import WindowFunc
+
+    cases = {
+        "legendre_l2_m1": {"type": "legendre_multipole", "len_args": {"R": 150.0}, "other_args": {"l": 2, "m": 1}},
+        "legendre_l3_mneg2": {"type": "legendre_multipole", "len_args": {"R": 120.0},
+                              "other_args": {"l": 3, "m": -2, "use_fast": False}},
+        "radial_thick_l2_mneg1": {"type": "radial_multipole", "len_args": {"R": 160.0, "delta_R": 60.0},
+                                  "other_args": {"radial_type": "thick_shell", "l": 2, "m": -1}},
+        "radial_sphere_l0": {"type": "radial_multipole", "len_args": {"R": 140.0},
+                             "other_args": {"radial_type": "sphere", "l": 0, "m": 0}},
+        "radial_shell_l1_m1": {"type": "radial_multipole", "len_args": {"R": 180.0},
+                               "other_args": {"radial_type": "shell", "l": 1, "m": 1}},
+    }
+    rng = np.random.default_rng(33)
+    pos = rng.uniform(0.0, 1000.0, (2500, 3))
+    pos[:900] = pos[:900] * 0.3 + 300.0
+    f = _projection(pos, 4)
+    out = {"pos": pos, "epsilon": f.epsilon}
+    for name, wp in cases.items():
+        w = WindowFunc(dict(wp), f.sfc_info)
+        out[name + "_kernel"] = np.asarray(w.as_array())
+        out[name + "_conv"] = np.asarray((f @ w).epsilon)
+    _save("full_fft_windows_J4", **out)
+
+
 def gen_mc_theta():
     """Corr_3PCF with angle_param='theta' (a min/max/n spec and a list)."""
     from pyhermes.theory.corr3pcf import Corr_3PCF
@@ -865,7 +895,7 @@ def gen_window_file():
     _save("window_file_J4", kernel=kernel)
 
 
-SECTIONS = {"custom_windows": gen_custom_windows, "mc_theta": gen_mc_theta, "composite_windows": gen_composite_windows, "particle_data": gen_particle_data, "catalogues": gen_catalogues, "field_algebra": gen_field_algebra, "rppi": gen_rppi, "io": gen_io, "cross": gen_cross, "normalization": gen_normalization, "mc3pcf_randoms": gen_mc3pcf_randoms, "random_catalogue": gen_random_catalogue, "mc3pcf_particle": gen_mc3pcf_particle, "window_file": gen_window_file, "tabulated": gen_tabulated, "counting": gen_counting, "mc3pcf": gen_mc3pcf, "phi": gen_phi, "deposit": gen_deposit, "windows": gen_windows,
+SECTIONS = {"full_fft_windows": gen_full_fft_windows, "custom_windows": gen_custom_windows, "mc_theta": gen_mc_theta, "composite_windows": gen_composite_windows, "particle_data": gen_particle_data, "catalogues": gen_catalogues, "field_algebra": gen_field_algebra, "rppi": gen_rppi, "io": gen_io, "cross": gen_cross, "normalization": gen_normalization, "mc3pcf_randoms": gen_mc3pcf_randoms, "random_catalogue": gen_random_catalogue, "mc3pcf_particle": gen_mc3pcf_particle, "window_file": gen_window_file, "tabulated": gen_tabulated, "counting": gen_counting, "mc3pcf": gen_mc3pcf, "phi": gen_phi, "deposit": gen_deposit, "windows": gen_windows,
             "convolution": gen_convolution, "corr2pcf": gen_corr2pcf, "multipole": gen_multipole}
 
 
