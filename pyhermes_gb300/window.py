@@ -557,6 +557,11 @@ def convolve_field(field, window):
         from .multipole import convolve_complex_full
 
         out = convolve_complex_full(field, window)
+    elif mode == "materialized" and window.kernel_device().shape[-1] == window.L:
+        # a stored complex full-FFT kernel (a composite of legendre /
+        # radial multipole windows): ifftn(fftn(eps) K), io/sfc_field.py:118-121
+        k = window.kernel_device()
+        out = torch.fft.ifftn(torch.fft.fftn(eps.to(torch.complex64)) * k.to(torch.complex64))
     else:
         out = apply_window(eps.to(torch.float32).contiguous(), window)
     new = field._spawn_like()

@@ -100,6 +100,20 @@ def test_full_fft_window_on_host(golden_dir, oracle_fields, name):
     assert np.iscomplexobj(conv) and _rel(conv, g[name + "_conv"]) < 2e-6
 
 
+def test_full_fft_composite_on_host(golden_dir, oracle_fields):
+    """A composite of two full-FFT windows keeps the [L, L, L] complex
+    kernel and convolves with it (io/sfc_field.py:112-121)."""
+    g = np.load(os.path.join(golden_dir, "full_fft_windows_J4.npz"))
+    a = WindowFunc(dict(CASES["legendre_l2_m1"]), SFC, device="cpu")
+    b = WindowFunc(dict(CASES["radial_shell_l1_m1"]), SFC, device="cpu")
+    c = a - 0.5 * b
+    ref_k = g["legendre_l2_m1_kernel"] - 0.5 * g["radial_shell_l1_m1_kernel"]
+    assert _rel(c.as_array(), ref_k) < 2e-6
+    conv = (_field(g["epsilon"], "cpu") @ c).epsilon
+    ref = g["legendre_l2_m1_conv"] - 0.5 * g["radial_shell_l1_m1_conv"]
+    assert _rel(conv, ref) < 2e-6
+
+
 def test_full_fft_window_argument_rules():
     with pytest.raises(ValueError, match="bandwidth=1"):
         mp.complex_full_window_bin(WindowFunc(dict(CASES["legendre_l2_m1"]), SFC, bandwidth=2, device="cpu"))
