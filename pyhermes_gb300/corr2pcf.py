@@ -19,14 +19,13 @@ mean-subtracted fields is added on the host in float64.
 import copy
 import itertools
 import logging
-import os
 import time
 
 import numpy as np
 import torch
 
 from .params import plain_copy, task_params
-from .sfc_field import (SFCField, describe_input, normalize_task_weight_normalization, read_numpy_pickle,
+from .sfc_field import (SFCField, check_fout, describe_input, normalize_task_weight_normalization, read_numpy_pickle,
                         write_numpy_pickle)
 from .window import (
     ANISOTROPIC_AUTO_WINDOW_TYPES, LOS_AWARE_WINDOW_TYPES, WindowFunc, materialized_pair_products, normalize_los_args,
@@ -215,17 +214,16 @@ class Corr2PCFData:
             setattr(self, n, a)
 
     def save_corr2pcf(self, f_out, overwrite=False):
-        if os.path.exists(f_out) and not overwrite:
-            raise FileExistsError(f_out)
-        d = os.path.dirname(f_out)
-        if d:
-            os.makedirs(d, exist_ok=True)
+        f_out = check_fout(self, f_out, overwrite)
+        if not f_out:
+            return None
         data = {"sfc_info1": self.sfc_info1, "sfc_info2": self.sfc_info2, "corr2pcf_info": self.corr2pcf_info,
                 "sampling_names": tuple(self.sampling_names)}
         data.update({p: getattr(self, p) for p in PRODUCT_NAMES})
         data.update({n: self.sampling[n] for n in self.sampling_names})
         with open(f_out, "wb") as f:
             write_numpy_pickle(f, data)
+        return f_out
 
     def load_corr2pcf(self, f_in):
         with open(f_in, "rb") as f:

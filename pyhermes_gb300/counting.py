@@ -11,13 +11,12 @@ the GPU.  ``CountingData`` saves the reference's framed pickle
 """
 
 import logging
-import os
 import time
 
 import numpy as np
 
 from .params import task_params
-from .sfc_field import (SFCField, describe_input, normalize_task_weight_normalization, read_numpy_pickle,
+from .sfc_field import (SFCField, check_fout, describe_input, normalize_task_weight_normalization, read_numpy_pickle,
                         write_numpy_pickle)
 from .window import WindowFunc
 
@@ -42,15 +41,14 @@ class CountingData:
             self.load_counting(data_path)
 
     def save_counting(self, f_out, overwrite=False):
-        if os.path.exists(f_out) and not overwrite:
-            raise FileExistsError(f"{f_out} exists; pass overwrite=True")
         if not self.counting_info:
             raise ValueError('The dictionary "counting_info" is empty.')
-        d = os.path.dirname(f_out)
-        if d:
-            os.makedirs(d, exist_ok=True)
+        f_out = check_fout(self, f_out, overwrite)
+        if not f_out:
+            return None
         with open(f_out, "wb") as f:
             write_numpy_pickle(f, {"sfc_info": self.sfc_info, "counting_info": self.counting_info, "nx": self.nx})
+        return f_out
 
     def load_counting(self, f_in):
         with open(f_in, "rb") as f:

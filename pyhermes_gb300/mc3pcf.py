@@ -32,7 +32,8 @@ from . import _lib
 from .kernels import _ptr, _stream_ptr
 from .params import task_params
 from .phi import sample_scaling_function
-from .sfc_field import SFCField, describe_input, normalize_task_weight_normalization, read_numpy_pickle, write_numpy_pickle
+from .sfc_field import (SFCField, check_fout, describe_input, normalize_task_weight_normalization, read_numpy_pickle,
+                        write_numpy_pickle)
 
 _WS = {}
 
@@ -203,15 +204,12 @@ class Corr3PCFData:
             self.load_corr3pcf(data_path)
 
     def save_corr3pcf(self, f_out, overwrite=False):
-        import os
-
-        if os.path.exists(f_out) and not overwrite:
-            raise FileExistsError(f_out)
-        d = os.path.dirname(f_out)
-        if d:
-            os.makedirs(d, exist_ok=True)
+        f_out = check_fout(self, f_out, overwrite)
+        if not f_out:
+            return None
         with open(f_out, "wb") as f:
             write_numpy_pickle(f, {k: getattr(self, k) for k in self.FILE_KEYS})
+        return f_out
 
     def load_corr3pcf(self, f_in):
         with open(f_in, "rb") as f:

@@ -32,7 +32,7 @@ from . import _lib
 from .kernels import _ptr, _stream_ptr
 from .params import task_params
 from .phi import cal_gamma, sample_scaling_function
-from .sfc_field import (SFCField, describe_input, normalize_task_weight_normalization, read_numpy_pickle,
+from .sfc_field import (SFCField, check_fout, describe_input, normalize_task_weight_normalization, read_numpy_pickle,
                         write_numpy_pickle)
 from .window import WindowFunc, phi_power_device, rfft_field
 
@@ -511,15 +511,12 @@ class Corr3PCFMultipoleData:
             self.load_corr3pcf_multipole(data_path)
 
     def save_corr3pcf_multipole(self, f_out, overwrite=False):
-        import os
-
-        if os.path.exists(f_out) and not overwrite:
-            raise FileExistsError(f_out)
-        d = os.path.dirname(f_out)
-        if d:
-            os.makedirs(d, exist_ok=True)
+        f_out = check_fout(self, f_out, overwrite)
+        if not f_out:
+            return None
         with open(f_out, "wb") as f:
             write_numpy_pickle(f, {k: getattr(self, k) for k in self.FILE_KEYS})
+        return f_out
 
     def load_corr3pcf_multipole(self, f_in):
         with open(f_in, "rb") as f:

@@ -12,6 +12,7 @@ on first access (the reference's dtype), so reference tools that read
 """
 
 import copy
+import logging
 import math
 import os
 import pickle
@@ -19,6 +20,8 @@ from io import BytesIO
 
 import numpy as np
 import torch
+
+logger = logging.getLogger(__name__)
 
 REQUIRED_ARGV = ("J", "box_size", "phi_resolution", "wavelet_mode", "wavelet_level")
 
@@ -53,6 +56,43 @@ def normalize_field_value_normalization(normalization):
     if mode not in {"raw", "catalog", "field", "unit"}:
         raise ValueError("normalization must be None, 'raw', 'catalog', 'field', or 'unit'.")
     return mode
+
+
+def check_fout(instance, fout_path, overwrite=False):
+    """Output path rules of the reference's savers (io/funcs.py:13-57):
+    no path -> None (nothing written); an existing file is replaced only
+    with overwrite, else the first free ``name_<n>.ext`` is used; a folder
+    (existing, or a path ending in a separator) receives
+    ``Output_<Class>_<YYYYmmddHHMM>.pkl``; missing parent folders are made."""
+    import datetime
+
+    if fout_path is None or fout_path == "":
+        logger.info("No <fout_path> specified, skipping disk output.")
+        return None
+    fout_path = os.fspath(fout_path)
+    is_folder = fout_path.endswith(("/", "\\"))
+    if os.path.exists(fout_path):
+        if os.path.isdir(fout_path):
+            is_folder = True
+        elif os.path.isfile(fout_path):
+            if overwrite:
+                logger.warning("Output file '%s' already exists and will be overwritten (overwrite=True).",
+                               fout_path)
+            else:
+                logger.warning("Output file '%s' already exists! Generating a new file name.", fout_path)
+                base, ext = os.path.splitext(fout_path)
+                n = 1
+                while os.path.exists(f"{base}_{n}{ext}"):
+                    n += 1
+                fout_path = f"{base}_{n}{ext}"
+    if not is_folder:
+        parent = os.path.dirname(fout_path)
+        if parent:
+            os.makedirs(parent, exist_ok=True)
+        return fout_path
+    os.makedirs(fout_path, exist_ok=True)
+    stamp = datetime.datetime.now().strftime("%Y%m%d%H%M")
+    return os.path.join(fout_path, f"Output_{instance.__class__.__name__}_{stamp}.pkl")
 
 
 def write_numpy_pickle(file_obj, value, protocol=4):
@@ -422,17 +462,31 @@ class SFCField:
         return value / volume
 
     # ---- persistence (byte-compatible with the reference) -------------------
+    def save(self, f_out, save_sfc_field=False, save_counting=False, save_2pcf=False, save_3pcf=False,
+             save_3pcf_multipole=False, single=True, overwrite=False):
+        """io/base.py:90-124: the flag picks the writer; a field object
+        writes its field file, and returns the path written (or None)."""
+        if save_counting or save_2pcf or save_3pcf or save_3pcf_multipole:
+            raise ValueError(f"{type(self).__name__} holds no counting / correlation results to save.")
+        return self.save_sfc_field(f_out, single=single, overwrite=overwrite)
+
+    def load(self, f_in, read_sfc_field=False, read_counting=False, read_2pcf=False, read_3pcf=False,
+             read_3pcf_multipole=False, single=True):
+        """io/base.py:24-88 for a field object: reads a field file."""
+        if read_counting or read_2pcf or read_3pcf or read_3pcf_multipole:
+            raise ValueError(f"{type(self).__name__} reads field files only.")
+        self.load_sfc_field(f_in, single=single)
+
     def save_sfc_field(self, f_out, single=True, overwrite=False):
-        """pyhermes/io/sfc_field.py:565-584: {'sfc_info', 'epsilon'} framed pickle."""
-        if os.path.exists(f_out) and not overwrite:
-            raise FileExistsError(f"{f_out} exists; pass overwrite=True")
-        d = os.path.dirname(f_out)
-        if d:
-            os.makedirs(d, exist_ok=True)
+        """pyhermes/io/sfc_field.py:565-584: {'sfc_info', 'epsilon'} framed
+        pickle, at the path check_fout resolves (returned)."""
         if not self.sfc_info:
             raise ValueError('The dictionary "sfc_info" is empty.')
-        with open(f_out, "wb") as f:
-            write_numpy_pickle(f, {"sfc_info": self.sfc_info, "epsilon": self.epsilon})
+        f_out = check_fout(self, f_out, overwrite)
+        if f_out:
+            with open(f_out, "wb") as f:
+                write_numpy_pickle(f, {"sfc_info": self.sfc_info, "epsilon": self.epsilon})
+        return f_out
 
     def load_sfc_field(self, f_in, single=True):
         """pyhermes/io/sfc_field.py:549-563."""

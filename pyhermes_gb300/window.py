@@ -412,23 +412,46 @@ class WindowFunc(SFCField):
                 self.w_kernel = (t.to(torch.complex128) if t.is_complex() else t.to(torch.float64)).cpu().numpy()
         return self.w_kernel
 
-    # ---- persistence (io/window.py:518-548, io/base.py:24-121) ---------------
-    def save(self, f_out, single=True, overwrite=False):
-        """Framed pickle {**input_params, 'window_kernal': kernel} as the
-        reference writes it (the key's spelling is the reference's)."""
-        from .sfc_field import write_numpy_pickle
+    def copy(self, copy_kernel=True):
+        """A copy that does not rebuild the kernel (io/window.py:487-516):
+        with copy_kernel the stored kernel (host and device) is copied, else
+        the copy rebuilds it on its next use.  The window callable is shared."""
+        if self.is_composite_window and not copy_kernel:
+            raise ValueError("Composite WindowFunc cannot be copied with copy_kernel=False.")
+        new = self.__class__.__new__(self.__class__)
+        for key, value in self.__dict__.items():
+            if key == "func":
+                new.func = value
+            elif key in ("w_kernel", "_kernel_dev"):
+                keep = copy_kernel and value is not None
+                setattr(new, key, (value.clone() if isinstance(value, torch.Tensor) else value.copy()) if keep
+                        else None)
+            elif isinstance(value, np.ndarray):
+                setattr(new, key, value.copy())
+            elif isinstance(value, torch.Tensor):
+                setattr(new, key, value.clone())
+            else:
+                setattr(new, key, copy.deepcopy(value))
+        return new
 
-        if os.path.exists(f_out) and not overwrite:
-            raise FileExistsError(f"{f_out} exists; pass overwrite=True")
+    # ---- persistence (io/window.py:518-548, io/base.py:24-121) ---------------
+    def save(self, f_out, single=True, overwrite=False, **flags):
+        """Framed pickle {**input_params, 'window_kernal': kernel} as the
+        reference writes it (io/window.py:530-548; the key's spelling is
+        the reference's), at the path check_fout resolves (returned)."""
+        from .sfc_field import check_fout, write_numpy_pickle
+
+        if any(flags.values()):
+            raise ValueError("WindowFunc.save writes the window file only.")
         if not self.input_params:
             raise ValueError('The dict_argv "win_params" is empty.')
-        d = os.path.dirname(f_out)
-        if d:
-            os.makedirs(d, exist_ok=True)
-        with open(f_out, "wb") as f:
-            write_numpy_pickle(f, {**self.input_params, "window_kernal": self.as_array()})
+        f_out = check_fout(self, f_out, overwrite)
+        if f_out:
+            with open(f_out, "wb") as f:
+                write_numpy_pickle(f, {**self.input_params, "window_kernal": self.as_array()})
+        return f_out
 
-    def load(self, f_in, single=True):
+    def load(self, f_in, single=True, **flags):
         """Reads a saved window: input_params from the file and its kernel,
         used from then on as a materialised kernel."""
         from .sfc_field import read_numpy_pickle

@@ -106,6 +106,26 @@ def test_custom_window_composites(golden_dir):
     assert np.abs(c.as_array() - ref).max() <= 1e-6 * np.abs(ref).max()
 
 
+def test_window_copy(golden_dir):
+    """WindowFunc.copy (io/window.py:487-516): the kernel copied or left to
+    be rebuilt; composites refuse copy_kernel=False."""
+    g = np.load(os.path.join(golden_dir, "custom_windows_J4.npz"))
+    w = WindowFunc(dict(CASES["skew_full"][0]), SFC, device="cpu")
+    k = w.as_array()
+    c = w.copy()
+    assert c.w_kernel is not k and np.array_equal(c.w_kernel, k) and c.func is w.func
+    assert c._kernel_dev is not w._kernel_dev and torch.equal(c._kernel_dev, w._kernel_dev)
+    c.w_kernel[0, 0, 0] = -1.0
+    assert w.as_array()[0, 0, 0] != -1.0
+    r = w.copy(copy_kernel=False)
+    assert r.w_kernel is None and r._kernel_dev is None
+    assert np.abs(r.as_array() - g["skew_full"]).max() <= 1e-12
+    comp = w + r
+    assert comp.copy().type == "composite"
+    with pytest.raises(ValueError, match="copy_kernel=False"):
+        comp.copy(copy_kernel=False)
+
+
 @pytest.mark.gpu
 def test_custom_window_convolution_matches_reference(golden_dir):
     from pyhermes_gb300.sfc_field import SFCField

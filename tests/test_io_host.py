@@ -128,3 +128,31 @@ def test_corr3pcf_multipole_file(golden_dir, oracle_kernels, tmp_path):
     _same_layout(d, ref, "corr3pcf_multipole_info")
     for k in ("ddd_l", "delta_ddd_l", "rrr_l", "zeta_l"):
         assert _rel(d[k], ref[k]) < 1e-5, k
+
+
+def test_output_path_rules(golden_dir, tmp_path, oracle_kernels):
+    """check_fout (io/funcs.py:13-57) as every saver applies it: no path
+    writes nothing, an existing file gets the next free name_<n> unless
+    overwrite, a folder receives Output_<Class>_<stamp>.pkl, and the generic
+    save / load flags of io/base.py:24-124 reach the field writer."""
+    import re
+
+    f = _field(golden_dir)
+    assert f.save_sfc_field("") is None and f.save_sfc_field(None) is None
+    first = f.save_sfc_field(str(tmp_path / "a" / "f.pkl"))
+    assert first == str(tmp_path / "a" / "f.pkl") and os.path.isfile(first)
+    assert f.save_sfc_field(first) == str(tmp_path / "a" / "f_1.pkl")
+    assert f.save(first, save_sfc_field=True) == str(tmp_path / "a" / "f_2.pkl")
+    assert f.save_sfc_field(first, overwrite=True) == first
+    out = f.save_sfc_field(str(tmp_path / "dir") + os.sep)
+    assert re.fullmatch(r"Output_SFCField_\d{12}\.pkl", os.path.basename(out)) and os.path.isfile(out)
+    g = SFCField(device="cpu")
+    g.sfc_info = {}
+    g.load(first, read_sfc_field=True)
+    assert np.array_equal(g.epsilon, f.epsilon)
+    with pytest.raises(ValueError):
+        f.save(first, save_2pcf=True)
+    d = CountingData()
+    d.counting_info, d.sfc_info, d.nx = {"seed": 1}, dict(f.sfc_info), np.arange(3.0)
+    p = d.save_counting(str(tmp_path / "c.pkl"))
+    assert d.save_counting(p) == str(tmp_path / "c_1.pkl")
