@@ -412,6 +412,25 @@ class SFCField:
             value_unit = "physical" if getattr(field, "field_kind", None) == "catalog_field" else "grid"
         return value_unit
 
+    def phi_at_pos(self, pos):
+        """Cell and scaling-function stencil of each position
+        (io/sfc_field.py:484-485, utils/wavelet_grid.py:121-140): the cell
+        floor(x * L / box) as int32 [N, 3], and float64 [N, 3, 3, 3] with
+        phi_x * phi_y * phi_z at stencil offset s stored at index -s per
+        axis (s = 0, 1, 2 -> 0, 2, 1), on the field's device."""
+        support, res = int(self.phi_support), int(self.phi_resolution)
+        dev = self.device if self.device is not None else "cpu"
+        p = torch.as_tensor(np.asarray(pos, dtype=np.float64), device=dev) * float(self.scale_factor)
+        coarse = torch.floor(p).to(torch.int32)
+        frac = ((p - coarse.double()) * res).to(torch.int64)
+        phi = torch.as_tensor(np.asarray(self.phi_array, dtype=np.float64), device=dev)
+        taps = phi[frac[:, :, None] + torch.arange(support, device=dev) * res]  # [N, 3 axes, support]
+        local = (taps[:, 0, :, None, None] * taps[:, 1, None, :, None]) * taps[:, 2, None, None, :]
+        # out[:, i] holds offset (-i) mod support on every axis
+        perm = torch.tensor([(-i) % support for i in range(support)], device=dev)
+        out = local.index_select(1, perm).index_select(2, perm).index_select(3, perm)
+        return coarse.cpu().numpy(), out.cpu().numpy()
+
     def field_density_at_pos(self, pos, epsilon=None, filter=None, normalization=None, value_unit="auto"):
         """pyhermes/io/sfc_field.py:487-530: the field's density at positions
         (box coordinates), by the 27-point scaling-function interpolation of

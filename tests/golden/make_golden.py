@@ -808,6 +808,17 @@ def gen_full_fft_windows():
     _save("full_fft_windows_J4", **out)
 
 
+def gen_phi_at_pos():
+    """SFCField.phi_at_pos (io/sfc_field.py:484-485,
+    utils/wavelet_grid.py:121-140): coarse cells and 3x3x3 stencils."""
+    rng = np.random.default_rng(44)
+    pos = rng.uniform(0.0, 1000.0, (200, 3))
+    pos[:5] = [[0.0, 0.0, 0.0], [999.999, 500.0, 62.5], [62.5, 125.0, 187.5], [1e-9, 999.0, 3.3], [500.0, 0.5, 0.0]]
+    f = _projection(pos, 4)
+    coarse, local = f.phi_at_pos(pos)
+    _save("phi_at_pos_J4", pos=pos, coarse=coarse, local=local)
+
+
 def gen_mc_theta():
     """Corr_3PCF with angle_param='theta' (a min/max/n spec and a list)."""
     from pyhermes.theory.corr3pcf import Corr_3PCF
@@ -895,7 +906,7 @@ def gen_window_file():
     _save("window_file_J4", kernel=kernel)
 
 
-SECTIONS = {"full_fft_windows": gen_full_fft_windows, "custom_windows": gen_custom_windows, "mc_theta": gen_mc_theta, "composite_windows": gen_composite_windows, "particle_data": gen_particle_data, "catalogues": gen_catalogues, "field_algebra": gen_field_algebra, "rppi": gen_rppi, "io": gen_io, "cross": gen_cross, "normalization": gen_normalization, "mc3pcf_randoms": gen_mc3pcf_randoms, "random_catalogue": gen_random_catalogue, "mc3pcf_particle": gen_mc3pcf_particle, "window_file": gen_window_file, "tabulated": gen_tabulated, "counting": gen_counting, "mc3pcf": gen_mc3pcf, "phi": gen_phi, "deposit": gen_deposit, "windows": gen_windows,
+SECTIONS = {"phi_at_pos": gen_phi_at_pos, "full_fft_windows": gen_full_fft_windows, "custom_windows": gen_custom_windows, "mc_theta": gen_mc_theta, "composite_windows": gen_composite_windows, "particle_data": gen_particle_data, "catalogues": gen_catalogues, "field_algebra": gen_field_algebra, "rppi": gen_rppi, "io": gen_io, "cross": gen_cross, "normalization": gen_normalization, "mc3pcf_randoms": gen_mc3pcf_randoms, "random_catalogue": gen_random_catalogue, "mc3pcf_particle": gen_mc3pcf_particle, "window_file": gen_window_file, "tabulated": gen_tabulated, "counting": gen_counting, "mc3pcf": gen_mc3pcf, "phi": gen_phi, "deposit": gen_deposit, "windows": gen_windows,
             "convolution": gen_convolution, "corr2pcf": gen_corr2pcf, "multipole": gen_multipole}
 
 

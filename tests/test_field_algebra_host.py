@@ -87,3 +87,16 @@ def test_mean_density_and_density_at_pos_match_reference(fields):
             got = np.asarray(a.field_density_at_pos(g["query"], normalization=norm, value_unit=unit))
             ref = g["at_" + key]
             assert np.abs(got - ref).max() <= 1e-5 * np.abs(ref).max(), key
+
+
+def test_phi_at_pos_matches_reference(golden_dir, oracle_kernels):
+    """SFCField.phi_at_pos (io/sfc_field.py:484-485): cells and stencils
+    bit-identical to the reference, boundary positions included."""
+    from pyhermes_gb300.projection import SFCProjection
+
+    g = np.load(os.path.join(golden_dir, "phi_at_pos_J4.npz"))
+    f = SFCProjection({"SFCProjection": {"particle_pos": g["pos"], "J": 4, "box_size": 1000.0}},
+                      device="cpu").run(save_result=False)
+    coarse, local = f.phi_at_pos(g["pos"])
+    assert coarse.dtype == np.int32 and np.array_equal(coarse, g["coarse"])
+    assert local.shape == (200, 3, 3, 3) and np.array_equal(local, g["local"])
