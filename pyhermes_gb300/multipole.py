@@ -636,8 +636,7 @@ class Corr_3PCF_Multipole:
                      "expanded_products": list(expanded),
                      "resolution_diagnostics": self._resolution_diagnostics(),
                      "radial_profile_diagnostics_result": [],
-                     "rho_vertices": [self.data[i].field_mean_density(value_unit="grid") if i in self.data else None
-                                      for i in (1, 2, 3)],
+                     "rho_vertices": list(getattr(self, "rho_vertices", [None, None, None])),
                      "fout_path": self.fout_path})
         return info
 
@@ -729,9 +728,15 @@ class Corr_3PCF_Multipole:
         ref = self._normalized(self._resolve(self.sfc_field1, "field vertex 1"))
         self.reference = ref
         self.rho = ref.field_mean_density(value_unit="grid")
+        # per-vertex density of the normalised field before its window
+        # (theory/corr3pcf_multipole.py:884-888)
+        self.rho_vertices = [self.rho, self.rho, self.rho]
+        normalized = {}
         for i in (1, 2, 3):
             if needs_data:
                 base = self._normalized(self._resolve(getattr(self, f"sfc_field{i}"), f"field vertex {i}"))
+                normalized[i] = base
+                self.rho_vertices[i - 1] = base.field_mean_density(value_unit="grid")
                 w = getattr(self, f"window{i}")
                 self.data[i] = base @ WindowFunc(w, base.sfc_info, device=self.device) if w else base.copy()
             if needs_random:
@@ -739,9 +744,8 @@ class Corr_3PCF_Multipole:
                 if r is None or r == "":
                     raise ValueError(f"Missing input for random vertex {i}.")
                 if r == "uniform":
-                    base = self.data.get(i) or ref
-                    rho_i = base.field_mean_density(value_unit="grid") if i in self.data else self.rho
-                    self.rand[i] = self._uniform_random_after_window(base, rho_i, getattr(self, f"window{i}"), i)
+                    self.rand[i] = self._uniform_random_after_window(normalized.get(i, ref), self.rho_vertices[i - 1],
+                                                                     getattr(self, f"window{i}"), i)
                 else:
                     base = self._normalized(self._resolve(r, f"random vertex {i}"))
                     w = getattr(self, f"window{i}")

@@ -754,7 +754,8 @@ def gen_custom_windows():
     from custom_window_funcs import doubled_gauss
     from pyhermes.theory.corr3pcf_multipole import Corr_3PCF_Multipole
 
-    win = {"func": doubled_gauss, "len_args": {"R": 40.0}}
+    # a vertex window needs a 'type' to be taken (theory/corr3pcf_multipole.py:71-74)
+    win = {"type": "custom", "func": doubled_gauss, "len_args": {"R": 40.0}}
     d = Corr_3PCF_Multipole({"Corr_3PCF_Multipole": {
         "sfc_field": f, "random": "uniform", "window1": dict(win), "window2": dict(win), "window3": dict(win),
         "binning_window12": {"type": "shell", "len_args": {}, "other_args": {}, "mapping": {"R": "r12"}},

@@ -191,7 +191,7 @@ def _corr2pcf_custom_bins(g, device):
 def _multipole_uniform_behind_w2(g, device):
     from pyhermes_gb300.multipole import Corr_3PCF_Multipole
 
-    win = {"func": cwf.doubled_gauss, "len_args": {"R": 40.0}}
+    win = {"type": "custom", "func": cwf.doubled_gauss, "len_args": {"R": 40.0}}
     return Corr_3PCF_Multipole({"Corr_3PCF_Multipole": {
         "sfc_field": _projected(g, device), "random": "uniform",
         "window1": dict(win), "window2": dict(win), "window3": dict(win),
