@@ -34,6 +34,7 @@ from .params import task_params
 from .phi import sample_scaling_function
 from .sfc_field import (SFCField, check_fout, describe_input, normalize_task_weight_normalization, read_numpy_pickle,
                         write_numpy_pickle)
+from .window import WindowFunc
 
 _WS = {}
 
@@ -232,6 +233,14 @@ class Corr_3PCF:
             r = tp.get(f"random{i}")
             setattr(self, f"random{i}", tp.get("random") if r in (None, "") else r)
         self.weight_normalization = normalize_task_weight_normalization(tp.get("weight_normalization", "catalog"))
+        # smoothing windows: a dict needs a 'type' or a 'func'; vertex windows
+        # fall back to the shared one (theory/corr3pcf.py:176-183)
+        window = tp.get("window")
+        self.window = window if (window and (window.get("type") or window.get("func"))) else None
+        for i in (1, 2, 3):
+            wi = tp.get(f"window{i}")
+            wi = wi if (wi and (wi.get("type") or wi.get("func"))) else None
+            setattr(self, f"window{i}", wi if wi else (dict(self.window) if self.window else None))
         self.r12, self.r13 = float(tp["r12"]), float(tp["r13"])
         self.n_rot = int(tp["n_rot"])
         self.center = tp["center"]
@@ -297,13 +306,29 @@ class Corr_3PCF:
             return f.copy()
         return f.switch_weight_normalization(self.weight_normalization)
 
+    def _windowed(self, i, field):
+        """A vertex field after its smoothing window, or a copy
+        (theory/corr3pcf.py:463-476, :1038-1050)."""
+        w = getattr(self, f"window{i}")
+        if w is None:
+            return field
+        if isinstance(w, WindowFunc):
+            return field @ w
+        if isinstance(w, dict):
+            return field @ WindowFunc(w, field.sfc_info, device=self.device)
+        raise ValueError(f"Unsupported window input for vertex {i}. Expected dict, WindowFunc, or None, "
+                         f"got {type(w)}.")
+
     def _rand(self, i, ref):
+        """A uniform random is the mean density of the vertex's windowed data
+        field (theory/corr3pcf.py:1076-1091); a random field gets the
+        vertex's window."""
         r = getattr(self, f"random{i}")
         if r == "uniform":
             return float(ref.field_mean_density(value_unit="grid"))
         if r is None or r == "":
             return None
-        return self._field(r, f"random vertex {i}")
+        return self._windowed(i, self._field(r, f"random vertex {i}"))
 
     @staticmethod
     def _density(x):
@@ -325,7 +350,8 @@ class Corr_3PCF:
         return np.asarray(t.run(save_result=False).dd)
 
     def run(self, save_result=True, overwrite=False):
-        data = {i: self._field(getattr(self, f"sfc_field{i}"), f"field vertex {i}") for i in (1, 2, 3)}
+        data = {i: self._windowed(i, self._field(getattr(self, f"sfc_field{i}"), f"field vertex {i}"))
+                for i in (1, 2, 3)}
         ref = data[1]
         rand = {i: self._rand(i, data[i]) for i in (1, 2, 3)}
         L, J = ref.L, ref.J
@@ -488,9 +514,9 @@ class Corr_3PCF:
         for i in (1, 2, 3):
             info[f"random{i}"] = describe_input(rand.get(i))
         info.update({"random_pos1": arr("random_pos1"), "random_weight1": arr("random_weight1"),
-                     "weight_normalization": self.weight_normalization, "window": describe_input(tp.get("window"))})
+                     "weight_normalization": self.weight_normalization, "window": describe_input(self.window)})
         for i in (1, 2, 3):
-            info[f"window{i}"] = describe_input(tp.get(f"window{i}"))
+            info[f"window{i}"] = describe_input(getattr(self, f"window{i}"))
         theta, mu = tp.get("theta"), tp.get("mu")
         info.update({"r12": self.r12, "r13": self.r13, "angle_param": str(tp["angle_param"]).strip().lower(),
                      "theta_spec": describe_input(theta), "mu_spec": describe_input(mu),

@@ -34,6 +34,35 @@ def plain_copy(obj):
     return copy.deepcopy(obj)
 
 
+def callable_metadata(value):
+    """A callable as result files record it (utils/window_params.py:97-101):
+    {'kind': 'callable', 'name': '<module>.<qualname>'} (a numba dispatcher
+    is named by its Python function)."""
+    target = getattr(value, "py_func", value)
+    module = getattr(target, "__module__", getattr(value, "__module__", type(value).__module__))
+    name = getattr(target, "__qualname__", getattr(target, "__name__", type(value).__name__))
+    return {"kind": "callable", "name": f"{module}.{name}"}
+
+
+def serialize_window_params(value):
+    """Window / sampling parameters as result files record them
+    (utils/window_params.py:104-121): 'func' becomes 'custom_func' metadata,
+    other callables their metadata, arrays lists, NumPy scalars Python ones."""
+    if isinstance(value, dict):
+        return {("custom_func" if k == "func" else k): (callable_metadata(v) if k == "func"
+                                                         else serialize_window_params(v))
+                for k, v in value.items()}
+    if callable(value):
+        return callable_metadata(value)
+    if isinstance(value, np.ndarray):
+        return value.tolist()
+    if isinstance(value, (list, tuple)):
+        return [serialize_window_params(v) for v in value]
+    if isinstance(value, np.generic):
+        return value.item()
+    return copy.deepcopy(value)
+
+
 REPLACE_KEYS = {
     "Corr_2PCF.binning_window",
     "Corr_2PCF.sampling",
@@ -43,7 +72,11 @@ REPLACE_KEYS = {
     "Corr_3PCF_Multipole.sample_mpi",
 }
 
-_EMPTY_WINDOW = {"type": "", "len_args": {}, "los_args": {}, "other_args": {}}
+def _empty_window():
+    # a fresh nested dict per key: task_params deep-copies the defaults, and
+    # deepcopy keeps any sharing between them, so one shared inner len_args
+    # dict would receive every window's arguments during the merge
+    return {"type": "", "len_args": {}, "los_args": {}, "other_args": {}}
 
 DEFAULTS = {
     "Counting": {
@@ -51,7 +84,7 @@ DEFAULTS = {
         "random_count": 1000000,
         "seed": 42,
         "weight_normalization": "catalog",
-        "window": dict(_EMPTY_WINDOW),
+        "window": _empty_window(),
         "threads": 1,
         "fout_path": "",
     },
@@ -78,7 +111,7 @@ DEFAULTS = {
         "sfc_field": "", "sfc_field1": "", "sfc_field2": "",
         "random": None, "random1": "", "random2": "",
         "weight_normalization": "catalog",
-        "window": dict(_EMPTY_WINDOW), "window1": dict(_EMPTY_WINDOW), "window2": dict(_EMPTY_WINDOW),
+        "window": _empty_window(), "window1": _empty_window(), "window2": _empty_window(),
         "binning_window": {"type": "shell", "len_args": ["R"], "los_args": {}, "other_args": {},
                            "mapping": "s_to_R", "kernel_mode": ""},
         "sampling": {"s": {"min": 1.0, "max": 150.0, "n": 30}},
@@ -93,8 +126,8 @@ DEFAULTS = {
         "sfc_field": "", "sfc_field1": "", "sfc_field2": "", "sfc_field3": "",
         "random": None, "random1": "", "random2": "", "random3": "",
         "weight_normalization": "catalog",
-        "window": dict(_EMPTY_WINDOW), "window1": dict(_EMPTY_WINDOW),
-        "window2": dict(_EMPTY_WINDOW), "window3": dict(_EMPTY_WINDOW),
+        "window": _empty_window(), "window1": _empty_window(),
+        "window2": _empty_window(), "window3": _empty_window(),
         "binning_window12": {"type": "shell", "len_args": {}, "other_args": {}, "mapping": {}},
         "binning_window13": {"type": "shell", "len_args": {}, "other_args": {}, "mapping": {}},
         "sampling": {},
@@ -120,6 +153,8 @@ DEFAULTS = {
         "particle_pos1": None, "particle_weight1": None, "random_pos1": None, "random_weight1": None,
         "random": None, "random1": "", "random2": "", "random3": "",
         "weight_normalization": "catalog",
+        "window": _empty_window(), "window1": _empty_window(),
+        "window2": _empty_window(), "window3": _empty_window(),
         "r12": 20.0, "r13": 40.0,
         "angle_param": "theta",
         "theta": {"theta_min": 0.0, "theta_max": 3.141592653589793, "n_theta": 20},

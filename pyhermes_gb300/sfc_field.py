@@ -128,18 +128,19 @@ def describe_input(value):
         return value
     if isinstance(value, (float, int, np.floating)):
         return float(value)
+    from .params import serialize_window_params
+
     if getattr(value, "is_window", False):
         return {"kind": "WindowFunc", "type": getattr(value, "type", "custom"),
-                "len_args": dict(getattr(value, "len_args", {}) or {}),
-                "los_args": dict(getattr(value, "los_args", {}) or {}),
-                "other_args": dict(getattr(value, "other_args", {}) or {})}
+                "len_args": serialize_window_params(getattr(value, "len_args", {}) or {}),
+                "los_args": serialize_window_params(getattr(value, "los_args", {}) or {}),
+                "other_args": serialize_window_params(getattr(value, "other_args", {}) or {})}
     if isinstance(value, SFCField):
         return {"kind": "SFCField", "L": value.L, "box_size": value.box_size, "wavelet_mode": value.wavelet_mode,
                 "wavelet_level": value.wavelet_level}
     if isinstance(value, dict):
-        from .params import plain_copy
-
-        return plain_copy(value)
+        # window dicts as utils/window_params.py:104-121 serialises them
+        return serialize_window_params(value)
     return value
 
 

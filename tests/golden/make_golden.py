@@ -262,6 +262,12 @@ def gen_mc3pcf_particle():
     d = Corr_3PCF({"Corr_3PCF": dict(common, products=["zeta", "ddd"])}).run(save_result=False)
     for k in ("ddd", "rrr", "d_delta_dd", "r_delta_dd", "delta_ddd", "xi23", "zeta"):
         out["uni_" + k] = np.asarray(getattr(d, k))
+    # smoothing windows: a shared one and a vertex-3 override (theory/corr3pcf.py:176-183, 1038-1104)
+    d = Corr_3PCF({"Corr_3PCF": dict(common, window={"type": "gaussian", "len_args": {"R": 40.0}},
+                                     window3={"type": "sphere", "len_args": {"R": 60.0}},
+                                     products=["zeta", "ddd"])}).run(save_result=False)
+    for k in ("ddd", "rrr", "d_delta_dd", "r_delta_dd", "delta_ddd", "xi23", "zeta"):
+        out["win_" + k] = np.asarray(getattr(d, k))
     _save("mc3pcf_particle_J4", **out)
 
 

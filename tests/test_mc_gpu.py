@@ -74,6 +74,24 @@ def test_corr3pcf_particle_centres_match_reference(golden_dir):
         assert _rel(getattr(d, k), g["uni_" + k]) < 1e-5, (k, getattr(d, k), g["uni_" + k])
 
 
+def test_corr3pcf_vertex_windows_match_reference(golden_dir):
+    """A shared gaussian window and a sphere on vertex 3 (particle centres,
+    uniform random): ddd, rrr, deltas, xi23 and zeta."""
+    from pyhermes_gb300.projection import SFCProjection
+
+    g = np.load(os.path.join(golden_dir, "mc3pcf_particle_J4.npz"))
+    f = SFCProjection({"SFCProjection": {"particle_pos": g["pos"], "catalog_weight": g["weights"], "J": 4,
+                                         "box_size": 1000.0}}).run(save_result=False)
+    d = mc3pcf.Corr_3PCF({"Corr_3PCF": {
+        "sfc_field": f, "random": "uniform", "r12": 150.0, "r13": 250.0, "angle_param": "mu",
+        "mu": {"mu_min": -0.8, "mu_max": 0.8, "n_mu": 3}, "n_rot": 3, "center": "particle", "base_seed": 7,
+        "particle_pos1": g["cpos"], "particle_weight1": g["cw"],
+        "window": {"type": "gaussian", "len_args": {"R": 40.0}},
+        "window3": {"type": "sphere", "len_args": {"R": 60.0}}, "products": ["zeta", "ddd"]}}).run()
+    for k in ("ddd", "rrr", "d_delta_dd", "r_delta_dd", "delta_ddd", "xi23", "zeta"):
+        assert _rel(getattr(d, k), g["win_" + k]) < 1e-4, k
+
+
 @pytest.mark.parametrize("case", ["fields", "uni1"])
 def test_corr3pcf_random_fields_match_reference(golden_dir, case):
     """Random catalogues as fields: rrr by Monte Carlo over three random

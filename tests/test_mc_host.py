@@ -93,3 +93,37 @@ def test_box_random_products_match_reference(golden_dir, oracle_kernels, monkeyp
         "products": ["ddd", "rrr", "delta_ddd"]}}, device="cpu").run()
     for k in ("ddd", "rrr", "delta_ddd"):
         assert _rel(getattr(d, k), g["box_" + k]) < 1e-5, (k, getattr(d, k), g["box_" + k])
+
+
+def test_particle_centre_products_with_windows(golden_dir, oracle_kernels, monkeypatch):
+    """Smoothing windows on the MC vertices (a shared gaussian and a sphere
+    on vertex 3): the windowed data fields, the uniform random as the
+    windowed field's mean density, xi23 and zeta (theory/corr3pcf.py:176-183,
+    1038-1104); convolutions by the oracle on the host."""
+    from pyhermes_gb300 import window as win_mod
+    from pyhermes_gb300.projection import SFCProjection
+
+    def apply_window(eps, w, out=None):
+        K = oracle.window_kernel(w.type, w.len_args, w.L, oracle.fourier_power(PHI, w.bandwidth, w.L),
+                                 mode=w.resolved_mode(), box=w.box_size)
+        return torch.as_tensor(oracle.convolve(eps.double().cpu().numpy(), K), dtype=torch.float32)
+
+    monkeypatch.setattr(win_mod, "apply_window", apply_window)
+    monkeypatch.setattr(mc3pcf, "triplet_sum", _cpu_triplet_sum)
+    g = np.load(os.path.join(golden_dir, "mc3pcf_particle_J4.npz"))
+    f = SFCProjection({"SFCProjection": {"particle_pos": g["pos"], "catalog_weight": g["weights"], "J": 4,
+                                         "box_size": 1000.0}}, device="cpu").run(save_result=False)
+    d = mc3pcf.Corr_3PCF({"Corr_3PCF": {
+        "sfc_field": f, "random": "uniform", "r12": 150.0, "r13": 250.0, "angle_param": "mu",
+        "mu": {"mu_min": -0.8, "mu_max": 0.8, "n_mu": 3}, "n_rot": 3, "center": "particle", "base_seed": 7,
+        "particle_pos1": g["cpos"], "particle_weight1": g["cw"],
+        "window": {"type": "gaussian", "len_args": {"R": 40.0}},
+        "window3": {"type": "sphere", "len_args": {"R": 60.0}},
+        "products": ["zeta", "ddd"]}}, device="cpu").run(save_result=False)
+    for k in ("ddd", "rrr", "d_delta_dd", "r_delta_dd", "delta_ddd", "xi23", "zeta"):
+        assert _rel(getattr(d, k), g["win_" + k]) < 1e-5, (k, getattr(d, k), g["win_" + k])
+    info = d.corr3pcf_info
+    # merged over the defaults; each window keeps its own len_args
+    assert info["window1"] == info["window2"] == {"type": "gaussian", "len_args": {"R": 40.0}, "los_args": {},
+                                                  "other_args": {}}
+    assert info["window3"] == {"type": "sphere", "len_args": {"R": 60.0}, "los_args": {}, "other_args": {}}

@@ -38,3 +38,15 @@ def test_ring_binning_params_per_sample_are_independent():
     assert p2["len_args"]["R"] == 20.0 and p2["len_args"]["H"] == 0.0
     assert "mapping" not in p1 and p1["len_args"] is not p2["len_args"]
     assert bw == before  # the task's template is untouched
+
+
+def test_window_defaults_are_not_shared():
+    """Each window default is its own dict: merging one vertex's len_args
+    must not reach another's."""
+    from pyhermes_gb300.params import task_params
+
+    for task in ("Corr_2PCF", "Corr_3PCF", "Corr_3PCF_Multipole"):
+        tp = task_params(task, {task: {"window1": {"type": "gaussian", "len_args": {"R": 40.0}},
+                                       "window2": {"type": "sphere", "len_args": {"R": 60.0}}}})
+        assert tp["window1"]["len_args"] == {"R": 40.0} and tp["window2"]["len_args"] == {"R": 60.0}
+        assert tp["window"]["len_args"] == {}
