@@ -22,6 +22,7 @@ unbiased for the pool mean whatever the network predicts.
 """
 
 import ctypes
+import logging
 import math
 import time
 
@@ -36,6 +37,7 @@ from .sfc_field import (SFCField, check_fout, describe_input, normalize_task_wei
                         write_numpy_pickle)
 from .window import WindowFunc
 
+logger = logging.getLogger(__name__)
 _WS = {}
 
 
@@ -311,6 +313,10 @@ class Corr_3PCF:
         (theory/corr3pcf.py:463-476, :1038-1050)."""
         w = getattr(self, f"window{i}")
         if w is None:
+            return field
+        if self.center == "particle" and i == 1:
+            # vertex 1 is the particle centres themselves (theory/corr3pcf.py:836-839)
+            logger.warning("window1 has no effect for center='particle'; vertex 1 uses particle centres directly.")
             return field
         if isinstance(w, WindowFunc):
             return field @ w
