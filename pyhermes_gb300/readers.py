@@ -368,10 +368,12 @@ def read_particle_data(path, data_format=None, download=None, **reader_params):
                          f"'{', '.join(FORMAT_READERS)}'")
     if download is not None and not isinstance(download, dict):
         raise TypeError("download must be a mapping of resolve_data_path options.")
-    if _is_remote(path):
+    from .resources import resolve_data_path
+
+    if _is_remote(path) and not str(path).lower().startswith(("http://", "https://")):
         raise ValueError(f"Remote catalogue '{path}' needs network access; fetch it and pass the local path.")
-    local = str(path)[7:] if str(path).startswith("file://") else str(path)
-    return FORMAT_READERS[data_format](local, **reader_params)
+    local = str(path)[7:] if str(path).startswith("file://") else path
+    return FORMAT_READERS[data_format](resolve_data_path(local, **(download or {})), **reader_params)
 
 
 def resolve_particle_value(particle_data, value_key, label="Particle value"):

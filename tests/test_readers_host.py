@@ -119,3 +119,35 @@ def test_corr3pcf_particle_centres_from_field_catalogue(golden_dir, oracle_kerne
     for k in ("ddd", "d_delta_dd", "rrr", "xi23", "r_delta_dd", "delta_ddd", "zeta"):
         ref = g["p3_" + k]
         assert np.abs(getattr(d, k) - ref).max() <= 1e-5 * np.abs(ref).max(), (k, getattr(d, k), ref)
+
+
+def test_catalogue_path_resolution(tmp_path):
+    """resolve_data_path (io/resources.py:87-160) as read_particle_data
+    uses it: SHA256 checks on local files, the deterministic cache path of
+    an http(s) catalogue, reuse of a cached copy without the network, and a
+    clear error for a catalogue that would need downloading."""
+    from pyhermes_gb300 import resources as rs
+
+    pos = np.arange(12, dtype=np.float32).reshape(4, 3)
+    local = tmp_path / "cat.bin"
+    pos.tofile(local)
+    digest = rs.file_sha256(local)
+    assert len(digest) == 64
+    d = read_particle_data(str(local), "bin", download={"sha256": "sha256:" + digest.upper()})
+    assert np.array_equal(d["pos"], pos)
+    with pytest.raises(ValueError, match="SHA256 mismatch"):
+        read_particle_data(str(local), "bin", download={"sha256": "0" * 64})
+    with pytest.raises(ValueError, match="64-character"):
+        read_particle_data(str(local), "bin", download={"sha256": "abc"})
+    url = "https://example.invalid/data/cat%201.bin"
+    assert rs.is_remote_url(url) and not rs.is_remote_url(str(local)) and not rs.is_remote_url(3)
+    target = rs.remote_cache_path(url, cache_dir=tmp_path / "cache")
+    assert target.name.endswith("-cat 1.bin") and len(target.name.split("-")[0]) == 12
+    with pytest.raises(ValueError, match="not in the cache"):
+        read_particle_data(url, "bin", download={"cache_dir": str(tmp_path / "cache")})
+    target.parent.mkdir(parents=True)
+    pos.tofile(target)
+    d = read_particle_data(url, "bin", download={"cache_dir": str(tmp_path / "cache"), "sha256": digest})
+    assert np.array_equal(d["pos"], pos)
+    with pytest.raises(ValueError, match="Set only one"):
+        rs.resolve_data_path(url, cache_path=str(target), cache_dir=str(tmp_path))
