@@ -190,7 +190,9 @@ def test_mixed_profile_bins_match_single_bins():
         assert f.shape == (L ** 3, 16) and torch.count_nonzero(f[:, len(bins):]) == 0
         for b, spec_b in enumerate(bins):
             one = mp.multipole_fields_bins(spec, J, l, m, [spec_b], 1000.0, P)
-            assert (f[:, b] - one).abs().max().item() <= 1e-6 * max(one.abs().max().item(), 1e-30), (l, m, b)
+            # batched and single-bin FFTs round differently: the bound of
+            # test_multi_bin_fields_match_single_bin
+            assert (f[:, b] - one).abs().max().item() <= 5e-6 * max(one.abs().max().item(), 1e-30), (l, m, b)
     eng = mp.MultipoleEngine(et, et, et, PHI, J, 1000.0)
     pairs = [(150.0, mp.BinSpec("sphere", {"R": 200.0})), (240.0, mp.BinSpec("sphere", {"R": 120.0}))]
     got = eng.ddd(pairs, 0, 2)
