@@ -25,8 +25,8 @@ import numpy as np
 import torch
 
 from .params import plain_copy, task_params
-from .sfc_field import (SFCField, check_fout, describe_input, normalize_task_weight_normalization, read_numpy_pickle,
-                        write_numpy_pickle)
+from .sfc_field import (ResultFileIO, SFCField, check_fout, describe_input, normalize_task_weight_normalization,
+                        read_numpy_pickle, write_numpy_pickle)
 from .window import (
     ANISOTROPIC_AUTO_WINDOW_TYPES, LOS_AWARE_WINDOW_TYPES, WindowFunc, materialized_pair_products, normalize_los_args,
     pair_products, rfft_field,
@@ -188,13 +188,15 @@ def build_binning_window_params_for_sample(sample, bw):
     return params
 
 
-class Corr2PCFData:
+class Corr2PCFData(ResultFileIO):
     """Result container (pyhermes/io/corr2pcf.py): sampling + products.
 
     The file written by ``save_corr2pcf`` / read by ``load_corr2pcf`` is the
     reference's NumPy-framed pickle with the same top-level keys and order:
     sfc_info1, sfc_info2, corr2pcf_info, sampling_names, the products
     dd .. xi, then one array per sampling name."""
+
+    _OWN_SAVE, _OWN_LOAD = "save_corr2pcf", "load_corr2pcf"
 
     def __init__(self, data_path=None):
         self.sampling_names = ()

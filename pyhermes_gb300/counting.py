@@ -16,8 +16,8 @@ import time
 import numpy as np
 
 from .params import task_params
-from .sfc_field import (SFCField, check_fout, describe_input, normalize_task_weight_normalization, read_numpy_pickle,
-                        write_numpy_pickle)
+from .sfc_field import (ResultFileIO, SFCField, check_fout, describe_input, normalize_task_weight_normalization,
+                        read_numpy_pickle, write_numpy_pickle)
 from .window import WindowFunc
 
 logger = logging.getLogger("pyhermes_gb300.Counting")
@@ -30,8 +30,10 @@ def random_box_positions(count, box_size, ndim=3, rng=None, seed=None):
     return rng.uniform(0.0, box_size, size=(count, ndim))
 
 
-class CountingData:
+class CountingData(ResultFileIO):
     """Result container (pyhermes/io/counting.py:9-62)."""
+
+    _OWN_SAVE, _OWN_LOAD = "save_counting", "load_counting"
 
     def __init__(self, data_path=None):
         self.sfc_info = {}

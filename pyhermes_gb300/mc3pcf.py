@@ -33,8 +33,8 @@ from . import _lib
 from .kernels import _ptr, _stream_ptr
 from .params import task_params
 from .phi import sample_scaling_function
-from .sfc_field import (SFCField, check_fout, describe_input, normalize_task_weight_normalization, read_numpy_pickle,
-                        write_numpy_pickle)
+from .sfc_field import (ResultFileIO, SFCField, check_fout, describe_input, normalize_task_weight_normalization,
+                        read_numpy_pickle, write_numpy_pickle)
 from .window import WindowFunc
 
 logger = logging.getLogger(__name__)
@@ -191,13 +191,15 @@ def _centre_arrays(pos, weight, pos_name, weight_name):
     return p, w
 
 
-class Corr3PCFData:
+class Corr3PCFData(ResultFileIO):
     """Result container (pyhermes/io/corr3pcf.py).  ``save_corr3pcf`` /
     ``load_corr3pcf`` use the reference's NumPy-framed pickle with the same
     top-level keys and order."""
 
     FILE_KEYS = ("sfc_info1", "sfc_info2", "sfc_info3", "corr3pcf_info", "mu", "theta", "r23", "ddd", "rrr",
                  "d_delta_dd", "r_delta_dd", "delta_ddd", "xi12", "xi13", "xi23", "zeta", "zeta_H", "Q")
+
+    _OWN_SAVE, _OWN_LOAD = "save_corr3pcf", "load_corr3pcf"
 
     def __init__(self, data_path=None):
         for k in self.FILE_KEYS:

@@ -32,8 +32,8 @@ from . import _lib
 from .kernels import _ptr, _stream_ptr
 from .params import task_params
 from .phi import cal_gamma, sample_scaling_function
-from .sfc_field import (SFCField, check_fout, describe_input, normalize_task_weight_normalization, read_numpy_pickle,
-                        write_numpy_pickle)
+from .sfc_field import (ResultFileIO, SFCField, check_fout, describe_input, normalize_task_weight_normalization,
+                        read_numpy_pickle, write_numpy_pickle)
 from .window import WindowFunc, phi_power_device, rfft_field
 
 logger = logging.getLogger("pyhermes_gb300.Corr_3PCF_Multipole")
@@ -492,7 +492,7 @@ def mixing_solve(A, B, lmax, device="cuda"):
     return C.cpu().numpy(), M.cpu().numpy(), cond.cpu().numpy()
 
 
-class Corr3PCFMultipoleData:
+class Corr3PCFMultipoleData(ResultFileIO):
     """Result container (pyhermes/io/corr3pcf_multipole.py:9-30).  The file
     written by ``save_corr3pcf_multipole`` / read by
     ``load_corr3pcf_multipole`` is the reference's NumPy-framed pickle with
@@ -501,6 +501,8 @@ class Corr3PCFMultipoleData:
     FILE_KEYS = ("sfc_info1", "sfc_info2", "sfc_info3", "corr3pcf_multipole_info", "sample_params",
                  "binning_window12", "binning_window13", "r12", "r13", "l", "ddd_l", "rrr_l", "delta_ddd_l",
                  "zeta_l", "zeta_condition")
+
+    _OWN_SAVE, _OWN_LOAD = "save_corr3pcf_multipole", "load_corr3pcf_multipole"
 
     def __init__(self, data_path=None):
         for k in self.FILE_KEYS:

@@ -120,6 +120,41 @@ def _normalize_pathlike(value):
     return value
 
 
+_SAVE_FLAGS = (("save_sfc_field", "save_sfc_field"), ("save_counting", "save_counting"),
+               ("save_2pcf", "save_corr2pcf"), ("save_3pcf", "save_corr3pcf"),
+               ("save_3pcf_multipole", "save_corr3pcf_multipole"))
+_READ_FLAGS = (("read_sfc_field", "load_sfc_field"), ("read_counting", "load_counting"),
+               ("read_2pcf", "load_corr2pcf"), ("read_3pcf", "load_corr3pcf"),
+               ("read_3pcf_multipole", "load_corr3pcf_multipole"))
+
+
+class ResultFileIO:
+    """The generic ``save`` / ``load`` of the reference's data containers
+    (io/base.py:24-124): a flag names the file kind, which must be the
+    container's own; without a flag the container's own kind is used."""
+
+    _OWN_SAVE = ""
+    _OWN_LOAD = ""
+
+    def save(self, f_out, save_sfc_field=False, save_counting=False, save_2pcf=False, save_3pcf=False,
+             save_3pcf_multipole=False, single=True, overwrite=False):
+        flags = dict(zip((k for k, _ in _SAVE_FLAGS),
+                         (save_sfc_field, save_counting, save_2pcf, save_3pcf, save_3pcf_multipole)))
+        picked = [m for k, m in _SAVE_FLAGS if flags[k]] or [self._OWN_SAVE]
+        if picked != [self._OWN_SAVE]:
+            raise ValueError(f"{type(self).__name__} cannot be saved as {picked[0].split('_', 1)[1]}.")
+        return getattr(self, self._OWN_SAVE)(f_out, overwrite=overwrite)
+
+    def load(self, f_in, read_sfc_field=False, read_counting=False, read_2pcf=False, read_3pcf=False,
+             read_3pcf_multipole=False, single=True):
+        flags = dict(zip((k for k, _ in _READ_FLAGS),
+                         (read_sfc_field, read_counting, read_2pcf, read_3pcf, read_3pcf_multipole)))
+        picked = [m for k, m in _READ_FLAGS if flags[k]] or [self._OWN_LOAD]
+        if picked != [self._OWN_LOAD]:
+            raise ValueError(f"{type(self).__name__} cannot read a {picked[0].split('_', 1)[1]} file.")
+        getattr(self, self._OWN_LOAD)(f_in)
+
+
 def describe_input(value):
     """A task input as the reference records it in result files
     (theory/corr2pcf.py:174-208): strings and 'uniform' as given, numbers as

@@ -156,3 +156,30 @@ def test_output_path_rules(golden_dir, tmp_path, oracle_kernels):
     d.counting_info, d.sfc_info, d.nx = {"seed": 1}, dict(f.sfc_info), np.arange(3.0)
     p = d.save_counting(str(tmp_path / "c.pkl"))
     assert d.save_counting(p) == str(tmp_path / "c_1.pkl")
+
+
+def test_result_containers_generic_save_load(tmp_path):
+    """io/base.py:24-124 on the result containers: save(..., save_2pcf=True)
+    / load(..., read_2pcf=True) and the flagless forms write and read the
+    container's own file; another kind's flag is refused."""
+    d = corr2pcf.Corr2PCFData()
+    d.set_sampling(("s",), {"s": np.array([1.0, 2.0])})
+    d.dd = np.array([3.0, 4.0])
+    d.corr2pcf_info = {"k": 1}
+    p1 = d.save(str(tmp_path / "c2.pkl"), save_2pcf=True)
+    p2 = d.save(str(tmp_path / "c2.pkl"))
+    assert p2.endswith("c2_1.pkl")
+    for p, kw in ((p1, {"read_2pcf": True}), (p2, {})):
+        e = corr2pcf.Corr2PCFData()
+        e.load(p, **kw)
+        assert np.array_equal(e.dd, d.dd) and np.array_equal(e.s, d.s)
+    with pytest.raises(ValueError):
+        d.save(str(tmp_path / "x.pkl"), save_counting=True)
+    with pytest.raises(ValueError):
+        corr2pcf.Corr2PCFData().load(p1, read_3pcf=True)
+    c = CountingData()
+    c.counting_info, c.sfc_info, c.nx = {"seed": 1}, {"J": 4}, np.arange(3.0)
+    q = c.save(str(tmp_path / "n.pkl"), save_counting=True)
+    c2 = CountingData()
+    c2.load(q, read_counting=True)
+    assert np.array_equal(c2.nx, c.nx)
