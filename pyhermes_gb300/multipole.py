@@ -607,6 +607,38 @@ class Corr_3PCF_Multipole:
                                "check J convergence.", name, self.l_max, pos.min(), q, ratio)
         return out
 
+    def _radial_profile_diagnostics(self):
+        """theory/corr3pcf_multipole.py:668-718: every tabulated radial
+        window of both edges checked per sample and l (from l_min, or 1 for
+        built-in profiles whose monopole is analytic), with a warning for a
+        table that misses the tolerance."""
+        from .radial_profiles import diagnose_radial_multipole_table
+
+        out = []
+        tp = self.task_params
+        if not bool(tp.get("radial_profile_diagnostics", True)):
+            return out
+        tol = float(tp.get("radial_profile_diagnostic_tolerance", 1e-5))
+        probes = int(tp.get("radial_profile_diagnostic_probes", 33))
+        k_max = float(np.sqrt(3.0) * self.reference.L / self.reference.box_size)
+        for name, windows in (("binning_window12", self.binning_window12), ("binning_window13", self.binning_window13)):
+            for idx, params in enumerate(windows):
+                kind = str(params["type"]).strip().lower()
+                if kind == "shell" or (kind == "gaussian_shell" and float(params["len_args"]["R_smooth"]) == 0.0):
+                    continue
+                first = self.l_min if kind.startswith("custom_") else max(1, self.l_min)
+                for l in range(first, self.l_max + 1):
+                    d = diagnose_radial_multipole_table(kind, params["len_args"], l, k_max,
+                                                        profile_config=params.get("other_args", {}), tolerance=tol,
+                                                        probe_count=probes)
+                    d.update({"edge": name, "sample_idx": int(idx)})
+                    out.append(d)
+                    if not d["passed"]:
+                        logger.warning("Radial profile diagnostic exceeded tolerance | %s[%d], type=%s, l=%d, "
+                                       "tolerance=%.3e. Increase profile quadrature/table points or verify the "
+                                       "profile support.", name, idx, kind, l, tol)
+        return out
+
     def _info_snapshot(self, expanded):
         """corr3pcf_multipole_info with the reference's keys
         (theory/corr3pcf_multipole.py:767 and the task parameters)."""
@@ -637,7 +669,7 @@ class Corr_3PCF_Multipole:
                      "radial_profile_diagnostic_probes": int(tp.get("radial_profile_diagnostic_probes", 33)),
                      "expanded_products": list(expanded),
                      "resolution_diagnostics": self._resolution_diagnostics(),
-                     "radial_profile_diagnostics_result": [],
+                     "radial_profile_diagnostics_result": list(getattr(self, "radial_profile_diagnostics", [])),
                      "rho_vertices": list(getattr(self, "rho_vertices", [None, None, None])),
                      "fout_path": self.fout_path})
         return info
@@ -752,6 +784,7 @@ class Corr_3PCF_Multipole:
                     base = self._normalized(self._resolve(r, f"random vertex {i}"))
                     w = getattr(self, f"window{i}")
                     self.rand[i] = base @ WindowFunc(w, base.sfc_info, device=self.device) if w else base.copy()
+        self.radial_profile_diagnostics = self._radial_profile_diagnostics()
         self._fields_prepared = True
 
     def _uniform_random_after_window(self, base, rho, w, vertex):

@@ -318,6 +318,102 @@ def build_radial_multipole_table(radial_type, len_args, l, k_max, profile_config
     return out
 
 
+DIAGNOSTIC_PROBES = 33
+
+
+def _quadrature(kind, len_args, profile_config, k_max):
+    """Normalised (radii, weights, w(r), options) of a tabulated profile."""
+    if kind in ("sphere", "thick_shell", "gaussian", "custom_real"):
+        r, w, vals, opts = _real_profile(kind, len_args, profile_config, k_max)
+    elif kind in ("gaussian_shell", "custom_kspace"):
+        r, w, vals, opts = _inverse_profile(kind, len_args, profile_config, k_max)
+    else:
+        raise ValueError(f"Unsupported tabulated radial profile '{kind}'.")
+    return r, w, _normalise(r, w, vals, opts), opts
+
+
+def _forward_hankel(r, w, vals, l, k):
+    """U_l(k) = sum_i 4 pi w_i r_i^2 w(r_i) j_l(2 pi k r_i)."""
+    pre = 4.0 * np.pi * w * r ** 2 * vals
+    out = np.empty(k.size)
+    for s in range(0, k.size, 64):
+        out[s:s + 64] = spherical_jn(int(l), 2.0 * np.pi * np.outer(k[s:s + 64], r)) @ pre
+    return out
+
+
+def interpolate_uniform_table(k, table, k_max):
+    """The table lookup the GPU kernel makes (utils/radial_profiles.py:
+    514-540): linear in the first and last intervals, the four-point local
+    cubic (Catmull-Rom form) inside, the last entry at and beyond k_max."""
+    k = np.clip(np.asarray(k, dtype=np.float64), 0.0, float(k_max))
+    x = k * (table.size - 1) / float(k_max)
+    i = np.floor(x).astype(np.intp)
+    t = x - i
+    top = i >= table.size - 1
+    i = np.minimum(i, table.size - 2)
+    out = table[i] * (1.0 - t) + table[i + 1] * t
+    mid = (i > 0) & (i < table.size - 2)
+    if np.any(mid):
+        j, u = i[mid], t[mid]
+        p0, p1, p2, p3 = table[j - 1], table[j], table[j + 1], table[j + 2]
+        out[mid] = 0.5 * (2.0 * p1 + (p2 - p0) * u + (2.0 * p0 - 5.0 * p1 + 4.0 * p2 - p3) * u * u
+                          + (3.0 * p1 - p0 - 3.0 * p2 + p3) * u * u * u)
+    out[top] = table[-1]
+    return out
+
+
+def diagnose_radial_multipole_table(radial_type, len_args, l, k_max, profile_config=None, *, tolerance=1.0e-5,
+                                    probe_count=DIAGNOSTIC_PROBES):
+    """Normalisation and convergence of one U_l table
+    (utils/radial_profiles.py:559-648): the table at probe_count mid-point
+    probes against a transform with doubled quadrature, the k = 0 value
+    against 4 pi int r^2 w (l = 0) or 0, and for k-space profiles at l = 0
+    the inverse / forward Hankel round trip against the given transfer."""
+    kind = str(radial_type).strip().lower()
+    if kind not in SUPPORTED:
+        raise ValueError(f"Unsupported radial profile '{kind}'. Supported profiles: {', '.join(sorted(SUPPORTED))}.")
+    if kind == "shell" or (kind == "gaussian_shell" and float(len_args["R_smooth"]) == 0.0):
+        return {"radial_type": kind, "l": int(l), "path": "analytic_shell", "passed": True}
+    if not np.isfinite(tolerance) or tolerance <= 0.0:
+        raise ValueError("Radial-profile diagnostic tolerance must be finite and positive.")
+    probe_count = int(probe_count)
+    if probe_count < 3:
+        raise ValueError("Radial-profile diagnostics require at least three probe points.")
+    table_k_max, table = build_radial_multipole_table(kind, len_args, l, k_max, profile_config)
+    r, w, vals, _ = _quadrature(kind, len_args, profile_config, k_max)
+    refined = dict(profile_config or {})
+    refined["quadrature_points"] = max(2 * int(r.size), 2 * QUAD_MIN)
+    if kind in ("gaussian_shell", "custom_kspace"):
+        refined["inverse_points"] = refined["quadrature_points"]
+    rr, rw, rv, _ = _quadrature(kind, len_args, refined, k_max)
+    probe_k = float(k_max) * (np.arange(probe_count, dtype=np.float64) + 0.5) / probe_count
+    exact = _forward_hankel(rr, rw, rv, l, probe_k)
+    convergence = float(np.max(np.abs(interpolate_uniform_table(probe_k, table, table_k_max) - exact))
+                        / max(1.0, float(np.max(np.abs(exact)))))
+    zero_target = float(4.0 * np.pi * np.sum(w * r ** 2 * vals)) if int(l) == 0 else 0.0
+    zero_mode = float(table[0])
+    roundtrip = None
+    if kind in ("gaussian_shell", "custom_kspace") and int(l) == 0:
+        if kind == "gaussian_shell":
+            given = monopole_transfer("gaussian_shell", probe_k, len_args)
+        else:
+            spec = _profile_spec(profile_config)
+            kw = dict(spec.get("args", {}))
+            kw.update(len_args)
+            given = np.asarray(spec["func"](probe_k, **kw), dtype=np.float64)
+            if given.ndim == 0:
+                given = np.full(probe_k.shape, float(given))
+        back = _forward_hankel(r, w, vals, 0, probe_k)
+        roundtrip = float(np.max(np.abs(back - given)) / max(1.0, float(np.max(np.abs(given)))))
+    errors = [convergence, abs(zero_mode - zero_target)] + ([roundtrip] if roundtrip is not None else [])
+    return {"radial_type": kind, "l": int(l),
+            "path": "inverse_hankel" if kind in ("gaussian_shell", "custom_kspace") else "real_space_hankel",
+            "table_points": int(table.size), "quadrature_points": int(r.size), "refined_quadrature_points": int(rr.size),
+            "probe_count": probe_count, "zero_mode": zero_mode, "zero_mode_target": zero_target,
+            "zero_mode_error": float(abs(zero_mode - zero_target)), "table_convergence_error": convergence,
+            "inverse_roundtrip_error": roundtrip, "tolerance": float(tolerance), "passed": bool(max(errors) <= tolerance)}
+
+
 def profile_mode(radial_type, len_args, l):
     """How the GPU evaluates U_l for one bin (radial_multipole_windows.py:
     269-313): 'shell' (j_l(2 pi k R), with R = R_shell for gaussian_shell with

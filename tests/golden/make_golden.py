@@ -904,6 +904,34 @@ def gen_tabulated():
           rrr_l=d.rrr_l, **out)
 
 
+def gen_radial_diagnostics():
+    """diagnose_radial_multipole_table (utils/radial_profiles.py:559-648) for
+    built-in profiles, and the multipole task's per-sample diagnostics
+    (theory/corr3pcf_multipole.py:668-718) after prepare_input_fields."""
+    from pyhermes.theory.corr3pcf_multipole import Corr_3PCF_Multipole
+    from pyhermes.utils.radial_profiles import diagnose_radial_multipole_table
+
+    kmax = np.sqrt(3.0) * 16 / 1000.0
+    cases = [("thick_shell", {"R": 150.0, "delta_R": 60.0}, 1, {}), ("gaussian", {"R": 80.0}, 2, {}),
+             ("sphere", {"R": 120.0}, 0, {}), ("gaussian_shell", {"R_shell": 150.0, "R_smooth": 40.0}, 0, {}),
+             ("gaussian_shell", {"R_shell": 150.0, "R_smooth": 40.0}, 2, {"quadrature_points": 600}),
+             ("shell", {"R": 100.0}, 3, {}), ("sphere", {"R": 120.0}, 1, {"table_points": 64})]
+    direct = [diagnose_radial_multipole_table(k, la, l, kmax, profile_config=pc) for k, la, l, pc in cases]
+    rng = np.random.default_rng(23)
+    pos = rng.uniform(0.0, 1000.0, (1000, 3))
+    f = _projection(pos, 4)
+    task = Corr_3PCF_Multipole({"Corr_3PCF_Multipole": {
+        "sfc_field": f, "random": "uniform",
+        "binning_window12": {"type": "thick_shell", "len_args": {"delta_R": 50.0}, "other_args": {},
+                             "mapping": {"R": "r12"}},
+        "binning_window13": {"type": "sphere", "len_args": {}, "other_args": {}, "mapping": {"R": "r13"}},
+        "sampling": {"mode": "paired", "r12": [150.0, 200.0], "r13": [250.0, 300.0]},
+        "l_min": 0, "l_max": 2, "products": ["ddd_l"], "summation_backend": "cpu"}})
+    task.prepare_input_fields()
+    _save("radial_diagnostics_J4", pos=pos, direct=np.array(_info_json({"d": direct})),
+          task=np.array(_info_json({"d": task.radial_profile_diagnostics})))
+
+
 def gen_window_file():
     from pyhermes.io.window import WindowFunc
 
@@ -913,7 +941,7 @@ def gen_window_file():
     _save("window_file_J4", kernel=kernel)
 
 
-SECTIONS = {"phi_at_pos": gen_phi_at_pos, "full_fft_windows": gen_full_fft_windows, "custom_windows": gen_custom_windows, "mc_theta": gen_mc_theta, "composite_windows": gen_composite_windows, "particle_data": gen_particle_data, "catalogues": gen_catalogues, "field_algebra": gen_field_algebra, "rppi": gen_rppi, "io": gen_io, "cross": gen_cross, "normalization": gen_normalization, "mc3pcf_randoms": gen_mc3pcf_randoms, "random_catalogue": gen_random_catalogue, "mc3pcf_particle": gen_mc3pcf_particle, "window_file": gen_window_file, "tabulated": gen_tabulated, "counting": gen_counting, "mc3pcf": gen_mc3pcf, "phi": gen_phi, "deposit": gen_deposit, "windows": gen_windows,
+SECTIONS = {"radial_diagnostics": gen_radial_diagnostics, "phi_at_pos": gen_phi_at_pos, "full_fft_windows": gen_full_fft_windows, "custom_windows": gen_custom_windows, "mc_theta": gen_mc_theta, "composite_windows": gen_composite_windows, "particle_data": gen_particle_data, "catalogues": gen_catalogues, "field_algebra": gen_field_algebra, "rppi": gen_rppi, "io": gen_io, "cross": gen_cross, "normalization": gen_normalization, "mc3pcf_randoms": gen_mc3pcf_randoms, "random_catalogue": gen_random_catalogue, "mc3pcf_particle": gen_mc3pcf_particle, "window_file": gen_window_file, "tabulated": gen_tabulated, "counting": gen_counting, "mc3pcf": gen_mc3pcf, "phi": gen_phi, "deposit": gen_deposit, "windows": gen_windows,
             "convolution": gen_convolution, "corr2pcf": gen_corr2pcf, "multipole": gen_multipole}
 
 
