@@ -81,12 +81,10 @@ class Counting:
         self.counting_data = CountingData()
 
     def _snapshot(self):
-        win = self.window
-        if isinstance(win, WindowFunc):
-            win = dict(getattr(win, "input_params", {}) or {})
+        # a window as theory/counting.py:89-100 records it
         return {"sfc_field": describe_input(self._sfc_input), "random_count": self.random_count, "seed": self.seed,
-                "weight_normalization": self.weight_normalization, "window": win, "threads": self.threads,
-                "fout_path": self.fout_path}
+                "weight_normalization": self.weight_normalization, "window": describe_input(self.window),
+                "threads": self.threads, "fout_path": self.fout_path}
 
     def prepare_input_fields(self, sfc_field=None, window=None):
         sfc_field = self.sfc_field if sfc_field is None else sfc_field
