@@ -554,8 +554,10 @@ class Corr_3PCF_Multipole:
             setattr(self, f"window{i}", wi or (dict(self.window) if self.window else None))
         self.sampling = self._normalize_sampling(tp.get("sampling"))
         self.samples = self._expand_sampling(self.sampling)
-        self.binning_window12 = [self._sample_window(tp.get("binning_window12"), s) for s in self.samples]
-        self.binning_window13 = [self._sample_window(tp.get("binning_window13"), s) for s in self.samples]
+        t12 = self.binning_window12_template = self._edge_template(tp.get("binning_window12"), "binning_window12")
+        t13 = self.binning_window13_template = self._edge_template(tp.get("binning_window13"), "binning_window13")
+        self.binning_window12 = [self._sample_window(t12, s, "binning_window12") for s in self.samples]
+        self.binning_window13 = [self._sample_window(t13, s, "binning_window13") for s in self.samples]
         self.l_min = int(tp["l_min"])
         self.l_max = int(tp["l_max"])
         if self.l_min < 0 or self.l_max < 0 or self.l_min > self.l_max:
@@ -654,8 +656,8 @@ class Corr_3PCF_Multipole:
             info[f"window{i}"] = describe_input(getattr(self, f"window{i}"))
         sampling = {"mode": self.sampling["mode"],
                     "values": {k: [float(x) for x in v] for k, v in self.sampling["values"].items()}}
-        info.update({"binning_window12_template": describe_input(tp.get("binning_window12")),
-                     "binning_window13_template": describe_input(tp.get("binning_window13")),
+        info.update({"binning_window12_template": describe_input(self.binning_window12_template),
+                     "binning_window13_template": describe_input(self.binning_window13_template),
                      "sampling": sampling, "n_samples": len(self.samples), "l_min": self.l_min, "l_max": self.l_max,
                      "gpu_device_id": int(tp.get("gpu_device_id", 0) or 0),
                      "gpu_threads_per_block": list(tp.get("gpu_threads_per_block") or [8, 8, 8]),
@@ -714,20 +716,48 @@ class Corr_3PCF_Multipole:
             raise ValueError("sampling.mode='paired' requires each parameter to have length 1 or the shared length.")
         return [{k: float(a[0] if a.size == 1 else a[i]) for k, a in values.items()} for i in range(n)]
 
-    def _sample_window(self, template, sample):
+    @staticmethod
+    def _edge_template(value, name):
+        """theory/corr3pcf_multipole.py:205-227: a binning-window template
+        with a non-empty (lower-cased) type and dict len_args / other_args /
+        mapping (None read as empty)."""
+        if not isinstance(value, dict):
+            raise TypeError(f"{name} must be a dictionary.")
+        if not value.get("type"):
+            raise ValueError(f"{name} must define a non-empty 'type'.")
+        params = copy.deepcopy(value)
+        params["type"] = str(params["type"]).strip().lower()
+        for key in ("len_args", "other_args", "mapping"):
+            if params.get(key) is None:
+                params[key] = {}
+            if not isinstance(params[key], dict):
+                raise TypeError(f"{name}.{key} must be a dictionary.")
+        return params
+
+    def _sample_window(self, template, sample, name="binning window"):
+        """theory/corr3pcf_multipole.py:296-324: mapping targets 'X' or
+        'len_args.X' / 'other_args.X' take a sampling parameter (by name)
+        or a number."""
         params = copy.deepcopy(template)
         mapping = params.pop("mapping", {}) or {}
         params["len_args"] = copy.deepcopy(params.get("len_args", {}) or {})
         params["other_args"] = copy.deepcopy(params.get("other_args", {}) or {})
         for target, source in mapping.items():
-            value = float(sample[source]) if isinstance(source, str) else float(source)
+            if isinstance(source, str):
+                if source not in sample:
+                    raise KeyError(f"Sampling parameter '{source}' is not defined.")
+                value = float(sample[source])
+            else:
+                value = float(source)
             if "." in target:
                 sec, key = target.split(".", 1)
+                if sec not in ("len_args", "other_args"):
+                    raise ValueError(f"Unsupported binning-window mapping target '{target}'.")
                 params.setdefault(sec, {})[key] = value
             else:
                 params["len_args"][target] = value
         if not params["len_args"]:
-            raise ValueError("binning window produced an empty len_args dictionary.")
+            raise ValueError(f"{name} produced an empty len_args dictionary.")
         return params
 
     # ---- inputs ----------------------------------------------------------------

@@ -4,6 +4,7 @@ binning windows carry the reference mapping (corr2pcf.py mapping_smu_to_RH)."""
 import copy
 
 import numpy as np
+import pytest
 
 from pyhermes_gb300.corr2pcf import build_binning_window_params_for_sample, normalize_binning_window
 from pyhermes_gb300.params import plain_copy
@@ -67,3 +68,33 @@ def test_reference_import_paths():
     assert SFCField is sfc_field.SFCField and check_fout is sfc_field.check_fout and callable(resolve_data_path)
     assert (Corr2PCFData, Corr3PCFData, Corr3PCFMultipoleData, CountingData) == (
         corr2pcf.Corr2PCFData, mc3pcf.Corr3PCFData, multipole.Corr3PCFMultipoleData, counting.CountingData)
+
+
+def test_multipole_binning_template_rules():
+    """theory/corr3pcf_multipole.py:205-227, 296-324: template checks and
+    mapping targets."""
+    from pyhermes_gb300.multipole import Corr_3PCF_Multipole
+
+    def task(bw12, sampling=None):
+        return Corr_3PCF_Multipole({"Corr_3PCF_Multipole": {
+            "binning_window12": bw12,
+            "binning_window13": {"type": "shell", "len_args": {}, "other_args": {}, "mapping": {"R": "r13"}},
+            "sampling": sampling or {"mode": "paired", "r12": [100.0], "r13": [200.0]},
+            "l_min": 0, "l_max": 1}}, device="cpu")
+
+    t = task({"type": " Thick_Shell ", "len_args": None, "other_args": None,
+              "mapping": {"R": "r12", "len_args.delta_R": 40.0, "other_args.x": "r13"}})
+    w = t.binning_window12[0]
+    assert w["type"] == "thick_shell" and w["len_args"] == {"R": 100.0, "delta_R": 40.0}
+    assert w["other_args"] == {"x": 200.0} and "mapping" not in w
+    assert t.binning_window12_template["type"] == "thick_shell"
+    with pytest.raises(ValueError, match="non-empty 'type'"):
+        task({"type": "", "mapping": {"R": "r12"}})
+    with pytest.raises(TypeError, match="mapping must be a dictionary"):
+        task({"type": "shell", "mapping": [("R", "r12")]})
+    with pytest.raises(KeyError, match="not defined"):
+        task({"type": "shell", "mapping": {"R": "s"}})
+    with pytest.raises(ValueError, match="Unsupported binning-window mapping target"):
+        task({"type": "shell", "mapping": {"R": "r12", "los_args.nx": 1.0}})
+    with pytest.raises(ValueError, match="empty len_args"):
+        task({"type": "shell", "mapping": {}})
