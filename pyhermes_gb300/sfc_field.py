@@ -338,6 +338,14 @@ class SFCField:
             return convolve_field(self, other)
         return NotImplemented
 
+    def __rmatmul__(self, other):
+        """io/sfc_field.py:157-160: field @ window reached from the window's side."""
+        from .window import convolve_field
+
+        if isinstance(other, SFCField) and getattr(self, "is_window", False):
+            return convolve_field(other, self)
+        return NotImplemented
+
     # ---- normalisation -----------------------------------------------------
     def _normalization_denominator(self, weight_normalization):
         """pyhermes/io/sfc_field.py:340-352."""
