@@ -744,7 +744,7 @@ __global__ void __launch_bounds__(ct::kThreads, 2) mp_contract_kernel(ContractAr
     }
     cp_async_wait<0>();
     // fixed-order reduction of the eight cell slices (lanes, then the warp
-    // pair in two ordered rounds), float64 per CTA
+    // pair in two ordered passes), float64 per CTA
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
       S[q].x += __shfl_xor_sync(0xffffffffu, S[q].x, 1);
@@ -762,7 +762,7 @@ __global__ void __launch_bounds__(ct::kThreads, 2) mp_contract_kernel(ContractAr
           dacc[o + 1] += (double)S[q].y;
         }
       }
-      __syncthreads();  // round 1 after round 0; all buffers idle before the next item
+      __syncthreads();  // pass 1 after pass 0; all buffers idle before the next item
     }
   }
   for (int i = tid; i < 2 * kMaxBins * kMaxBins; i += ct::kThreads)
