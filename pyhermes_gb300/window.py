@@ -170,9 +170,12 @@ def custom_window_kernel(func, args, L, bandwidth, power, mode, rows=8):
             arr[x0:x0 + xs.size] = acc
         X, Xm = np.arange(L), L - np.arange(L)
         Y, Ym, Z, Zm = y, L - y, z, L - z
-        return (arr[np.ix_(X, Y, Z)] + arr[np.ix_(Xm, Y, Z)] + arr[np.ix_(X, Ym, Z)] + arr[np.ix_(X, Y, Zm)]
-                + arr[np.ix_(Xm, Ym, Z)] + arr[np.ix_(Xm, Y, Zm)] + arr[np.ix_(X, Ym, Zm)]
-                + arr[np.ix_(Xm, Ym, Zm)])
+        # the reference's left-to-right sum of the eight reflections, one
+        # gathered term at a time
+        out = arr[np.ix_(X, Y, Z)]
+        for ix, iy, iz in ((Xm, Y, Z), (X, Ym, Z), (X, Y, Zm), (Xm, Ym, Z), (Xm, Y, Zm), (X, Ym, Zm), (Xm, Ym, Zm)):
+            out += arr[np.ix_(ix, iy, iz)]
+        return out
     if mode not in ("full_rfft", "complex_rfft"):
         raise ValueError(f"Custom window functions do not support kernel_mode='{mode}'. "
                          "Use a real or complex RFFT kernel mode.")
