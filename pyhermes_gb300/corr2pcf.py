@@ -188,6 +188,34 @@ def build_binning_window_params_for_sample(sample, bw):
     return params
 
 
+def compute_pair_product_at_sample(sample, sfc_field1, sfc_field2=None, binning_window=None):
+    """One pair product in grid units at one sample (theory/corr2pcf.py:
+    375-382): the product of mean densities when a vertex is a scalar, else
+    the mean over cells of (field1 convolved with the sample's binning
+    window) * field2, on the GPU."""
+    if sfc_field2 is None:
+        sfc_field2 = sfc_field1
+    if _is_scalar(sfc_field1) or _is_scalar(sfc_field2):
+        return field_mean_density(sfc_field1) * field_mean_density(sfc_field2)
+    params = build_binning_window_params_for_sample(sample, normalize_binning_window(binning_window))
+    window = WindowFunc(params, sfc_field1.sfc_info, threads=getattr(sfc_field1, "threads", None),
+                        device=sfc_field1.device)
+    e1 = sfc_field1.epsilon_device.to(torch.float32).contiguous()
+    e2 = e1 if sfc_field2 is sfc_field1 else sfc_field2.epsilon_device.to(torch.float32).contiguous()
+    if window.materialized:
+        v, _ = materialized_pair_products([e1, e2], [(0, 1)], [window], exclude_k0=False)
+        return float(v[0, 0])
+    if window.resolved_mode() == "complex_full_fft":
+        raise ValueError("A complex full-FFT window has no rFFT pair product.")
+    s1 = rfft_field(e1)
+    specs, pair = ([s1], (0, 0)) if e2 is e1 else ([s1, rfft_field(e2)], (0, 1))
+    v, k0 = pair_products(specs, [pair], [window], exclude_k0=True)
+    # the k = 0 term in float64
+    dc1 = float(e1.double().sum().item())
+    dc2 = dc1 if e2 is e1 else float(e2.double().sum().item())
+    return float(v[0, 0] + dc1 * dc2 * k0[0] / float(e1.shape[0]) ** 6)
+
+
 class Corr2PCFData(ResultFileIO):
     """Result container (pyhermes/io/corr2pcf.py): sampling + products.
 
@@ -380,6 +408,12 @@ class Corr_2PCF:
         self._fields_prepared = True
 
     # ---- products ---------------------------------------------------------------
+    def calc_pair_product(self, sample, field1, field2=None, binning_window=None):
+        """theory/corr2pcf.py:632-645: one pair product at one sample with
+        the task's binning window (or the one given)."""
+        return compute_pair_product_at_sample(sample, field1, field2,
+                                              self.binning_window if binning_window is None else binning_window)
+
     def _binning_windows(self, ref_field):
         bws = []
         for idx in itertools.product(*(range(self.sampling_arrays[n].size) for n in self.sampling_names)):

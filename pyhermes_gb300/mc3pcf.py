@@ -357,6 +357,11 @@ class Corr_3PCF:
         t._density_physical_scale = 1.0
         return np.asarray(t.run(save_result=False).dd)
 
+    def calc_pair_product(self, radius, field1, field2):
+        """theory/corr3pcf.py:730-734: the thin-shell pair product at radius
+        (a scalar vertex gives the product of mean densities)."""
+        return self._pair(radius, field1, field2)
+
     def run(self, save_result=True, overwrite=False):
         data = {i: self._windowed(i, self._field(getattr(self, f"sfc_field{i}"), f"field vertex {i}"))
                 for i in (1, 2, 3)}

@@ -932,6 +932,24 @@ def gen_radial_diagnostics():
           task=np.array(_info_json({"d": task.radial_profile_diagnostics})))
 
 
+def gen_pair_at_sample():
+    """Corr_2PCF.calc_pair_product / compute_pair_product_at_sample
+    (theory/corr2pcf.py:375-382, 632-645): grid-unit pair products at one
+    sample, and a scalar vertex."""
+    from pyhermes.theory.corr2pcf import Corr_2PCF, compute_pair_product_at_sample
+
+    rng = np.random.default_rng(52)
+    pos = rng.uniform(0.0, 1000.0, (3000, 3))
+    pos[:1000] = pos[:1000] * 0.3 + 300.0
+    f = _projection(pos, 4)
+    bw = {"type": "thick_shell", "len_args": {"R": None, "delta_R": 60.0}, "mapping": "s_to_R"}
+    v1 = compute_pair_product_at_sample({"s": 150.0}, f, None, bw)
+    task = Corr_2PCF({"Corr_2PCF": {"sfc_field": f, "binning_window": bw, "sampling": {"s": [150.0]}}})
+    v2 = task.calc_pair_product({"s": 220.0}, f)
+    v3 = task.calc_pair_product({"s": 220.0}, f, 2.5e-4)
+    _save("pair_at_sample_J4", pos=pos, values=np.array([v1, v2, v3]))
+
+
 def gen_window_file():
     from pyhermes.io.window import WindowFunc
 
@@ -941,7 +959,7 @@ def gen_window_file():
     _save("window_file_J4", kernel=kernel)
 
 
-SECTIONS = {"radial_diagnostics": gen_radial_diagnostics, "phi_at_pos": gen_phi_at_pos, "full_fft_windows": gen_full_fft_windows, "custom_windows": gen_custom_windows, "mc_theta": gen_mc_theta, "composite_windows": gen_composite_windows, "particle_data": gen_particle_data, "catalogues": gen_catalogues, "field_algebra": gen_field_algebra, "rppi": gen_rppi, "io": gen_io, "cross": gen_cross, "normalization": gen_normalization, "mc3pcf_randoms": gen_mc3pcf_randoms, "random_catalogue": gen_random_catalogue, "mc3pcf_particle": gen_mc3pcf_particle, "window_file": gen_window_file, "tabulated": gen_tabulated, "counting": gen_counting, "mc3pcf": gen_mc3pcf, "phi": gen_phi, "deposit": gen_deposit, "windows": gen_windows,
+SECTIONS = {"pair_at_sample": gen_pair_at_sample, "radial_diagnostics": gen_radial_diagnostics, "phi_at_pos": gen_phi_at_pos, "full_fft_windows": gen_full_fft_windows, "custom_windows": gen_custom_windows, "mc_theta": gen_mc_theta, "composite_windows": gen_composite_windows, "particle_data": gen_particle_data, "catalogues": gen_catalogues, "field_algebra": gen_field_algebra, "rppi": gen_rppi, "io": gen_io, "cross": gen_cross, "normalization": gen_normalization, "mc3pcf_randoms": gen_mc3pcf_randoms, "random_catalogue": gen_random_catalogue, "mc3pcf_particle": gen_mc3pcf_particle, "window_file": gen_window_file, "tabulated": gen_tabulated, "counting": gen_counting, "mc3pcf": gen_mc3pcf, "phi": gen_phi, "deposit": gen_deposit, "windows": gen_windows,
             "convolution": gen_convolution, "corr2pcf": gen_corr2pcf, "multipole": gen_multipole}
 
 

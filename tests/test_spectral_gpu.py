@@ -221,3 +221,20 @@ def test_corr2pcf_rppi_sampling_matches_reference(golden_dir, kind):
         "products": ["delta_dd", "xi"]}}).run(save_result=False)
     for k in ("delta_dd", "xi"):
         assert _rel(getattr(d, k), g[f"{kind}_{k}"]) <= 1e-5, (kind, k)
+
+
+def test_pair_product_at_sample_matches_reference(golden_dir):
+    """compute_pair_product_at_sample / Corr_2PCF.calc_pair_product on the
+    GPU (theory/corr2pcf.py:375-382, 632-645)."""
+    from pyhermes_gb300 import corr2pcf
+    from pyhermes_gb300.projection import SFCProjection
+
+    g = np.load(os.path.join(golden_dir, "pair_at_sample_J4.npz"))
+    f = SFCProjection({"SFCProjection": {"particle_pos": g["pos"], "J": 4, "box_size": 1000.0}}).run(
+        save_result=False)
+    bw = {"type": "thick_shell", "len_args": {"R": None, "delta_R": 60.0}, "mapping": "s_to_R"}
+    v1 = corr2pcf.compute_pair_product_at_sample({"s": 150.0}, f, None, bw)
+    task = corr2pcf.Corr_2PCF({"Corr_2PCF": {"sfc_field": f, "binning_window": bw, "sampling": {"s": [150.0]}}})
+    v2 = task.calc_pair_product({"s": 220.0}, f)
+    v3 = task.calc_pair_product({"s": 220.0}, f, 2.5e-4)
+    np.testing.assert_allclose([v1, v2, v3], g["values"], rtol=1e-5)

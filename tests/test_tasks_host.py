@@ -260,3 +260,19 @@ def test_mc3pcf_theta_sampling_matches_reference(golden_dir, oracle_kernels, mon
         np.testing.assert_allclose(getattr(d, k), g[f"{case}_{k}"], rtol=1e-14, atol=1e-14)
     for k in ("ddd", "rrr", "delta_ddd", "xi23"):
         assert _rel(getattr(d, k), g[f"{case}_{k}"]) < 1e-5, (k, getattr(d, k), g[f"{case}_{k}"])
+
+
+def test_pair_product_at_sample_matches_reference(golden_dir, oracle_kernels):
+    """compute_pair_product_at_sample and Corr_2PCF.calc_pair_product
+    (theory/corr2pcf.py:375-382, 632-645) in grid units, a scalar vertex
+    included."""
+    g = np.load(os.path.join(golden_dir, "pair_at_sample_J4.npz"))
+    f = SFCProjection({"SFCProjection": {"particle_pos": g["pos"], "J": 4, "box_size": 1000.0}},
+                      device="cpu").run(save_result=False)
+    bw = {"type": "thick_shell", "len_args": {"R": None, "delta_R": 60.0}, "mapping": "s_to_R"}
+    v1 = corr2pcf.compute_pair_product_at_sample({"s": 150.0}, f, None, bw)
+    task = corr2pcf.Corr_2PCF({"Corr_2PCF": {"sfc_field": f, "binning_window": bw, "sampling": {"s": [150.0]}}},
+                              device="cpu")
+    v2 = task.calc_pair_product({"s": 220.0}, f)
+    v3 = task.calc_pair_product({"s": 220.0}, f, 2.5e-4)
+    np.testing.assert_allclose([v1, v2, v3], g["values"], rtol=1e-5)
