@@ -287,6 +287,11 @@ class Corr_2PCF:
         self.task_params = task_params(self.task_name, param_task)
         self.device = torch.device(device)
         self.rank, self.size = 0, 1
+        self.format_params()
+
+    def format_params(self):
+        """The task parameters into attributes (theory/corr2pcf.py:419-470); call again after
+        editing task_params."""
         tp = self.task_params
         self.sfc_field = tp.get("sfc_field", "")
         self.sfc_field1 = tp.get("sfc_field1", "") or self.sfc_field

@@ -228,9 +228,14 @@ class Corr_3PCF:
     task_name = "Corr_3PCF"
 
     def __init__(self, param_task=None, device="cuda"):
-        tp = task_params(self.task_name, param_task)
-        self.task_params = tp
+        self.task_params = task_params(self.task_name, param_task)
         self.device = torch.device(device)
+        self.format_params()
+
+    def format_params(self):
+        """The task parameters into attributes (theory/corr3pcf.py:154-230); call again after
+        editing task_params."""
+        tp = self.task_params
         self.sfc_field = tp.get("sfc_field", "")
         for i in (1, 2, 3):
             setattr(self, f"sfc_field{i}", tp.get(f"sfc_field{i}", "") or self.sfc_field)

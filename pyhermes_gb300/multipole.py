@@ -537,6 +537,11 @@ class Corr_3PCF_Multipole:
     def __init__(self, param_task=None, device="cuda"):
         self.task_params = task_params(self.task_name, param_task)
         self.device = torch.device(device)
+        self.format_params()
+
+    def format_params(self):
+        """The task parameters into attributes (theory/corr3pcf_multipole.py:60-160); call again after
+        editing task_params."""
         tp = self.task_params
         self.sfc_field = tp.get("sfc_field", "")
         for i in (1, 2, 3):

@@ -98,3 +98,26 @@ def test_multipole_binning_template_rules():
         task({"type": "shell", "mapping": {"R": "r12", "los_args.nx": 1.0}})
     with pytest.raises(ValueError, match="empty len_args"):
         task({"type": "shell", "mapping": {}})
+
+
+def test_format_params_rereads_task_params():
+    """Task.format_params (theory/*.py format_params) re-reads task_params."""
+    from pyhermes_gb300.corr2pcf import Corr_2PCF
+    from pyhermes_gb300.mc3pcf import Corr_3PCF
+    from pyhermes_gb300.multipole import Corr_3PCF_Multipole
+
+    t = Corr_2PCF({"Corr_2PCF": {"random": "uniform"}}, device="cpu")
+    t.task_params["random2"] = "r.pkl"
+    t.format_params()
+    assert (t.random1, t.random2) == ("uniform", "r.pkl")
+    m = Corr_3PCF({"Corr_3PCF": {"r12": 10.0}}, device="cpu")
+    m.task_params["r13"] = 55.0
+    m.format_params()
+    assert (m.r12, m.r13) == (10.0, 55.0)
+    q = Corr_3PCF_Multipole({"Corr_3PCF_Multipole": {
+        "binning_window12": {"type": "shell", "mapping": {"R": "r12"}},
+        "binning_window13": {"type": "shell", "mapping": {"R": "r13"}},
+        "sampling": {"mode": "paired", "r12": [100.0], "r13": [200.0]}}}, device="cpu")
+    q.task_params["l_max"] = 6
+    q.format_params()
+    assert q.l_max == 6
