@@ -66,8 +66,14 @@ class Counting:
     """GPU mirror of pyhermes.theory.counting.Counting."""
 
     def __init__(self, param_task=None, device="cuda"):
-        p = task_params("Counting", param_task or {"Counting": {}})
+        self.task_params = task_params("Counting", param_task or {"Counting": {}})
         self.device = device
+        self.format_params()
+
+    def format_params(self):
+        """The task parameters into attributes (theory/counting.py:28-40);
+        call again after editing task_params."""
+        p = self.task_params
         self.sfc_field = p.get("sfc_field", "")
         self._sfc_input = self.sfc_field
         self.random_count = int(p["random_count"])
