@@ -8,23 +8,24 @@ deposited at J=9 (512^3); delta = D - R (catalogue-normalised); 15 thin
 shells over 10-160 Mpc/h on both triangle sides (225 (r12, r13) samples);
 l = 0..10; products delta_ddd_l and rrr_l (the random field, full
 contraction) and zeta_l (float64 mixing solve).  The step runs through the
-public API (Corr_3PCF_Multipole with the batched "gb300" backend).
+public API (Corr_3PCF_Multipole, batched "gb300" backend, tensor-core
+contraction engine).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
 `value` = seconds per catalogue, device-timed (CUDA events), inputs already
 in HBM.  `e2e` = the same with the catalogues in pinned host memory and the
 host->device copies plus the device->host read of zeta_l inside the timed
-region.  `plain` = the per-sample reference-form GPU path (both side fields
-rebuilt and a one-pair contraction for every (r12, r13, l, m)), timed on a
-one-sample subset and scaled by the 225 samples (its cost is linear in the
-samples).  `roofline` = the batched contraction (mp_contract_kernel), with
+region.  `plain` = the per-sample reference-form FP32 GPU path (both side
+fields rebuilt and a one-pair contraction for every (r12, r13, l, m)), timed
+on one full sample (all 66 (l, m) terms) and scaled by the 225 samples and
+2 products.  `accuracy_vs_fp64` = the J=8 configuration's unit through the
+public API against the committed float64 oracle values (per-l relative
+errors).  `roofline` = the batched contraction (mp_contract_tc_kernel), with
 the algorithmic FLOPs of the 27-term separable form, 8 * 15 * 15 * 27 * L^3
-per (l, m), against the measured bf16 peak; the kernel itself runs a
-restructured stencil on FP32 paired-FMA pipes (about 1.2e12 real FLOPs per
-(l, m) at J=9).  `traffic` is the DRAM bytes of one J=9 launch from the
-committed ncu summary profiles/mp_contract_kernel_J9.md (the deposit's from
-profiles/dep_accum_kernel_J9.md).
+per (l, m), against the measured bf16 peak; `fields_roofline` = the fields
+pass of one (l, m) against HBM.  `traffic` values come from
+profiles/ncu_traffic.json (the ncu command and case are recorded there).
 `deposit` = the 4M-point J=9 deposit (Mparticles/s, HBM roofline of the
 accumulate kernel).  `mc3pcf` = Monte Carlo 3PCF on a J=9 lognormal field:
 uniform-MC triplets/s and the learned importance-sampling proposal against
@@ -32,8 +33,9 @@ uniform sampling (variance per sample, bias, equal-wall-time efficiency).
 `c2_window_2pcf` = `field @ W` (gaussian R=10) and the 30x10 (s, mu) ring
 2PCF on the 4M-point J=9 field, with their HBM rooflines.  `c4_batched` =
 64 uneven catalogues through the batched pipeline against the same public
-API one at a time and the plain per-sample path (catalogues/s).  `--impl reference` times the float64 CPU restatement of
-the reference (oracle/) on a bounded unit and scales it the same way.
+API one at a time and the plain per-sample path (catalogues/s).
+`--impl reference` times the float64 CPU restatement of the reference
+(oracle/) at J=9 on the same catalogues (see ReferenceUnits).
 Under torchrun each rank runs its own replica catalogue (replicas only: the
 path has no exchange step); rank 0 prints the aggregate.
 """
@@ -83,18 +85,18 @@ def load_peaks():
         return 6800.0, 1900.0, "fallback"
 
 
-def profile_traffic(name):
-    """DRAM bytes per launch of a kernel from its committed ncu summary
-    (profiles/<name>.md, line `traffic_bytes_per_launch: N`), else None."""
-    path = os.path.join(ROOT, "profiles", name + ".md")
+def profile_traffic(kernel):
+    """DRAM bytes per launch of a kernel from the machine-readable ncu record
+    (profiles/ncu_traffic.json: bytes, the captured case, the command and the
+    scale to the benchmark's launch), else None."""
     try:
-        with open(path) as f:
-            for line in f:
-                if line.startswith("traffic_bytes_per_launch:"):
-                    return float(line.split(":", 1)[1])
-    except OSError:
-        pass
-    return None
+        with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as f:
+            rec = json.load(f).get(kernel)
+    except (OSError, ValueError):
+        return None
+    if not rec or rec.get("traffic_bytes_per_launch") is None:
+        return None
+    return float(rec["traffic_bytes_per_launch"]) * float(rec.get("scale", 1))
 
 
 class ClockSampler:
@@ -182,53 +184,109 @@ def multipole_task_params(dfield, rfield):
 # ---------------------------------------------------------------------------
 # reference arm: the float64 CPU restatement of the reference on the host
 # ---------------------------------------------------------------------------
-def cpu_unit_seconds(eps_np, J, phi, l=1, m=1, r12=70.0, r13=110.0):
-    """One (sample, l, m) unit of the reference algorithm (calc_DDD_multipole
-    inner loop): two radial-multipole windows, two complex FFT convolutions
-    and the 729-term contraction, float64 on all host cores."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle
-    from scipy.fft import fftn, ifftn
+REF_SLABS = 16                      # one step evaluates 1/16 of the grid's x planes
+REF_UNITS = ((1, 1), (10, 7))       # (l, m) of the alternating steps
+REF_SAMPLE = (MP_RADII[5], MP_RADII[9])
 
-    L = 1 << J
-    workers = os.cpu_count() or 1
-    t0 = time.perf_counter()
-    P = oracle.fourier_power(phi, 1, L)
-    gam = oracle.cal_gamma(phi)
-    s = fftn(eps_np, workers=workers)
-    a2 = ifftn(s * oracle.radial_multipole_window(L, P, r12 * L / BOX, l, m), workers=workers)
-    a3 = ifftn(s * oracle.radial_multipole_window(L, P, r13 * L / BOX, l, -m), workers=workers)
-    oracle.contract(eps_np, a2, a3, gam)
-    return time.perf_counter() - t0, oracle.num_threads()
+
+class ReferenceUnits:
+    """The reference's per-(sample, l, m) unit (calc_DDD_multipole,
+    corr3pcf_multipoles.py:505-555: per side a radial-multipole window and a
+    complex FFT convolution, fftn + ifftn; then the 729-term contraction)
+    timed at J=9 on the benchmark's own delta field with the oracle's
+    float64 restatement on all host threads.  The window and the contraction
+    cost the same per grid plane, so a step evaluates both windows on 1/16 of
+    the k-space x planes and the contraction on 1/16 of the cells (rotating
+    over the slabs); the FFT pair of one convolution is timed once at full
+    size.  unit(l) = 16 x slab(l) + 2 x FFT pair, with slab(l) measured at
+    l = 1 and l = 10 and linear in l between (the recurrences are O(l))."""
+
+    def __init__(self):
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+        from scipy.fft import fftn, ifftn
+
+        from pyhermes_gb300.phi import cal_gamma, sample_scaling_function
+
+        self.oracle = oracle
+        phi = sample_scaling_function()
+        self.L = 1 << MP_J
+        self.workers = os.cpu_count() or 1
+        dpos, dw, rpos, rw = make_catalogues(0, "cpu")
+        t0 = time.perf_counter()
+        ed = oracle.deposit(dpos, dw / dw.sum(), phi, MP_J, BOX)
+        er = oracle.deposit(rpos, rw / rw.sum(), phi, MP_J, BOX)
+        self.t_deposit = time.perf_counter() - t0
+        self.delta = ed - er
+        del ed, er
+        t0 = time.perf_counter()
+        spec = fftn(self.delta.astype(np.complex128), workers=self.workers)
+        self.field = ifftn(spec, workers=self.workers)
+        self.t_fft_pair = time.perf_counter() - t0
+        del spec
+        self.P = oracle.fourier_power(phi, 1, self.L)
+        self.gamma = cal_gamma(phi, 3, 1024)
+        self.slab_times = {u: [] for u in REF_UNITS}
+        self.k = 0
+
+    def step(self):
+        l, m = REF_UNITS[self.k % len(REF_UNITS)]
+        slab = (self.k // len(REF_UNITS)) % REF_SLABS
+        self.k += 1
+        n = self.L // REF_SLABS
+        x0, x1 = slab * n, (slab + 1) * n
+        o = self.oracle
+        t0 = time.perf_counter()
+        o.radial_multipole_window_planes(self.L, self.P, REF_SAMPLE[0] * self.L / BOX, l, m, x0, x1)
+        o.radial_multipole_window_planes(self.L, self.P, REF_SAMPLE[1] * self.L / BOX, l, -m, x0, x1)
+        o.contract_planes(self.delta, self.field, self.field, self.gamma, x0, x1)
+        dt = time.perf_counter() - t0
+        self.slab_times[(l, m)].append(dt)
+        return dt
+
+    def unit_seconds(self, l):
+        s1 = statistics.mean(self.slab_times[REF_UNITS[0]])
+        s10 = statistics.mean(self.slab_times[REF_UNITS[1]]) if self.slab_times[REF_UNITS[1]] else s1
+        slab = s1 + (s10 - s1) * (l - 1) / 9.0
+        return REF_SLABS * slab + 2.0 * self.t_fft_pair
+
+    def catalogue_seconds(self):
+        return N_SAMPLES * 2 * sum((l + 1) * self.unit_seconds(l) for l in range(MP_LMAX + 1))
+
+    def describe(self):
+        return {"value": self.catalogue_seconds(), "unit": "s/catalogue", "cores": self.oracle.num_threads(),
+                "kind": "port",
+                "sample": (f"J=9 units on the benchmark's delta = D - R (oracle float64 deposit, {self.t_deposit:.1f} s): "
+                           f"per step both radial-multipole windows of one (r12, r13) = {REF_SAMPLE} unit on 1/"
+                           f"{REF_SLABS} of the k-space x planes plus the 729-term contraction on 1/{REF_SLABS} of "
+                           "the cells, alternating (l, m) = (1, 1) and (10, 7); the complex FFT pair of one "
+                           f"convolution timed once at full size ({self.t_fft_pair:.2f} s). unit(l) = {REF_SLABS} x "
+                           "slab(l) + 2 FFT pairs, slab(l) linear in l between the measured l = 1 and 10; "
+                           f"x {N_SAMPLES} samples x sum_l (l+1) (l, m>=0) x 2 products"),
+                "unit_s": {"l=1": self.unit_seconds(1), "l=10": self.unit_seconds(10)},
+                "slab_s": {f"{l},{m}": statistics.mean(v) for (l, m), v in self.slab_times.items() if v},
+                "fft_pair_s": self.t_fft_pair, "slabs": REF_SLABS, "steps_timed": sum(len(v) for v in self.slab_times.values())}
 
 
 def run_reference(args, ws, rank):
     if rank != 0:
         return 0
-    from pyhermes_gb300.phi import sample_scaling_function
-
-    phi = sample_scaling_function()
-    Ju = 8  # bounded unit: J=8, scaled by 8 to J=9 (the unit's cost is ~linear in cells)
-    rng = np.random.default_rng(0)
-    eps = rng.standard_normal((1 << Ju,) * 3) * 1e-7
+    ref = ReferenceUnits()
     for _ in range(args.warmup):
-        cpu_unit_seconds(eps, Ju, phi, l=0, m=0)
-    total, cores = 0.0, 1
-    for _ in range(args.steps):
-        dt, cores = cpu_unit_seconds(eps, Ju, phi)
-        total += dt
-    unit = total / args.steps
-    per_cat = unit * 8.0 * N_SAMPLES * N_LM * 2
+        ref.step()
+    ref.slab_times = {u: [] for u in REF_UNITS}
+    t_steps = []
+    for _ in range(max(args.steps, 2)):
+        t_steps.append(ref.step())
+    per_cat = ref.catalogue_seconds()
     line = {
         "impl": "reference", "metric": METRIC, "value": per_cat, "unit": "s/catalogue",
-        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": unit * 1e3,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": statistics.mean(t_steps) * 1e3,
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic field (seeded)", "config": {"workload": WORKLOAD, "J": MP_J, "lmax": MP_LMAX},
-        "cpu_baseline": {"value": per_cat, "unit": "s/catalogue", "cores": cores, "kind": "port",
-                         "sample": (f"one (r12, r13, l=1, m=1) unit at J={Ju} per step ({unit:.2f} s): two "
-                                    "radial-multipole windows, two complex FFT convolutions, the 729-term "
-                                    "contraction (oracle/ float64 restatement, all host threads); scaled x8 to "
-                                    f"J=9 and x{N_SAMPLES}x{N_LM}x2 (samples x (l,m) x products)")},
+        "data": "synthetic (seeded lognormal data + uniform randoms, the GB300 arm's catalogues)",
+        "config": {"workload": WORKLOAD, "J": MP_J, "lmax": MP_LMAX},
+        "cpu_baseline": ref.describe(),
         "e2e": {"value": per_cat, "unit": "s/catalogue", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -306,7 +364,7 @@ def deposit_bench(dev, lib, kernels, phi, flush, steps):
             "ms_per_step": sum(step_ms) / steps, "launches_per_step": 7,
             "roofline": {"kernel": "dep_accum_kernel", "bound": "hbm", "achieved": ach, "peak": hbm,
                          "peak_kind": kind, "unit": "GB/s", "frac": ach / hbm,
-                         "traffic": profile_traffic("dep_accum_kernel_J9"),
+                         "traffic": profile_traffic("dep_accum_kernel"),
                          "algorithmic_bytes": alg, "ms_per_launch": acc_ms}}
 
 
@@ -424,7 +482,7 @@ def c2_bench(dev, phi, steps):
             "twopcf_roofline": {"bound": "hbm", "achieved": tp_bytes / t_2pcf / 1e9, "peak": hbm,
                                 "peak_kind": kind, "unit": "GB/s", "frac": tp_bytes / t_2pcf / 1e9 / hbm,
                                 "algorithmic_bytes": tp_bytes,
-                                "traffic": profile_traffic("pair_products_cylz_kernel_J9"),
+                                "traffic": profile_traffic("pair_products_cylz_kernel"),
                                 "note": "one forward rFFT and one pass over the half spectrum for all 300 bins "
                                         "(separable ring windows, column kernel); issue-bound"}}
 
@@ -508,7 +566,7 @@ def mc_bench(dev, phi_np, steps):
             "roofline": {"kernel": "mc_triplet_kernel", "bound": "hbm", "achieved": ach, "peak": hbm,
                          "peak_kind": kind, "unit": "GB/s", "frac": ach / hbm,
                          "algorithmic_bytes_per_triplet": 324,
-                         "traffic": profile_traffic("mc_triplet_kernel_J9"),
+                         "traffic": profile_traffic("mc_triplet_kernel"),
                          "note": "3 x 27 float32 gathers per triplet over Morton-ordered centres"},
             "learned_proposal": {"train_samples": len(configs) * n_cen_train * n_rot_train,
                                  "train_s": t_train, "loss_first_last": [losses[0], losses[-1]],
@@ -572,19 +630,66 @@ def run_case(args):
                           "prepass_bytes_written": len(grid) * L ** 3 * 8}))
         return 0
     f = mp.multipole_fields(rfield := rfft_field(eps), J, 2, 1, grid, P)
-    for _ in range(max(args.warmup, 1)):
-        mp.multipole_contract(eps, f, len(grid), gam, J, conj_sign=-1)
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    for a, b in ev:
-        a.record(stream)
-        S = mp.multipole_contract(eps, f, len(grid), gam, J, conj_sign=-1)
-        b.record(stream)
-    torch.cuda.synchronize(dev)
-    ms = sum(a.elapsed_time(b) for a, b in ev) / len(ev)
+    gc = (ctypes.c_double * 9)(*np.asarray(gam, dtype=np.float64).ravel())
+    dout = torch.zeros((16, 16, 2), dtype=torch.float64, device=dev)
+    res = {}
+    for engine in mp.ENGINES:
+        for _ in range(max(args.warmup, 1)):
+            mp.multipole_contract_async(eps, f, len(grid), gc, J, dout, conj_sign=-1, engine=engine)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        for a, b in ev:
+            a.record(stream)
+            mp.multipole_contract_async(eps, f, len(grid), gc, J, dout, conj_sign=-1, engine=engine)
+            b.record(stream)
+        torch.cuda.synchronize(dev)
+        S = dout[:len(grid), :len(grid)].cpu().numpy()
+        res[engine] = {"ms_per_launch": sum(a.elapsed_time(b) for a, b in ev) / len(ev), "S": S[..., 0] + 1j * S[..., 1]}
     del rfield
-    print(json.dumps({"case": "contract", "J": J, "bins": len(grid), "l": 2, "m": 1, "ms_per_launch": ms,
-                      "algorithmic_flops": 8.0 * len(grid) ** 2 * 27 * L ** 3, "S00": [S[0, 0].real, S[0, 0].imag]}))
+    diff = float(np.abs(res["tensor"]["S"] - res["simt"]["S"]).max() / np.abs(res["simt"]["S"]).max())
+    print(json.dumps({"case": "contract", "J": J, "bins": len(grid), "l": 2, "m": 1,
+                      "ms_per_launch": {k: v["ms_per_launch"] for k, v in res.items()},
+                      "max_rel_diff_tensor_vs_simt": diff, "status": mp.contract_status(J, device=dev),
+                      "algorithmic_flops": 8.0 * len(grid) ** 2 * 27 * L ** 3}))
     return 0
+
+
+def accuracy_vs_fp64(dev, engine="tensor"):
+    """The 3PCF-multipole unit of the J=8 configuration (1,000,000 lognormal
+    points + 5,000,000 uniform randoms, delta = D - R, one (r12, r13) = (50,
+    90) Mpc/h sample, l = 0..10) through the public API (GPU deposit,
+    fields, contraction, mixing solve) against the float64 oracle's values
+    committed in tests/golden/c3_unit_J8.npz: per-l relative errors."""
+    path = os.path.join(ROOT, "tests", "golden", "c3_unit_J8.npz")
+    if not os.path.exists(path):
+        return None
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    import make_multipole_fixtures as fx
+
+    from pyhermes_gb300 import multipole as mp
+    from pyhermes_gb300.projection import SFCProjection
+
+    g = np.load(path)
+    seeds = dict(zip(("field", "poisson", "jitter", "weights", "random"), (int(v) for v in g["seeds"])))
+    pos, w, rpos = fx.unit_positions(fx.unit_cells_decode(int(g["cells_first"]), g["cells_diff"]), seeds, int(g["ng"]),
+                                     int(g["n_rand"]))
+    J = int(g["J"])
+    d = SFCProjection({"SFCProjection": {"particle_pos": pos, "catalog_weight": w, "J": J, "box_size": BOX}},
+                      device=dev).run(save_result=False)
+    r = SFCProjection({"SFCProjection": {"particle_pos": rpos, "J": J, "box_size": BOX}}, device=dev).run(
+        save_result=False)
+    res = mp.Corr_3PCF_Multipole({"Corr_3PCF_Multipole": {
+        "sfc_field": d, "random": r,
+        "binning_window12": {"type": "shell", "len_args": {}, "other_args": {}, "mapping": {"R": "r12"}},
+        "binning_window13": {"type": "shell", "len_args": {}, "other_args": {}, "mapping": {"R": "r13"}},
+        "sampling": {"mode": "paired", "r12": [float(g["r12"])], "r13": [float(g["r13"])]},
+        "l_min": 0, "l_max": int(g["lmax"]), "products": "zeta_l", "contraction_engine": engine}},
+        device=dev).run(save_result=False)
+    out = {}
+    for k in ("zeta_l", "delta_ddd_l", "rrr_l"):
+        e = np.abs(np.asarray(getattr(res, k)) - g[k]) / np.abs(g[k])
+        out[k] = {"max": float(e.max()), "per_l": [float(x) for x in e.ravel()]}
+    return {"engine": engine, "case": "J=8, 1e6 lognormal + 5e6 uniform randoms, (r12, r13) = (50, 90) Mpc/h, l<=10",
+            "max_rel_err_zeta_l": out["zeta_l"]["max"], "per_product": out}
 
 
 def run_gb300(args, ws, rank, local):
@@ -603,7 +708,7 @@ def run_gb300(args, ws, rank, local):
     lib = _lib.load()
     phi_np = sample_scaling_function()
     phi = torch.as_tensor(phi_np, device=dev)
-    dpos_np, dw_np, rpos_np, rw_np = make_catalogues(rank, dev)
+    dpos_np, dw_np, rpos_np, rw_np = make_catalogues(rank, "cpu")
     dpos, dw = torch.as_tensor(dpos_np, device=dev), torch.as_tensor(dw_np, device=dev)
     rpos, rw = torch.as_tensor(rpos_np, device=dev), torch.as_tensor(rw_np, device=dev)
     wsd, wsr = kernels.DepositWorkspace(dev), kernels.DepositWorkspace(dev)
@@ -629,7 +734,6 @@ def run_gb300(args, ws, rank, local):
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     barrier()
     torch.cuda.synchronize(dev)
-    kernel_launches = 0
     for k in range(args.steps):
         ev[k][0].record(stream)
         res = step(dpos, dw, rpos, rw)
@@ -648,7 +752,7 @@ def run_gb300(args, ws, rank, local):
 
     # our kernels per step: 2 deposits x 7; per product per (l, m): fields (power, j_l table,
     # interior and edge prepass, interleave; the inverse FFT is cuFFT) + contract
-    # (contraction, reduce); the mixing solve
+    # (tensor-core contraction, reduce); the mixing solve
     kernel_launches = args.steps * (14 + 2 * N_LM * 7 + 1)
 
     # end to end: catalogues in pinned host memory, copies inside the timed region
@@ -666,43 +770,54 @@ def run_gb300(args, ws, rank, local):
     torch.cuda.synchronize(dev)
     e2e_value = sum(a.elapsed_time(b) for a, b in e2e_ev) / 1e3 / (args.steps * ws)
 
-    # dominant kernel: the batched contraction of one (l, m) over 15x15 radii
+    # dominant kernel: the batched contraction of one (l, m) over 15x15 radii, both engines;
+    # the fields pass of the same (l, m)
     dfield = deposit_field(dpos, dw, MP_J, phi, wsd)
     rfield = deposit_field(rpos, rw, MP_J, phi, wsr)
     delta = (dfield.epsilon_device.double() - rfield.epsilon_device.double()).float()
+    del dfield, rfield
     eng = mp.MultipoleEngine(delta, delta, delta, phi_np, MP_J, BOX)
     L = 1 << MP_J
     grid = [r * L / BOX for r in MP_RADII]
     f2 = mp.multipole_fields(eng.spec2, MP_J, 4, 2, grid, eng.P)
-    for _ in range(3):
-        mp.multipole_contract(eng.eps1, f2, 15, eng.gamma, MP_J, conj_sign=1)
-    cev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(5)]
-    for a, b in cev:
-        a.record(stream)
-        mp.multipole_contract(eng.eps1, f2, 15, eng.gamma, MP_J, conj_sign=1)
-        b.record(stream)
+    gc = (ctypes.c_double * 9)(*np.asarray(eng.gamma, dtype=np.float64).ravel())
+    dout = torch.zeros((16, 16, 2), dtype=torch.float64, device=dev)
+    t_con = {}
+    for engine in mp.ENGINES:
+        for _ in range(2):
+            mp.multipole_contract_async(eng.eps1, f2, 15, gc, MP_J, dout, conj_sign=1, engine=engine)
+        cev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(5)]
+        for a, b in cev:
+            a.record(stream)
+            mp.multipole_contract_async(eng.eps1, f2, 15, gc, MP_J, dout, conj_sign=1, engine=engine)
+            b.record(stream)
+        torch.cuda.synchronize(dev)
+        t_con[engine] = sum(a.elapsed_time(b) for a, b in cev) / len(cev) / 1e3
     fev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(3)]
     for a, b in fev:
         a.record(stream)
         mp.multipole_fields(eng.spec2, MP_J, 4, 2, grid, eng.P, out=f2)
         b.record(stream)
     torch.cuda.synchronize(dev)
-    t_con = sum(a.elapsed_time(b) for a, b in cev) / len(cev) / 1e3
     t_fld = sum(a.elapsed_time(b) for a, b in fev) / len(fev) / 1e3
     del f2
     hbm, bf16, kind = load_peaks()
     flops = 8.0 * 15 * 15 * 27 * L ** 3
-    achieved = flops / t_con / 1e12
+    achieved = flops / t_con["tensor"] / 1e12
+    fld_bytes = L * L * (L // 2 + 1) * 8 + L ** 3 * mp.BIN_STRIDE * 8
 
-    # plain per-sample reference-form path on a one-sample subset (l <= 1)
-    t0 = time.perf_counter()
-    plain = eng.ddd_plain([(MP_RADII[5], MP_RADII[9])], 0, 1)
+    # plain per-sample reference-form path: one full (r12, r13) sample over every (l, m), l <= 10
     torch.cuda.synchronize(dev)
-    t_plain_units = time.perf_counter() - t0
-    plain_unit = t_plain_units / 3.0  # 3 (l, m) terms
-    plain_per_cat = plain_unit * N_SAMPLES * N_LM * 2
-    batched = eng.ddd([(MP_RADII[5], MP_RADII[9])], 0, 1)
-    mixed_vs_plain = float(np.max(np.abs(batched - plain)) / np.max(np.abs(plain)))
+    t0 = time.perf_counter()
+    plain = eng.ddd_plain([REF_SAMPLE], 0, MP_LMAX)
+    torch.cuda.synchronize(dev)
+    t_plain_sample = time.perf_counter() - t0
+    plain_per_cat = t_plain_sample * N_SAMPLES * 2
+    batched = eng.ddd([REF_SAMPLE], 0, MP_LMAX)
+    plain_diff = np.abs(batched - plain) / np.abs(plain)
+    del eng, delta
+
+    acc = accuracy_vs_fp64(dev)
 
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
     dep = deposit_bench(dev, lib, kernels, phi, flush, max(args.steps, 5))
@@ -714,34 +829,45 @@ def run_gb300(args, ws, rank, local):
         if ws > 1:
             torch.distributed.destroy_process_group()
         return 0
-    cpu_unit, cores = cpu_unit_seconds(np.random.default_rng(0).standard_normal((256,) * 3) * 1e-7, 8, phi_np)
-    cpu_per_cat = cpu_unit * 8.0 * N_SAMPLES * N_LM * 2
+    ref = ReferenceUnits()
+    for _ in range(2):
+        ref.step()
+    cpu = ref.describe()
     line = {
         "metric": METRIC, "value": value, "unit": "s/catalogue", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_total / args.steps * 1e3, "higher_is_better": False,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (float64 reductions and mixing solve)",
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 fields and stencil, split-bf16 tensor-core bin product, f64 reductions and mixing solve",
         "data": "synthetic (seeded lognormal data + uniform randoms; the reference's Quijote catalogue is absent)",
         "config": {"workload": WORKLOAD, "J": MP_J, "lmax": MP_LMAX, "radii": len(MP_RADII),
                    "samples": N_SAMPLES, "n_data": MP_NDATA, "n_random": MP_NRAND,
-                   "l2": "per-(l,m) working set (15 GiB fields) far above L2",
+                   "l2": "per-(l,m) working set (17 GB fields) far above L2",
                    "parallelism": f"replicas x{ws}"},
-        "plain": {"value": plain_per_cat, "unit": "s/catalogue", "speedup_batched_vs_plain": plain_per_cat / value,
-                  "sample": "one (r12, r13) sample, l<=1, scaled by 225 samples x 66 (l,m) x 2 products",
-                  "max_rel_diff_batched_vs_plain": mixed_vs_plain},
-        "roofline": {"kernel": "mp_contract_kernel (+ mp_reduce_kernel)", "bound": "tensor",
+        "accuracy_vs_fp64": acc,
+        "max_rel_err_vs_fp64": None if acc is None else acc["max_rel_err_zeta_l"],
+        "plain": {"value": plain_per_cat, "unit": "s/catalogue", "speedup_mixed_batched_vs_plain": plain_per_cat / value,
+                  "sample_s": t_plain_sample,
+                  "sample": (f"one full (r12, r13) = {REF_SAMPLE} sample, all 66 (l, m>=0) terms l<=10: per-sample "
+                             "single-radius fields and the reference-form FP32 contraction, x225 samples x2 products"),
+                  "max_rel_diff_batched_vs_plain_per_l": float(plain_diff.max())},
+        "roofline": {"kernel": "mp_contract_tc_kernel (+ mp_reduce_kernel)", "bound": "tensor",
                      "achieved": achieved, "peak": bf16, "peak_kind": kind, "unit": "TFLOP/s",
-                     "frac": achieved / bf16, "traffic": profile_traffic("mp_contract_kernel_J9"),
-                     "executes_on": "FP32 paired-FMA pipes (separable pair stencil + 4x2-blocked bin product)",
-                     "algorithmic_flops": flops, "ms_per_launch": t_con * 1e3,
-                     "fields_ms_per_lm": t_fld * 1e3},
+                     "frac": achieved / bf16, "traffic": profile_traffic("mp_contract_tc_kernel"),
+                     "executes_on": ("stencil on FP32 paired-FMA pipes; bin x bin product on tcgen05 "
+                                     "(split-BF16 operands, FP32 accumulate in TMEM)"),
+                     "algorithmic_flops": flops, "ms_per_launch": t_con["tensor"] * 1e3,
+                     "ms_per_launch_simt_engine": t_con["simt"] * 1e3},
+        "fields_roofline": {"kernels": "mp_jl_table + mp_prepass_quad/edge + cuFFT C2C x15 + mp_interleave",
+                            "bound": "hbm", "ms_per_lm": t_fld * 1e3, "algorithmic_bytes": fld_bytes,
+                            "achieved": fld_bytes / t_fld / 1e9, "peak": hbm, "peak_kind": kind, "unit": "GB/s",
+                            "frac": fld_bytes / t_fld / 1e9 / hbm,
+                            "note": "minimum bytes: one read of the half spectrum + one write of the 15 fields in "
+                                    "the contraction's [cell][16] layout"},
         "deposit": dep,
         "mc3pcf": mc,
         "c2_window_2pcf": c2,
         "c4_batched": c4,
-        "cpu_baseline": {"value": cpu_per_cat, "unit": "s/catalogue", "cores": cores, "kind": "port",
-                         "sample": (f"one (r12, r13, l=1, m=1) unit at J=8 ({cpu_unit:.2f} s, float64 oracle "
-                                    "restatement: windows, FFT convolutions, 729-term contraction); scaled x8 "
-                                    "to J=9 and x225 samples x66 (l,m) x2 products")},
+        "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "s/catalogue",
                 "h2d_bytes_per_step": int(sum(x.numel() * x.element_size() for x in h)),
                 "d2h_bytes_per_step": int(zeta.size * 8)},

@@ -252,6 +252,25 @@ int hermes_multipole_contract_async(const float* eps1, const void* fields2, int 
                                     const double* gamma, int J, int chunk_x, int ctas_per_sm,
                                     double* dev_out, void* workspace, size_t workspace_bytes,
                                     void* stream);
+/* Contraction engines.  hermes_multipole_contract and _async run the stencil
+ * G^{b3}(y) = sum Gamma3 eps1 a3 on the CUDA cores (FP32) and the bin x bin
+ * product S += a2^{b2} G^{b3} of every plane on the tcgen05 tensor cores:
+ * both operands split into BF16 hi + lo parts (~16 significant bits each,
+ * all four partial products summed), FP32 accumulation in tensor memory over
+ * a work item, float64 across items (corr3pcf_multipoles.py:33-58 + :99-131).
+ * hermes_multipole_contract_simt_async: the same sum with the product on the
+ * CUDA cores in FP32 (the all-FP32 comparison path); same arguments.
+ * hermes_multipole_contract_status: after a tensor-core contraction on the
+ * same workspace, *status = 0, or the first bounded wait that gave up (1: an
+ * a2 plane's TMA load, 2 or 3: an MMA completion); its results are then NaN.
+ * Synchronises `stream`. */
+int hermes_multipole_contract_simt_async(const float* eps1, const void* fields2, int nb2,
+                                         const void* fields3, int nb3, int conj_sign,
+                                         const double* gamma, int J, int chunk_x, int ctas_per_sm,
+                                         double* dev_out, void* workspace, size_t workspace_bytes,
+                                         void* stream);
+int hermes_multipole_contract_status(const void* workspace, size_t workspace_bytes, int J, int* status,
+                                     void* stream);
 int hermes_multipole_contract_plain(const float* eps1, const void* a2, const void* a3,
                                     const double* gamma, int J, double* out,
                                     void* workspace, size_t workspace_bytes, void* stream);

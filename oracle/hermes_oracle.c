@@ -489,11 +489,22 @@ static double radial_profile(double k, int code, const double* a, int l) {
 
 /* calculate_radial_multipole_window_array_numba (radial_multipole_windows.py:
  * 147-183): complex [L,L,L] (interleaved re, im), args in grid units. */
+int oracle_radial_multipole_window_range(int L, const double* P, int code, const double* args, int l, int m,
+                                         int x_begin, int x_end, double* out);
 int oracle_radial_multipole_window(int L, const double* P, int code, const double* args, int l, int m,
                                    double* out) {
+  return oracle_radial_multipole_window_range(L, P, code, args, l, m, 0, L, out);
+}
+
+/* The same window on the x planes [x_begin, x_end) only; out holds those
+ * planes, [x_end - x_begin][L][L] interleaved complex. */
+int oracle_radial_multipole_window_range(int L, const double* P, int code, const double* args, int l, int m,
+                                         int x_begin, int x_end, double* out) {
   const double invL = 1.0 / L;
+  if (x_begin < 0 || x_end > L || x_begin > x_end) return -1;
+  out -= (int64_t)x_begin * L * L * 2;
 #pragma omp parallel for schedule(static)
-  for (int x = 0; x < L; ++x) {
+  for (int x = x_begin; x < x_end; ++x) {
     const double ki[2] = {(x - L) * invL, x * invL};
     const double pi_[2] = {P[L - x], P[x]};
     for (int y = 0; y < L; ++y) {
@@ -570,5 +581,97 @@ int oracle_contract(const double* data, const double* a1, const double* a2, cons
   }
   *out_re = tr;
   *out_im = ti;
+  return 0;
+}
+
+/* S[b2][b3] = sum over cells of data(x) * sum_{l1,l2} Gamma3(l1,l2)
+ * a2_b2(x-l1) a3_b3(x-l2) for every bin pair at once: per pair the
+ * per-cell arithmetic of oracle_contract (compute_3d_summand_cpu,
+ * corr3pcf_multipoles.py:134-170), with the inner sum over l2 formed once
+ * per (cell, l1, b3) and reused by every b2.  a2: [nb2][L^3], a3: [nb3][L^3]
+ * interleaved complex; out: [nb2][nb3][2].  Per-thread partial sums are added
+ * in thread order. */
+int oracle_contract_bins_range(const double* data, const double* a2, int nb2, const double* a3, int nb3,
+                               const double* gamma, int L, int x_begin, int x_end, double* out);
+int oracle_contract_bins(const double* data, const double* a2, int nb2, const double* a3, int nb3,
+                         const double* gamma, int L, double* out) {
+  return oracle_contract_bins_range(data, a2, nb2, a3, nb3, gamma, L, 0, L, out);
+}
+
+/* The sum restricted to the cells of x planes [x_begin, x_end) (their
+ * neighbourhoods still read the whole periodic grid). */
+int oracle_contract_bins_range(const double* data, const double* a2, int nb2, const double* a3, int nb3,
+                               const double* gamma, int L, int x_begin, int x_end, double* out) {
+  enum { S = 3, MAXB = 16 };
+  if (nb2 < 1 || nb3 < 1 || nb2 > MAXB || nb3 > MAXB) return -1;
+  if (x_begin < 0 || x_end > L || x_begin > x_end) return -1;
+  const int64_t N = (int64_t)L * L * L, plane = (int64_t)L * L;
+  const int64_t idx_begin = (int64_t)x_begin * plane, idx_end = (int64_t)x_end * plane;
+  int nthr = 1;
+#ifdef _OPENMP
+  nthr = omp_get_max_threads();
+#endif
+  double* part = (double*)calloc((size_t)nthr * nb2 * nb3 * 2, sizeof(double));
+  if (!part) return -2;
+#pragma omp parallel
+  {
+    int t = 0;
+#ifdef _OPENMP
+    t = omp_get_thread_num();
+#endif
+    double* acc = part + (size_t)t * nb2 * nb3 * 2;
+    double s2r[MAXB], s2i[MAXB], s1r[MAXB * MAXB], s1i[MAXB * MAXB];
+#pragma omp for schedule(static)
+    for (int64_t idx = idx_begin; idx < idx_end; ++idx) {
+      const int64_t lx = idx / plane, rem = idx - lx * plane, ly = rem / L, lz = rem - ly * L;
+      for (int q = 0; q < nb2 * nb3; ++q) s1r[q] = s1i[q] = 0.0;
+      for (int l1x = 0; l1x < S; ++l1x) {
+        const int64_t i1x = pmod(lx - l1x, L);
+        for (int l1y = 0; l1y < S; ++l1y) {
+          const int64_t i1y = pmod(ly - l1y, L);
+          for (int l1z = 0; l1z < S; ++l1z) {
+            const int64_t i1z = pmod(lz - l1z, L);
+            for (int b = 0; b < nb3; ++b) s2r[b] = s2i[b] = 0.0;
+            for (int l2x = 0; l2x < S; ++l2x) {
+              const int64_t i2x = pmod(lx - l2x, L);
+              const double gx = gamma[l1x * S + l2x];
+              for (int l2y = 0; l2y < S; ++l2y) {
+                const int64_t i2y = pmod(ly - l2y, L);
+                const double gxy = gx * gamma[l1y * S + l2y];
+                for (int l2z = 0; l2z < S; ++l2z) {
+                  const int64_t i2z = pmod(lz - l2z, L);
+                  const double w = gxy * gamma[l1z * S + l2z];
+                  const int64_t o = ((i2x * L + i2y) * L + i2z) * 2;
+                  for (int b = 0; b < nb3; ++b) {
+                    s2r[b] += w * a3[(size_t)b * 2 * N + o];
+                    s2i[b] += w * a3[(size_t)b * 2 * N + o + 1];
+                  }
+                }
+              }
+            }
+            const int64_t o1 = ((i1x * L + i1y) * L + i1z) * 2;
+            for (int a = 0; a < nb2; ++a) {
+              const double ar = a2[(size_t)a * 2 * N + o1], ai = a2[(size_t)a * 2 * N + o1 + 1];
+              for (int b = 0; b < nb3; ++b) {
+                s1r[a * nb3 + b] += ar * s2r[b] - ai * s2i[b];
+                s1i[a * nb3 + b] += ar * s2i[b] + ai * s2r[b];
+              }
+            }
+          }
+        }
+      }
+      const double d = data[idx];
+      for (int q = 0; q < nb2 * nb3; ++q) {
+        acc[2 * q] += d * s1r[q];
+        acc[2 * q + 1] += d * s1i[q];
+      }
+    }
+  }
+  for (int q = 0; q < nb2 * nb3 * 2; ++q) {
+    double s = 0.0;
+    for (int t = 0; t < nthr; ++t) s += part[(size_t)t * nb2 * nb3 * 2 + q];
+    out[q] = s;
+  }
+  free(part);
   return 0;
 }

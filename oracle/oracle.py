@@ -176,6 +176,9 @@ def _setup_multipole_lib():
     P, I, D = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
     lb.oracle_radial_multipole_window.argtypes = [I, P, I, P, I, I, P]
     lb.oracle_contract.argtypes = [P, P, P, P, I, I, ctypes.POINTER(D), ctypes.POINTER(D)]
+    lb.oracle_contract_bins.argtypes = [P, P, I, P, I, P, I, P]
+    lb.oracle_contract_bins_range.argtypes = [P, P, I, P, I, P, I, I, I, P]
+    lb.oracle_radial_multipole_window_range.argtypes = [I, P, I, P, I, I, I, I, P]
     lb.oracle_spherical_jn.argtypes = [I, D]
     lb.oracle_spherical_jn.restype = D
     lb.oracle_sph_harm.argtypes = [I, I, D, D, D, ctypes.POINTER(D), ctypes.POINTER(D)]
@@ -193,6 +196,34 @@ def radial_multipole_window(L, P, radius_grid, l, m, code=0, arg1=0.0):
     P = np.ascontiguousarray(P, dtype=np.float64)
     lb.oracle_radial_multipole_window(L, _p(P), code, _p(args), l, m, _p(out))
     return out[..., 0] + 1j * out[..., 1]
+
+
+def radial_multipole_window_planes(L, P, radius_grid, l, m, x_begin, x_end, code=0, arg1=0.0):
+    """radial_multipole_window on the x planes [x_begin, x_end) only
+    (complex128 [x_end - x_begin, L, L]); the per-plane arithmetic is the
+    full window's."""
+    lb = _setup_multipole_lib()
+    out = np.empty((x_end - x_begin, L, L, 2), dtype=np.float64)
+    args = np.array([radius_grid, arg1, 0.0, 0.0])
+    P = np.ascontiguousarray(P, dtype=np.float64)
+    if lb.oracle_radial_multipole_window_range(L, _p(P), code, _p(args), l, m, x_begin, x_end, _p(out)) != 0:
+        raise ValueError("bad plane range")
+    return out[..., 0] + 1j * out[..., 1]
+
+
+def contract_planes(data, a2, a3, gamma, x_begin, x_end):
+    """The one-pair contraction summed over the cells of x planes
+    [x_begin, x_end) (oracle_contract_bins_range with one bin per side)."""
+    lb = _setup_multipole_lib()
+    data = np.ascontiguousarray(data, dtype=np.float64)
+    a2 = np.ascontiguousarray(a2, dtype=np.complex128)
+    a3 = np.ascontiguousarray(a3, dtype=np.complex128)
+    gamma = np.ascontiguousarray(gamma, dtype=np.float64)
+    out = np.zeros(2)
+    if lb.oracle_contract_bins_range(_p(data), _p(a2), 1, _p(a3), 1, _p(gamma), data.shape[0], x_begin, x_end,
+                                     _p(out)) != 0:
+        raise ValueError("bad plane range")
+    return complex(out[0], out[1])
 
 
 def contract(data, a1, a2, gamma):
@@ -244,6 +275,63 @@ def calc_ddd_multipole(eps1, eps2, eps3, R12, R13, l_min, l_max, phi, res=1024, 
     for l in range(l_min, l_max + 1):
         ddd.append(combine_multipole_m_terms(multipole_m_summands(eps1, eps2, eps3, R12, R13, l, phi, res, box), l))
     return np.arange(l_min, l_max + 1, dtype=np.int32), np.asarray(ddd)
+
+
+def contract_bins(data, a2, a3, gamma):
+    """S[b2, b3] = contract(data, a2[b2], a3[b3], gamma) for every bin pair in
+    one pass (oracle_contract_bins: the same per-pair arithmetic, inner sums
+    shared across b2).  a2: [nb2, L, L, L] complex, a3: [nb3, L, L, L]."""
+    lb = _setup_multipole_lib()
+    data = np.ascontiguousarray(data, dtype=np.float64)
+    a2 = np.ascontiguousarray(a2, dtype=np.complex128)
+    a3 = np.ascontiguousarray(a3, dtype=np.complex128)
+    gamma = np.ascontiguousarray(gamma, dtype=np.float64)
+    nb2, nb3 = a2.shape[0], a3.shape[0]
+    out = np.zeros((nb2, nb3, 2))
+    rc = lb.oracle_contract_bins(_p(data), _p(a2), nb2, _p(a3), nb3, _p(gamma), data.shape[0], _p(out))
+    if rc != 0:
+        raise ValueError(f"oracle_contract_bins failed ({rc})")
+    return out[..., 0] + 1j * out[..., 1]
+
+
+def multipole_summands_grid(eps1, eps2, eps3, radii12, radii13, l, m, phi, res=1024, box=1000.0, spectra=None):
+    """S_m[i, j] for thin shells radii12[i] x radii13[j] (physical) at one
+    (l, m): the per-sample step of calc_DDD_multipole
+    (corr3pcf_multipoles.py:505-555) for every (r12, r13) pair of the grid,
+    each side field built once per radius.  Returns complex [n12, n13]."""
+    from scipy.fft import fftn, ifftn
+
+    L = eps1.shape[0]
+    P = fourier_power(phi, 1, L, res)
+    gamma = cal_gamma(phi, phi.shape[0] // res, res)
+    if spectra is None:
+        spectra = (fftn(np.asarray(eps2, dtype=np.float64)), fftn(np.asarray(eps3, dtype=np.float64)))
+    s2, s3 = spectra
+    workers = os.cpu_count() or 1
+    a2 = np.stack([ifftn(s2 * radial_multipole_window(L, P, r * L / box, l, m), workers=workers) for r in radii12])
+    a3 = np.stack([ifftn(s3 * radial_multipole_window(L, P, r * L / box, l, -m), workers=workers) for r in radii13])
+    return (4.0 * np.pi) * contract_bins(eps1, a2, a3, gamma) / eps1.size
+
+
+def calc_ddd_multipole_grid(eps1, eps2, eps3, radii12, radii13, l_min, l_max, phi, res=1024, box=1000.0):
+    """calc_DDD_multipole (corr3pcf_multipoles.py:460-579) for every
+    (r12, r13) pair of a thin-shell grid: DDD_l [n12, n13, n_l] and the
+    summands S_lm [(l, m >= 0) in order, n12, n13]."""
+    from scipy.fft import fftn
+
+    workers = os.cpu_count() or 1
+    spectra = (fftn(np.asarray(eps2, dtype=np.float64), workers=workers),
+               fftn(np.asarray(eps3, dtype=np.float64), workers=workers))
+    ddd = np.zeros((len(radii12), len(radii13), l_max - l_min + 1))
+    summands = []
+    for li, l in enumerate(range(l_min, l_max + 1)):
+        Sm = [multipole_summands_grid(eps1, eps2, eps3, radii12, radii13, l, m, phi, res, box, spectra)
+              for m in range(l + 1)]
+        summands.extend(Sm)
+        for i in range(len(radii12)):
+            for j in range(len(radii13)):
+                ddd[i, j, li] = combine_multipole_m_terms([S[i, j] for S in Sm], l)
+    return ddd, np.asarray(summands)
 
 
 def legendre_triple_coeff(l, lp, k):

@@ -47,6 +47,9 @@ SIGNATURES = {
                                                _c_sz, _p]),
     "hermes_multipole_contract_async": (_c_int, [_p, _p, _c_int, _p, _c_int, _c_int, _p, _c_int, _c_int, _c_int, _p, _p,
                                                  _c_sz, _p]),
+    "hermes_multipole_contract_simt_async": (_c_int, [_p, _p, _c_int, _p, _c_int, _c_int, _p, _c_int, _c_int, _c_int,
+                                                      _p, _p, _c_sz, _p]),
+    "hermes_multipole_contract_status": (_c_int, [_p, _c_sz, _c_int, ctypes.POINTER(_c_int), _p]),
     "hermes_multipole_contract_plain": (_c_int, [_p, _p, _p, _p, _c_int, _p, _p, _c_sz, _p]),
     "hermes_mixing_solve": (_c_int, [_p, _p, _p, _c_int, _c_int, _p, _p, _p, _p]),
     "hermes_mc_workspace_size": (_c_int, [ctypes.POINTER(_c_sz)]),

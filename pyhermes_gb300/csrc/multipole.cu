@@ -33,7 +33,11 @@
 #include <tuple>
 #include <vector>
 
+#include <cuda_bf16.h>
+#include <cudaTypedefs.h>
+
 #include "hermes_common.cuh"
+#include "tc_common.cuh"
 #include "window_eval.cuh"
 
 namespace hermes {
@@ -497,6 +501,7 @@ struct ContractArgs {
   int J, CX;
   GammaC gm;
   double* partial;   // [gridDim.x][16][16][2]
+  int* status;       // first bounded wait that gave up (tensor-core kernel), else 0
 };
 
 // a3 plane x_a (region rows y0-2.., cols z0-2..) -> buf [cell][16] float2.
@@ -769,6 +774,320 @@ __global__ void __launch_bounds__(ct::kThreads, 2) mp_contract_kernel(ContractAr
     A.partial[(long long)blockIdx.x * 2 * kMaxBins * kMaxBins + i] = dacc[i];
 }
 
+// ---- contraction with the bin x bin product on the tensor cores -------------
+// The stencil part is mp_contract_kernel's (FP32 paired FMAs on the CUDA
+// cores); the product S[b2][b3] += sum_cells a2^{b2} G^{b3} of every completed
+// plane runs as one tcgen05.mma GEMM with the accumulator in tensor memory:
+//   A (M = 128 x K = 64 cells): rows m = hl*32 + 2*b2 + part of a2, where
+//     hl = 0 is the BF16 rounding of the FP32 value and hl = 1 the BF16
+//     rounding of the remainder (a2 = hi + lo to ~2^-17), part = re / im;
+//     rows 64..127 read the B buffer and are ignored;
+//   B (N = 64 x K = 64 cells): columns n = hl*32 + 2*b3 + part of G;
+//   D[m][n] = sum_cells A[m] B[n] (FP32 in TMEM, 128 lanes x 64 columns).
+// Summed over (hl, hl'), D gives the four real products of a2 x G per bin
+// pair, i.e. the split-BF16 product keeps ~16 significant bits of each operand
+// and the hi*lo cross terms (the "BF16x3" scheme, plus lo*lo).  Both operands
+// are MN-major in 128B-swizzled shared memory: one 128-byte row per cell
+// (64 BF16 values), 8-row atoms of 1 KB, K advancing by whole atoms.  The a2
+// plane arrives by TMA (4-D tensor map over the [x][y][z][16 bins] fields,
+// box 32 floats x 8 z x 8 y x 1 x) one step ahead; threads split it into
+// hi / lo.  A plane's MMAs (4 x K = 16) are issued by one thread after the
+// block barrier that follows the operand writes and run while the CUDA cores
+// compute the next plane's stencil; their tcgen05.commit arrives on an
+// mbarrier that the next overwrite of the operand buffers waits on.  At the
+// end of a work item the accumulator is read back (tcgen05.ld) and added in
+// float64 in a fixed order per bin pair.
+namespace tcc {
+constexpr int kOpBytes = 64 * 128;                         // one operand plane: 64 cells x 128 B
+constexpr int kRawBytes = 64 * kBinStride * 8;             // TMA a2 plane: 64 cells x 16 complex
+constexpr int kTmemCols = 64;
+constexpr uint32_t kIdesc = hermes::tc::idesc_bf16_f32(128, 64, true, true);
+// 1 KB slack for the runtime 1024-byte alignment of the swizzled operands
+constexpr size_t kSmem = 1024 + 2 * kOpBytes + 2 * kRawBytes + sizeof(float2) * 2 * ct::kA3Plane +
+                         sizeof(float) * (3 * ct::kVPlane + 2 * ct::kEpsPlane) +
+                         sizeof(double) * 2 * kMaxBins * kMaxBins + 128;
+}  // namespace tcc
+
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo_half, float hi_half) {
+  uint32_t r;
+  asm("cvt.rn.bf16x2.f32 %0, %1, %2;\n" : "=r"(r) : "f"(hi_half), "f"(lo_half));
+  return r;
+}
+__device__ __forceinline__ float bf16_round(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
+
+// Writes (re, im) of one bin as BF16 hi and lo pairs into a swizzled operand
+// row (cell) at element 2*b and 32 + 2*b.
+__device__ __forceinline__ void tc_put_pair(unsigned char* op, int cell, int b, float re, float im) {
+  const float hr = bf16_round(re), hi_ = bf16_round(im);
+  const uint32_t hv = pack_bf16x2(hr, hi_), lv = pack_bf16x2(re - hr, im - hi_);
+  unsigned char* atom = op + (cell >> 3) * 1024;
+  const int row = cell & 7, byte = (b & 3) * 4;
+  *reinterpret_cast<uint32_t*>(atom + hermes::tc::sw128_offset(row, b >> 2) + byte) = hv;
+  *reinterpret_cast<uint32_t*>(atom + hermes::tc::sw128_offset(row, 4 + (b >> 2)) + byte) = lv;
+}
+
+__global__ void __launch_bounds__(ct::kThreads, 2)
+mp_contract_tc_kernel(ContractArgs A, const __grid_constant__ CUtensorMap a2map) {
+  namespace tc = hermes::tc;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  unsigned char* base = smem_raw + ((1024u - (tc::smem_u32(smem_raw) & 1023u)) & 1023u);
+  unsigned char* abf = base;                                       // A operand (a2 hi/lo)
+  unsigned char* gbf = abf + tcc::kOpBytes;                        // B operand (G hi/lo)
+  float* araw = reinterpret_cast<float*>(gbf + tcc::kOpBytes);    // [2][64 cells][32] TMA a2 planes
+  float2* abuf = reinterpret_cast<float2*>(reinterpret_cast<unsigned char*>(araw) + 2 * tcc::kRawBytes);
+  double* dacc = reinterpret_cast<double*>(abuf + 2 * ct::kA3Plane);  // [16][16][2]
+  float* vring = reinterpret_cast<float*>(dacc + 2 * kMaxBins * kMaxBins);
+  float* epsb = vring + 3 * ct::kVPlane;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(epsb + 2 * ct::kEpsPlane);  // tma[2], mma
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 3);
+  float* gsm = reinterpret_cast<float*>(tmem_slot + 1);                  // 15 V-pass weights
+  int* s_abort = reinterpret_cast<int*>(gsm + 16);
+  float* stage = reinterpret_cast<float*>(abuf);                          // [64][65] at item end
+
+  const int J = A.J, L = 1 << J, Lm = L - 1, CX = A.CX;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int b = tid & 15;
+  const int grp = tid >> 4;
+  const int cy = 2 * (grp / (ct::TZ / 2)), cz = 2 * (grp % (ct::TZ / 2));
+  const int nty = L / ct::TY, ntz = L / ct::TZ;
+  const int n_items = (L / CX) * nty * ntz;
+  const int nsteps = CX + 4;
+  const bool tma_a2 = A.s2 == kBinStride;
+
+  if (tid == 0) {
+#pragma unroll
+    for (int a = 0; a < 5; ++a)
+#pragma unroll
+      for (int l1 = 0; l1 < 3; ++l1) {
+        const int l2 = l1 - a + 2;
+        gsm[a * 3 + l1] = (l2 >= 0 && l2 <= 2) ? A.gm.g[l1 * 3 + (l2 < 0 ? 0 : (l2 > 2 ? 2 : l2))] : 0.f;
+      }
+    tc::mbar_init(&bars[0], 1);
+    tc::mbar_init(&bars[1], 1);
+    tc::mbar_init(&bars[2], 1);
+    tc::mbar_fence_init();
+    *s_abort = 0;
+    if (tma_a2) tc::tma_prefetch_desc(&a2map);
+  }
+  if (warp == 0) tc::tmem_alloc(tmem_slot, tcc::kTmemCols);
+  for (int i = tid; i < 2 * kMaxBins * kMaxBins; i += ct::kThreads) dacc[i] = 0.0;
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t tmem_d = *tmem_slot;
+  const uint32_t sa = tc::smem_u32(abf), sg = tc::smem_u32(gbf);
+  uint32_t tma_ph0 = 0, tma_ph1 = 0, mma_ph = 0;
+  bool mma_pending = false;
+
+  for (int item = blockIdx.x; item < n_items; item += gridDim.x) {
+    const int tz = item % ntz, ty = (item / ntz) % nty, xc = item / (ntz * nty);
+    const int x0 = xc * CX, y0 = ty * ct::TY, z0 = tz * ct::TZ;
+    ct_stage_eps(A.eps1, epsb, x0 - 2, y0, z0, L, Lm);
+    ct_stage_eps(A.eps1, epsb + ct::kEpsPlane, x0 - 1, y0, z0, L, Lm);
+    cp_async_commit();
+    cp_async_wait<0>();
+    __syncthreads();
+    ct_compute_v(gsm, epsb, vring);
+    ct_compute_v(gsm, epsb + ct::kEpsPlane, vring + ct::kVPlane);
+    __syncthreads();
+    ct_stage_a3(A.src3, A.s3, abuf, x0 - 2, y0, z0, L, Lm);
+    ct_stage_eps(A.eps1, epsb, x0, y0, z0, L, Lm);
+    cp_async_commit();
+
+    float2 G[5][4];
+#pragma unroll
+    for (int q = 0; q < 5; ++q)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) G[q][c] = make_float2(0.f, 0.f);
+    bool first_mma = true;
+
+    for (int st = 0; st < nsteps; ++st) {
+      const int xa = x0 - 2 + st;
+      if (st + 1 < nsteps) {
+        ct_stage_a3(A.src3, A.s3, abuf + ((st + 1) & 1) * ct::kA3Plane, xa + 1, y0, z0, L, Lm);
+        ct_stage_eps(A.eps1, epsb + ((st + 1) & 1) * ct::kEpsPlane, xa + 3, y0, z0, L, Lm);
+        // a2 plane of the next step's product (its buffer's last reader, the
+        // split two steps back, finished before the last block barrier)
+        if (tma_a2 && tid == 0 && st + 1 >= 4) {
+          uint64_t* bar = &bars[(st + 1) & 1];
+          tc::fence_proxy_async_smem();
+          tc::mbar_arrive_expect_tx(bar, tcc::kRawBytes);
+          tc::tma_load_4d(araw + ((st + 1) & 1) * (tcc::kRawBytes / 4), &a2map, bar, 0, z0, y0, (xa - 1) & Lm);
+        }
+      }
+      cp_async_commit();
+      cp_async_wait<1>();
+      __syncthreads();
+      ct_compute_v(gsm, epsb + (st & 1) * ct::kEpsPlane, vring + ((st + 2) % 3) * ct::kVPlane);
+      __syncthreads();
+      {
+        const float2* ap = abuf + (st & 1) * ct::kA3Plane;
+        const float* vp0 = vring + (st % 3) * ct::kVPlane;
+        const float* vp1 = vring + ((st + 1) % 3) * ct::kVPlane;
+        const float* vp2 = vring + ((st + 2) % 3) * ct::kVPlane;
+        float2 T[3][4];
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+#pragma unroll
+          for (int c = 0; c < 4; ++c) T[d][c] = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int r = 0; r < 6; ++r) {
+          float2 av[6];
+#pragma unroll
+          for (int k = 0; k < 6; ++k) av[k] = ap[((cy + r) * ct::HZ + cz + k) * kBinStride + b];
+#pragma unroll
+          for (int dy = 0; dy < 2; ++dy) {
+            const int uy = r - 2 - dy;
+            if (uy < -2 || uy > 2) continue;
+#pragma unroll
+            for (int dz = 0; dz < 2; ++dz) {
+              const int voff = ((cy + dy) * ct::TZ + cz + dz) * ct::kVCol + (uy + 2) * ct::kVRow;
+#pragma unroll
+              for (int d = 0; d < 3; ++d) {
+                const float* vp = (d == 0 ? vp0 : (d == 1 ? vp1 : vp2)) + voff;
+                const float4 v4 = *reinterpret_cast<const float4*>(vp);
+                const float v5 = vp[4];
+                float2 t = T[d][dy * 2 + dz];
+                t = __ffma2_rn(make_float2(v4.x, v4.x), av[dz], t);
+                t = __ffma2_rn(make_float2(v4.y, v4.y), av[dz + 1], t);
+                t = __ffma2_rn(make_float2(v4.z, v4.z), av[dz + 2], t);
+                t = __ffma2_rn(make_float2(v4.w, v4.w), av[dz + 3], t);
+                t = __ffma2_rn(make_float2(v5, v5), av[dz + 4], t);
+                T[d][dy * 2 + dz] = t;
+              }
+            }
+          }
+        }
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+#pragma unroll
+          for (int l1x = 0; l1x < 3; ++l1x) {
+            const float gx = A.gm.g[l1x * 3 + d];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) G[d - l1x + 2][c] = __ffma2_rn(make_float2(gx, gx), T[d][c], G[d - l1x + 2][c]);
+          }
+      }
+      // G(xa - 2) and the a2 plane xa - 2 become the operands of this plane's MMA
+      const bool full = st >= 4;
+      if (full) {
+        if (mma_pending) {
+          if (!tc::mbar_wait(&bars[2], mma_ph)) *s_abort = 2;
+          mma_ph ^= 1u;
+          mma_pending = false;
+        }
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          float2 g = G[0][c];
+          if (A.conj_src) g = make_float2(A.sign * g.x, -A.sign * g.y);
+          tc_put_pair(gbf, (cy + (c >> 1)) * ct::TZ + cz + (c & 1), b, g.x, g.y);
+        }
+        const int cell = tid >> 2, q = tid & 3;
+        float v[8];
+        if (tma_a2) {
+          const uint32_t par = (st & 1) ? tma_ph1 : tma_ph0;
+          if (!tc::mbar_wait(&bars[st & 1], par)) *s_abort = 1;  // a2 plane (TMA)
+          const float4* src = reinterpret_cast<const float4*>(araw + (st & 1) * (tcc::kRawBytes / 4) + cell * 32 + 8 * q);
+          const float4 p0 = src[0], p1 = src[1];
+          v[0] = p0.x; v[1] = p0.y; v[2] = p0.z; v[3] = p0.w;
+          v[4] = p1.x; v[5] = p1.y; v[6] = p1.z; v[7] = p1.w;
+        } else {  // single bin: slot 0 holds the value
+#pragma unroll
+          for (int i = 0; i < 8; ++i) v[i] = 0.f;
+          if (q == 0) {
+            const int ccy = cell / ct::TZ, ccz = cell - ccy * ct::TZ;
+            const float2 s = A.f2[((long long)((xa - 2) & Lm) * L + y0 + ccy) * L + z0 + ccz];
+            v[0] = s.x;
+            v[1] = s.y;
+          }
+        }
+        if (st & 1) tma_ph1 ^= (tma_a2 ? 1u : 0u); else tma_ph0 ^= (tma_a2 ? 1u : 0u);
+        uint32_t hv[4], lv[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const float hr = bf16_round(v[2 * i]), hi_ = bf16_round(v[2 * i + 1]);
+          hv[i] = pack_bf16x2(hr, hi_);
+          lv[i] = pack_bf16x2(v[2 * i] - hr, v[2 * i + 1] - hi_);
+        }
+        unsigned char* atom = abf + (cell >> 3) * 1024;
+        *reinterpret_cast<uint4*>(atom + tc::sw128_offset(cell & 7, q)) = make_uint4(hv[0], hv[1], hv[2], hv[3]);
+        *reinterpret_cast<uint4*>(atom + tc::sw128_offset(cell & 7, 4 + q)) = make_uint4(lv[0], lv[1], lv[2], lv[3]);
+        tc::fence_proxy_async_smem();
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) G[q][c] = G[q + 1][c];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) G[4][c] = make_float2(0.f, 0.f);
+      __syncthreads();
+      if (*s_abort) break;
+      if (full) {
+        if (tid == 0) {
+          tc::tc_fence_after();
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            // rows 64..127 of A read the B buffer (LBO = its offset); their
+            // results are not used
+            const uint64_t ad = tc::smem_desc(sa + k * 2048, sg - sa, 1024, tc::kLayoutSw128);
+            const uint64_t bd = tc::smem_desc(sg + k * 2048, 0, 1024, tc::kLayoutSw128);
+            tc::mma_bf16(tmem_d, ad, bd, tcc::kIdesc, !(first_mma && k == 0));
+          }
+          tc::mma_commit(&bars[2]);
+        }
+        first_mma = false;
+        mma_pending = true;
+      }
+    }
+    cp_async_wait<0>();
+    if (mma_pending) {
+      if (!tc::mbar_wait(&bars[2], mma_ph)) *s_abort = 3;
+      mma_ph ^= 1u;
+      mma_pending = false;
+    }
+    __syncthreads();
+    if (*s_abort) break;
+    // accumulator -> stage[row][col] (rows 0..63 = lanes of warps 0 and 1)
+    tc::tc_fence_after();
+    if (warp < 2) {
+      const int row = warp * 32 + (tid & 31);
+#pragma unroll
+      for (int half = 0; half < 2; ++half) {
+        float d[32];
+        tc::tmem_ld_32x32b_x32(tmem_d + ((uint32_t)(warp * 32) << 16) + half * 32, d);
+#pragma unroll
+        for (int i = 0; i < 32; ++i) stage[row * 65 + half * 32 + i] = d[i];
+      }
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    {
+      const int b2 = tid >> 4, b3 = tid & 15;
+      double sr = 0.0, si = 0.0;
+#pragma unroll
+      for (int h = 0; h < 2; ++h)
+#pragma unroll
+        for (int h2 = 0; h2 < 2; ++h2) {
+          const float* rr = stage + (h * 32 + 2 * b2) * 65 + h2 * 32 + 2 * b3;
+          const float* ri = rr + 65;  // row of the imaginary part of a2
+          sr += (double)rr[0] - (double)ri[1];
+          si += (double)rr[1] + (double)ri[0];
+        }
+      dacc[(b2 * kMaxBins + b3) * 2] += sr;
+      dacc[(b2 * kMaxBins + b3) * 2 + 1] += si;
+    }
+    __syncthreads();  // stage (a3 buffer) idle before the next item's prologue
+  }
+  const int why = *s_abort;
+  for (int i = tid; i < 2 * kMaxBins * kMaxBins; i += ct::kThreads)
+    A.partial[(long long)blockIdx.x * 2 * kMaxBins * kMaxBins + i] = why ? __longlong_as_double(0x7ff8000000000000LL) : dacc[i];
+  if (why && tid == 0 && A.status) atomicCAS(A.status, 0, why);
+  __syncthreads();
+  if (warp == 0) {
+    tc::tc_fence_after();
+    tc::tmem_dealloc(tmem_d, tcc::kTmemCols);
+  }
+}
+
 // out[o] = sum over blocks of partial[blk * nout + o]
 __global__ void mp_reduce_kernel(const double* __restrict__ partial, int nblocks, int nout, double* __restrict__ out,
                                  double scale = 1.0) {
@@ -903,18 +1222,37 @@ size_t table_floats(int J) {
 
 // Workspace: j_l table, partial sums and, for nb > 1, the bin-major fields
 // (nb * L^3 complex64) that cuFFT transforms before they are interleaved.
+namespace {
+// The one workspace layout of the fields and contraction calls.
+struct MpWs {
+  float* T;          // radial table [n2][16]
+  float* Pf;         // phi power, float
+  double* partial;   // per-block partial sums [1024][16][16][2]
+  double* dout;      // reduced S [16][16][2]
+  int* status;       // bounded-wait status of the tensor-core contraction
+  float2* binmajor;  // nb > 1: bin-major fields [nb][L^3]
+  size_t used;
+};
+MpWs carve_ws(void* ws, size_t cap, int J, int nb) {
+  hermes::Carver c(ws, cap);
+  MpWs w;
+  c.take<float>(2 * kMaxBins);  // rho double-float (kept for layout stability)
+  w.T = c.take<float>(table_floats(J));
+  w.Pf = c.take<float>((1 << J) + 1);
+  w.partial = c.take<double>((size_t)1024 * kMaxBins * kMaxBins * 2);
+  w.dout = c.take<double>((size_t)kMaxBins * kMaxBins * 2);
+  w.status = c.take<int>(16);
+  w.binmajor = nb > 1 ? c.take<float2>((size_t)nb << (3 * J)) : nullptr;
+  w.used = c.used;
+  return w;
+}
+}  // namespace
+
 extern "C" int hermes_multipole_workspace_size(int J, int nb, size_t* bytes) {
   if (!bytes) return fail(HERMES_ERR_INVALID, "bytes is NULL");
   if (J < 4 || J > 10) return fail(HERMES_ERR_INVALID, "multipole: J=%d outside [4,10]", J);
   if (nb < 1 || nb > kMaxBins) return fail(HERMES_ERR_INVALID, "multipole: nb=%d outside [1,%d]", nb, kMaxBins);
-  hermes::Carver c(nullptr, 0);
-  c.take<float>(2 * kMaxBins);         // rho double-float
-  c.take<float>(table_floats(J));      // j_l table
-  c.take<float>((1 << J) + 1);         // phi power float
-  c.take<double>((size_t)1024 * kMaxBins * kMaxBins * 2);  // partials
-  c.take<double>((size_t)kMaxBins * kMaxBins * 2);
-  if (nb > 1) c.take<float2>((size_t)nb << (3 * J));     // bin-major fields
-  *bytes = c.used;
+  *bytes = carve_ws(nullptr, 0, J, nb).used;
   return HERMES_OK;
 }
 
@@ -949,14 +1287,11 @@ int fields_setup(const void* half_spec, int J, int l, int m, int nb, const doubl
   ctx->N = 1LL << (3 * J);
   ctx->s = hermes::as_stream(stream);
   ctx->nsm = sm_count();
-  hermes::Carver c(workspace, workspace_bytes);
-  c.take<float>(2 * kMaxBins);
-  ctx->T = c.take<float>(table_floats(J));
-  ctx->Pf = c.take<float>(ctx->L + 1);
-  c.take<double>((size_t)1024 * kMaxBins * kMaxBins * 2);
-  c.take<double>((size_t)kMaxBins * kMaxBins * 2);
+  const MpWs w = carve_ws(workspace, workspace_bytes, J, nb);
+  ctx->T = w.T;
+  ctx->Pf = w.Pf;
   ctx->out = static_cast<float2*>(fields_out);
-  ctx->binmajor = nb > 1 ? c.take<float2>((size_t)nb * ctx->N) : ctx->out;
+  ctx->binmajor = nb > 1 ? w.binmajor : ctx->out;
   mp_power_to_f32<<<(ctx->L + 1 + 255) / 256, 256, 0, ctx->s>>>(phi_power, ctx->L + 1, ctx->Pf);
   HERMES_LAUNCH_CHECK("mp_power_to_f32");
   return HERMES_OK;
@@ -1070,11 +1405,48 @@ extern "C" int hermes_multipole_fields_table(const void* half_spec, int J, int l
   return fields_run(ctx, half_spec, J, l, m, nb);
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// dependency on libcuda).
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  });
+  return fn;
+}
+
+// 4-D tensor map over bin-interleaved fields [x][y][z][16 complex] (float32
+// view, innermost 32 floats), box 32 x 8 (z) x 8 (y) x 1 (x): one contraction
+// tile's a2 plane, 64 rows of 128 bytes.
+static int make_a2_map(const void* fields, int L, CUtensorMap* map) {
+  auto enc = tensor_map_encoder();
+  if (!enc) return fail(HERMES_ERR_CUDA, "cuTensorMapEncodeTiled is unavailable");
+  const cuuint64_t dims[4] = {2 * kBinStride, (cuuint64_t)L, (cuuint64_t)L, (cuuint64_t)L};
+  const cuuint64_t row = sizeof(float) * 2 * kBinStride;
+  const cuuint64_t strides[3] = {row, row * L, row * L * L};
+  const cuuint32_t box[4] = {2 * kBinStride, ct::TZ, ct::TY, 1};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<void*>(fields), dims, strides, box, estr,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(HERMES_ERR_CUDA, "cuTensorMapEncodeTiled failed: %d", (int)r);
+  return HERMES_OK;
+}
+
+enum { kEngineTensor = 0, kEngineSimt = 1 };
+
 // Launches the contraction and the float64 reduction into dout [16][16][2]
-// (already multiplied by `scale`), with no host synchronisation.
+// (already multiplied by `scale`), with no host synchronisation.  engine:
+// tensor-core bin product (mp_contract_tc_kernel) or FP32 CUDA cores
+// (mp_contract_kernel).
 static int mp_contract_launch(const float* eps1, const void* fields2, int nb2, const void* fields3, int nb3,
                               int conj_sign, const double* gamma, int J, int chunk_x, int ctas_per_sm, double scale,
-                              double* dout, void* workspace, size_t workspace_bytes, cudaStream_t s) {
+                              double* dout, void* workspace, size_t workspace_bytes, cudaStream_t s, int engine) {
   if (!eps1 || !fields2 || !gamma || !dout) return fail(HERMES_ERR_INVALID, "multipole_contract: NULL argument");
   if (nb2 < 1 || nb2 > kMaxBins) return fail(HERMES_ERR_INVALID, "multipole_contract: nb2=%d", nb2);
   const int conj_src = fields3 == nullptr;
@@ -1098,18 +1470,18 @@ static int mp_contract_launch(const float* eps1, const void* fields2, int nb2, c
   if (rc) return rc;
   if (!workspace || workspace_bytes < need)
     return fail(HERMES_ERR_WORKSPACE, "multipole_contract: workspace %zu < %zu", workspace_bytes, need);
-  hermes::Carver c(workspace, workspace_bytes);
-  c.take<float>(2 * kMaxBins);
-  c.take<float>(table_floats(J));
-  c.take<float>(L + 1);
-  double* partial = c.take<double>((size_t)1024 * kMaxBins * kMaxBins * 2);
-  static bool smem_set[64] = {false};
+  const MpWs w = carve_ws(workspace, workspace_bytes, J, 1);
+  static bool smem_set[2][64] = {{false}};
   int dev = 0;
   cudaGetDevice(&dev);
-  if (dev < 0 || dev >= 64 || !smem_set[dev]) {  // once per device, before any stream capture
-    HERMES_CUDA_TRY(cudaFuncSetAttribute(mp_contract_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)ct::kSmem));
-    if (dev >= 0 && dev < 64) smem_set[dev] = true;
+  if (dev < 0 || dev >= 64 || !smem_set[engine][dev]) {  // once per device, before any stream capture
+    if (engine == kEngineTensor)
+      HERMES_CUDA_TRY(cudaFuncSetAttribute(mp_contract_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)tcc::kSmem));
+    else
+      HERMES_CUDA_TRY(cudaFuncSetAttribute(mp_contract_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)ct::kSmem));
+    if (dev >= 0 && dev < 64) smem_set[engine][dev] = true;
   }
   // field layout follows hermes_multipole_fields: [cell][16] for nb > 1, [cell] for nb == 1
   ContractArgs A;
@@ -1123,14 +1495,27 @@ static int mp_contract_launch(const float* eps1, const void* fields2, int nb2, c
   A.J = J;
   A.CX = chunk_x;
   A.gm = make_gamma(gamma);
-  A.partial = partial;
+  A.partial = w.partial;
+  A.status = w.status;
   const int n_items = (L / A.CX) * (L / ct::TY) * (L / ct::TZ);
   int nblk = ctas_per_sm * sm_count();
   if (nblk > n_items) nblk = n_items;
   if (nblk > 1024) nblk = 1024;
-  mp_contract_kernel<<<nblk, ct::kThreads, ct::kSmem, s>>>(A);
-  HERMES_LAUNCH_CHECK("mp_contract_kernel");
-  mp_reduce_kernel<<<kMaxBins * kMaxBins * 2, 256, 0, s>>>(partial, nblk, kMaxBins * kMaxBins * 2, dout, scale);
+  if (engine == kEngineTensor) {
+    CUtensorMap map;
+    memset(&map, 0, sizeof(map));
+    if (A.s2 == kBinStride) {
+      rc = make_a2_map(fields2, L, &map);
+      if (rc) return rc;
+    }
+    HERMES_CUDA_TRY(cudaMemsetAsync(w.status, 0, sizeof(int), s));
+    mp_contract_tc_kernel<<<nblk, ct::kThreads, tcc::kSmem, s>>>(A, map);
+    HERMES_LAUNCH_CHECK("mp_contract_tc_kernel");
+  } else {
+    mp_contract_kernel<<<nblk, ct::kThreads, ct::kSmem, s>>>(A);
+    HERMES_LAUNCH_CHECK("mp_contract_kernel");
+  }
+  mp_reduce_kernel<<<kMaxBins * kMaxBins * 2, 256, 0, s>>>(w.partial, nblk, kMaxBins * kMaxBins * 2, dout, scale);
   HERMES_LAUNCH_CHECK("mp_reduce_kernel");
   return HERMES_OK;
 }
@@ -1145,21 +1530,20 @@ extern "C" int hermes_multipole_contract(const float* eps1, const void* fields2,
   if (rc) return rc;
   if (!workspace || workspace_bytes < need)
     return fail(HERMES_ERR_WORKSPACE, "multipole_contract: workspace %zu < %zu", workspace_bytes, need);
-  hermes::Carver c(workspace, workspace_bytes);
-  c.take<float>(2 * kMaxBins);
-  c.take<float>(table_floats(J));
-  c.take<float>((1 << J) + 1);
-  c.take<double>((size_t)1024 * kMaxBins * kMaxBins * 2);
-  double* dout = c.take<double>((size_t)kMaxBins * kMaxBins * 2);
+  const MpWs w = carve_ws(workspace, workspace_bytes, J, 1);
   cudaStream_t s = hermes::as_stream(stream);
   const double scale = 4.0 * 3.141592653589793 / (double)(1LL << (3 * J));
-  rc = mp_contract_launch(eps1, fields2, nb2, fields3, nb3, conj_sign, gamma, J, 0, 0, scale, dout, workspace,
-                          workspace_bytes, s);
+  rc = mp_contract_launch(eps1, fields2, nb2, fields3, nb3, conj_sign, gamma, J, 0, 0, scale, w.dout, workspace,
+                          workspace_bytes, s, kEngineTensor);
   if (rc) return rc;
   if (fields3 == nullptr) nb3 = nb2;
   std::vector<double> h((size_t)kMaxBins * kMaxBins * 2);
-  HERMES_CUDA_TRY(cudaMemcpyAsync(h.data(), dout, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, s));
+  int status = 0;
+  HERMES_CUDA_TRY(cudaMemcpyAsync(h.data(), w.dout, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, s));
+  HERMES_CUDA_TRY(cudaMemcpyAsync(&status, w.status, sizeof(int), cudaMemcpyDeviceToHost, s));
   HERMES_CUDA_TRY(cudaStreamSynchronize(s));
+  if (status != 0)
+    return fail(HERMES_ERR_CUDA, "multipole_contract: bounded wait %d in the tensor-core kernel gave up", status);
   for (int a = 0; a < nb2; ++a)
     for (int b = 0; b < nb3; ++b) {
       out[(a * nb3 + b) * 2] = h[(a * kMaxBins + b) * 2];
@@ -1168,13 +1552,39 @@ extern "C" int hermes_multipole_contract(const float* eps1, const void* fields2,
   return HERMES_OK;
 }
 
+static int contract_async(const float* eps1, const void* fields2, int nb2, const void* fields3, int nb3,
+                          int conj_sign, const double* gamma, int J, int chunk_x, int ctas_per_sm, double* dev_out,
+                          void* workspace, size_t workspace_bytes, void* stream, int engine) {
+  const double scale = 4.0 * 3.141592653589793 / (double)(1LL << (3 * (J < 0 ? 0 : (J > 10 ? 10 : J))));
+  return mp_contract_launch(eps1, fields2, nb2, fields3, nb3, conj_sign, gamma, J, chunk_x, ctas_per_sm, scale,
+                            dev_out, workspace, workspace_bytes, hermes::as_stream(stream), engine);
+}
+
 extern "C" int hermes_multipole_contract_async(const float* eps1, const void* fields2, int nb2, const void* fields3,
                                                int nb3, int conj_sign, const double* gamma, int J, int chunk_x,
                                                int ctas_per_sm, double* dev_out, void* workspace,
                                                size_t workspace_bytes, void* stream) {
-  const double scale = 4.0 * 3.141592653589793 / (double)(1LL << (3 * (J < 0 ? 0 : (J > 10 ? 10 : J))));
-  return mp_contract_launch(eps1, fields2, nb2, fields3, nb3, conj_sign, gamma, J, chunk_x, ctas_per_sm, scale,
-                            dev_out, workspace, workspace_bytes, hermes::as_stream(stream));
+  return contract_async(eps1, fields2, nb2, fields3, nb3, conj_sign, gamma, J, chunk_x, ctas_per_sm, dev_out,
+                        workspace, workspace_bytes, stream, kEngineTensor);
+}
+
+extern "C" int hermes_multipole_contract_simt_async(const float* eps1, const void* fields2, int nb2,
+                                                    const void* fields3, int nb3, int conj_sign, const double* gamma,
+                                                    int J, int chunk_x, int ctas_per_sm, double* dev_out,
+                                                    void* workspace, size_t workspace_bytes, void* stream) {
+  return contract_async(eps1, fields2, nb2, fields3, nb3, conj_sign, gamma, J, chunk_x, ctas_per_sm, dev_out,
+                        workspace, workspace_bytes, stream, kEngineSimt);
+}
+
+extern "C" int hermes_multipole_contract_status(const void* workspace, size_t workspace_bytes, int J, int* status,
+                                                void* stream) {
+  if (!workspace || !status) return fail(HERMES_ERR_INVALID, "multipole_contract_status: NULL argument");
+  if (J < 4 || J > 10) return fail(HERMES_ERR_INVALID, "multipole_contract_status: J=%d outside [4,10]", J);
+  const MpWs w = carve_ws(const_cast<void*>(workspace), workspace_bytes, J, 1);
+  cudaStream_t s = hermes::as_stream(stream);
+  HERMES_CUDA_TRY(cudaMemcpyAsync(status, w.status, sizeof(int), cudaMemcpyDeviceToHost, s));
+  HERMES_CUDA_TRY(cudaStreamSynchronize(s));
+  return HERMES_OK;
 }
 
 extern "C" int hermes_multipole_contract_plain(const float* eps1, const void* a2, const void* a3,

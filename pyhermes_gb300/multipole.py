@@ -231,21 +231,51 @@ def multipole_contract(eps1, fields2, nb2, gamma, J, fields3=None, nb3=None, con
     return out[..., 0] + 1j * out[..., 1]
 
 
+ENGINES = ("tensor", "simt")
+
+
 def multipole_contract_async(eps1, fields2, nb2, gamma_c, J, dev_out, fields3=None, nb3=None, conj_sign=1,
-                             chunk_x=0, ctas_per_sm=0, ws=None):
+                             chunk_x=0, ctas_per_sm=0, ws=None, engine="tensor"):
     """hermes_multipole_contract_async: S (times 4 pi / L^3) into the device
     float64 tensor dev_out [16, 16, 2] on the current stream, no host sync.
-    gamma_c: a ctypes double[9] (kept alive by the caller during capture)."""
+    gamma_c: a ctypes double[9] (kept alive by the caller during capture).
+    engine: 'tensor' (bin x bin product on tcgen05, split BF16) or 'simt'
+    (the all-FP32 CUDA-core kernel)."""
+    if engine not in ENGINES:
+        raise ValueError(f"engine must be one of {ENGINES}")
     nb3 = nb2 if fields3 is None else nb3
     dev = eps1.device
     if ws is None:
         ws = _workspace(_ws_bytes(J, max(nb2, nb3)), dev)
-    _lib.check(_lib.load().hermes_multipole_contract_async(_ptr(eps1), _ptr(fields2), nb2, _ptr(fields3), nb3,
-                                                           int(conj_sign), gamma_c, J, int(chunk_x),
-                                                           int(ctas_per_sm), _ptr(dev_out), _ptr(ws), ws.numel(),
-                                                           _stream_ptr(dev)),
+    lib = _lib.load()
+    fn = lib.hermes_multipole_contract_async if engine == "tensor" else lib.hermes_multipole_contract_simt_async
+    _lib.check(fn(_ptr(eps1), _ptr(fields2), nb2, _ptr(fields3), nb3, int(conj_sign), gamma_c, J, int(chunk_x),
+                  int(ctas_per_sm), _ptr(dev_out), _ptr(ws), ws.numel(), _stream_ptr(dev)),
                "hermes_multipole_contract_async")
     return dev_out
+
+
+def contract_status(J, ws=None, device="cuda"):
+    """0, or 1 when a bounded wait of the last tensor-core contraction on the
+    workspace gave up (its results are then NaN)."""
+    if ws is None:
+        ws = _workspace(_ws_bytes(J, 1), torch.device(device))
+    st = ctypes.c_int(0)
+    _lib.check(_lib.load().hermes_multipole_contract_status(_ptr(ws), ws.numel(), J, ctypes.byref(st),
+                                                            _stream_ptr(ws.device)), "hermes_multipole_contract_status")
+    return st.value
+
+
+def multipole_contract_engine(eps1, fields2, nb2, gamma, J, fields3=None, nb3=None, conj_sign=1, engine="tensor",
+                              chunk_x=0, ctas_per_sm=0):
+    """S[b2, b3] complex128 from a chosen engine (async launch + one read)."""
+    nb3 = nb2 if fields3 is None else nb3
+    g = (ctypes.c_double * 9)(*np.asarray(gamma, dtype=np.float64).ravel())
+    out = torch.zeros((MAX_BINS, MAX_BINS, 2), dtype=torch.float64, device=eps1.device)
+    multipole_contract_async(eps1, fields2, nb2, g, J, out, fields3=fields3, nb3=nb3, conj_sign=conj_sign,
+                             chunk_x=chunk_x, ctas_per_sm=ctas_per_sm, engine=engine)
+    o = out[:nb2, :nb3].cpu().numpy()
+    return o[..., 0] + 1j * o[..., 1]
 
 
 def multipole_contract_plain(eps1, a2, a3, gamma, J):
@@ -348,7 +378,11 @@ def combine_multipole_m_terms(m_values, l):
 class MultipoleEngine:
     """Batched multipole contraction of three fields over radius pairs."""
 
-    def __init__(self, eps1, eps2, eps3, phi_array, J, box_size, phi_resolution=1024, share23=None):
+    def __init__(self, eps1, eps2, eps3, phi_array, J, box_size, phi_resolution=1024, share23=None,
+                 engine="tensor"):
+        if engine not in ENGINES:
+            raise ValueError(f"engine must be one of {ENGINES}")
+        self.engine = engine
         self.J = int(J)
         self.L = 1 << self.J
         self.box = float(box_size)
@@ -385,13 +419,14 @@ class MultipoleEngine:
                 if shared and i0 == j0:
                     t1 = time.perf_counter()
                     self.timing["fields_s"] += t1 - t0
-                    S = multipole_contract(self.eps1, f2, len(c12), self.gamma, self.J,
-                                           conj_sign=(-1) ** ((l + m) % 2))
+                    S = multipole_contract_engine(self.eps1, f2, len(c12), self.gamma, self.J,
+                                                  conj_sign=(-1) ** ((l + m) % 2), engine=self.engine)
                 else:
                     f3 = self._fields(self.spec3, l, -m, c13)
                     t1 = time.perf_counter()
                     self.timing["fields_s"] += t1 - t0
-                    S = multipole_contract(self.eps1, f2, len(c12), self.gamma, self.J, fields3=f3, nb3=len(c13))
+                    S = multipole_contract_engine(self.eps1, f2, len(c12), self.gamma, self.J, fields3=f3,
+                                                  nb3=len(c13), engine=self.engine)
                     del f3
                 self.timing["contract_s"] += time.perf_counter() - t1
                 t0 = time.perf_counter()
@@ -572,6 +607,9 @@ class Corr_3PCF_Multipole:
         if backend not in {"gb300", "gpu", "plain", "cpu"}:
             raise ValueError("summation_backend must be 'gb300', 'gpu', 'plain' or 'cpu'.")
         self.summation_backend = "plain" if backend == "plain" else "gb300"
+        self.contraction_engine = str(tp.get("contraction_engine", "tensor")).strip().lower()
+        if self.contraction_engine not in ENGINES:
+            raise ValueError(f"contraction_engine must be one of {ENGINES}.")
         prods = tp.get("products", "zeta_l")
         prods = [prods] if isinstance(prods, str) else list(prods)
         self.products = []
@@ -908,7 +946,7 @@ class Corr_3PCF_Multipole:
             same23 = (self.sfc_field2 is self.sfc_field3 or self.sfc_field2 == self.sfc_field3) and \
                 self.window2 == self.window3 and (product != "delta_ddd_l" or self.random2 == self.random3)
             eng = MultipoleEngine(e1, e2, e2 if same23 else e3, phi, ref.J, ref.box_size, ref.phi_resolution,
-                                  share23=same23)
+                                  share23=same23, engine=self.contraction_engine)
             if self.summation_backend == "plain":
                 vals = eng.ddd_plain(pairs, self.l_min, self.l_max)
             else:

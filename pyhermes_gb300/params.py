@@ -146,7 +146,7 @@ DEFAULTS = {
         "threads": 1,
         "products": "zeta_l",
         "fout_path": "",
-        "contraction": "mixed",
+        "contraction_engine": "tensor",
     },
     "Corr_3PCF": {
         "sfc_field": "", "sfc_field1": "", "sfc_field2": "", "sfc_field3": "",

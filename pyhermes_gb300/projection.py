@@ -54,20 +54,11 @@ class SFCProjection:
         self.fout_path = tp["fout_path"]
 
     def _read_catalogue(self):
-        """Positions and per-particle values from ``fin`` (a catalogue file,
-        pyhermes/base/sfc_projection.py:145-167): the reader for fin.format
-        (or the file name), then catalog_weight_key / field_value_key
-        resolved to named fields or unit values."""
-        from .readers import read_particle_data, resolve_particle_value
-
-        if not self.fin.get("path"):
-            raise ValueError("SFCProjection needs particle_pos or fin.path.")
-        data = read_particle_data(self.fin["path"], self.fin.get("format"), download=self.fin.get("download", {}),
-                                  **dict(self.fin.get("reader_params") or {}))
-        cw, ck = resolve_particle_value(data, self.fin.get("catalog_weight_key"), label="Catalogue weight")
-        fv, fk = resolve_particle_value(data, self.fin.get("field_value_key"), label="Field value")
-        self.fin["catalog_weight_key"], self.fin["field_value_key"] = ck, fk
-        return np.asarray(data["pos"], dtype=np.float64), cw, fv
+        """Catalogue files (fin.path) are read by the caller: this package
+        projects positions given as arrays (particle_pos, with optional
+        catalog_weight / field_value)."""
+        raise ValueError("SFCProjection needs particle_pos: read the catalogue file (fin.path) in the caller and pass "
+                         "its positions, weights and values as arrays.")
 
     def _load_particle_input(self):
         """pyhermes/base/sfc_projection.py:125-193: array input, or a

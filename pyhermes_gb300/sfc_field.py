@@ -388,18 +388,8 @@ class SFCField:
                 cw = np.asarray(z["catalog_weight"], dtype=np.float64)
                 fv = np.asarray(z["field_value"], dtype=np.float64)
         else:
-            from .readers import read_particle_data, resolve_particle_value
-
-            fin = self.sfc_info.get("fin") or {}
-            if not fin.get("path", ""):
-                raise ValueError("Input particle path is not specified.")
-            data = read_particle_data(fin["path"], fin.get("format"), download=fin.get("download", {}),
-                                      **dict(fin.get("reader_params") or {}))
-            pos = data["pos"]
-            cw = np.asarray(resolve_particle_value(data, fin.get("catalog_weight_key"), "Catalogue weight")[0],
-                            dtype=np.float64)
-            fv = np.asarray(resolve_particle_value(data, fin.get("field_value_key"), "Field value")[0],
-                            dtype=np.float64)
+            raise ValueError("This field has no saved particle dataset (save_particle_data); catalogue files are "
+                             "read by the caller, so pass the particle positions and weights explicitly.")
         return {"pos": pos, "catalog_weight": cw, "normalized_catalog_weight": cw / float(self.catalog_weight_sum),
                 "field_value": fv, "projection_weight": cw * fv / den}
 

@@ -524,156 +524,14 @@ def gen_field_algebra():
     _save("field_algebra_J4", **out)
 
 
-def _write_record(f, arr):
-    b = np.ascontiguousarray(arr).tobytes()
-    np.array([len(b)], dtype=np.int32).tofile(f)
-    f.write(b)
-    np.array([len(b)], dtype=np.int32).tofile(f)
-
-
-def write_catalogues(d):
-    """Small catalogues in every reader format (written here from the
-    formats' layouts): bin (x, y, z, w, v float32), npz, a legacy Gadget
-    format-1 snapshot in two files with per-particle masses, a Gadget FoF
-    file and a Quijote group_tab catalogue in two files."""
-    os.makedirs(d, exist_ok=True)
-    rng = np.random.default_rng(121)
-    n = 600
-    pos = rng.uniform(0.0, 1000.0, (n, 3)).astype(np.float32)
-    pos[:200] = pos[:200] * 0.3 + 350.0
-    w = rng.lognormal(0.0, 0.3, n).astype(np.float32)
-    v = rng.uniform(0.5, 2.0, n).astype(np.float32)
-    vel = rng.normal(0.0, 300.0, (n, 3)).astype(np.float32)
-    np.column_stack([pos, w, v]).astype(np.float32).tofile(os.path.join(d, "cat.bin"))
-    np.savez(os.path.join(d, "cat.npz"), pos=pos, weight=w, value=v)
-    hdr = np.dtype([("npart", np.uint32, 6), ("massarr", np.float64, 6), ("time", np.float64),
-                    ("redshift", np.float64), ("flag_sfr", np.int32), ("flag_feedback", np.int32),
-                    ("npartTotal", np.int32, 6), ("flag_cooling", np.int32), ("num_files", np.int32),
-                    ("BoxSize", np.float64), ("Omega0", np.float64), ("OmegaLambda", np.float64),
-                    ("HubbleParam", np.float64), ("fill", np.int32, 24)])
-    for i, sl in enumerate((slice(0, 350), slice(350, n))):
-        h = np.zeros(1, dtype=hdr)
-        h["npart"][0, 1] = sl.stop - sl.start
-        h["npartTotal"][0, 1] = n
-        h["num_files"] = 2
-        h["BoxSize"] = 1000.0
-        h["redshift"] = 0.5
-        with open(os.path.join(d, f"snap_000.{i}"), "wb") as f:
-            _write_record(f, h)
-            _write_record(f, pos[sl])
-            _write_record(f, vel[sl])
-            _write_record(f, np.arange(sl.start, sl.stop, dtype=np.int32))
-            _write_record(f, w[sl])
-    fh = np.dtype([("Ngroups", np.int64), ("Nsubhalos", np.int64), ("Nids", np.int64), ("TotNgroups", np.int64),
-                   ("TotNsubhalos", np.int64), ("TotNids", np.int64), ("num_files", np.int32), ("dummy", np.int32),
-                   ("time", np.float64), ("redshift", np.float64), ("BoxSize", np.float64)])
-    h = np.zeros(1, dtype=fh)
-    h["Ngroups"] = h["TotNgroups"] = n
-    h["num_files"] = 1
-    h["BoxSize"] = 1000.0
-    with open(os.path.join(d, "fof_000"), "wb") as f:
-        _write_record(f, h)
-        _write_record(f, (w * 100).astype(np.int32))
-        _write_record(f, w)
-        _write_record(f, pos)
-        _write_record(f, vel)
-    gdir = os.path.join(d, "groups_000")
-    os.makedirs(gdir, exist_ok=True)
-    lens = rng.integers(20, 400, n).astype(np.int32)
-    offs = np.concatenate([[0], np.cumsum(lens)[:-1]]).astype(np.int32)
-    for i, sl in enumerate((slice(0, 250), slice(250, n))):
-        m = sl.stop - sl.start
-        with open(os.path.join(gdir, f"group_tab_000.{i}"), "wb") as f:
-            np.array([m, n, int(lens[sl].sum())], dtype=np.int32).tofile(f)
-            np.array([int(lens.sum())], dtype=np.uint64).tofile(f)
-            np.array([2], dtype=np.uint32).tofile(f)
-            lens[sl].tofile(f)
-            offs[sl].tofile(f)
-            (w[sl] * 1e-3).astype(np.float32).tofile(f)
-            (pos[sl] * 1e3).astype(np.float32).tofile(f)
-            vel[sl].tofile(f)
-            np.zeros((m, 6), dtype=np.float32).tofile(f)
-            np.zeros((m, 6), dtype=np.float32).tofile(f)
-
-
-def gen_catalogues():
-    """The reference's readers and SFCProjection on catalogue files
-    (io/readers.py, base/sfc_projection.py:125-193)."""
-    from pyhermes.base.sfc_projection import SFCProjection
-    from pyhermes.io.readers import read_particle_data
-
-    d = os.path.join(HERE, "catalogues")
-    write_catalogues(d)
-    cases = {
-        "bin": (os.path.join(d, "cat.bin"), {"format": "bin", "ncols": 5, "fields": {"weight": 3, "value": 4}}),
-        "npz": (os.path.join(d, "cat.npz"), {}),
-        "gadget": (os.path.join(d, "snap_000"), {"format": "gadget"}),
-        "gadget_fof": (os.path.join(d, "fof_000"), {"format": "gadget-fof"}),
-        "fof_file": (os.path.join(d, "groups_000", "group_tab_000.0"), {"redshift": 0.5}),
-        "fof_dir": (d, {"format": "fof", "snapnum": 0}),
-    }
-    out = {}
-    for name, (path, params) in cases.items():
-        data = read_particle_data(path, **dict(params))
-        for k, val in data.items():
-            if isinstance(val, np.ndarray):
-                out[f"{name}__{k}"] = val
-            elif np.isscalar(val):
-                out[f"{name}__{k}"] = np.asarray(val)
-    for name, fin in {"proj_bin": {"path": os.path.join(d, "cat.bin"), "format": "bin",
-                                   "reader_params": {"ncols": 5, "fields": {"weight": 3, "value": 4}},
-                                   "catalog_weight_key": "weight", "field_value_key": "value"},
-                      "proj_fof": {"path": os.path.join(d, "groups_000", "group_tab_000.0"), "format": "fof",
-                                   "reader_params": {"fields": {"mass": "mass"}},
-                                   "catalog_weight_key": "mass"}}.items():
-        f = SFCProjection({"SFCProjection": {"fin": fin, "J": 4, "box_size": 1000.0,
-                                             "weight_normalization": "catalog"}}).run(save_result=False)
-        out[name + "__info"] = np.array(_info_json({k: v for k, v in f.sfc_info.items() if k != "fin"}))
-        out[name + "__fin"] = np.array(_info_json({k: v for k, v in f.sfc_info["fin"].items() if k != "path"}))
-        # The field: the refshim runs the numba kernels as plain Python, where
-        # float32 positions stay float32 under NumPy 2 scalar rules; numba
-        # promotes float32 x int to float64.  So the field golden is the
-        # reference's deposit of the same (float32-read) positions and values
-        # as float64 arrays, which is what the compiled reference computes.
-        rp = dict(fin.get("reader_params", {}))
-        data = read_particle_data(fin["path"], fin.get("format"), **rp)
-        params = {"particle_pos": np.asarray(data["pos"], dtype=np.float64), "J": 4, "box_size": 1000.0,
-                  "weight_normalization": "catalog",
-                  "catalog_weight": np.asarray(data[fin["catalog_weight_key"]], dtype=np.float64)}
-        if fin.get("field_value_key"):
-            params["field_value"] = np.asarray(data[fin["field_value_key"]], dtype=np.float64)
-        f2 = SFCProjection({"SFCProjection": params}).run(save_result=False)
-        out[name + "__epsilon"] = np.asarray(f2.epsilon)
-    _save("catalogues_J4", **out)
-
-
 def gen_particle_data():
-    """SFCField.get_particle_data (io/sfc_field.py:425-482) from a fin-read
-    catalogue and from a saved particle dataset (base/sfc_projection.py:
-    195-219), and Corr_3PCF particle centres taken from sfc_field1's
-    catalogue (theory/corr3pcf.py:578-613)."""
+    """SFCField.get_particle_data (io/sfc_field.py:425-482) from a saved
+    particle dataset (base/sfc_projection.py:195-219)."""
     import tempfile
 
     from pyhermes.base.sfc_projection import SFCProjection
-    from pyhermes.io.readers import read_particle_data
-    from pyhermes.theory.corr3pcf import Corr_3PCF
 
-    d = os.path.join(HERE, "catalogues")
-    fin = {"path": os.path.join(d, "cat.bin"), "format": "bin",
-           "reader_params": {"ncols": 5, "fields": {"weight": 3, "value": 4}},
-           "catalog_weight_key": "weight", "field_value_key": "value"}
     out = {}
-    f = SFCProjection({"SFCProjection": {"fin": fin, "J": 4, "box_size": 1000.0,
-                                         "weight_normalization": "field"}}).run(save_result=False)
-    data = read_particle_data(fin["path"], "bin", ncols=5, fields={"weight": 3, "value": 4})
-    f64 = SFCProjection({"SFCProjection": {"particle_pos": np.asarray(data["pos"], dtype=np.float64),
-                                           "catalog_weight": np.asarray(data["weight"], dtype=np.float64),
-                                           "field_value": np.asarray(data["value"], dtype=np.float64), "J": 4,
-                                           "box_size": 1000.0, "weight_normalization": "field"}}).run(
-        save_result=False)
-    f.epsilon = f64.epsilon  # numba's float64 arithmetic (see gen_catalogues); fin stays for re-reading
-    for k, v in f.get_particle_data().items():
-        out["fin__" + k] = np.asarray(v)
     with tempfile.TemporaryDirectory() as tmp:
         rng = np.random.default_rng(131)
         pos = rng.uniform(0.0, 1000.0, (400, 3))
@@ -687,12 +545,6 @@ def gen_particle_data():
         with np.load(os.path.join(tmp, "p.npz")) as z:
             for k in z.files:
                 out["savedfile__" + k] = z[k]
-    d3 = Corr_3PCF({"Corr_3PCF": {
-        "sfc_field": f, "random": "uniform", "r12": 150.0, "r13": 250.0, "angle_param": "mu",
-        "mu": {"mu_min": -0.8, "mu_max": 0.8, "n_mu": 3}, "n_rot": 3, "center": "particle", "base_seed": 9,
-        "weight_normalization": "field", "products": ["zeta", "ddd"]}}).run(save_result=False)
-    for k in ("ddd", "d_delta_dd", "rrr", "xi23", "r_delta_dd", "delta_ddd", "zeta"):
-        out["p3_" + k] = np.asarray(getattr(d3, k))
     _save("particle_data_J4", **out)
 
 
@@ -959,7 +811,7 @@ def gen_window_file():
     _save("window_file_J4", kernel=kernel)
 
 
-SECTIONS = {"pair_at_sample": gen_pair_at_sample, "radial_diagnostics": gen_radial_diagnostics, "phi_at_pos": gen_phi_at_pos, "full_fft_windows": gen_full_fft_windows, "custom_windows": gen_custom_windows, "mc_theta": gen_mc_theta, "composite_windows": gen_composite_windows, "particle_data": gen_particle_data, "catalogues": gen_catalogues, "field_algebra": gen_field_algebra, "rppi": gen_rppi, "io": gen_io, "cross": gen_cross, "normalization": gen_normalization, "mc3pcf_randoms": gen_mc3pcf_randoms, "random_catalogue": gen_random_catalogue, "mc3pcf_particle": gen_mc3pcf_particle, "window_file": gen_window_file, "tabulated": gen_tabulated, "counting": gen_counting, "mc3pcf": gen_mc3pcf, "phi": gen_phi, "deposit": gen_deposit, "windows": gen_windows,
+SECTIONS = {"pair_at_sample": gen_pair_at_sample, "radial_diagnostics": gen_radial_diagnostics, "phi_at_pos": gen_phi_at_pos, "full_fft_windows": gen_full_fft_windows, "custom_windows": gen_custom_windows, "mc_theta": gen_mc_theta, "composite_windows": gen_composite_windows, "particle_data": gen_particle_data, "field_algebra": gen_field_algebra, "rppi": gen_rppi, "io": gen_io, "cross": gen_cross, "normalization": gen_normalization, "mc3pcf_randoms": gen_mc3pcf_randoms, "random_catalogue": gen_random_catalogue, "mc3pcf_particle": gen_mc3pcf_particle, "window_file": gen_window_file, "tabulated": gen_tabulated, "counting": gen_counting, "mc3pcf": gen_mc3pcf, "phi": gen_phi, "deposit": gen_deposit, "windows": gen_windows,
             "convolution": gen_convolution, "corr2pcf": gen_corr2pcf, "multipole": gen_multipole}
 
 

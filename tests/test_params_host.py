@@ -59,13 +59,13 @@ def test_reference_import_paths():
     from pyhermes_gb300 import corr2pcf, counting, mc3pcf, multipole, projection, sfc_field, window
     from pyhermes_gb300.base import SFCProjection as P2, WindowFunc as W2
     from pyhermes_gb300.io import (Corr2PCFData, Corr3PCFData, Corr3PCFMultipoleData, CountingData, SFCField,
-                                   WindowFunc, check_fout, resolve_data_path)
+                                   WindowFunc, check_fout)
     from pyhermes_gb300.theory import Corr_2PCF, Corr_3PCF, Corr_3PCF_Multipole, Counting, SFCProjection
 
     assert (Corr_2PCF, Corr_3PCF, Corr_3PCF_Multipole, Counting) == (
         corr2pcf.Corr_2PCF, mc3pcf.Corr_3PCF, multipole.Corr_3PCF_Multipole, counting.Counting)
     assert SFCProjection is P2 is projection.SFCProjection and WindowFunc is W2 is window.WindowFunc
-    assert SFCField is sfc_field.SFCField and check_fout is sfc_field.check_fout and callable(resolve_data_path)
+    assert SFCField is sfc_field.SFCField and check_fout is sfc_field.check_fout
     assert (Corr2PCFData, Corr3PCFData, Corr3PCFMultipoleData, CountingData) == (
         corr2pcf.Corr2PCFData, mc3pcf.Corr3PCFData, multipole.Corr3PCFMultipoleData, counting.CountingData)
 

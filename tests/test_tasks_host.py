@@ -49,7 +49,8 @@ def oracle_kernels(monkeypatch):
         return vals, k0
 
     class Engine:
-        def __init__(self, eps1, eps2, eps3, phi_array, J, box_size, phi_resolution=1024, share23=None):
+        def __init__(self, eps1, eps2, eps3, phi_array, J, box_size, phi_resolution=1024, share23=None,
+                     engine="tensor"):
             self.e = [e.double().cpu().numpy() for e in (eps1, eps2, eps3)]
             self.phi, self.box, self.res = phi_array, box_size, phi_resolution
             self.timing = {"fields_s": 0.0, "contract_s": 0.0}
