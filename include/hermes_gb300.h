@@ -255,9 +255,10 @@ int hermes_multipole_contract_async(const float* eps1, const void* fields2, int 
 /* Contraction engines.  hermes_multipole_contract and _async run the stencil
  * G^{b3}(y) = sum Gamma3 eps1 a3 on the CUDA cores (FP32) and the bin x bin
  * product S += a2^{b2} G^{b3} of every plane on the tcgen05 tensor cores:
- * both operands split into BF16 hi + lo parts (~16 significant bits each,
- * all four partial products summed), FP32 accumulation in tensor memory over
- * a work item, float64 across items (corr3pcf_multipoles.py:33-58 + :99-131).
+ * BF16x3 operands (each FP32 value split into three BF16 parts, ~24
+ * significant bits, all nine partial products summed), FP32 accumulation
+ * in tensor memory over a work item, float64 across items
+ * (corr3pcf_multipoles.py:33-58 + :99-131).
  * hermes_multipole_contract_simt_async: the same sum with the product on the
  * CUDA cores in FP32 (the all-FP32 comparison path); same arguments.
  * hermes_multipole_contract_status: after a tensor-core contraction on the
@@ -350,6 +351,15 @@ int hermes_mse_grad(const float* y, const float* target, int64_t n, float* dy,
 int hermes_adam_step(float* params, const float* grads, float* m, float* v, int64_t n,
                      float lr, float b1, float b2, float eps, int step, void* stream);
 int hermes_to_bf16(const float* in, int64_t n, void* out, void* stream);
+/* hermes_mlp_infer_tc: the network's output y [batch] for inputs x
+ * [batch][dims[0]] with the 128 x 128 hidden layers on the tcgen05 tensor
+ * cores (BF16 weights and activations, FP32 accumulation), for networks
+ * dims = (d0 <= 16, 128, ..., 128, 1) with 1..4 hidden 128 x 128 layers
+ * (HERMES_ERR_UNSUPPORTED otherwise).  params: the float32 layout above.
+ * status: one device int, 0 on return of the kernel or 1 when a bounded
+ * wait gave up (y is then incomplete).  Asynchronous on `stream`. */
+int hermes_mlp_infer_tc(const float* params, const int32_t* dims, int n_layers, const float* x,
+                        int64_t batch, float* y, int* status, void* stream);
 
 #ifdef __cplusplus
 }

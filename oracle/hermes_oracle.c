@@ -539,12 +539,23 @@ int oracle_radial_multipole_window_range(int L, const double* P, int code, const
 /* compute_3d_summand_cpu (corr3pcf_multipoles.py:134-170): sum over cells of
  * data(x) * sum_{l1,l2} Gamma3(l1,l2) a1(x-l1) a2(x-l2); a1/a2 interleaved
  * complex [L^3]; returns re/im. */
+int oracle_contract_range(const double* data, const double* a1, const double* a2, const double* gamma, int L,
+                          int S, int x_begin, int x_end, double* out_re, double* out_im);
 int oracle_contract(const double* data, const double* a1, const double* a2, const double* gamma, int L, int S,
                     double* out_re, double* out_im) {
-  const int64_t N = (int64_t)L * L * L, plane = (int64_t)L * L;
+  return oracle_contract_range(data, a1, a2, gamma, L, S, 0, L, out_re, out_im);
+}
+
+/* The same sum over the cells of the x planes [x_begin, x_end) only (their
+ * neighbourhoods still read the whole periodic grid). */
+int oracle_contract_range(const double* data, const double* a1, const double* a2, const double* gamma, int L,
+                          int S, int x_begin, int x_end, double* out_re, double* out_im) {
+  const int64_t plane = (int64_t)L * L;
+  if (x_begin < 0 || x_end > L || x_begin > x_end) return -1;
+  const int64_t idx_begin = (int64_t)x_begin * plane, idx_end = (int64_t)x_end * plane;
   double tr = 0.0, ti = 0.0;
 #pragma omp parallel for reduction(+ : tr, ti) schedule(static)
-  for (int64_t idx = 0; idx < N; ++idx) {
+  for (int64_t idx = idx_begin; idx < idx_end; ++idx) {
     const int64_t lx = idx / plane, rem = idx - lx * plane, ly = rem / L, lz = rem - ly * L;
     double s1r = 0.0, s1i = 0.0;
     for (int l1x = 0; l1x < S; ++l1x) {

@@ -178,6 +178,7 @@ def _setup_multipole_lib():
     lb.oracle_contract.argtypes = [P, P, P, P, I, I, ctypes.POINTER(D), ctypes.POINTER(D)]
     lb.oracle_contract_bins.argtypes = [P, P, I, P, I, P, I, P]
     lb.oracle_contract_bins_range.argtypes = [P, P, I, P, I, P, I, I, I, P]
+    lb.oracle_contract_range.argtypes = [P, P, P, P, I, I, I, I, ctypes.POINTER(D), ctypes.POINTER(D)]
     lb.oracle_radial_multipole_window_range.argtypes = [I, P, I, P, I, I, I, I, P]
     lb.oracle_spherical_jn.argtypes = [I, D]
     lb.oracle_spherical_jn.restype = D
@@ -212,18 +213,19 @@ def radial_multipole_window_planes(L, P, radius_grid, l, m, x_begin, x_end, code
 
 
 def contract_planes(data, a2, a3, gamma, x_begin, x_end):
-    """The one-pair contraction summed over the cells of x planes
-    [x_begin, x_end) (oracle_contract_bins_range with one bin per side)."""
+    """compute_3d_summand_cpu (corr3pcf_multipoles.py:134-170) summed over
+    the cells of the x planes [x_begin, x_end) only (oracle_contract_range,
+    the per-cell arithmetic of contract)."""
     lb = _setup_multipole_lib()
     data = np.ascontiguousarray(data, dtype=np.float64)
     a2 = np.ascontiguousarray(a2, dtype=np.complex128)
     a3 = np.ascontiguousarray(a3, dtype=np.complex128)
     gamma = np.ascontiguousarray(gamma, dtype=np.float64)
-    out = np.zeros(2)
-    if lb.oracle_contract_bins_range(_p(data), _p(a2), 1, _p(a3), 1, _p(gamma), data.shape[0], x_begin, x_end,
-                                     _p(out)) != 0:
+    re, im = ctypes.c_double(0.0), ctypes.c_double(0.0)
+    if lb.oracle_contract_range(_p(data), _p(a2), _p(a3), _p(gamma), data.shape[0], gamma.shape[0], x_begin, x_end,
+                                ctypes.byref(re), ctypes.byref(im)) != 0:
         raise ValueError("bad plane range")
-    return complex(out[0], out[1])
+    return complex(re.value, im.value)
 
 
 def contract(data, a1, a2, gamma):

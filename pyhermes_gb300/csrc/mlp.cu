@@ -349,3 +349,220 @@ extern "C" int hermes_to_bf16(const float* in, int64_t n, void* out, void* strea
   HERMES_LAUNCH_CHECK("to_bf16_kernel");
   return HERMES_OK;
 }
+
+// ---- inference on the tensor cores ----------------------------------------------
+// For networks dims = (d0 <= 16, 128, ..., 128, 1): the first layer (K = d0)
+// and the last (128 -> 1) on the CUDA cores, every 128 x 128 hidden layer as
+// one tcgen05.mma GEMM per tile of 128 rows: A = the tile's activations
+// (BF16, M = 128 rows x K = 128), B = the layer's weights W[k][n] (BF16,
+// N = 128 x K = 128), D in tensor memory (FP32, 128 lanes x 128 columns);
+// bias and tanh applied on the way back (tcgen05.ld), the result written as
+// the next layer's A.  Both operands are MN-major in 128B-swizzled shared
+// memory (8-row atoms of 1 KB along K; two 64-element atom columns 16 KB
+// apart along M or N), K advancing by 16 per MMA.  One persistent CTA per SM
+// keeps every hidden layer's weights in shared memory and walks the tiles.
+#include "tc_common.cuh"
+
+namespace {
+
+namespace mi {
+constexpr int kWidth = 128;
+constexpr int kMaxIn = 16;
+constexpr int kMaxTc = 4;                       // hidden 128 x 128 layers
+constexpr int kAtomCol = 128 * 128;             // 128 K rows x 128 B
+constexpr int kMat = 2 * kAtomCol;              // one 128 x 128 BF16 operand
+constexpr int kThreads = 256;
+constexpr uint32_t kIdesc = hermes::tc::idesc_bf16_f32(128, 128, true, true);
+
+__host__ __device__ constexpr size_t smem_bytes(int n_tc) {
+  return 1024 + (size_t)(n_tc + 1) * kMat + sizeof(float) * (kMaxIn * kWidth + (kMaxTc + 2) * kWidth + kWidth +
+                                                              128 * kMaxIn + 2 * 128) + 128;
+}
+}  // namespace mi
+
+struct MlpTcArgs {
+  const float* params;
+  const float* x;
+  float* y;
+  int64_t batch;
+  int d0, n_tc;
+  int64_t off_w[kMaxLayers], off_b[kMaxLayers];
+  int* status;
+};
+
+// Byte offset of element (mn, k) in an MN-major 128B-swizzled BF16 operand.
+__device__ __forceinline__ uint32_t mi_off(int mn, int k) {
+  return (uint32_t)(mn >> 6) * mi::kAtomCol + (uint32_t)(k >> 3) * 1024u +
+         hermes::tc::sw128_offset((uint32_t)(k & 7), (uint32_t)((mn & 63) >> 3)) + (uint32_t)(mn & 7) * 2u;
+}
+
+__device__ __forceinline__ void mi_put(unsigned char* op, int mn, int k, float v) {
+  *reinterpret_cast<__nv_bfloat16*>(op + mi_off(mn, k)) = __float2bfloat16_rn(v);
+}
+
+__global__ void __launch_bounds__(mi::kThreads, 1) mlp_infer_tc_kernel(MlpTcArgs A) {
+  namespace tc = hermes::tc;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  unsigned char* base = smem_raw + ((1024u - (tc::smem_u32(smem_raw) & 1023u)) & 1023u);
+  unsigned char* wop = base;                                    // [n_tc][kMat] hidden weights
+  unsigned char* aop = wop + (size_t)A.n_tc * mi::kMat;         // activations of the tile
+  float* w1 = reinterpret_cast<float*>(aop + mi::kMat);         // [d0][128]
+  float* bias = w1 + mi::kMaxIn * mi::kWidth;                   // [n_tc + 1][128], then the last bias
+  float* wl = bias + (mi::kMaxTc + 2) * mi::kWidth;             // [128] last layer
+  float* xt = wl + mi::kWidth;                                  // [128][d0]
+  float* red = xt + 128 * mi::kMaxIn;                           // [2][128]
+  uint64_t* bar = reinterpret_cast<uint64_t*>(red + 2 * 128);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 1);
+  int* s_abort = reinterpret_cast<int*>(tmem_slot + 1);
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int d0 = A.d0, n_tc = A.n_tc;
+  const float* P = A.params;
+  // weights: hidden layers as BF16 operands, the rest as float
+  for (int l = 0; l < n_tc; ++l) {
+    const float* W = P + A.off_w[l + 1];
+    unsigned char* op = wop + (size_t)l * mi::kMat;
+    for (int i = tid; i < mi::kWidth * mi::kWidth; i += mi::kThreads) {
+      const int k = i >> 7, n = i & 127;
+      mi_put(op, n, k, W[i]);
+    }
+  }
+  for (int i = tid; i < d0 * mi::kWidth; i += mi::kThreads) w1[i] = P[A.off_w[0] + i];
+  for (int l = 0; l <= n_tc; ++l)
+    for (int i = tid; i < mi::kWidth; i += mi::kThreads) bias[l * mi::kWidth + i] = P[A.off_b[l] + i];
+  for (int i = tid; i < mi::kWidth; i += mi::kThreads) wl[i] = P[A.off_w[n_tc + 1] + i];
+  const float b_last = P[A.off_b[n_tc + 1]];
+  if (tid == 0) {
+    tc::mbar_init(bar, 1);
+    tc::mbar_fence_init();
+    *s_abort = 0;
+  }
+  if (warp == 0) tc::tmem_alloc(tmem_slot, 128);
+  tc::fence_proxy_async_smem();
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  const uint32_t sw = tc::smem_u32(wop), sa = tc::smem_u32(aop);
+  uint32_t phase = 0;
+  const int64_t ntiles = (A.batch + 127) / 128;
+  // epilogue mapping: lane quarter (rows) and column half
+  const int quarter = warp & 3, chalf = warp >> 2;
+  const int erow = quarter * 32 + lane;
+
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int64_t r0 = t * 128;
+    for (int i = tid; i < 128 * d0; i += mi::kThreads) {
+      const int64_t r = r0 + i / d0;
+      xt[i] = r < A.batch ? A.x[r * d0 + i % d0] : 0.f;
+    }
+    __syncthreads();
+    {  // layer 0 on the CUDA cores: row m, outputs [64 h, 64 h + 64)
+      const int m = tid & 127, h = tid >> 7;
+      float xv[mi::kMaxIn];
+#pragma unroll
+      for (int k = 0; k < mi::kMaxIn; ++k) xv[k] = k < d0 ? xt[m * d0 + k] : 0.f;
+      for (int j = 0; j < 64; ++j) {
+        const int n = 64 * h + j;
+        float z = bias[n];
+#pragma unroll
+        for (int k = 0; k < mi::kMaxIn; ++k)
+          if (k < d0) z = fmaf(xv[k], w1[k * mi::kWidth + n], z);
+        mi_put(aop, m, n, tanhf(z));
+      }
+    }
+    tc::fence_proxy_async_smem();
+    __syncthreads();
+    for (int l = 0; l < n_tc; ++l) {
+      if (tid == 0) {
+        tc::tc_fence_after();
+#pragma unroll
+        for (int kk = 0; kk < 8; ++kk) {
+          const uint64_t ad = tc::smem_desc(sa + kk * 2048, mi::kAtomCol, 1024, tc::kLayoutSw128);
+          const uint64_t bd = tc::smem_desc(sw + (uint32_t)l * mi::kMat + kk * 2048, mi::kAtomCol, 1024,
+                                            tc::kLayoutSw128);
+          tc::mma_bf16(tmem, ad, bd, mi::kIdesc, kk > 0);
+        }
+        tc::mma_commit(bar);
+      }
+      if (!tc::mbar_wait(bar, phase)) *s_abort = 1;
+      phase ^= 1u;
+      tc::tc_fence_after();
+      const float* bl = bias + (l + 1) * mi::kWidth;
+      float part = 0.f;
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        float d[32];
+        const int c0 = chalf * 64 + j * 32;
+        tc::tmem_ld_32x32b_x32(tmem + ((uint32_t)(quarter * 32) << 16) + c0, d);
+#pragma unroll
+        for (int i = 0; i < 32; ++i) {
+          const float v = tanhf(d[i] + bl[c0 + i]);
+          if (l + 1 < n_tc) mi_put(aop, erow, c0 + i, v);
+          else part = fmaf(v, wl[c0 + i], part);
+        }
+      }
+      if (l + 1 == n_tc) red[chalf * 128 + erow] = part;
+      tc::fence_proxy_async_smem();
+      tc::tc_fence_before();
+      __syncthreads();
+      if (*s_abort) break;
+    }
+    if (*s_abort) break;
+    if (tid < 128 && r0 + tid < A.batch) A.y[r0 + tid] = red[tid] + red[128 + tid] + b_last;
+    __syncthreads();  // xt / red / aop idle before the next tile
+  }
+  if (*s_abort && tid == 0 && A.status) atomicExch(A.status, 1);
+  __syncthreads();
+  if (warp == 0) {
+    tc::tc_fence_after();
+    tc::tmem_dealloc(tmem, 128);
+  }
+}
+
+}  // namespace
+
+extern "C" int hermes_mlp_infer_tc(const float* params, const int32_t* dims, int n_layers, const float* x,
+                                   int64_t batch, float* y, int* status, void* stream) {
+  if (!params || !dims || !x || !y || !status) return fail(HERMES_ERR_INVALID, "mlp_infer_tc: NULL argument");
+  if (n_layers < 3 || n_layers - 2 > mi::kMaxTc)
+    return fail(HERMES_ERR_UNSUPPORTED, "mlp_infer_tc: needs 3..%d layers", mi::kMaxTc + 2);
+  if (dims[0] < 1 || dims[0] > mi::kMaxIn || dims[n_layers] != 1)
+    return fail(HERMES_ERR_UNSUPPORTED, "mlp_infer_tc: needs 1..%d inputs and one output", mi::kMaxIn);
+  for (int l = 1; l < n_layers; ++l)
+    if (dims[l] != mi::kWidth) return fail(HERMES_ERR_UNSUPPORTED, "mlp_infer_tc: hidden widths must be 128");
+  if (batch < 0) return fail(HERMES_ERR_INVALID, "mlp_infer_tc: batch < 0");
+  cudaStream_t s = hermes::as_stream(stream);
+  HERMES_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int), s));
+  if (batch == 0) return HERMES_OK;
+  MlpTcArgs A;
+  A.params = params;
+  A.x = x;
+  A.y = y;
+  A.batch = batch;
+  A.d0 = dims[0];
+  A.n_tc = n_layers - 2;
+  A.status = status;
+  int64_t off = 0;
+  for (int l = 0; l < n_layers; ++l) {
+    A.off_w[l] = off;
+    off += (int64_t)dims[l] * dims[l + 1];
+    A.off_b[l] = off;
+    off += dims[l + 1];
+  }
+  const size_t smem = mi::smem_bytes(A.n_tc);
+  static bool smem_set[64] = {false};
+  int dev = 0, nsm = 148;
+  HERMES_CUDA_TRY(cudaGetDevice(&dev));
+  HERMES_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  if (dev < 0 || dev >= 64 || !smem_set[dev]) {  // once per device, before any stream capture
+    HERMES_CUDA_TRY(cudaFuncSetAttribute(mlp_infer_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)mi::smem_bytes(mi::kMaxTc)));
+    if (dev >= 0 && dev < 64) smem_set[dev] = true;
+  }
+  const int64_t ntiles = (batch + 127) / 128;
+  const int grid = (int)(ntiles < nsm ? ntiles : nsm);
+  mlp_infer_tc_kernel<<<grid, mi::kThreads, smem, s>>>(A);
+  HERMES_LAUNCH_CHECK("mlp_infer_tc_kernel");
+  return HERMES_OK;
+}

@@ -33,7 +33,6 @@
 #include <tuple>
 #include <vector>
 
-#include <cuda_bf16.h>
 #include <cudaTypedefs.h>
 
 #include "hermes_common.cuh"
@@ -774,56 +773,104 @@ __global__ void __launch_bounds__(ct::kThreads, 2) mp_contract_kernel(ContractAr
     A.partial[(long long)blockIdx.x * 2 * kMaxBins * kMaxBins + i] = dacc[i];
 }
 
+// ---- h form of the per-plane stencil ------------------------------------------
+//   T_d(c) = sum_{uy in [-2,2]} sum_{l1z in [0,2]} h_{uy,l1z}(x_e; c) Rz_{l1z}(x_a; c_y + uy, c_z)
+//   h_{uy,l1z}(c) = sum_{l1y} Gamma[l1y][l1y-uy] eps1(x_e, c_y + l1y, c_z + l1z)   (bin independent)
+//   Rz_{l1z}(y, z) = sum_{l2z} Gamma[l1z][l2z] a3(x_a, y, z + l1z - l2z)           (fixed z filter)
+// This is the V form above with its z sum split through the separable Gamma:
+// 15 weights per column and plane instead of 25, and per (column, uy, plane)
+// 3 FMAs instead of 5 (plus the 9-FMA z filter per row, shared by the planes).
+namespace hf {
+constexpr int kHCol = 20;                      // floats per column: [5 uy][4] (3 used)
+constexpr int kHPlane = ct::kCols * kHCol;
+}  // namespace hf
+
+// h plane from a staged eps plane: H[col][uy+2][l1z].  Four threads per
+// column; thread `part` writes uy + 2 = part (and 4 for part 0).
+__device__ __forceinline__ void ct_compute_h(const float* __restrict__ w, const float* __restrict__ e,
+                                             float* __restrict__ h) {
+  const int col = threadIdx.x >> 2, part = threadIdx.x & 3;
+  const int cy = col / ct::TZ, cz = col - cy * ct::TZ;
+  float ev[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) ev[i][j] = e[(cy + i) * ct::EZ + cz + j];
+#pragma unroll
+  for (int rep = 0; rep < 2; ++rep) {
+    const int ay = rep == 0 ? part : 4;
+    if (rep == 1 && part != 0) break;
+    const float w0 = w[ay * 3], w1 = w[ay * 3 + 1], w2 = w[ay * 3 + 2];
+    float o[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) o[j] = fmaf(w2, ev[2][j], fmaf(w1, ev[1][j], w0 * ev[0][j]));
+    *reinterpret_cast<float4*>(h + col * hf::kHCol + ay * 4) = make_float4(o[0], o[1], o[2], 0.f);
+  }
+}
+
 // ---- contraction with the bin x bin product on the tensor cores -------------
-// The stencil part is mp_contract_kernel's (FP32 paired FMAs on the CUDA
-// cores); the product S[b2][b3] += sum_cells a2^{b2} G^{b3} of every completed
-// plane runs as one tcgen05.mma GEMM with the accumulator in tensor memory:
-//   A (M = 128 x K = 64 cells): rows m = hl*32 + 2*b2 + part of a2, where
-//     hl = 0 is the BF16 rounding of the FP32 value and hl = 1 the BF16
-//     rounding of the remainder (a2 = hi + lo to ~2^-17), part = re / im;
-//     rows 64..127 read the B buffer and are ignored;
-//   B (N = 64 x K = 64 cells): columns n = hl*32 + 2*b3 + part of G;
-//   D[m][n] = sum_cells A[m] B[n] (FP32 in TMEM, 128 lanes x 64 columns).
-// Summed over (hl, hl'), D gives the four real products of a2 x G per bin
-// pair, i.e. the split-BF16 product keeps ~16 significant bits of each operand
-// and the hi*lo cross terms (the "BF16x3" scheme, plus lo*lo).  Both operands
-// are MN-major in 128B-swizzled shared memory: one 128-byte row per cell
-// (64 BF16 values), 8-row atoms of 1 KB, K advancing by whole atoms.  The a2
+// The stencil runs on the CUDA cores in FP32 (the h form); the product
+// S[b2][b3] += sum_cells a2^{b2} G^{b3} of every completed plane runs as one
+// tcgen05.mma GEMM (kind::f16, BF16 operands, FP32 accumulate) with the
+// accumulator in tensor memory, in the BF16x3 split: every FP32 operand value
+// v = hi + mid + lo with hi = bf16(v), mid = bf16(v - hi),
+// lo = bf16(v - hi - mid) (~24 significant bits: the FP32 value to rounding).
+//   A (M = 128 x K = 64 cells): rows m = s*32 + 2*b2 + part of a2, s = 0, 1,
+//     2 for hi, mid, lo, part = re / im; rows 96..127 are padding (unused);
+//   B (N = 96 x K = 64 cells): columns n = s*32 + 2*b3 + part of G;
+//   D[m][n] = sum_cells A[m] B[n] (FP32 in TMEM, 128 lanes x 96 columns).
+// Summed over (s, s'), D gives the four real products of a2 x G per bin pair
+// from all nine partial products.  Both operands are MN-major in
+// 128B-swizzled shared memory: per cell one 128-byte row holding (hi, mid)
+// (64 BF16) in atom column 0 and one holding (lo, padding) in atom column 1
+// (8 KB further), 8-row atoms of 1 KB, K advancing by whole atoms.  The a2
 // plane arrives by TMA (4-D tensor map over the [x][y][z][16 bins] fields,
-// box 32 floats x 8 z x 8 y x 1 x) one step ahead; threads split it into
-// hi / lo.  A plane's MMAs (4 x K = 16) are issued by one thread after the
-// block barrier that follows the operand writes and run while the CUDA cores
-// compute the next plane's stencil; their tcgen05.commit arrives on an
-// mbarrier that the next overwrite of the operand buffers waits on.  At the
-// end of a work item the accumulator is read back (tcgen05.ld) and added in
-// float64 in a fixed order per bin pair.
+// box 32 floats x 8 z x 8 y x 1 x) one step ahead; threads split it.  A
+// plane's MMAs (4 x K = 16) are issued by one thread after the block barrier
+// that follows the operand writes and run while the CUDA cores compute the
+// next plane's stencil; their tcgen05.commit arrives on an mbarrier that the
+// next overwrite of the operand buffers waits on.  At the end of a work item
+// the accumulator is read back (tcgen05.ld) and added in float64 in a fixed
+// order per bin pair.
 namespace tcc {
-constexpr int kOpBytes = 64 * 128;                         // one operand plane: 64 cells x 128 B
+constexpr int kAtomCol = 64 * 128;                         // one atom column: 64 cells x 128 B
+constexpr int kOpBytes = 2 * kAtomCol;                     // (hi, mid) + (lo, pad) atom columns
 constexpr int kRawBytes = 64 * kBinStride * 8;             // TMA a2 plane: 64 cells x 16 complex
-constexpr int kTmemCols = 64;
-constexpr uint32_t kIdesc = hermes::tc::idesc_bf16_f32(128, 64, true, true);
+constexpr int kTmemCols = 128;                             // D: 96 columns used
+constexpr int kN = 96;
+constexpr uint32_t kIdesc = hermes::tc::idesc_bf16_f32(128, kN, true, true);
 // 1 KB slack for the runtime 1024-byte alignment of the swizzled operands
 constexpr size_t kSmem = 1024 + 2 * kOpBytes + 2 * kRawBytes + sizeof(float2) * 2 * ct::kA3Plane +
-                         sizeof(float) * (3 * ct::kVPlane + 2 * ct::kEpsPlane) +
+                         sizeof(float) * (3 * hf::kHPlane + 2 * ct::kEpsPlane) +
                          sizeof(double) * 2 * kMaxBins * kMaxBins + 128;
 }  // namespace tcc
 
+// (lower half, upper half) -> packed BF16x2, round to nearest even
 __device__ __forceinline__ uint32_t pack_bf16x2(float lo_half, float hi_half) {
   uint32_t r;
   asm("cvt.rn.bf16x2.f32 %0, %1, %2;\n" : "=r"(r) : "f"(hi_half), "f"(lo_half));
   return r;
 }
-__device__ __forceinline__ float bf16_round(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
+__device__ __forceinline__ float bf16_lo(uint32_t p) { return __uint_as_float(p << 16); }
+__device__ __forceinline__ float bf16_hi(uint32_t p) { return __uint_as_float(p & 0xFFFF0000u); }
 
-// Writes (re, im) of one bin as BF16 hi and lo pairs into a swizzled operand
-// row (cell) at element 2*b and 32 + 2*b.
+// BF16x3 split of a pair (x, y): packed hi, mid and lo pairs.
+__device__ __forceinline__ void split3(float x, float y, uint32_t& h, uint32_t& m, uint32_t& l) {
+  h = pack_bf16x2(x, y);
+  const float rx = x - bf16_lo(h), ry = y - bf16_hi(h);
+  m = pack_bf16x2(rx, ry);
+  l = pack_bf16x2(rx - bf16_lo(m), ry - bf16_hi(m));
+}
+
+// Writes (re, im) of one bin into a swizzled operand, row `cell`: hi at
+// element 2b and mid at 32 + 2b of atom column 0, lo at 2b of atom column 1.
 __device__ __forceinline__ void tc_put_pair(unsigned char* op, int cell, int b, float re, float im) {
-  const float hr = bf16_round(re), hi_ = bf16_round(im);
-  const uint32_t hv = pack_bf16x2(hr, hi_), lv = pack_bf16x2(re - hr, im - hi_);
-  unsigned char* atom = op + (cell >> 3) * 1024;
-  const int row = cell & 7, byte = (b & 3) * 4;
-  *reinterpret_cast<uint32_t*>(atom + hermes::tc::sw128_offset(row, b >> 2) + byte) = hv;
-  *reinterpret_cast<uint32_t*>(atom + hermes::tc::sw128_offset(row, 4 + (b >> 2)) + byte) = lv;
+  uint32_t h, m, l;
+  split3(re, im, h, m, l);
+  const uint32_t row = (cell >> 3) * 1024, r = cell & 7, byte = (b & 3) * 4;
+  *reinterpret_cast<uint32_t*>(op + row + hermes::tc::sw128_offset(r, b >> 2) + byte) = h;
+  *reinterpret_cast<uint32_t*>(op + row + hermes::tc::sw128_offset(r, 4 + (b >> 2)) + byte) = m;
+  *reinterpret_cast<uint32_t*>(op + tcc::kAtomCol + row + hermes::tc::sw128_offset(r, b >> 2) + byte) = l;
 }
 
 __global__ void __launch_bounds__(ct::kThreads, 2)
@@ -831,18 +878,18 @@ mp_contract_tc_kernel(ContractArgs A, const __grid_constant__ CUtensorMap a2map)
   namespace tc = hermes::tc;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   unsigned char* base = smem_raw + ((1024u - (tc::smem_u32(smem_raw) & 1023u)) & 1023u);
-  unsigned char* abf = base;                                       // A operand (a2 hi/lo)
-  unsigned char* gbf = abf + tcc::kOpBytes;                        // B operand (G hi/lo)
+  unsigned char* abf = base;                                       // A operand (a2 split)
+  unsigned char* gbf = abf + tcc::kOpBytes;                        // B operand (G split)
   float* araw = reinterpret_cast<float*>(gbf + tcc::kOpBytes);    // [2][64 cells][32] TMA a2 planes
   float2* abuf = reinterpret_cast<float2*>(reinterpret_cast<unsigned char*>(araw) + 2 * tcc::kRawBytes);
   double* dacc = reinterpret_cast<double*>(abuf + 2 * ct::kA3Plane);  // [16][16][2]
-  float* vring = reinterpret_cast<float*>(dacc + 2 * kMaxBins * kMaxBins);
-  float* epsb = vring + 3 * ct::kVPlane;
+  float* hring = reinterpret_cast<float*>(dacc + 2 * kMaxBins * kMaxBins);  // [3][kHPlane]
+  float* epsb = hring + 3 * hf::kHPlane;
   uint64_t* bars = reinterpret_cast<uint64_t*>(epsb + 2 * ct::kEpsPlane);  // tma[2], mma
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 3);
-  float* gsm = reinterpret_cast<float*>(tmem_slot + 1);                  // 15 V-pass weights
+  float* gsm = reinterpret_cast<float*>(tmem_slot + 1);                  // 15 h-pass weights
   int* s_abort = reinterpret_cast<int*>(gsm + 16);
-  float* stage = reinterpret_cast<float*>(abuf);                          // [64][65] at item end
+  float* stage = reinterpret_cast<float*>(abuf);                          // [96][33] at item end
 
   const int J = A.J, L = 1 << J, Lm = L - 1, CX = A.CX;
   const int tid = threadIdx.x, warp = tid >> 5;
@@ -882,17 +929,21 @@ mp_contract_tc_kernel(ContractArgs A, const __grid_constant__ CUtensorMap a2map)
   for (int item = blockIdx.x; item < n_items; item += gridDim.x) {
     const int tz = item % ntz, ty = (item / ntz) % nty, xc = item / (ntz * nty);
     const int x0 = xc * CX, y0 = ty * ct::TY, z0 = tz * ct::TZ;
+    // prologue: h(x0-2), h(x0-1), h(x0) into ring slots 0, 1, 2; a3 plane x0-2
     ct_stage_eps(A.eps1, epsb, x0 - 2, y0, z0, L, Lm);
     ct_stage_eps(A.eps1, epsb + ct::kEpsPlane, x0 - 1, y0, z0, L, Lm);
     cp_async_commit();
     cp_async_wait<0>();
     __syncthreads();
-    ct_compute_v(gsm, epsb, vring);
-    ct_compute_v(gsm, epsb + ct::kEpsPlane, vring + ct::kVPlane);
+    ct_compute_h(gsm, epsb, hring);
+    ct_compute_h(gsm, epsb + ct::kEpsPlane, hring + hf::kHPlane);
     __syncthreads();
     ct_stage_a3(A.src3, A.s3, abuf, x0 - 2, y0, z0, L, Lm);
     ct_stage_eps(A.eps1, epsb, x0, y0, z0, L, Lm);
     cp_async_commit();
+    cp_async_wait<0>();
+    __syncthreads();
+    ct_compute_h(gsm, epsb, hring + 2 * hf::kHPlane);
 
     float2 G[5][4];
 #pragma unroll
@@ -901,9 +952,14 @@ mp_contract_tc_kernel(ContractArgs A, const __grid_constant__ CUtensorMap a2map)
       for (int c = 0; c < 4; ++c) G[q][c] = make_float2(0.f, 0.f);
     bool first_mma = true;
 
+    // Two block barriers per step: the first makes the h plane computed at
+    // the end of the previous step visible; the second the staged a3 / eps
+    // planes (each thread waited for its own copies) and the MMA operands.
     for (int st = 0; st < nsteps; ++st) {
       const int xa = x0 - 2 + st;
       if (st + 1 < nsteps) {
+        // a3 plane xa+1 and eps plane xa+3: their buffers' last readers (the
+        // stencil one step back, the h pass two steps back) are done
         ct_stage_a3(A.src3, A.s3, abuf + ((st + 1) & 1) * ct::kA3Plane, xa + 1, y0, z0, L, Lm);
         ct_stage_eps(A.eps1, epsb + ((st + 1) & 1) * ct::kEpsPlane, xa + 3, y0, z0, L, Lm);
         // a2 plane of the next step's product (its buffer's last reader, the
@@ -916,15 +972,12 @@ mp_contract_tc_kernel(ContractArgs A, const __grid_constant__ CUtensorMap a2map)
         }
       }
       cp_async_commit();
-      cp_async_wait<1>();
-      __syncthreads();
-      ct_compute_v(gsm, epsb + (st & 1) * ct::kEpsPlane, vring + ((st + 2) % 3) * ct::kVPlane);
       __syncthreads();
       {
         const float2* ap = abuf + (st & 1) * ct::kA3Plane;
-        const float* vp0 = vring + (st % 3) * ct::kVPlane;
-        const float* vp1 = vring + ((st + 1) % 3) * ct::kVPlane;
-        const float* vp2 = vring + ((st + 2) % 3) * ct::kVPlane;
+        const float* hp0 = hring + (st % 3) * hf::kHPlane;
+        const float* hp1 = hring + ((st + 1) % 3) * hf::kHPlane;
+        const float* hp2 = hring + ((st + 2) % 3) * hf::kHPlane;
         float2 T[3][4];
 #pragma unroll
         for (int d = 0; d < 3; ++d)
@@ -935,24 +988,31 @@ mp_contract_tc_kernel(ContractArgs A, const __grid_constant__ CUtensorMap a2map)
           float2 av[6];
 #pragma unroll
           for (int k = 0; k < 6; ++k) av[k] = ap[((cy + r) * ct::HZ + cz + k) * kBinStride + b];
+          // Rz_{l1z}(row, cz + dz) = sum_{l2z} Gamma[l1z][l2z] a3(row, cz + dz + l1z - l2z)
+          float2 rz[2][3];
+#pragma unroll
+          for (int dz = 0; dz < 2; ++dz)
+#pragma unroll
+            for (int l1z = 0; l1z < 3; ++l1z) {
+              const float g0 = A.gm.g[l1z * 3], g1 = A.gm.g[l1z * 3 + 1], g2 = A.gm.g[l1z * 3 + 2];
+              float2 t = __fmul2_rn(make_float2(g2, g2), av[dz + l1z]);
+              t = __ffma2_rn(make_float2(g1, g1), av[dz + l1z + 1], t);
+              rz[dz][l1z] = __ffma2_rn(make_float2(g0, g0), av[dz + l1z + 2], t);
+            }
 #pragma unroll
           for (int dy = 0; dy < 2; ++dy) {
             const int uy = r - 2 - dy;
             if (uy < -2 || uy > 2) continue;
 #pragma unroll
             for (int dz = 0; dz < 2; ++dz) {
-              const int voff = ((cy + dy) * ct::TZ + cz + dz) * ct::kVCol + (uy + 2) * ct::kVRow;
+              const int hoff = ((cy + dy) * ct::TZ + cz + dz) * hf::kHCol + (uy + 2) * 4;
 #pragma unroll
               for (int d = 0; d < 3; ++d) {
-                const float* vp = (d == 0 ? vp0 : (d == 1 ? vp1 : vp2)) + voff;
-                const float4 v4 = *reinterpret_cast<const float4*>(vp);
-                const float v5 = vp[4];
+                const float4 h4 = *reinterpret_cast<const float4*>((d == 0 ? hp0 : (d == 1 ? hp1 : hp2)) + hoff);
                 float2 t = T[d][dy * 2 + dz];
-                t = __ffma2_rn(make_float2(v4.x, v4.x), av[dz], t);
-                t = __ffma2_rn(make_float2(v4.y, v4.y), av[dz + 1], t);
-                t = __ffma2_rn(make_float2(v4.z, v4.z), av[dz + 2], t);
-                t = __ffma2_rn(make_float2(v4.w, v4.w), av[dz + 3], t);
-                t = __ffma2_rn(make_float2(v5, v5), av[dz + 4], t);
+                t = __ffma2_rn(make_float2(h4.x, h4.x), rz[dz][0], t);
+                t = __ffma2_rn(make_float2(h4.y, h4.y), rz[dz][1], t);
+                t = __ffma2_rn(make_float2(h4.z, h4.z), rz[dz][2], t);
                 T[d][dy * 2 + dz] = t;
               }
             }
@@ -1001,16 +1061,15 @@ mp_contract_tc_kernel(ContractArgs A, const __grid_constant__ CUtensorMap a2map)
           }
         }
         if (st & 1) tma_ph1 ^= (tma_a2 ? 1u : 0u); else tma_ph0 ^= (tma_a2 ? 1u : 0u);
-        uint32_t hv[4], lv[4];
+        uint32_t hv[4], mv[4], lv[4];
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          const float hr = bf16_round(v[2 * i]), hi_ = bf16_round(v[2 * i + 1]);
-          hv[i] = pack_bf16x2(hr, hi_);
-          lv[i] = pack_bf16x2(v[2 * i] - hr, v[2 * i + 1] - hi_);
-        }
+        for (int i = 0; i < 4; ++i) split3(v[2 * i], v[2 * i + 1], hv[i], mv[i], lv[i]);
         unsigned char* atom = abf + (cell >> 3) * 1024;
+        // elements 8q .. 8q+7 of the row: chunk q (hi), 4 + q (mid), q of column 1 (lo)
         *reinterpret_cast<uint4*>(atom + tc::sw128_offset(cell & 7, q)) = make_uint4(hv[0], hv[1], hv[2], hv[3]);
-        *reinterpret_cast<uint4*>(atom + tc::sw128_offset(cell & 7, 4 + q)) = make_uint4(lv[0], lv[1], lv[2], lv[3]);
+        *reinterpret_cast<uint4*>(atom + tc::sw128_offset(cell & 7, 4 + q)) = make_uint4(mv[0], mv[1], mv[2], mv[3]);
+        *reinterpret_cast<uint4*>(atom + tcc::kAtomCol + tc::sw128_offset(cell & 7, q)) =
+            make_uint4(lv[0], lv[1], lv[2], lv[3]);
         tc::fence_proxy_async_smem();
       }
 #pragma unroll
@@ -1019,17 +1078,19 @@ mp_contract_tc_kernel(ContractArgs A, const __grid_constant__ CUtensorMap a2map)
         for (int c = 0; c < 4; ++c) G[q][c] = G[q + 1][c];
 #pragma unroll
       for (int c = 0; c < 4; ++c) G[4][c] = make_float2(0.f, 0.f);
+      cp_async_wait<0>();
       __syncthreads();
       if (*s_abort) break;
+      // h(xa + 3) for the next step, into the ring slot this step's T_0 used
+      if (st + 1 < nsteps) ct_compute_h(gsm, epsb + ((st + 1) & 1) * ct::kEpsPlane, hring + (st % 3) * hf::kHPlane);
       if (full) {
         if (tid == 0) {
           tc::tc_fence_after();
 #pragma unroll
           for (int k = 0; k < 4; ++k) {
-            // rows 64..127 of A read the B buffer (LBO = its offset); their
-            // results are not used
-            const uint64_t ad = tc::smem_desc(sa + k * 2048, sg - sa, 1024, tc::kLayoutSw128);
-            const uint64_t bd = tc::smem_desc(sg + k * 2048, 0, 1024, tc::kLayoutSw128);
+            // K = 16 cells = two 1 KB atoms; the two atom columns 8 KB apart
+            const uint64_t ad = tc::smem_desc(sa + k * 2048, tcc::kAtomCol, 1024, tc::kLayoutSw128);
+            const uint64_t bd = tc::smem_desc(sg + k * 2048, tcc::kAtomCol, 1024, tc::kLayoutSw128);
             tc::mma_bf16(tmem_d, ad, bd, tcc::kIdesc, !(first_mma && k == 0));
           }
           tc::mma_commit(&bars[2]);
@@ -1046,17 +1107,22 @@ mp_contract_tc_kernel(ContractArgs A, const __grid_constant__ CUtensorMap a2map)
     }
     __syncthreads();
     if (*s_abort) break;
-    // accumulator -> stage[row][col] (rows 0..63 = lanes of warps 0 and 1)
+    // accumulator rows 0..95 (lanes of warps 0..2): the three G parts s' are
+    // summed per row (FP32, hi first), then stage[row][j], j = 2*b3 + part
     tc::tc_fence_after();
-    if (warp < 2) {
+    if (warp < 3) {
       const int row = warp * 32 + (tid & 31);
+      float acc[32];
+      tc::tmem_ld_32x32b_x32(tmem_d + ((uint32_t)(warp * 32) << 16), acc);
 #pragma unroll
-      for (int half = 0; half < 2; ++half) {
+      for (int part = 1; part < 3; ++part) {
         float d[32];
-        tc::tmem_ld_32x32b_x32(tmem_d + ((uint32_t)(warp * 32) << 16) + half * 32, d);
+        tc::tmem_ld_32x32b_x32(tmem_d + ((uint32_t)(warp * 32) << 16) + part * 32, d);
 #pragma unroll
-        for (int i = 0; i < 32; ++i) stage[row * 65 + half * 32 + i] = d[i];
+        for (int i = 0; i < 32; ++i) acc[i] += d[i];
       }
+#pragma unroll
+      for (int i = 0; i < 32; ++i) stage[row * 33 + i] = acc[i];
     }
     tc::tc_fence_before();
     __syncthreads();
@@ -1064,14 +1130,12 @@ mp_contract_tc_kernel(ContractArgs A, const __grid_constant__ CUtensorMap a2map)
       const int b2 = tid >> 4, b3 = tid & 15;
       double sr = 0.0, si = 0.0;
 #pragma unroll
-      for (int h = 0; h < 2; ++h)
-#pragma unroll
-        for (int h2 = 0; h2 < 2; ++h2) {
-          const float* rr = stage + (h * 32 + 2 * b2) * 65 + h2 * 32 + 2 * b3;
-          const float* ri = rr + 65;  // row of the imaginary part of a2
-          sr += (double)rr[0] - (double)ri[1];
-          si += (double)rr[1] + (double)ri[0];
-        }
+      for (int sp = 0; sp < 3; ++sp) {
+        const float* rr = stage + (sp * 32 + 2 * b2) * 33 + 2 * b3;
+        const float* ri = rr + 33;  // row of the imaginary part of a2
+        sr += (double)rr[0] - (double)ri[1];
+        si += (double)rr[1] + (double)ri[0];
+      }
       dacc[(b2 * kMaxBins + b3) * 2] += sr;
       dacc[(b2 * kMaxBins + b3) * 2 + 1] += si;
     }

@@ -601,6 +601,17 @@ class MLP:
         y = acts[-x.shape[0] * self.dims[-1]:].view(x.shape[0], self.dims[-1])
         return (y, acts) if return_acts else y
 
+    def infer(self, x):
+        """Outputs [batch] with the 128 x 128 hidden layers on the tensor
+        cores (hermes_mlp_infer_tc; BF16 weights and activations)."""
+        x = x.to(torch.float32).contiguous()
+        y = torch.empty(x.shape[0], dtype=torch.float32, device=self.device)
+        st = torch.zeros(1, dtype=torch.int32, device=self.device)
+        _lib.check(_lib.load().hermes_mlp_infer_tc(_ptr(self.params), self.cdims, len(self.dims) - 1, _ptr(x),
+                                                   x.shape[0], _ptr(y), _ptr(st), _stream_ptr(self.device)),
+                   "hermes_mlp_infer_tc")
+        return y
+
     def grads(self, x, target):
         """(loss, gradient of the mean squared error) for one batch."""
         lib = _lib.load()
@@ -643,22 +654,55 @@ class MLP:
 
 
 class LearnedProposal:
-    """Importance sampling of triangle centres with a trained MLP proposal."""
+    """Importance sampling of triangle centres with a trained MLP proposal.
 
-    def __init__(self, eps1, eps2, eps3, J, phi, rho, device="cuda", mix=0.2):
+    Features of a candidate centre c for a triangle (r12, r13, mu): the
+    triangle's shape, the density n1(c) of vertex 1 at the centre and the
+    densities of vertices 2 and 3 averaged over the thin shells of radius r12
+    and r13 around c (the fields convolved with a shell window, evaluated with
+    the same 27-point interpolation).  The shell averages carry
+    E_rot[n2 n3 | c], which the centre density alone cannot."""
+
+    N_FEATURES = 6
+
+    def __init__(self, eps1, eps2, eps3, J, phi, rho, device="cuda", mix=0.1):
         self.e1, self.e2, self.e3 = (e.to(torch.float32).contiguous() for e in (eps1, eps2, eps3))
         self.J, self.L = J, 1 << J
-        self.phi_t = torch.as_tensor(np.asarray(phi, dtype=np.float64), device=device)
+        self.phi_np = np.asarray(phi, dtype=np.float64)
+        self.phi_t = torch.as_tensor(self.phi_np, device=device)
         self.rho = float(rho)
         self.device = torch.device(device)
         self.mix = mix
-        self.net = MLP(device=device)
+        self.net = MLP(dims=(self.N_FEATURES, 128, 128, 128, 1), device=device)
+        self._shells = {}
+
+    def shell_field(self, vertex, radius):
+        """Field of vertex 2 or 3 averaged over a thin shell of `radius`
+        (grid units) around every cell: field @ shell window (W(0) = 1)."""
+        src = self.e2 if vertex == 2 else self.e3
+        key = (src.data_ptr(), round(float(radius), 6))
+        f = self._shells.get(key)
+        if f is None:
+            from .window import WindowFunc, apply_window
+
+            w = WindowFunc({"type": "shell", "len_args": {"R": float(radius)}},
+                           {"J": self.J, "box_size": float(self.L), "phi_resolution": 1024, "wavelet_mode": "db2",
+                            "wavelet_level": 10, "phi_array": self.phi_np}, device=self.device)
+            f = apply_window(src, w)
+            self._shells[key] = f
+        return f
 
     def features(self, centers, r12s, r13s, mu):
         n1 = interp(self.e1, self.J, centers, self.phi_t)
+        s2 = interp(self.shell_field(2, r12s), self.J, centers, self.phi_t)
+        s3 = interp(self.shell_field(3, r13s), self.J, centers, self.phi_t)
         dl = (n1 / self.rho - 1.0).clamp(-1.0, 50.0)
+
+        def logd(v):
+            return torch.log((v / self.rho).clamp(0.01, 50.0))
+
         f = torch.stack([torch.full_like(dl, r12s / self.L * 10), torch.full_like(dl, r13s / self.L * 10),
-                         torch.full_like(dl, mu), torch.log1p(dl.clamp_min(-0.99))], dim=1)
+                         torch.full_like(dl, mu), torch.log1p(dl.clamp_min(-0.99)), logd(s2), logd(s3)], dim=1)
         return f.float()
 
     def training_data(self, configs, n_centers, n_rot_train, seed=0):
@@ -681,7 +725,10 @@ class LearnedProposal:
         return self.net.train(X, (T - self.t_mean) / self.t_std, epochs=epochs, seed=seed)
 
     def proposal(self, pool, r12s, r13s, mu, bf16=True):
-        pred = self.net.forward(self.features(pool, r12s, r13s, mu), bf16=bf16).reshape(-1).double()
+        """q over the pool; bf16=True evaluates the network on the tensor
+        cores (hermes_mlp_infer_tc), False in FP32 on the CUDA cores."""
+        feats = self.features(pool, r12s, r13s, mu)
+        pred = (self.net.infer(feats) if bf16 else self.net.forward(feats)).reshape(-1).double()
         logh = 0.5 * (pred * self.t_std + self.t_mean)
         h = torch.exp(logh - logh.max())
         M = pool.shape[0]

@@ -239,7 +239,7 @@ def multipole_contract_async(eps1, fields2, nb2, gamma_c, J, dev_out, fields3=No
     """hermes_multipole_contract_async: S (times 4 pi / L^3) into the device
     float64 tensor dev_out [16, 16, 2] on the current stream, no host sync.
     gamma_c: a ctypes double[9] (kept alive by the caller during capture).
-    engine: 'tensor' (bin x bin product on tcgen05, split BF16) or 'simt'
+    engine: 'tensor' (bin x bin product on tcgen05, BF16x3 operands) or 'simt'
     (the all-FP32 CUDA-core kernel)."""
     if engine not in ENGINES:
         raise ValueError(f"engine must be one of {ENGINES}")

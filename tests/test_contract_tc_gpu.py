@@ -1,10 +1,10 @@
-"""The tensor-core contraction (bin x bin product on tcgen05, split-BF16
+"""The tensor-core contraction (bin x bin product on tcgen05, BF16x3
 operands) against the float64 oracle and the all-FP32 CUDA-core kernel.
 
 Bounds: against the oracle, every S[b2, b3] within 2e-5 of the largest |S|
 of the set (the FP32 fields and stencil set the floor, as for the FP32
 kernel); tensor-core vs FP32 kernel within 1e-5 of the largest |S|, which is
-the split-BF16 product's representation error (~2^-17 per operand) summed
+the BF16x3 product's representation error (~2^-24 per operand) summed
 over the cells.  Runs are bitwise reproducible.
 """
 import numpy as np

@@ -135,6 +135,24 @@ def test_mlp_gradients_match_oracle():
     assert _rel(y16, yref) < 2e-2
 
 
+@pytest.mark.parametrize("dims,batch", [([6, 128, 128, 128, 1], 50_000), ([4, 128, 128, 1], 1000),
+                                        ([16, 128, 128, 128, 128, 128, 1], 128 * 152 * 3 + 77)])
+def test_mlp_tensor_core_inference_matches_oracle(dims, batch):
+    """hermes_mlp_infer_tc (hidden 128 x 128 layers on tcgen05, BF16 weights
+    and activations) against the float64 oracle forward: within 2e-2 of the
+    largest |y| (the BF16 rounding of weights and activations), several
+    tiles per CTA and a ragged last tile."""
+    net = mc3pcf.MLP(dims, seed=4)
+    rng = np.random.default_rng(7)
+    x = rng.standard_normal((batch, dims[0])).astype(np.float32)
+    ytc = net.infer(torch.as_tensor(x, device="cuda")).cpu().numpy()
+    p = net.params.double().cpu().numpy()
+    yref = oracle.mlp_forward(p, dims, x.astype(np.float64))[-1].ravel()
+    assert ytc.shape == (batch,)
+    assert _rel(ytc, yref) < 2e-2, _rel(ytc, yref)
+    assert np.array_equal(ytc, net.infer(torch.as_tensor(x, device="cuda")).cpu().numpy())
+
+
 def test_mlp_training_reduces_loss():
     net = mc3pcf.MLP([4, 64, 64, 1], seed=1)
     rng = np.random.default_rng(5)
