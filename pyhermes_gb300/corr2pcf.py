@@ -427,6 +427,29 @@ class Corr_2PCF:
             bws.append(WindowFunc(params, ref_field.sfc_info, threads=self.threads, device=self.device))
         return bws
 
+    def _binning_family(self, ref_field):
+        """The bins as one template WindowFunc plus per-bin descriptors when
+        every sample's window is the same built-in window with different
+        len_args (the mappings of corr2pcf.py:267-315 only set lengths), else
+        None (then every bin gets its own WindowFunc)."""
+        from .window import family_descriptors
+
+        params = []
+        for idx in itertools.product(*(range(self.sampling_arrays[n].size) for n in self.sampling_names)):
+            sample = {n: float(self.sampling_arrays[n][i]) for n, i in zip(self.sampling_names, idx)}
+            params.append(build_binning_window_params_for_sample(sample, self.binning_window))
+        rest = [{k: v for k, v in p.items() if k != "len_args"} for p in params]
+        if any(r != rest[0] for r in rest[1:]):
+            return None
+        template = WindowFunc(params[0], ref_field.sfc_info, threads=self.threads, device=self.device)
+        if template.materialized or template.has_custom_func or template.is_composite_window:
+            return None
+        try:
+            template.descriptor()
+        except ValueError:
+            return None
+        return template, family_descriptors(template, [p.get("len_args") or {} for p in params])
+
     @staticmethod
     def _dc(field):
         """float64 sum of a field (its k = 0 Fourier coefficient)."""
@@ -488,24 +511,37 @@ class Corr_2PCF:
             pair_products_of[prod] = len(pairs)
             pairs.append(tuple(keys))
         if pairs:
-            windows = self._binning_windows(ref)
-            # split into groups of <= 4 pairs per pass
-            vals = np.zeros((len(windows), len(pairs)))
-            k0 = np.zeros(len(windows))
-            # built-in bins evaluate their kernels on the fly; bins with a
-            # stored kernel (custom callables) go through the convolution
-            on_fly = [b for b, w in enumerate(windows) if not w.materialized]
-            stored = [b for b, w in enumerate(windows) if w.materialized]
-            for s in range(0, len(pairs), 4):
-                if on_fly:
-                    v, kb = pair_products(spectra, pairs[s:s + 4], [windows[b] for b in on_fly], exclude_k0=True)
-                    vals[on_fly, s:s + 4] = v
-                    k0[on_fly] = kb
-            if stored:
-                v, kb = materialized_pair_products(reals, pairs, [windows[b] for b in stored], exclude_k0=True)
-                vals[stored, :] = v
-                k0[stored] = kb
-            L = windows[0].L
+            family = self._binning_family(ref)
+            if family is not None:
+                # one built-in window family: descriptors without per-bin objects
+                template, descs = family
+                vals = np.zeros((len(descs), len(pairs)))
+                k0 = np.zeros(len(descs))
+                for s in range(0, len(pairs), 4):
+                    v, kb = pair_products(spectra, pairs[s:s + 4], [template], exclude_k0=True, descs=descs)
+                    vals[:, s:s + 4] = v
+                    k0[:] = kb
+                L = template.L
+            else:
+                windows = self._binning_windows(ref)
+                # split into groups of <= 4 pairs per pass
+                vals = np.zeros((len(windows), len(pairs)))
+                k0 = np.zeros(len(windows))
+                # built-in bins evaluate their kernels on the fly; bins with a
+                # stored kernel (custom callables) go through the convolution
+                on_fly = [b for b, w in enumerate(windows) if not w.materialized]
+                stored = [b for b, w in enumerate(windows) if w.materialized]
+                for s in range(0, len(pairs), 4):
+                    if on_fly:
+                        v, kb = pair_products(spectra, pairs[s:s + 4], [windows[b] for b in on_fly],
+                                              exclude_k0=True)
+                        vals[on_fly, s:s + 4] = v
+                        k0[on_fly] = kb
+                if stored:
+                    v, kb = materialized_pair_products(reals, pairs, [windows[b] for b in stored], exclude_k0=True)
+                    vals[stored, :] = v
+                    k0[stored] = kb
+                L = windows[0].L
             N2 = float(L) ** 6
             for prod, col in pair_products_of.items():
                 a, b = operand[prod]

@@ -12,13 +12,16 @@ and the scale_factor**9 rescale.  Triplet sums run in
 ``hermes_mc_triplets`` (csrc/mc.cu).
 
 ``LearnedProposal`` (no reference counterpart): a tanh MLP over
-(r12, r13, mu, local delta) trained with the hand-written kernels of
-csrc/mlp.cu on uniform-MC triplet samples to predict log E_rot[f^2] at a
-centre.  Centres are then drawn from a pool with probability
-q_i = a/M + (1-a) h_i / sum h, h = exp(prediction / 2) (the variance-optimal
-shape sqrt(E f^2), mixed with the uniform pool distribution so weights stay
-bounded), and each sample is weighted by (1/M)/q_i: the estimator stays
-unbiased for the pool mean whatever the network predicts.
+(r12, r13, mu, the density at the centre and the shell-averaged densities at
+r12 and r13 around it) trained with the hand-written kernels of csrc/mlp.cu
+on uniform-MC triplet samples to predict log E_rot[f] at a centre (f =
+n1 n2 n3 averaged over rotations).  Centres are then drawn from a pool of
+uniform candidates with probability q_i = a/M + (1-a) h_i / sum h,
+h = exp(prediction) (the shape that makes the centres x rotations estimator's
+per-centre terms equal, mixed with the uniform pool distribution so weights
+stay bounded), and each sample is weighted by (1/M)/q_i: the estimator stays
+unbiased for the pool mean, hence for the box mean, whatever the network
+predicts.  Inference runs on the tensor cores (hermes_mlp_infer_tc).
 """
 
 import ctypes
@@ -692,30 +695,34 @@ class LearnedProposal:
             self._shells[key] = f
         return f
 
+    # densities enter (and the target leaves) on a log scale clamped to
+    # [1e-2, 1e3] times the mean density (its cube for the target): centres
+    # with no particles in reach give ~0 and must not dominate the fit
+    LOG_FLOOR, LOG_CEIL = 1e-2, 1e3
+
+    def _logd(self, v, power=1):
+        return torch.log((v / self.rho ** power).clamp(self.LOG_FLOOR, self.LOG_CEIL ** power))
+
     def features(self, centers, r12s, r13s, mu):
         n1 = interp(self.e1, self.J, centers, self.phi_t)
         s2 = interp(self.shell_field(2, r12s), self.J, centers, self.phi_t)
         s3 = interp(self.shell_field(3, r13s), self.J, centers, self.phi_t)
-        dl = (n1 / self.rho - 1.0).clamp(-1.0, 50.0)
-
-        def logd(v):
-            return torch.log((v / self.rho).clamp(0.01, 50.0))
-
-        f = torch.stack([torch.full_like(dl, r12s / self.L * 10), torch.full_like(dl, r13s / self.L * 10),
-                         torch.full_like(dl, mu), torch.log1p(dl.clamp_min(-0.99)), logd(s2), logd(s3)], dim=1)
+        f = torch.stack([torch.full_like(n1, r12s / self.L * 10), torch.full_like(n1, r13s / self.L * 10),
+                         torch.full_like(n1, mu), self._logd(n1), self._logd(s2), self._logd(s3)], dim=1)
         return f.float()
 
     def training_data(self, configs, n_centers, n_rot_train, seed=0):
-        """Uniform-MC samples: features and target log(mean_r f^2 / scale^2)."""
+        """Uniform-MC samples: features and the target log E_rot[f | centre]
+        (the mean of f = n1 n2 n3 over n_rot_train rotations, in units of the
+        cubed mean density, clamped as the features)."""
         X, T = [], []
         rng = np.random.default_rng(seed)
         for (r12s, r13s, mu) in configs:
             c = torch.as_tensor(rng.uniform(0.0, float(self.L), (n_centers, 3)), device=self.device)
             off = rotation_offsets(r12s, r13s, mu, n_rot_train, rng=np.random.RandomState(rng.integers(1 << 31)))
             _, smp = triplet_sum(self.e1, self.e2, self.e3, self.J, c, off, self.phi_t, samples=True)
-            m2 = (smp.double() ** 2).mean(dim=1) / self.rho ** 6
             X.append(self.features(c, r12s, r13s, mu))
-            T.append(torch.log(m2 + 1e-12).float())
+            T.append(self._logd(smp.double().mean(dim=1), power=3).float())
         return torch.cat(X), torch.cat(T)
 
     def train(self, configs, n_centers=200_000, n_rot_train=8, epochs=4, seed=0):
@@ -729,7 +736,7 @@ class LearnedProposal:
         cores (hermes_mlp_infer_tc), False in FP32 on the CUDA cores."""
         feats = self.features(pool, r12s, r13s, mu)
         pred = (self.net.infer(feats) if bf16 else self.net.forward(feats)).reshape(-1).double()
-        logh = 0.5 * (pred * self.t_std + self.t_mean)
+        logh = pred * self.t_std + self.t_mean  # predicted log E_rot[f | centre]
         h = torch.exp(logh - logh.max())
         M = pool.shape[0]
         q = self.mix / M + (1.0 - self.mix) * h / h.sum()

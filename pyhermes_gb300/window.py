@@ -636,18 +636,45 @@ def materialized_pair_products(fields, pairs, windows, exclude_k0=True):
     return out, k0
 
 
-def pair_products(spectra, pairs, windows, exclude_k0=True):
+def family_descriptors(template, len_args_list):
+    """Descriptors of a family of built-in windows that differ from
+    `template` only in their physical len_args (one dict per member): the
+    template's descriptor with each member's lengths rescaled to grid units,
+    as WindowFunc.descriptor() gives for the member itself."""
+    base = template.descriptor()
+    names = WIN_ARGS[template.type]
+    L, box = template.L, template.box_size
+    arr = (HermesWindow * len(len_args_list))()
+    size = ctypes.sizeof(HermesWindow)
+    for i, la in enumerate(len_args_list):
+        ctypes.memmove(ctypes.byref(arr[i]), ctypes.byref(base), size)
+        for j, nm in enumerate(names):
+            v = la.get(nm)
+            if v is None:
+                raise ValueError(f"Missing keyword arguments: ['{nm}'] for window '{template.type}'")
+            arr[i].len[j] = float(v * L / box)  # the rescale order of WindowFunc.__init__
+        if template.type == "thick_shell" and not (arr[i].len[0] >= 0.0 and arr[i].len[1] > 0.0
+                                                   and np.isfinite(arr[i].len[0]) and np.isfinite(arr[i].len[1])):
+            raise ValueError("thick_shell requires a finite non-negative R and a finite positive delta_R.")
+    return arr
+
+
+def pair_products(spectra, pairs, windows, exclude_k0=True, descs=None):
     """sum_k F_i K_b conj(F_j) / L^6 for every window b and pair (i, j).
 
     spectra: list of complex64 half spectra; pairs: list of (i, j);
-    windows: list of WindowFunc (built-in, non-composite).  Returns a float64
-    array [n_bins, n_pairs] and the kernel values at k = 0 [n_bins].
+    windows: list of WindowFunc (built-in, non-composite), or the template of
+    a family whose descriptors are given in `descs` (family_descriptors).
+    Returns a float64 array [n_bins, n_pairs] and the kernel values at
+    k = 0 [n_bins].
     """
     lib = _lib.load()
     w0 = windows[0]
     J, dev = w0.J, spectra[0].device
-    n_bins, n_pairs = len(windows), len(pairs)
-    descs = (HermesWindow * n_bins)(*[w.descriptor() for w in windows])
+    n_pairs = len(pairs)
+    if descs is None:
+        descs = (HermesWindow * len(windows))(*[w.descriptor() for w in windows])
+    n_bins = len(descs)
     ptrs = (ctypes.c_void_p * len(spectra))(*[s.data_ptr() for s in spectra])
     pr = (ctypes.c_int32 * (2 * n_pairs))(*[v for p in pairs for v in p])
     need = ctypes.c_size_t(0)

@@ -34,12 +34,20 @@ def oracle_kernels(monkeypatch):
     def rfft_field(eps):  # the "spectrum" handed to pair_products is the real field itself
         return eps.detach().double().cpu().clone()
 
-    def pair_products(spectra, pairs, windows, exclude_k0=True):
+    def pair_products(spectra, pairs, windows, exclude_k0=True, descs=None):
+        from pyhermes_gb300.window import WIN_ARGS
+
         L = windows[0].L
         P = oracle.fourier_power(PHI, windows[0].bandwidth, L)
+        if descs is not None:  # a window family: the template with each bin's lengths
+            t = windows[0]
+            specs = [{nm: d.len[j] * t.box_size / L for j, nm in enumerate(WIN_ARGS[t.type])} for d in descs]
+            windows = [t] * len(descs)
+        else:
+            specs = [w.len_args for w in windows]
         vals, k0 = np.zeros((len(windows), len(pairs))), np.zeros(len(windows))
         for b, w in enumerate(windows):
-            K = oracle.window_kernel(w.type, w.len_args, L, P, mode=w.resolved_mode(), box=w.box_size)
+            K = oracle.window_kernel(w.type, specs[b], L, P, mode=w.resolved_mode(), box=w.box_size)
             k0[b] = K[0, 0, 0]
             for c, (i, j) in enumerate(pairs):
                 ei, ej = spectra[i].numpy(), spectra[j].numpy()
