@@ -496,8 +496,8 @@ def mc_bench(dev, phi_np, steps):
     (centres x 100 rotations, hermes_mc_triplets with centre weights; the
     learned centres are drawn from the proposal over a fresh uniform pool of
     16x candidates per replicate; the proposal sees the centre density and
-    the shell-averaged densities at r12 and r13), 32 independent replicates
-    of ~1e6 triplets per triangle and estimator: estimator variance from the
+    the shell-averaged densities at r12 and r13), 64 independent replicates
+    of ~5e5 triplets per triangle and estimator: estimator variance from the
     replicate spread, bias in units of the combined standard error, and
     variance x time at equal wall time (the learned time includes the
     proposal on the candidate pools)."""
@@ -532,7 +532,7 @@ def mc_bench(dev, phi_np, steps):
 
     grid_r = [20.0, 53.3, 86.7, 120.0]
     configs = [(r1 * sc, r2 * sc, mu) for r1 in grid_r for r2 in grid_r if r2 >= r1 for mu in (-0.75, -0.25, 0.25, 0.75)]
-    n_rot_train = 8
+    n_rot_train = 32
     n_cen_train = MC_TRAIN // (len(configs) * n_rot_train)
     t0 = time.perf_counter()
     losses = lp.train(configs, n_centers=n_cen_train, n_rot_train=n_rot_train, epochs=3, seed=1)
@@ -541,7 +541,7 @@ def mc_bench(dev, phi_np, steps):
     tests = [(30.0, 60.0, 0.8), (60.0, 90.0, -0.3), (100.0, 120.0, 0.0)]
     n_rot = 100
     pool_factor = 16
-    replicates = 32
+    replicates = 64
     n_cen = MC_SAMPLES // (len(tests) * n_rot * replicates)  # centres per replicate
     rows = []
     for k, (r1, r2, mu) in enumerate(tests):

@@ -348,6 +348,11 @@ int hermes_mlp_backward(const float* params, const int32_t* dims, int n_layers,
                         float* grads, float* scratch, void* stream);
 int hermes_mse_grad(const float* y, const float* target, int64_t n, float* dy,
                     double* loss_out, double* scratch, void* stream);
+/* hermes_poisson_grad: as mse_grad for the Poisson deviance of log-mean
+ * predictions y against non-negative targets: loss = mean(exp(y) - t y),
+ * dy = (exp(y) - t) / n (minimised by y = log E[t | input]). */
+int hermes_poisson_grad(const float* y, const float* target, int64_t n, float* dy,
+                        double* loss_out, double* scratch, void* stream);
 int hermes_adam_step(float* params, const float* grads, float* m, float* v, int64_t n,
                      float lr, float b1, float b2, float eps, int step, void* stream);
 int hermes_to_bf16(const float* in, int64_t n, void* out, void* stream);

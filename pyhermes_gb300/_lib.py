@@ -60,6 +60,7 @@ SIGNATURES = {
     "hermes_mc_triplets": (_c_int, [_p, _p, _p, _c_int, _p, _p, _c_i64, _p, _c_int, _p, _c_int, _c_int, _dbl,
                                     ctypes.POINTER(_dbl), _p, _p, _c_sz, _p]),
     "hermes_mlp_infer_tc": (_c_int, [_p, _p, _c_int, _p, _c_i64, _p, _p, _p]),
+    "hermes_poisson_grad": (_c_int, [_p, _p, _c_i64, _p, ctypes.POINTER(_dbl), _p, _p]),
     "hermes_mlp_param_count": (_c_int, [_p, _c_int, ctypes.POINTER(_c_i64)]),
     "hermes_mlp_scratch_floats": (_c_int, [_c_i64, ctypes.POINTER(_c_i64)]),
     "hermes_mlp_forward": (_c_int, [_p, _p, _p, _c_int, _p, _c_i64, _p, _p]),

@@ -350,6 +350,29 @@ extern "C" int hermes_to_bf16(const float* in, int64_t n, void* out, void* strea
   return HERMES_OK;
 }
 
+// Poisson deviance of predictions y = log(mu) against non-negative targets
+// t: loss = mean(exp(y) - t y), dy = (exp(y) - t) / n.  Its minimiser is
+// y = log E[t | input], the log of a conditional mean, where a squared error
+// on log t would give E[log t | input].  y is clamped to <= 30 in exp.
+__global__ void poisson_grad_kernel(const float* __restrict__ y, const float* __restrict__ t, int64_t n,
+                                    float* __restrict__ dy, double* __restrict__ partial) {
+  double acc = 0.0;
+  const float inv = 1.f / (float)n;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float e = expf(fminf(y[i], 30.f));
+    dy[i] = inv * (e - t[i]);
+    acc += (double)e - (double)t[i] * (double)y[i];
+  }
+  __shared__ double sh[256];
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) atomicAdd(partial, sh[0]);
+}
+
 // ---- inference on the tensor cores ----------------------------------------------
 // For networks dims = (d0 <= 16, 128, ..., 128, 1): the first layer (K = d0)
 // and the last (128 -> 1) on the CUDA cores, every 128 x 128 hidden layer as
@@ -564,5 +587,20 @@ extern "C" int hermes_mlp_infer_tc(const float* params, const int32_t* dims, int
   const int grid = (int)(ntiles < nsm ? ntiles : nsm);
   mlp_infer_tc_kernel<<<grid, mi::kThreads, smem, s>>>(A);
   HERMES_LAUNCH_CHECK("mlp_infer_tc_kernel");
+  return HERMES_OK;
+}
+
+extern "C" int hermes_poisson_grad(const float* y, const float* target, int64_t n, float* dy, double* loss_out,
+                                   double* scratch, void* stream) {
+  if (!y || !target || !dy || !loss_out || !scratch) return fail(HERMES_ERR_INVALID, "poisson_grad: NULL argument");
+  cudaStream_t s = hermes::as_stream(stream);
+  HERMES_CUDA_TRY(cudaMemsetAsync(scratch, 0, sizeof(double), s));
+  if (n > 0) {
+    poisson_grad_kernel<<<256, 256, 0, s>>>(y, target, n, dy, scratch);
+    HERMES_LAUNCH_CHECK("poisson_grad_kernel");
+  }
+  HERMES_CUDA_TRY(cudaMemcpyAsync(loss_out, scratch, sizeof(double), cudaMemcpyDeviceToHost, s));
+  HERMES_CUDA_TRY(cudaStreamSynchronize(s));
+  *loss_out = n > 0 ? *loss_out / (double)n : 0.0;
   return HERMES_OK;
 }

@@ -894,8 +894,11 @@ mp_contract_tc_kernel(ContractArgs A, const __grid_constant__ CUtensorMap a2map)
   const int J = A.J, L = 1 << J, Lm = L - 1, CX = A.CX;
   const int tid = threadIdx.x, warp = tid >> 5;
   const int b = tid & 15;
-  const int grp = tid >> 4;
-  const int cy = 2 * (grp / (ct::TZ / 2)), cz = 2 * (grp % (ct::TZ / 2));
+  // 2x2 column block of this half-warp: the two half-warps of a warp take
+  // blocks 4 cells apart in z, so their rows of the swizzled G operand fall
+  // in complementary halves of the 128-byte rows (no bank conflict)
+  const int hw = (tid >> 4) & 1, wq = tid >> 5;
+  const int cy = 2 * (wq >> 1), cz = 4 * hw + 2 * (wq & 1);
   const int nty = L / ct::TY, ntz = L / ct::TZ;
   const int n_items = (L / CX) * nty * ntz;
   const int nsteps = CX + 4;

@@ -14,11 +14,11 @@ and the scale_factor**9 rescale.  Triplet sums run in
 ``LearnedProposal`` (no reference counterpart): a tanh MLP over
 (r12, r13, mu, the density at the centre and the shell-averaged densities at
 r12 and r13 around it) trained with the hand-written kernels of csrc/mlp.cu
-on uniform-MC triplet samples to predict log E_rot[f] at a centre (f =
-n1 n2 n3 averaged over rotations).  Centres are then drawn from a pool of
-uniform candidates with probability q_i = a/M + (1-a) h_i / sum h,
-h = exp(prediction) (the shape that makes the centres x rotations estimator's
-per-centre terms equal, mixed with the uniform pool distribution so weights
+on uniform-MC triplet samples to predict log E[mbar^2] at a centre, mbar
+being the rotation average of f = n1 n2 n3 that the estimator forms.
+Centres are then drawn from a pool of uniform candidates with probability
+q_i = a/M + (1-a) h_i / sum h, h = exp(prediction / 2) (the variance-optimal
+shape sqrt(E mbar^2), mixed with the uniform pool distribution so weights
 stay bounded), and each sample is weighted by (1/M)/q_i: the estimator stays
 unbiased for the pool mean, hence for the box mean, whatever the network
 predicts.  Inference runs on the tensor cores (hermes_mlp_infer_tc).
@@ -615,17 +615,19 @@ class MLP:
                    "hermes_mlp_infer_tc")
         return y
 
-    def grads(self, x, target):
-        """(loss, gradient of the mean squared error) for one batch."""
+    def grads(self, x, target, loss="mse"):
+        """(loss, gradient) for one batch: the mean squared error, or
+        loss='poisson' the Poisson deviance of log-mean outputs."""
         lib = _lib.load()
         x = x.to(torch.float32).contiguous()
         y, acts = self.forward(x, return_acts=True)
         t = target.to(torch.float32).reshape(-1).contiguous()
         dy = torch.empty_like(t)
-        loss = ctypes.c_double(0.0)
         scratch_d = torch.empty(1, dtype=torch.float64, device=self.device)
-        _lib.check(lib.hermes_mse_grad(_ptr(y.reshape(-1).contiguous()), _ptr(t), t.numel(), _ptr(dy),
-                                       ctypes.byref(loss), _ptr(scratch_d), _stream_ptr(self.device)), "mse_grad")
+        fn = lib.hermes_poisson_grad if loss == "poisson" else lib.hermes_mse_grad
+        lv = ctypes.c_double(0.0)
+        _lib.check(fn(_ptr(y.reshape(-1).contiguous()), _ptr(t), t.numel(), _ptr(dy), ctypes.byref(lv), _ptr(scratch_d),
+                      _stream_ptr(self.device)), "loss_grad")
         n = ctypes.c_int64(0)
         lib.hermes_mlp_scratch_floats(x.shape[0], ctypes.byref(n))
         scratch = torch.empty(n.value, dtype=torch.float32, device=self.device)
@@ -633,7 +635,7 @@ class MLP:
         _lib.check(lib.hermes_mlp_backward(_ptr(self.params), self.cdims, len(self.dims) - 1, _ptr(x), x.shape[0],
                                            _ptr(acts), _ptr(dy), _ptr(g), _ptr(scratch), _stream_ptr(self.device)),
                    "mlp_backward")
-        return loss.value, g
+        return lv.value, g
 
     def adam(self, g, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8):
         self.step_count += 1
@@ -642,7 +644,7 @@ class MLP:
                                                 self.n_params, lr, b1, b2, eps, self.step_count,
                                                 _stream_ptr(self.device)), "adam_step")
 
-    def train(self, x, t, epochs=5, batch=8192, lr=2e-3, seed=0):
+    def train(self, x, t, epochs=5, batch=8192, lr=2e-3, seed=0, loss="mse"):
         n = x.shape[0]
         gen = torch.Generator(device=self.device).manual_seed(seed)
         losses = []
@@ -650,9 +652,9 @@ class MLP:
             perm = torch.randperm(n, device=self.device, generator=gen)
             for s in range(0, n - batch + 1, batch):
                 idx = perm[s:s + batch]
-                loss, g = self.grads(x[idx], t[idx])
+                loss_v, g = self.grads(x[idx], t[idx], loss=loss)
                 self.adam(g, lr=lr)
-                losses.append(loss)
+                losses.append(loss_v)
         return losses
 
 
@@ -711,33 +713,44 @@ class LearnedProposal:
                          torch.full_like(n1, mu), self._logd(n1), self._logd(s2), self._logd(s3)], dim=1)
         return f.float()
 
-    def training_data(self, configs, n_centers, n_rot_train, seed=0):
-        """Uniform-MC samples: features and the target log E_rot[f | centre]
-        (the mean of f = n1 n2 n3 over n_rot_train rotations, in units of the
-        cubed mean density, clamped as the features)."""
+    def training_data(self, configs, n_centers, n_rot_train, seed=0, n_rot_eval=100):
+        """Uniform-MC samples: features and, per centre, an unbiased estimate
+        of E[mbar^2 | centre] for the rotation average mbar of an estimator
+        that uses n_rot_eval rotations per centre: from the n_rot_train
+        rotations' mean m and variance s^2 (f = n1 n2 n3 in units of the
+        cubed mean density), m^2 - (1/n_rot_train - 1/n_rot_eval) s^2,
+        clamped at 0."""
         X, T = [], []
         rng = np.random.default_rng(seed)
+        k = 1.0 / n_rot_train - 1.0 / n_rot_eval
         for (r12s, r13s, mu) in configs:
             c = torch.as_tensor(rng.uniform(0.0, float(self.L), (n_centers, 3)), device=self.device)
             off = rotation_offsets(r12s, r13s, mu, n_rot_train, rng=np.random.RandomState(rng.integers(1 << 31)))
             _, smp = triplet_sum(self.e1, self.e2, self.e3, self.J, c, off, self.phi_t, samples=True)
+            f = smp.double() / self.rho ** 3
+            m, v = f.mean(dim=1), f.var(dim=1)
             X.append(self.features(c, r12s, r13s, mu))
-            T.append(self._logd(smp.double().mean(dim=1), power=3).float())
+            T.append((m * m - k * v).clamp_min(0.0).float())
         return torch.cat(X), torch.cat(T)
 
-    def train(self, configs, n_centers=200_000, n_rot_train=8, epochs=4, seed=0):
-        X, T = self.training_data(configs, n_centers, n_rot_train, seed)
-        self.t_mean = float(T.mean())
-        self.t_std = float(T.std()) + 1e-6
-        return self.net.train(X, (T - self.t_mean) / self.t_std, epochs=epochs, seed=seed)
+    def train(self, configs, n_centers=200_000, n_rot_train=8, epochs=4, seed=0, n_rot_eval=100):
+        """Fits log E[mbar^2 | centre] (in units of the targets' mean) with
+        the Poisson deviance, whose minimiser is the log of the conditional
+        mean even though each target is a noisy few-rotation estimate; the
+        proposal is then q ~ sqrt(E[mbar^2 | centre]), the variance-optimal
+        shape for a weighted mean of per-centre rotation averages."""
+        X, T = self.training_data(configs, n_centers, n_rot_train, seed, n_rot_eval)
+        self.t_scale = float(T.double().mean()) or 1.0
+        t = (T / self.t_scale).clamp_max(1.0e4)
+        return self.net.train(X, t, epochs=epochs, seed=seed, loss="poisson")
 
     def proposal(self, pool, r12s, r13s, mu, bf16=True):
         """q over the pool; bf16=True evaluates the network on the tensor
         cores (hermes_mlp_infer_tc), False in FP32 on the CUDA cores."""
         feats = self.features(pool, r12s, r13s, mu)
         pred = (self.net.infer(feats) if bf16 else self.net.forward(feats)).reshape(-1).double()
-        logh = pred * self.t_std + self.t_mean  # predicted log E_rot[f | centre]
-        h = torch.exp(logh - logh.max())
+        p = 0.5 * pred.clamp_max(60.0)  # log sqrt(E[mbar^2 | centre]), relative
+        h = torch.exp(p - p.max())
         M = pool.shape[0]
         q = self.mix / M + (1.0 - self.mix) * h / h.sum()
         return q

@@ -43,6 +43,9 @@ _WS = {}
 
 
 def _workspace(nbytes, device):
+    device = torch.device(device)
+    if device.type == "cuda" and device.index is None:
+        device = torch.device("cuda", torch.cuda.current_device())
     key = ("multipole", str(device))
     buf = _WS.get(key)
     if buf is None or buf.numel() < nbytes:

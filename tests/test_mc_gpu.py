@@ -153,6 +153,29 @@ def test_mlp_tensor_core_inference_matches_oracle(dims, batch):
     assert np.array_equal(ytc, net.infer(torch.as_tensor(x, device="cuda")).cpu().numpy())
 
 
+def test_poisson_deviance_gradient_matches_numpy():
+    """hermes_poisson_grad: loss = mean(exp(y) - t y), dy = (exp(y) - t)/n
+    against float64 numpy."""
+    import ctypes
+
+    from pyhermes_gb300 import _lib
+    from pyhermes_gb300.kernels import _ptr, _stream_ptr
+
+    rng = np.random.default_rng(8)
+    n = 100_003
+    y = rng.normal(0.0, 1.5, n).astype(np.float32)
+    t = rng.gamma(0.5, 2.0, n).astype(np.float32)
+    yt, tt = torch.as_tensor(y, device="cuda"), torch.as_tensor(t, device="cuda")
+    dy = torch.empty_like(yt)
+    loss = ctypes.c_double(0.0)
+    scratch = torch.empty(1, dtype=torch.float64, device="cuda")
+    _lib.check(_lib.load().hermes_poisson_grad(_ptr(yt), _ptr(tt), n, _ptr(dy), ctypes.byref(loss), _ptr(scratch),
+                                                _stream_ptr(yt.device)), "poisson_grad")
+    yd, td = y.astype(np.float64), t.astype(np.float64)
+    assert abs(loss.value - np.mean(np.exp(yd) - td * yd)) < 1e-6 * np.mean(np.exp(yd))
+    assert _rel(dy.cpu().numpy(), (np.exp(yd) - td) / n) < 1e-5
+
+
 def test_mlp_training_reduces_loss():
     net = mc3pcf.MLP([4, 64, 64, 1], seed=1)
     rng = np.random.default_rng(5)
@@ -175,7 +198,7 @@ def test_learned_proposal_is_unbiased_and_reduces_variance():
     rho = 1.0 / L ** 3
     lp = mc3pcf.LearnedProposal(eps, eps, eps, J, PHI, rho)
     configs = [(r1, r2, mu) for r1 in (1.5, 3.0) for r2 in (2.5, 5.0) for mu in (-0.5, 0.5)]
-    losses = lp.train(configs, n_centers=100_000, n_rot_train=8, epochs=3)
+    losses = lp.train(configs, n_centers=100_000, n_rot_train=8, epochs=3, n_rot_eval=1)
     assert losses[-1] < losses[0]
     pool = torch.as_tensor(np.random.default_rng(9).uniform(0, L, (400_000, 3)), device="cuda")
     K = 400_000
@@ -220,7 +243,7 @@ def test_mc_sample_matches_interp_path_and_draws_unbiased_rotations():
     assert abs(m_dev - m_host) < 5 * se, (m_dev, m_host, se)
     # learned proposal through the fused kernel: unbiased, smaller estimator variance
     configs = [(r1, r2, mu) for r1 in (1.5, 3.0) for r2 in (2.5, 5.0) for mu in (-0.5, 0.5)]
-    lp.train(configs, n_centers=100_000, n_rot_train=8, epochs=3)
+    lp.train(configs, n_centers=100_000, n_rot_train=8, epochs=3, n_rot_eval=1)
     m_l, se_l, v_l = lp.sample_stats(pool, 2.0, 4.0, 0.3, K, seed=23)
     se = np.sqrt(se_dev ** 2 + se_l ** 2)
     assert abs(m_l - m_dev) < 5 * se, (m_l, m_dev, se)
