@@ -62,3 +62,29 @@ def test_noalloc_deposit_rejects_sizes_beyond_its_scratch():
     rc = lib.hermes_deposit_noalloc(_ptr(pos), _ptr(w), 131_073, 5, 1000.0, _ptr(phi), phi.numel(), 1024,
                                     _ptr(eps), None, None, stream)
     assert rc == -1 and b"n=131073" in lib.hermes_last_error()
+
+
+def test_noalloc_deposit_float64_output_and_output_choice():
+    """The float64 field output on the built-in scratch equals
+    kernels.deposit(..., out_dtype=float64) bit for bit, and giving both
+    outputs or neither is refused."""
+    lib = _lib.load()
+    phi = torch.as_tensor(sample_scaling_function(), device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    n, J = 50_000, 6
+    pos, w = _catalogue(4, n)
+    L = 1 << J
+    e64 = torch.empty((L, L, L), dtype=torch.float64, device="cuda")
+    rc = lib.hermes_deposit_noalloc(_ptr(pos), _ptr(w), n, J, 1000.0, _ptr(phi), phi.numel(), 1024, None, _ptr(e64),
+                                    None, stream)
+    _lib.check(rc, "hermes_deposit_noalloc")
+    ref, _, _ = kernels.deposit(pos, w, J, 1000.0, phi, out_dtype=torch.float64)
+    torch.cuda.synchronize()
+    assert torch.equal(e64, ref)
+    e32 = torch.empty((L, L, L), dtype=torch.float32, device="cuda")
+    rc = lib.hermes_deposit_noalloc(_ptr(pos), _ptr(w), n, J, 1000.0, _ptr(phi), phi.numel(), 1024, _ptr(e32),
+                                    _ptr(e64), None, stream)
+    assert rc == -1
+    rc = lib.hermes_deposit_noalloc(_ptr(pos), _ptr(w), n, J, 1000.0, _ptr(phi), phi.numel(), 1024, None, None,
+                                    None, stream)
+    assert rc == -1
