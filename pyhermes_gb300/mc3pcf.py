@@ -615,18 +615,25 @@ class MLP:
                    "hermes_mlp_infer_tc")
         return y
 
-    def grads(self, x, target, loss="mse"):
+    def grads(self, x, target, loss="mse", offset=None):
         """(loss, gradient) for one batch: the mean squared error, or
-        loss='poisson' the Poisson deviance of log-mean outputs."""
+        loss='poisson' the Poisson deviance of log-mean outputs.  `offset`
+        (per sample) is added to the output before the loss, a known term
+        of the log-mean that the network does not have to learn; the
+        gradient with respect to the output is unchanged by it."""
         lib = _lib.load()
         x = x.to(torch.float32).contiguous()
         y, acts = self.forward(x, return_acts=True)
+        yv = y.reshape(-1)
+        if offset is not None:
+            yv = yv + offset.to(torch.float32).reshape(-1)
+        yv = yv.contiguous()
         t = target.to(torch.float32).reshape(-1).contiguous()
         dy = torch.empty_like(t)
         scratch_d = torch.empty(1, dtype=torch.float64, device=self.device)
         fn = lib.hermes_poisson_grad if loss == "poisson" else lib.hermes_mse_grad
         lv = ctypes.c_double(0.0)
-        _lib.check(fn(_ptr(y.reshape(-1).contiguous()), _ptr(t), t.numel(), _ptr(dy), ctypes.byref(lv), _ptr(scratch_d),
+        _lib.check(fn(_ptr(yv), _ptr(t), t.numel(), _ptr(dy), ctypes.byref(lv), _ptr(scratch_d),
                       _stream_ptr(self.device)), "loss_grad")
         n = ctypes.c_int64(0)
         lib.hermes_mlp_scratch_floats(x.shape[0], ctypes.byref(n))
@@ -644,7 +651,7 @@ class MLP:
                                                 self.n_params, lr, b1, b2, eps, self.step_count,
                                                 _stream_ptr(self.device)), "adam_step")
 
-    def train(self, x, t, epochs=5, batch=8192, lr=2e-3, seed=0, loss="mse"):
+    def train(self, x, t, epochs=5, batch=8192, lr=2e-3, seed=0, loss="mse", offset=None):
         n = x.shape[0]
         gen = torch.Generator(device=self.device).manual_seed(seed)
         losses = []
@@ -652,7 +659,7 @@ class MLP:
             perm = torch.randperm(n, device=self.device, generator=gen)
             for s in range(0, n - batch + 1, batch):
                 idx = perm[s:s + batch]
-                loss_v, g = self.grads(x[idx], t[idx], loss=loss)
+                loss_v, g = self.grads(x[idx], t[idx], loss=loss, offset=None if offset is None else offset[idx])
                 self.adam(g, lr=lr)
                 losses.append(loss_v)
         return losses
@@ -661,12 +668,20 @@ class MLP:
 class LearnedProposal:
     """Importance sampling of triangle centres with a trained MLP proposal.
 
-    Features of a candidate centre c for a triangle (r12, r13, mu): the
-    triangle's shape, the density n1(c) of vertex 1 at the centre and the
-    densities of vertices 2 and 3 averaged over the thin shells of radius r12
-    and r13 around c (the fields convolved with a shell window, evaluated with
-    the same 27-point interpolation).  The shell averages carry
-    E_rot[n2 n3 | c], which the centre density alone cannot."""
+    The per-centre value of the reference estimator is a rotation average
+    g(c) = n1(c) * mean_r n2 n3, so its second moment given the centre is
+    E[g^2 | c] = n1(c)^2 * E[(mean_r n2 n3)^2 | c].  The first factor is known
+    exactly at every candidate (the same 27-point interpolation the triplet
+    kernel uses), so the proposal keeps it as a fixed factor and the network
+    learns only the second: log E[(mean_r n2 n3)^2 | c] as a Poisson-deviance
+    fit with log n1^2 as an offset.  Its features are the triangle's shape,
+    log n1, and the densities of vertices 2 and 3 averaged over the thin
+    shells of radius r12 and r13 around c (the fields convolved with a shell
+    window, evaluated with the same interpolation).  Centres with n1 = 0
+    contribute exactly 0 to the estimate, so they get no samples; the
+    defensive mixture is uniform over the others.  The variance-optimal
+    proposal for a weighted mean of per-centre rotation averages is
+    q ~ sqrt(E[g^2 | c]), which is what is sampled."""
 
     N_FEATURES = 6
 
@@ -697,63 +712,71 @@ class LearnedProposal:
             self._shells[key] = f
         return f
 
-    # densities enter (and the target leaves) on a log scale clamped to
-    # [1e-2, 1e3] times the mean density (its cube for the target): centres
-    # with no particles in reach give ~0 and must not dominate the fit
+    # densities enter on a log scale clamped to [1e-2, 1e3] times the mean
+    # density: centres with nothing in reach must not dominate the inputs
     LOG_FLOOR, LOG_CEIL = 1e-2, 1e3
 
     def _logd(self, v, power=1):
         return torch.log((v / self.rho ** power).clamp(self.LOG_FLOOR, self.LOG_CEIL ** power))
 
-    def features(self, centers, r12s, r13s, mu):
+    def features(self, centers, r12s, r13s, mu, return_n1=False):
+        """[n, 6] float32 network inputs; with return_n1 also the float64
+        centre density n1 (in units of the mean density)."""
         n1 = interp(self.e1, self.J, centers, self.phi_t)
         s2 = interp(self.shell_field(2, r12s), self.J, centers, self.phi_t)
         s3 = interp(self.shell_field(3, r13s), self.J, centers, self.phi_t)
         f = torch.stack([torch.full_like(n1, r12s / self.L * 10), torch.full_like(n1, r13s / self.L * 10),
-                         torch.full_like(n1, mu), self._logd(n1), self._logd(s2), self._logd(s3)], dim=1)
-        return f.float()
+                         torch.full_like(n1, mu), self._logd(n1), self._logd(s2), self._logd(s3)], dim=1).float()
+        return (f, n1.double() / self.rho) if return_n1 else f
 
     def training_data(self, configs, n_centers, n_rot_train, seed=0, n_rot_eval=100):
-        """Uniform-MC samples: features and, per centre, an unbiased estimate
-        of E[mbar^2 | centre] for the rotation average mbar of an estimator
-        that uses n_rot_eval rotations per centre: from the n_rot_train
-        rotations' mean m and variance s^2 (f = n1 n2 n3 in units of the
-        cubed mean density), m^2 - (1/n_rot_train - 1/n_rot_eval) s^2,
-        clamped at 0."""
-        X, T = [], []
+        """Uniform-MC samples at centres with n1 != 0: features, the offset
+        log n1^2 and, per centre, an unbiased estimate of E[g^2 | centre]
+        for the rotation average g of an estimator that uses n_rot_eval
+        rotations per centre: from the n_rot_train rotations' mean m and
+        variance s^2 (f = n1 n2 n3 in units of the cubed mean density),
+        m^2 - (1/n_rot_train - 1/n_rot_eval) s^2, clamped at 0."""
+        X, T, O = [], [], []
         rng = np.random.default_rng(seed)
         k = 1.0 / n_rot_train - 1.0 / n_rot_eval
         for (r12s, r13s, mu) in configs:
             c = torch.as_tensor(rng.uniform(0.0, float(self.L), (n_centers, 3)), device=self.device)
+            feats, n1 = self.features(c, r12s, r13s, mu, return_n1=True)
+            keep = n1 != 0.0
+            c, feats, n1 = c[keep].contiguous(), feats[keep], n1[keep]
             off = rotation_offsets(r12s, r13s, mu, n_rot_train, rng=np.random.RandomState(rng.integers(1 << 31)))
             _, smp = triplet_sum(self.e1, self.e2, self.e3, self.J, c, off, self.phi_t, samples=True)
             f = smp.double() / self.rho ** 3
             m, v = f.mean(dim=1), f.var(dim=1)
-            X.append(self.features(c, r12s, r13s, mu))
-            T.append((m * m - k * v).clamp_min(0.0).float())
-        return torch.cat(X), torch.cat(T)
+            X.append(feats)
+            T.append((m * m - k * v).clamp_min(0.0))
+            O.append(torch.log(n1 * n1))
+        return torch.cat(X), torch.cat(T), torch.cat(O)
 
     def train(self, configs, n_centers=200_000, n_rot_train=8, epochs=4, seed=0, n_rot_eval=100):
-        """Fits log E[mbar^2 | centre] (in units of the targets' mean) with
-        the Poisson deviance, whose minimiser is the log of the conditional
-        mean even though each target is a noisy few-rotation estimate; the
-        proposal is then q ~ sqrt(E[mbar^2 | centre]), the variance-optimal
-        shape for a weighted mean of per-centre rotation averages."""
-        X, T = self.training_data(configs, n_centers, n_rot_train, seed, n_rot_eval)
-        self.t_scale = float(T.double().mean()) or 1.0
-        t = (T / self.t_scale).clamp_max(1.0e4)
-        return self.net.train(X, t, epochs=epochs, seed=seed, loss="poisson")
+        """Fits log E[g^2 | centre] - log n1^2 (targets in units of their
+        mean) with the Poisson deviance, whose minimiser is the log of the
+        conditional mean even though each target is a noisy few-rotation
+        estimate."""
+        X, T, O = self.training_data(configs, n_centers, n_rot_train, seed, n_rot_eval)
+        self.t_scale = float(T.mean()) or 1.0
+        t = (T / self.t_scale).clamp_max(1.0e4).float()
+        return self.net.train(X, t, epochs=epochs, seed=seed, loss="poisson", offset=O.float())
 
     def proposal(self, pool, r12s, r13s, mu, bf16=True):
-        """q over the pool; bf16=True evaluates the network on the tensor
-        cores (hermes_mlp_infer_tc), False in FP32 on the CUDA cores."""
-        feats = self.features(pool, r12s, r13s, mu)
+        """q over the pool: mix uniform over the candidates with n1 != 0 plus
+        (1 - mix) |n1| sqrt(exp(network)), normalised; bf16=True evaluates
+        the network on the tensor cores (hermes_mlp_infer_tc), False in FP32
+        on the CUDA cores."""
+        feats, n1 = self.features(pool, r12s, r13s, mu, return_n1=True)
         pred = (self.net.infer(feats) if bf16 else self.net.forward(feats)).reshape(-1).double()
-        p = 0.5 * pred.clamp_max(60.0)  # log sqrt(E[mbar^2 | centre]), relative
-        h = torch.exp(p - p.max())
-        M = pool.shape[0]
-        q = self.mix / M + (1.0 - self.mix) * h / h.sum()
-        return q
+        p = 0.5 * pred.clamp(-60.0, 60.0)  # log sqrt(E[g^2 | centre] / n1^2), relative
+        h = n1.abs() * torch.exp(p - p.max())
+        support = (n1 != 0.0).double()
+        n_sup = float(support.sum())
+        if n_sup == 0.0:  # every candidate contributes 0
+            return torch.full_like(h, 1.0 / pool.shape[0])
+        return self.mix * support / n_sup + (1.0 - self.mix) * h / h.sum()
 
     def estimate(self, pool, r12s, r13s, mu, n_samples, seed=0, uniform=False, bf16=True):
         """Mean over the pool of E_rot[f]: returns (estimate, per-sample values)."""

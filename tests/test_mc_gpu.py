@@ -202,6 +202,11 @@ def test_learned_proposal_is_unbiased_and_reduces_variance():
     assert losses[-1] < losses[0]
     pool = torch.as_tensor(np.random.default_rng(9).uniform(0, L, (400_000, 3)), device="cuda")
     K = 400_000
+    # centres with n1 = 0 contribute exactly 0: no mass there, mass everywhere else
+    q = lp.proposal(pool, 2.0, 4.0, 0.3)
+    _, n1 = lp.features(pool, 2.0, 4.0, 0.3, return_n1=True)
+    assert float(q[n1 == 0].abs().sum()) == 0.0 and bool((q[n1 != 0] > 0).all())
+    assert abs(float(q.sum()) - 1.0) < 1e-9
     est_u, vu = lp.estimate(pool, 2.0, 4.0, 0.3, K, seed=11, uniform=True)
     est_l, vl = lp.estimate(pool, 2.0, 4.0, 0.3, K, seed=12)
     var_u, var_l = float(vu.var()), float(vl.var())
