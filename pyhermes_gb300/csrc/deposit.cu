@@ -423,6 +423,77 @@ dep_accum_kernel(const DepRec* __restrict__ sorted, const unsigned* __restrict__
 
   const float scale_f = st->scale_f;
   const int Lm = g.L - 1;
+  // Split accumulation.  A 64-bit shared-memory atomic add costs about four
+  // 32-bit ones on this part, so when the tile's sums allow it each int64
+  // contribution q = hi * 2^sb + lo (0 <= lo < 2^sb, hi = q >> sb) goes into
+  // two 32-bit words per cell: LO += lo (unsigned) and HI += hi (two's
+  // complement).  With T records reaching the tile no cell gets more than T
+  // contributions, so LO is exact when T * (2^sb - 1) < 2^32, and HI's final
+  // value is exact (wrap-around addition is associative) when the true sum
+  // of the hi parts fits in 31 bits: |sum hi| <= T * (qmax / 2^sb + 1), with
+  // qmax = max|w| * max|phi|^3 * scale the largest |q|.  The cell total
+  // HI * 2^sb + LO is then the same int64 as the plain path's, bit for bit.
+  // Otherwise (dense tiles) sb = 0 and the tile uses int64 atomics.
+  int sb = 0;
+  {
+    const int clog = total > 1u ? 32 - __clz((int)(total - 1u)) : 0;  // ceil(log2 T)
+    const int cand = 32 - clog;
+    if (cand >= 8 && cand <= 31) {
+      const double pm = (double)__uint_as_float(st->phimax_bits);
+      const double qmax = (double)__uint_as_float(st->wmax_bits) * pm * pm * pm * st->scale_d;
+      // factor 2 margin for the float32 rounding of each product
+      if ((double)total * (2.0 * ldexp(qmax, -cand) + 1.0) < 2147483648.0) sb = cand;
+    }
+  }
+  if (sb > 0) {
+    unsigned* acc_lo = reinterpret_cast<unsigned*>(acc);
+    int* acc_hi = reinterpret_cast<int*>(acc) + ncell;
+    const long long lo_mask = (1LL << sb) - 1;
+    for (unsigned k = threadIdx.x; k < total; k += blockDim.x) {
+      int lo = 0, hi = nr - 1;  // largest r with r_pref[r] <= k
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (r_pref[mid] <= k) lo = mid; else hi = mid - 1;
+      }
+      const int r = lo;
+      const DepRec rec = sorted[r_start[r] + (k - r_pref[r])];
+      const int cx = rec.cell >> 20, cy = (rec.cell >> 10) & 1023, cz = rec.cell & 1023;
+      const int fx = rec.frac >> 20, fy = (rec.frac >> 10) & 1023, fz = rec.frac & 1023;
+      int lx[S], ly[S], lz[S];
+      float px[S], py[S], pz[S];
+#pragma unroll
+      for (int s = 0; s < S; ++s) {
+        lx[s] = (cx - s - x0) & Lm;
+        ly[s] = (cy - s - y0) & Lm;
+        lz[s] = (cz - s - z0) & Lm;
+        px[s] = rec.w * __ldg(&phif[fx + g.res * s]);
+        py[s] = __ldg(&phif[fy + g.res * s]);
+        pz[s] = __ldg(&phif[fz + g.res * s]);
+      }
+#pragma unroll
+      for (int a = 0; a < S; ++a) {
+        if (lx[a] >= g.tx) continue;
+#pragma unroll
+        for (int b = 0; b < S; ++b) {
+          if (ly[b] >= g.ty) continue;
+          const float pxy = px[a] * py[b];
+          const int row = (lx[a] << tyzl) + (ly[b] << tzl);
+#pragma unroll
+          for (int c = 0; c < S; ++c) {
+            if (lz[c] >= g.tz) continue;
+            const long long q = f32_to_ll_rn(pxy * pz[c] * scale_f);
+            const int cell = row + lz[c];
+            atomicAdd(&acc_lo[cell], (unsigned)(q & lo_mask));
+            const int qh = (int)(q >> sb);
+            if (qh != 0) atomicAdd(&acc_hi[cell], qh);
+          }
+        }
+      }
+      if (counts_out && r_home[r]) {
+        atomicAdd(&cnt[((cx - x0) << tyzl) + ((cy - y0) << tzl) + (cz - z0)], 1u);
+      }
+    }
+  } else
   for (unsigned k = threadIdx.x; k < total; k += blockDim.x) {
     int lo = 0, hi = nr - 1;  // largest r with r_pref[r] <= k
     while (lo < hi) {
@@ -472,8 +543,17 @@ dep_accum_kernel(const DepRec* __restrict__ sorted, const unsigned* __restrict__
   for (int i = 4 * threadIdx.x; i < ncell; i += 4 * blockDim.x) {
     const int lz_ = i & (g.tz - 1), ly_ = (i >> tzl) & (g.ty - 1), lx_ = i >> tyzl;
     const size_t gi = ((size_t)(x0 + lx_) * g.L + (y0 + ly_)) * g.L + (z0 + lz_);
-    const longlong2 a01 = *reinterpret_cast<const longlong2*>(acc + i);
-    const longlong2 a23 = *reinterpret_cast<const longlong2*>(acc + i + 2);
+    longlong2 a01, a23;
+    if (sb > 0) {  // cell total = HI * 2^sb + LO
+      const uint4 l4 = *reinterpret_cast<const uint4*>(reinterpret_cast<const unsigned*>(acc) + i);
+      const int4 h4 = *reinterpret_cast<const int4*>(reinterpret_cast<const int*>(acc) + ncell + i);
+      const long long m = 1LL << sb;
+      a01 = make_longlong2((long long)h4.x * m + l4.x, (long long)h4.y * m + l4.y);
+      a23 = make_longlong2((long long)h4.z * m + l4.z, (long long)h4.w * m + l4.w);
+    } else {
+      a01 = *reinterpret_cast<const longlong2*>(acc + i);
+      a23 = *reinterpret_cast<const longlong2*>(acc + i + 2);
+    }
     if (kF64Out) {
       reinterpret_cast<double2*>(out64 + gi)[0] = make_double2((double)a01.x * inv_d, (double)a01.y * inv_d);
       reinterpret_cast<double2*>(out64 + gi)[1] = make_double2((double)a23.x * inv_d, (double)a23.y * inv_d);

@@ -469,26 +469,75 @@ extern "C" int hermes_spectrum_multiply(void* spec, const float* k_real, const v
 // on z: the kernel is K(x, y, z) = scale * A(x, y) * B(z) with
 //   A = sum over the (x, y) images of P P f(k_perp R),  B = sum over the z
 //   images of P g(k_par H)   (cyl_image_sum).
-// A block takes kCylBins bins; B is tabulated for them in shared memory
-// (z in [0, L/2]).  A warp takes one (x, y) column at a time: it stages the
-// column's spectrum values in shared memory, each lane computes A for its
-// kCylBins/32 bins and then streams the column's modes, so per mode and bin
-// there is one table load and two FMAs, and the spectra are read once per
-// block group of bins.
+// So sum_k T(k) K_b(k) = sum_(x,y) A_b(x, y) * [sum_z T(x, y, z) B_b(z)]: per
+// column a [columns x z] by [z x bins] product, then a weighted sum.
+//
+// A depends on (x, y) only through the image set {x, L-x} x {y, L-y} and
+// p^2 + q^2, so A(x, y) = A(min(x, L-x), min(y, L-y)) = A(y, x).
+// cyl_perp_table_kernel evaluates it once per (x, y) in the triangle
+// 0 <= y <= x <= L/2 and bin (1/8 of the plane), into a table that the
+// column kernel reads.
+//
+// Column kernel: a block takes kCylBins bins (two per lane); B is tabulated
+// for them in shared memory as [z][bin].  A warp takes CW consecutive
+// columns (their modes are contiguous), stages the weighted products
+// T = w_z Re(u conj v) in chunks of kCylZ z-planes as [z][pair][column], and
+// per z reads CW columns' T (broadcast, 128-bit) and its two bins' B (64-bit)
+// for 2 x CW FMAs per pair: a register tile instead of one shared-memory load
+// per FMA.  The spectra are read once per bin group; the groups run side by
+// side, so the second and later reads mostly hit L2.
 constexpr int kCylBins = 64;
-constexpr int kCylPerLane = kCylBins / 32;
+constexpr int kCylZ = 64;
+
+template <int NP>
+struct CylCols {
+  static constexpr int value = NP == 1 ? 8 : 4;  // columns per warp task
+};
+
+__global__ void cyl_perp_table_kernel(const WinDev* __restrict__ wins, int n_bins, int nbp,
+                                      const double* __restrict__ pd, int np, int L, int bw,
+                                      float* __restrict__ atab) {
+  extern __shared__ float Pt[];
+  for (int i = threadIdx.x; i < np; i += blockDim.x) Pt[i] = (float)pd[i];
+  __syncthreads();
+  const int H = L / 2 + 1;
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (long long)H * H * nbp) return;
+  const int b = (int)(i % nbp);
+  const long long cell = i / nbp;
+  const int x = (int)(cell / H), y = (int)(cell - (long long)x * H);
+  if (y > x) return;
+  float av = 0.f;
+  if (b < n_bins) {
+    const WinDev& w = wins[b];
+    const int sgn = w.mode == HERMES_KMODE_OCTANT ? 1 : -1;
+    const int n_img = 4 * bw * bw;
+    for (int t = 0; t < n_img; ++t) {
+      const int pair = t >> 2, sp = t & 1, sq = (t >> 1) & 1;
+      const int ii = pair / bw, jj = pair - ii * bw;
+      const int pu = sp ? ii * L + (L - x) : ii * L + x;
+      const int qu = sq ? jj * L + (L - y) : jj * L + y;
+      av = fmaf(Pt[pu] * Pt[qu], cyl_perp(w, sp ? sgn * pu : pu, sq ? sgn * qu : qu), av);
+    }
+  }
+  atab[((size_t)x * H + y) * nbp + b] = av;
+  atab[((size_t)y * H + x) * nbp + b] = av;
+}
 
 template <int NP>
 __global__ void __launch_bounds__(kPPThreads, 2)
 pair_products_cylz_kernel(PPArgs a, const WinDev* __restrict__ wins, const double* __restrict__ pd,
-                          double* __restrict__ partial, double* __restrict__ k0) {
+                          const float* __restrict__ atab, int nbp, double* __restrict__ partial,
+                          double* __restrict__ k0) {
   constexpr int kWarps = kPPThreads / 32;
+  constexpr int CW = CylCols<NP>::value;
+  constexpr int TZ = CW * NP;  // floats per z-plane of a warp's staged chunk
   extern __shared__ __align__(16) unsigned char cyl_sm[];
   const int L = a.L, H = L / 2 + 1;
   float* P = reinterpret_cast<float*>(cyl_sm);
-  float* B = P + ((a.np + 3) & ~3);                          // [kCylBins][H]
-  float* T = B + (size_t)kCylBins * H;                        // [kWarps][NP][H] column products
-  double* red = reinterpret_cast<double*>(T + (size_t)kWarps * NP * H + 2);  // [kWarps][kCylBins][NP]
+  float* B = P + ((a.np + 3) & ~3);                                  // [H][kCylBins]
+  float* T = B + (size_t)H * kCylBins;                               // [kWarps][kCylZ][NP][CW]
+  double* red = reinterpret_cast<double*>(T + (size_t)kWarps * kCylZ * TZ);  // [kWarps][kCylBins][NP]
   for (int i = threadIdx.x; i < a.np; i += blockDim.x) P[i] = (float)pd[i];
   const int b0 = blockIdx.y * kCylBins;
   const int nb = min(kCylBins, a.n_bins - b0);
@@ -496,7 +545,7 @@ pair_products_cylz_kernel(PPArgs a, const WinDev* __restrict__ wins, const doubl
   if (blockIdx.x == 0 && threadIdx.x < nb) k0[b0 + threadIdx.x] = (double)kernel_value(wins[b0 + threadIdx.x], 0, 0, 0, L, P, a.bw).x;
   const int sgn = wins[b0].mode == HERMES_KMODE_OCTANT ? 1 : -1;
   for (int i = threadIdx.x; i < kCylBins * H; i += blockDim.x) {
-    const int b = i / H, z = i - b * H;
+    const int z = i / kCylBins, b = i - z * kCylBins;
     float v = 0.f;
     if (b < nb) {
       const WinDev& w = wins[b0 + b];
@@ -511,80 +560,93 @@ pair_products_cylz_kernel(PPArgs a, const WinDev* __restrict__ wins, const doubl
   }
   __syncthreads();
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  float* Tw = T + (size_t)wid * NP * H;
-  double acc[kCylPerLane][NP];
-  int zk[kCylPerLane];
+  float* Tw = T + (size_t)wid * kCylZ * TZ;
+  double acc[2][NP];
+  int zk[2];
 #pragma unroll
-  for (int j = 0; j < kCylPerLane; ++j) {
-    const int b = lane + 32 * j;
+  for (int j = 0; j < 2; ++j) {
+    const int b = 2 * lane + j;
     zk[j] = b < nb ? wins[b0 + b].zero_k0 : 0;
 #pragma unroll
     for (int p = 0; p < NP; ++p) acc[j][p] = 0.0;
   }
-  const int n_img = 4 * a.bw * a.bw;
-  for (long long col = (long long)blockIdx.x * kWarps + wid; col < (long long)L * L;
-       col += (long long)gridDim.x * kWarps) {
-    const int x = (int)(col / L), y = (int)(col % L);
-    const long long mbase = col * H;
-    __syncwarp();
-    for (int z = lane; z < H; z += 32) {  // weighted Re(u conj v) of the column's modes
-      const long long m = mbase + z;
-      const float wgt = (z == 0 || z == L / 2) ? 1.f : 2.f;
+  const long long ncol = (long long)L * L;  // a multiple of CW
+  for (long long col0 = ((long long)blockIdx.x * kWarps + wid) * CW; col0 < ncol;
+       col0 += (long long)gridDim.x * kWarps * CW) {
+    float fac[CW][2][NP];
 #pragma unroll
-      for (int p = 0; p < NP; ++p) {
-        const float2 u = a.si[p][m], v = a.sj[p][m];
-        Tw[p * H + z] = (a.exclude_k0 && m == 0) ? 0.f : wgt * (u.x * v.x + u.y * v.y);
-      }
-    }
-    float A[kCylPerLane];
+    for (int c = 0; c < CW; ++c)
 #pragma unroll
-    for (int j = 0; j < kCylPerLane; ++j) {
-      const int b = lane + 32 * j;
-      float av = 0.f;
-      if (b < nb) {
-        const WinDev& w = wins[b0 + b];
-        for (int t = 0; t < n_img; ++t) {
-          const int pair = t >> 2, sp = t & 1, sq = (t >> 1) & 1;
-          const int ii = pair / a.bw, jj = pair - ii * a.bw;
-          const int pu = sp ? ii * L + (L - x) : ii * L + x;
-          const int qu = sq ? jj * L + (L - y) : jj * L + y;
-          av = fmaf(P[pu] * P[qu], cyl_perp(w, sp ? sgn * pu : pu, sq ? sgn * qu : qu), av);
+      for (int j = 0; j < 2; ++j)
+#pragma unroll
+        for (int p = 0; p < NP; ++p) fac[c][j][p] = 0.f;
+    float t00[NP];
+    for (int zc = 0; zc < H; zc += kCylZ) {
+      const int zn = min(kCylZ, H - zc);
+      __syncwarp();
+#pragma unroll
+      for (int c = 0; c < CW; ++c) {
+        const long long mb = (col0 + c) * H + zc;
+        for (int i = lane; i < zn; i += 32) {
+          const int z = zc + i;
+          const float wgt = (z == 0 || z == L / 2) ? 1.f : 2.f;
+#pragma unroll
+          for (int p = 0; p < NP; ++p) {
+            const float2 u = a.si[p][mb + i], v = a.sj[p][mb + i];
+            Tw[(i * NP + p) * CW + c] = (a.exclude_k0 && mb + i == 0) ? 0.f : wgt * (u.x * v.x + u.y * v.y);
+          }
         }
       }
-      A[j] = av;
-    }
-    __syncwarp();
-    float fac[kCylPerLane][NP];
+      __syncwarp();
+      if (zc == 0) {
 #pragma unroll
-    for (int j = 0; j < kCylPerLane; ++j)
+        for (int p = 0; p < NP; ++p) t00[p] = Tw[p * CW];  // column col0 at z = 0
+      }
+      const float* Bz = B + (size_t)zc * kCylBins + 2 * lane;
+#pragma unroll 4
+      for (int z = 0; z < zn; ++z) {
+        const float2 bz = *reinterpret_cast<const float2*>(Bz + (size_t)z * kCylBins);
 #pragma unroll
-      for (int p = 0; p < NP; ++p) fac[j][p] = 0.f;
-    for (int z = 0; z < H; ++z) {
-      float tr[NP];
+        for (int p = 0; p < NP; ++p) {
+          float tv[CW];
 #pragma unroll
-      for (int p = 0; p < NP; ++p) tr[p] = Tw[p * H + z];
+          for (int c4 = 0; c4 < CW; c4 += 4) {
+            const float4 t4 = *reinterpret_cast<const float4*>(Tw + (z * NP + p) * CW + c4);
+            tv[c4] = t4.x;
+            tv[c4 + 1] = t4.y;
+            tv[c4 + 2] = t4.z;
+            tv[c4 + 3] = t4.w;
+          }
 #pragma unroll
-      for (int j = 0; j < kCylPerLane; ++j) {
-        const float bz = B[(lane + 32 * j) * H + z];
-#pragma unroll
-        for (int p = 0; p < NP; ++p) fac[j][p] = fmaf(tr[p], bz, fac[j][p]);
+          for (int c = 0; c < CW; ++c) {
+            fac[c][0][p] = fmaf(tv[c], bz.x, fac[c][0][p]);
+            fac[c][1][p] = fmaf(tv[c], bz.y, fac[c][1][p]);
+          }
+        }
       }
     }
-    const bool origin = col == 0;
 #pragma unroll
-    for (int j = 0; j < kCylPerLane; ++j)
+    for (int c = 0; c < CW; ++c) {
+      const long long col = col0 + c;
+      const int x = (int)(col / L), y = (int)(col - (long long)x * L);
+      const int xq = min(x, L - x), yq = min(y, L - y);
+      const float2 av = *reinterpret_cast<const float2*>(atab + ((size_t)xq * H + yq) * nbp + b0 + 2 * lane);
+      const float aj[2] = {av.x, av.y};
 #pragma unroll
-      for (int p = 0; p < NP; ++p) {
-        float f = fac[j][p];
-        if (origin && zk[j]) f -= Tw[p * H] * B[(lane + 32 * j) * H];  // K(0,0,0) forced to 0
-        acc[j][p] += (double)A[j] * (double)f;
-      }
+      for (int j = 0; j < 2; ++j)
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+          float f = fac[c][j][p];
+          if (col == 0 && zk[j]) f -= t00[p] * B[2 * lane + j];  // K(0,0,0) forced to 0
+          acc[j][p] += (double)aj[j] * (double)f;
+        }
+    }
   }
   // block reduction over warps (fixed order -> deterministic)
 #pragma unroll
-  for (int j = 0; j < kCylPerLane; ++j)
+  for (int j = 0; j < 2; ++j)
 #pragma unroll
-    for (int p = 0; p < NP; ++p) red[((size_t)wid * kCylBins + lane + 32 * j) * NP + p] = acc[j][p];
+    for (int p = 0; p < NP; ++p) red[((size_t)wid * kCylBins + 2 * lane + j) * NP + p] = acc[j][p];
   __syncthreads();
   for (int i = threadIdx.x; i < nb * NP; i += blockDim.x) {
     double v = 0.0;
@@ -596,9 +658,14 @@ pair_products_cylz_kernel(PPArgs a, const WinDev* __restrict__ wins, const doubl
 
 static size_t cylz_smem(int np, int L, int n_pairs) {
   const int H = L / 2 + 1;
-  return sizeof(float) * ((((size_t)np + 3) & ~(size_t)3) + (size_t)kCylBins * H + (size_t)(kPPThreads / 32) * n_pairs * H + 2) +
-         sizeof(double) * (size_t)(kPPThreads / 32) * kCylBins * n_pairs + 16;
+  const int cw = n_pairs == 1 ? 8 : 4;
+  return sizeof(float) * ((((size_t)np + 3) & ~(size_t)3) + (size_t)H * kCylBins +
+                          (size_t)(kPPThreads / 32) * kCylZ * cw * n_pairs) +
+         sizeof(double) * (size_t)(kPPThreads / 32) * kCylBins * n_pairs;
 }
+
+// Bins padded to whole groups of kCylBins (the A table's row stride).
+static int cylz_nbp(int n_bins) { return (n_bins + kCylBins - 1) / kCylBins * kCylBins; }
 
 // True when every bin is a cylindrical window with the line of sight on z
 // and all bins use the same image mode (the column kernel's precondition).
@@ -623,11 +690,13 @@ extern "C" int hermes_pair_products_workspace_size(int J, int n_bins, int n_pair
   if (J < 2 || J > 10) return fail(HERMES_ERR_INVALID, "J=%d outside [2,10]", J);
   if (n_bins < 1 || n_pairs < 1 || n_pairs > kMaxPairs)
     return fail(HERMES_ERR_INVALID, "pair_products: n_bins >= 1 and 1 <= n_pairs <= %d", kMaxPairs);
+  const size_t H = ((size_t)1 << J) / 2 + 1;
   Carver c(nullptr, 0);
   c.take<WinDev>(n_bins);
   c.take<double>((size_t)pp_mode_blocks(J) * n_bins * n_pairs);
   c.take<double>((size_t)n_bins * n_pairs);
   c.take<double>((size_t)n_bins);
+  c.take<float>(H * H * (size_t)cylz_nbp(n_bins));  // A table of cylindrical bins
   *bytes = c.used;
   return HERMES_OK;
 }
@@ -673,39 +742,42 @@ extern "C" int hermes_pair_products(const void* const* spectra, int n_spec, cons
   double* partial = c.take<double>((size_t)nblk * n_bins * n_pairs);
   double* dout = c.take<double>((size_t)n_bins * n_pairs);
   double* dk0 = c.take<double>((size_t)n_bins);
+  const int H = L / 2 + 1;
+  const int nbp = cylz_nbp(n_bins);
+  float* atab = c.take<float>((size_t)H * H * nbp);
   cudaStream_t s = as_stream(stream);
   HERMES_CUDA_TRY(cudaMemcpyAsync(dwin, hw.data(), sizeof(WinDev) * n_bins, cudaMemcpyHostToDevice, s));
   if (all_cyl_z(hw) && n_pairs <= 4 && cylz_smem(a.np, L, n_pairs) <= 200 * 1024) {
-    // about 2 resident blocks per SM over all bin groups, so each block's
-    // table of B(z) is reused over many columns
-    int dev = 0, nsm = 148;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    const int groups = (n_bins + kCylBins - 1) / kCylBins;
-    long long cblk = (2LL * nsm + groups - 1) / groups;
-    const long long max_cols = (long long)L * L / (kPPThreads / 32);
-    if (cblk > max_cols) cblk = max_cols;
+    const long long tab_threads = (long long)H * H * nbp;
+    cyl_perp_table_kernel<<<(unsigned)((tab_threads + 255) / 256), 256, a.np * sizeof(float), s>>>(
+        dwin, n_bins, nbp, phi_power, a.np, L, bandwidth, atab);
+    HERMES_LAUNCH_CHECK("cyl_perp_table_kernel");
+    const size_t csm = cylz_smem(a.np, L, n_pairs);
+    const void* fn = n_pairs == 1 ? (const void*)pair_products_cylz_kernel<1>
+                   : n_pairs == 2 ? (const void*)pair_products_cylz_kernel<2>
+                   : n_pairs == 3 ? (const void*)pair_products_cylz_kernel<3>
+                                  : (const void*)pair_products_cylz_kernel<4>;
+    HERMES_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm));
+    // every block resident at once over all bin groups (whole waves), so
+    // each block's table of B(z) is reused over many columns and the groups
+    // read the same columns at about the same time
+    int dev = 0, nsm = 148, per_sm = 1;
+    HERMES_CUDA_TRY(cudaGetDevice(&dev));
+    HERMES_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    HERMES_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kPPThreads, csm));
+    if (per_sm < 1) per_sm = 1;
+    const int groups = nbp / kCylBins;
+    long long cblk = (long long)per_sm * nsm / groups;
+    const long long max_tasks = (long long)L * L / ((kPPThreads / 32) * (n_pairs == 1 ? 8 : 4));
+    if (cblk > max_tasks) cblk = max_tasks;
     if (cblk > nblk) cblk = nblk;  // partial sums sized for nblk blocks
     if (cblk < 1) cblk = 1;
     dim3 cgrid((unsigned)cblk, (unsigned)groups);
-    const size_t csm = cylz_smem(a.np, L, n_pairs);
     switch (n_pairs) {
-      case 1:
-        HERMES_CUDA_TRY(cudaFuncSetAttribute(pair_products_cylz_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm));
-        pair_products_cylz_kernel<1><<<cgrid, kPPThreads, csm, s>>>(a, dwin, phi_power, partial, dk0);
-        break;
-      case 2:
-        HERMES_CUDA_TRY(cudaFuncSetAttribute(pair_products_cylz_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm));
-        pair_products_cylz_kernel<2><<<cgrid, kPPThreads, csm, s>>>(a, dwin, phi_power, partial, dk0);
-        break;
-      case 3:
-        HERMES_CUDA_TRY(cudaFuncSetAttribute(pair_products_cylz_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm));
-        pair_products_cylz_kernel<3><<<cgrid, kPPThreads, csm, s>>>(a, dwin, phi_power, partial, dk0);
-        break;
-      default:
-        HERMES_CUDA_TRY(cudaFuncSetAttribute(pair_products_cylz_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm));
-        pair_products_cylz_kernel<4><<<cgrid, kPPThreads, csm, s>>>(a, dwin, phi_power, partial, dk0);
-        break;
+      case 1: pair_products_cylz_kernel<1><<<cgrid, kPPThreads, csm, s>>>(a, dwin, phi_power, atab, nbp, partial, dk0); break;
+      case 2: pair_products_cylz_kernel<2><<<cgrid, kPPThreads, csm, s>>>(a, dwin, phi_power, atab, nbp, partial, dk0); break;
+      case 3: pair_products_cylz_kernel<3><<<cgrid, kPPThreads, csm, s>>>(a, dwin, phi_power, atab, nbp, partial, dk0); break;
+      default: pair_products_cylz_kernel<4><<<cgrid, kPPThreads, csm, s>>>(a, dwin, phi_power, atab, nbp, partial, dk0); break;
     }
     HERMES_LAUNCH_CHECK("pair_products_cylz_kernel");
     const double cscale = 1.0 / ((double)L * L * L * (double)L * L * L);
