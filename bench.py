@@ -578,8 +578,9 @@ def mc_bench(dev, phi_np, steps):
 
 
 def run_case(args):
-    """Single-part workloads for profiling (`--case contract|fields|deposit|
-    mc|c2|c4`): one JSON line with CUDA-event times; not the headline metric.
+    """Single-part workloads for profiling (`--case step|contract|fields|
+    deposit|mc|c2|c4`): one JSON line with CUDA-event times; not the headline
+    line (`step` is the headline step alone, for launch lists).
     `fields` is one radial multipole fields call (l=4, m=2, the 15 headline
     radii) on the deposited lognormal field at level --J."""
     import torch
@@ -603,6 +604,29 @@ def run_case(args):
     if args.case == "mc":
         print(json.dumps({"case": "mc", **mc_bench(dev, phi_np, args.steps)}))
         return 0
+    if args.case == "step":
+        # the headline step alone (deposits, fields, contractions, mixing solve), W + K times
+        dpos_np, dw_np, rpos_np, rw_np = make_catalogues(0, "cpu")
+        t = [torch.as_tensor(a, device=dev) for a in (dpos_np, dw_np, rpos_np, rw_np)]
+        wsd, wsr = kernels.DepositWorkspace(dev), kernels.DepositWorkspace(dev)
+
+        def step():
+            task = mp.Corr_3PCF_Multipole(multipole_task_params(deposit_field(t[0], t[1], MP_J, phi, wsd),
+                                                                deposit_field(t[2], t[3], MP_J, phi, wsr)),
+                                          device=dev)
+            return task.run(save_result=False)
+
+        for _ in range(args.warmup):
+            step()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        for a, b in ev:
+            a.record(stream)
+            step()
+            b.record(stream)
+        torch.cuda.synchronize(dev)
+        print(json.dumps({"case": "step", "s_per_catalogue": sum(a.elapsed_time(b) for a, b in ev) / len(ev) / 1e3,
+                          "steps": args.steps, "warmup": args.warmup}))
+        return 0
     if args.case == "deposit":
         flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
         out = deposit_bench(dev, _lib.load(), kernels, phi, flush, args.steps)
@@ -619,35 +643,41 @@ def run_case(args):
     grid = [r * L / BOX for r in MP_RADII]
     if args.case == "fields":
         spec = rfft_field(eps)
-        out = torch.empty((L ** 3, mp.BIN_STRIDE), dtype=torch.complex64, device=dev)
-        wsf = mp._workspace(mp._ws_bytes(J, len(grid)), dev)
-        for _ in range(max(args.warmup, 1)):
-            mp.multipole_fields(spec, J, 4, 2, grid, P, out=out, ws=wsf)
-        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-        for a, b in ev:
-            a.record(stream)
-            mp.multipole_fields(spec, J, 4, 2, grid, P, out=out, ws=wsf)
-            b.record(stream)
-        torch.cuda.synchronize(dev)
-        ms = sum(a.elapsed_time(b) for a, b in ev) / len(ev)
-        print(json.dumps({"case": "fields", "J": J, "bins": len(grid), "l": 4, "m": 2, "ms_per_call": ms,
+        res = {}
+        for bm in (True, False):
+            out = mp._fields_out(J, len(grid), bm, dev)
+            wsf = mp._workspace(mp.fields_ws_bytes(J, len(grid), bm), dev)
+            for _ in range(max(args.warmup, 1)):
+                mp.multipole_fields(spec, J, 4, 2, grid, P, out=out, ws=wsf, bin_major=bm)
+            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                  for _ in range(args.steps)]
+            for a, b in ev:
+                a.record(stream)
+                mp.multipole_fields(spec, J, 4, 2, grid, P, out=out, ws=wsf, bin_major=bm)
+                b.record(stream)
+            torch.cuda.synchronize(dev)
+            res["bin_major" if bm else "interleaved"] = sum(a.elapsed_time(b) for a, b in ev) / len(ev)
+            del out
+        print(json.dumps({"case": "fields", "J": J, "bins": len(grid), "l": 4, "m": 2, "ms_per_call": res,
                           "prepass_bytes_written": len(grid) * L ** 3 * 8}))
         return 0
-    f = mp.multipole_fields(rfield := rfft_field(eps), J, 2, 1, grid, P)
+    rfield = rfft_field(eps)
     gc = (ctypes.c_double * 9)(*np.asarray(gam, dtype=np.float64).ravel())
     dout = torch.zeros((16, 16, 2), dtype=torch.float64, device=dev)
     res = {}
-    for engine in mp.ENGINES:
+    for engine, bm in (("tensor", True), ("simt", False)):
+        f = mp.multipole_fields(rfield, J, 2, 1, grid, P, bin_major=bm)
         for _ in range(max(args.warmup, 1)):
-            mp.multipole_contract_async(eps, f, len(grid), gc, J, dout, conj_sign=-1, engine=engine)
+            mp.multipole_contract_async(eps, f, len(grid), gc, J, dout, conj_sign=-1, engine=engine, bin_major=bm)
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
         for a, b in ev:
             a.record(stream)
-            mp.multipole_contract_async(eps, f, len(grid), gc, J, dout, conj_sign=-1, engine=engine)
+            mp.multipole_contract_async(eps, f, len(grid), gc, J, dout, conj_sign=-1, engine=engine, bin_major=bm)
             b.record(stream)
         torch.cuda.synchronize(dev)
         S = dout[:len(grid), :len(grid)].cpu().numpy()
         res[engine] = {"ms_per_launch": sum(a.elapsed_time(b) for a, b in ev) / len(ev), "S": S[..., 0] + 1j * S[..., 1]}
+        del f
     del rfield
     diff = float(np.abs(res["tensor"]["S"] - res["simt"]["S"]).max() / np.abs(res["simt"]["S"]).max())
     print(json.dumps({"case": "contract", "J": J, "bins": len(grid), "l": 2, "m": 1,
@@ -758,9 +788,9 @@ def run_gb300(args, ws, rank, local):
     zeta = np.asarray(res.zeta_l)
 
     # our kernels per step: 2 deposits x 7; per product per (l, m): fields (power, j_l table,
-    # interior and edge prepass, interleave; the inverse FFT is cuFFT) + contract
-    # (tensor-core contraction, reduce); the mixing solve
-    kernel_launches = args.steps * (14 + 2 * N_LM * 7 + 1)
+    # interior and edge prepass; the inverse FFT is cuFFT, its bin-major output is read as is) +
+    # contract (tensor-core contraction, reduce); the mixing solve
+    kernel_launches = args.steps * (14 + 2 * N_LM * 6 + 1)
 
     # end to end: catalogues in pinned host memory, copies inside the timed region
     h = [torch.as_tensor(a).pin_memory() for a in (dpos_np, dw_np, rpos_np, rw_np)]
@@ -777,8 +807,9 @@ def run_gb300(args, ws, rank, local):
     torch.cuda.synchronize(dev)
     e2e_value = sum(a.elapsed_time(b) for a, b in e2e_ev) / 1e3 / (args.steps * ws)
 
-    # dominant kernel: the batched contraction of one (l, m) over 15x15 radii, both engines;
-    # the fields pass of the same (l, m)
+    # dominant kernel: the batched contraction of one (l, m) over 15x15 radii, the tensor engine on
+    # the bin-major fields the headline path uses and the FP32 engine on the interleaved layout; the
+    # fields pass of the same (l, m) in both layouts
     dfield = deposit_field(dpos, dw, MP_J, phi, wsd)
     rfield = deposit_field(rpos, rw, MP_J, phi, wsr)
     delta = (dfield.epsilon_device.double() - rfield.epsilon_device.double()).float()
@@ -786,32 +817,32 @@ def run_gb300(args, ws, rank, local):
     eng = mp.MultipoleEngine(delta, delta, delta, phi_np, MP_J, BOX)
     L = 1 << MP_J
     grid = [r * L / BOX for r in MP_RADII]
-    f2 = mp.multipole_fields(eng.spec2, MP_J, 4, 2, grid, eng.P)
     gc = (ctypes.c_double * 9)(*np.asarray(eng.gamma, dtype=np.float64).ravel())
     dout = torch.zeros((16, 16, 2), dtype=torch.float64, device=dev)
-    t_con = {}
-    for engine in mp.ENGINES:
+    t_con, t_fld = {}, {}
+    for engine, bm in (("tensor", True), ("simt", False)):
+        f2 = mp.multipole_fields(eng.spec2, MP_J, 4, 2, grid, eng.P, bin_major=bm)
         for _ in range(2):
-            mp.multipole_contract_async(eng.eps1, f2, 15, gc, MP_J, dout, conj_sign=1, engine=engine)
+            mp.multipole_contract_async(eng.eps1, f2, 15, gc, MP_J, dout, conj_sign=1, engine=engine, bin_major=bm)
         cev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(5)]
         for a, b in cev:
             a.record(stream)
-            mp.multipole_contract_async(eng.eps1, f2, 15, gc, MP_J, dout, conj_sign=1, engine=engine)
+            mp.multipole_contract_async(eng.eps1, f2, 15, gc, MP_J, dout, conj_sign=1, engine=engine, bin_major=bm)
             b.record(stream)
         torch.cuda.synchronize(dev)
         t_con[engine] = sum(a.elapsed_time(b) for a, b in cev) / len(cev) / 1e3
-    fev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(3)]
-    for a, b in fev:
-        a.record(stream)
-        mp.multipole_fields(eng.spec2, MP_J, 4, 2, grid, eng.P, out=f2)
-        b.record(stream)
-    torch.cuda.synchronize(dev)
-    t_fld = sum(a.elapsed_time(b) for a, b in fev) / len(fev) / 1e3
-    del f2
+        fev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(3)]
+        for a, b in fev:
+            a.record(stream)
+            mp.multipole_fields(eng.spec2, MP_J, 4, 2, grid, eng.P, out=f2, bin_major=bm)
+            b.record(stream)
+        torch.cuda.synchronize(dev)
+        t_fld["bin_major" if bm else "interleaved"] = sum(a.elapsed_time(b) for a, b in fev) / len(fev) / 1e3
+        del f2
     hbm, bf16, kind = load_peaks()
     flops = 8.0 * 15 * 15 * 27 * L ** 3
     achieved = flops / t_con["tensor"] / 1e12
-    fld_bytes = L * L * (L // 2 + 1) * 8 + L ** 3 * mp.BIN_STRIDE * 8
+    fld_bytes = L * L * (L // 2 + 1) * 8 + L ** 3 * 15 * 8
 
     # plain per-sample reference-form path: one full (r12, r13) sample over every (l, m), l <= 10
     torch.cuda.synchronize(dev)
@@ -848,7 +879,7 @@ def run_gb300(args, ws, rank, local):
         "data": "synthetic (seeded lognormal data + uniform randoms; the reference's Quijote catalogue is absent)",
         "config": {"workload": WORKLOAD, "J": MP_J, "lmax": MP_LMAX, "radii": len(MP_RADII),
                    "samples": N_SAMPLES, "n_data": MP_NDATA, "n_random": MP_NRAND,
-                   "l2": "per-(l,m) working set (17 GB fields) far above L2",
+                   "l2": "per-(l,m) working set (16 GB fields) far above L2",
                    "parallelism": f"replicas x{ws}"},
         "accuracy_vs_fp64": acc,
         "max_rel_err_vs_fp64": None if acc is None else acc["max_rel_err_zeta_l"],
@@ -864,12 +895,14 @@ def run_gb300(args, ws, rank, local):
                                      "(BF16x3 operands, FP32 accumulate in TMEM)"),
                      "algorithmic_flops": flops, "ms_per_launch": t_con["tensor"] * 1e3,
                      "ms_per_launch_simt_engine": t_con["simt"] * 1e3},
-        "fields_roofline": {"kernels": "mp_jl_table + mp_prepass_quad/edge + cuFFT C2C x15 + mp_interleave",
-                            "bound": "hbm", "ms_per_lm": t_fld * 1e3, "algorithmic_bytes": fld_bytes,
-                            "achieved": fld_bytes / t_fld / 1e9, "peak": hbm, "peak_kind": kind, "unit": "GB/s",
-                            "frac": fld_bytes / t_fld / 1e9 / hbm,
-                            "note": "minimum bytes: one read of the half spectrum + one write of the 15 fields in "
-                                    "the contraction's [cell][16] layout"},
+        "fields_roofline": {"kernels": "mp_jl_table + mp_prepass_quad/edge + cuFFT C2C x15 (bin-major output, "
+                                       "read as is by the tensor-core contraction)",
+                            "bound": "hbm", "ms_per_lm": t_fld["bin_major"] * 1e3, "algorithmic_bytes": fld_bytes,
+                            "achieved": fld_bytes / t_fld["bin_major"] / 1e9, "peak": hbm, "peak_kind": kind,
+                            "unit": "GB/s", "frac": fld_bytes / t_fld["bin_major"] / 1e9 / hbm,
+                            "ms_per_lm_interleaved": t_fld["interleaved"] * 1e3,
+                            "note": "minimum bytes: one read of the half spectrum + one write of the 15 fields; "
+                                    "the interleaved layout (FP32 engine) adds the mp_interleave pass"},
         "deposit": dep,
         "mc3pcf": mc,
         "c2_window_2pcf": c2,
@@ -894,7 +927,8 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--case", default="headline", choices=["headline", "contract", "fields", "deposit", "mc", "c2", "c4"],
+    ap.add_argument("--case", default="headline", choices=["headline", "step", "contract", "fields", "deposit", "mc", "c2",
+                                                           "c4"],
                     help="headline = the benchmark line; contract/fields/deposit/mc/c2/c4 = one part, for profiling")
     ap.add_argument("--J", type=int, default=7, help="grid level of --case contract and --case fields")
     args = ap.parse_args()

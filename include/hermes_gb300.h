@@ -272,6 +272,33 @@ int hermes_multipole_contract_simt_async(const float* eps1, const void* fields2,
                                          void* stream);
 int hermes_multipole_contract_status(const void* workspace, size_t workspace_bytes, int J, int* status,
                                      void* stream);
+
+/* Bin-major layout (same reference functions as the calls above).
+ * hermes_multipole_fields_bm / _window_bm / _table_bm: the fields of
+ * hermes_multipole_fields / _window / _table written as complex64
+ * [nb][L^3], bin b at fields_out + b * L^3, the layout the batched inverse
+ * FFT produces: no interleave pass, and the workspace is
+ * hermes_multipole_workspace_size(J, 1) (no bin-major staging copy).
+ * hermes_multipole_contract_bm_async: hermes_multipole_contract_async on
+ * fields in that layout (tensor-core engine; a2 planes by a 4-D TMA map
+ * over (z, y, x, bin), a3 planes staged per bin); workspace as above.
+ * The sums are the same operations on the same values as the interleaved
+ * path, so S is bit-identical to it. */
+int hermes_multipole_fields_bm(const void* half_spec, int J, int l, int m, const double* radii, int nb,
+                               const double* phi_power, void* fields_out, void* workspace,
+                               size_t workspace_bytes, void* stream);
+int hermes_multipole_fields_window_bm(const void* half_spec, int J, int l, int m, const hermes_window_t* bins,
+                                      int nb, const double* phi_power, void* fields_out, void* workspace,
+                                      size_t workspace_bytes, void* stream);
+int hermes_multipole_fields_table_bm(const void* half_spec, int J, int l, int m, const double* tables,
+                                     const int64_t* offsets, const int32_t* sizes, const double* k_max,
+                                     double grid_to_physical, int nb, const double* phi_power, void* fields_out,
+                                     void* workspace, size_t workspace_bytes, void* stream);
+int hermes_multipole_contract_bm_async(const float* eps1, const void* fields2, int nb2,
+                                       const void* fields3, int nb3, int conj_sign,
+                                       const double* gamma, int J, int chunk_x, int ctas_per_sm,
+                                       double* dev_out, void* workspace, size_t workspace_bytes,
+                                       void* stream);
 int hermes_multipole_contract_plain(const float* eps1, const void* a2, const void* a3,
                                     const double* gamma, int J, double* out,
                                     void* workspace, size_t workspace_bytes, void* stream);

@@ -326,6 +326,28 @@ __device__ __forceinline__ float ll_to_f32(long long a) {
   return fmaf(hi, 4294967296.0f, lo);
 }
 
+// The (hi, lo) words of q = f32_to_ll_rn(v) split at bit sb, for
+// |q| < 2^(31 + sb), in 32-bit arithmetic: with a = |v|, qa = floor(a) +
+// (a - floor(a) >= 1/2) is the same round-half-away magnitude (floor(a) and
+// a - floor(a) are exact), hi_a = qa >> sb and lo_a = qa - hi_a 2^sb are
+// exact in float32 (qa has at most 24 significant bits), and a negative q
+// takes hi = -hi_a - (lo_a != 0), lo = 2^sb - lo_a (two's complement).
+__device__ __forceinline__ void split_q(float v, float two_sb, float inv_two_sb, unsigned lo_one, int& hi,
+                                        unsigned& lo) {
+  const float a = fabsf(v);
+  const float fl = floorf(a);
+  const float qa = (a - fl >= 0.5f) ? fl + 1.0f : fl;
+  const int ha = __float2int_rz(qa * inv_two_sb);
+  const unsigned la = __float2uint_rz(fmaf(-(float)ha, two_sb, qa));
+  if (v < 0.f) {
+    hi = -ha - (la != 0u ? 1 : 0);
+    lo = la != 0u ? lo_one - la : 0u;
+  } else {
+    hi = ha;
+    lo = la;
+  }
+}
+
 template <int S, bool kF64Out>
 __global__ void __launch_bounds__(kAccThreads)
 dep_accum_kernel(const DepRec* __restrict__ sorted, const unsigned* __restrict__ offsets,
@@ -433,7 +455,9 @@ dep_accum_kernel(const DepRec* __restrict__ sorted, const unsigned* __restrict__
   // of the hi parts fits in 31 bits: |sum hi| <= T * (qmax / 2^sb + 1), with
   // qmax = max|w| * max|phi|^3 * scale the largest |q|.  The cell total
   // HI * 2^sb + LO is then the same int64 as the plain path's, bit for bit.
-  // Otherwise (dense tiles) sb = 0 and the tile uses int64 atomics.
+  // Otherwise (dense tiles) sb = 0 and the tile uses int64 atomics.  The
+  // same bound gives |q| / 2^sb < 2^31 for every contribution, which
+  // split_q needs.
   int sb = 0;
   {
     const int clog = total > 1u ? 32 - __clz((int)(total - 1u)) : 0;  // ceil(log2 T)
@@ -448,7 +472,8 @@ dep_accum_kernel(const DepRec* __restrict__ sorted, const unsigned* __restrict__
   if (sb > 0) {
     unsigned* acc_lo = reinterpret_cast<unsigned*>(acc);
     int* acc_hi = reinterpret_cast<int*>(acc) + ncell;
-    const long long lo_mask = (1LL << sb) - 1;
+    const float two_sb = ldexpf(1.0f, sb), inv_two_sb = ldexpf(1.0f, -sb);
+    const unsigned lo_one = 1u << sb;
     for (unsigned k = threadIdx.x; k < total; k += blockDim.x) {
       int lo = 0, hi = nr - 1;  // largest r with r_pref[r] <= k
       while (lo < hi) {
@@ -481,10 +506,11 @@ dep_accum_kernel(const DepRec* __restrict__ sorted, const unsigned* __restrict__
 #pragma unroll
           for (int c = 0; c < S; ++c) {
             if (lz[c] >= g.tz) continue;
-            const long long q = f32_to_ll_rn(pxy * pz[c] * scale_f);
+            int qh;
+            unsigned ql;
+            split_q(pxy * pz[c] * scale_f, two_sb, inv_two_sb, lo_one, qh, ql);
             const int cell = row + lz[c];
-            atomicAdd(&acc_lo[cell], (unsigned)(q & lo_mask));
-            const int qh = (int)(q >> sb);
+            if (ql != 0u) atomicAdd(&acc_lo[cell], ql);
             if (qh != 0) atomicAdd(&acc_hi[cell], qh);
           }
         }

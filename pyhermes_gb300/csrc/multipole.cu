@@ -495,6 +495,8 @@ struct ContractArgs {
   const float2* f2;
   const float2* src3;
   int s2, s3;        // field strides (kBinStride, or 1 for a single bin)
+  long long bstride; // bin-major fields (tensor-core kernel): float2 stride between bins
+  int nb3s;          // bin-major fields: bins of the a3 source to stage
   int conj_src;      // a3 = sign * conj(src3)
   float sign;
   int J, CX;
@@ -838,9 +840,15 @@ constexpr int kOpBytes = 2 * kAtomCol;                     // (hi, mid) + (lo, p
 constexpr int kRawBytes = 64 * kBinStride * 8;             // TMA a2 plane: 64 cells x 16 complex
 constexpr int kTmemCols = 128;                             // D: 96 columns used
 constexpr int kN = 96;
+// a3 plane buffer: [cell][16] (bin-interleaved fields) or [16][kA3P]
+// (bin-major fields; kA3P = 145 = 1 mod 16 puts the 16 bins of one cell on
+// distinct bank pairs)
+constexpr int kA3P = ct::HY * ct::HZ + 1;
+constexpr int kA3Buf = kBinStride * kA3P;
+static_assert(kA3Buf >= ct::kA3Plane, "a3 buffer");
 constexpr uint32_t kIdesc = hermes::tc::idesc_bf16_f32(128, kN, true, true);
 // 1 KB slack for the runtime 1024-byte alignment of the swizzled operands
-constexpr size_t kSmem = 1024 + 2 * kOpBytes + 2 * kRawBytes + sizeof(float2) * 2 * ct::kA3Plane +
+constexpr size_t kSmem = 1024 + 2 * kOpBytes + 2 * kRawBytes + sizeof(float2) * 2 * kA3Buf +
                          sizeof(float) * (3 * hf::kHPlane + 2 * ct::kEpsPlane) +
                          sizeof(double) * 2 * kMaxBins * kMaxBins + 128;
 }  // namespace tcc
@@ -873,6 +881,32 @@ __device__ __forceinline__ void tc_put_pair(unsigned char* op, int cell, int b, 
   *reinterpret_cast<uint32_t*>(op + tcc::kAtomCol + row + hermes::tc::sw128_offset(r, b >> 2) + byte) = l;
 }
 
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+
+// a3 plane x_a from bin-major fields (bin b at src3 + b * bstride) -> buf
+// [16][kA3P] float2; bins nb3 .. 15 are written as zeros.
+__device__ __forceinline__ void ct_stage_a3_bm(const float2* __restrict__ src3, long long bstride, int nb3,
+                                               float2* buf, int xa, int y0, int z0, int L, int Lm) {
+  constexpr int kPlane = ct::HY * ct::HZ;
+  const long long xb = (long long)(xa & Lm) * L;
+  for (int c = threadIdx.x; c < kBinStride * kPlane; c += ct::kThreads) {
+    const int bb = c / kPlane, cell = c - bb * kPlane;
+    const int hy = cell / ct::HZ, hz = cell - hy * ct::HZ;
+    float2* dst = buf + bb * tcc::kA3P + cell;
+    if (bb < nb3)
+      cp_async8(dst, src3 + bb * bstride + (xb + ((y0 - 2 + hy) & Lm)) * L + ((z0 - 2 + hz) & Lm));
+    else
+      *dst = make_float2(0.f, 0.f);
+  }
+}
+
+// kBM: fields in the bin-major layout [bin][cell] that cuFFT writes (a2 by a
+// 4-D TMA map over (z, y, x, bin), a3 staged per bin); otherwise the
+// bin-interleaved [cell][16] layout or a single [cell] field.
+template <bool kBM>
 __global__ void __launch_bounds__(ct::kThreads, 2)
 mp_contract_tc_kernel(ContractArgs A, const __grid_constant__ CUtensorMap a2map) {
   namespace tc = hermes::tc;
@@ -882,7 +916,7 @@ mp_contract_tc_kernel(ContractArgs A, const __grid_constant__ CUtensorMap a2map)
   unsigned char* gbf = abf + tcc::kOpBytes;                        // B operand (G split)
   float* araw = reinterpret_cast<float*>(gbf + tcc::kOpBytes);    // [2][64 cells][32] TMA a2 planes
   float2* abuf = reinterpret_cast<float2*>(reinterpret_cast<unsigned char*>(araw) + 2 * tcc::kRawBytes);
-  double* dacc = reinterpret_cast<double*>(abuf + 2 * ct::kA3Plane);  // [16][16][2]
+  double* dacc = reinterpret_cast<double*>(abuf + 2 * tcc::kA3Buf);  // [16][16][2]
   float* hring = reinterpret_cast<float*>(dacc + 2 * kMaxBins * kMaxBins);  // [3][kHPlane]
   float* epsb = hring + 3 * hf::kHPlane;
   uint64_t* bars = reinterpret_cast<uint64_t*>(epsb + 2 * ct::kEpsPlane);  // tma[2], mma
@@ -902,7 +936,7 @@ mp_contract_tc_kernel(ContractArgs A, const __grid_constant__ CUtensorMap a2map)
   const int nty = L / ct::TY, ntz = L / ct::TZ;
   const int n_items = (L / CX) * nty * ntz;
   const int nsteps = CX + 4;
-  const bool tma_a2 = A.s2 == kBinStride;
+  const bool tma_a2 = kBM || A.s2 == kBinStride;
 
   if (tid == 0) {
 #pragma unroll
@@ -941,7 +975,10 @@ mp_contract_tc_kernel(ContractArgs A, const __grid_constant__ CUtensorMap a2map)
     ct_compute_h(gsm, epsb, hring);
     ct_compute_h(gsm, epsb + ct::kEpsPlane, hring + hf::kHPlane);
     __syncthreads();
-    ct_stage_a3(A.src3, A.s3, abuf, x0 - 2, y0, z0, L, Lm);
+    if (kBM)
+      ct_stage_a3_bm(A.src3, A.bstride, A.nb3s, abuf, x0 - 2, y0, z0, L, Lm);
+    else
+      ct_stage_a3(A.src3, A.s3, abuf, x0 - 2, y0, z0, L, Lm);
     ct_stage_eps(A.eps1, epsb, x0, y0, z0, L, Lm);
     cp_async_commit();
     cp_async_wait<0>();
@@ -963,7 +1000,10 @@ mp_contract_tc_kernel(ContractArgs A, const __grid_constant__ CUtensorMap a2map)
       if (st + 1 < nsteps) {
         // a3 plane xa+1 and eps plane xa+3: their buffers' last readers (the
         // stencil one step back, the h pass two steps back) are done
-        ct_stage_a3(A.src3, A.s3, abuf + ((st + 1) & 1) * ct::kA3Plane, xa + 1, y0, z0, L, Lm);
+        if (kBM)
+          ct_stage_a3_bm(A.src3, A.bstride, A.nb3s, abuf + ((st + 1) & 1) * tcc::kA3Buf, xa + 1, y0, z0, L, Lm);
+        else
+          ct_stage_a3(A.src3, A.s3, abuf + ((st + 1) & 1) * tcc::kA3Buf, xa + 1, y0, z0, L, Lm);
         ct_stage_eps(A.eps1, epsb + ((st + 1) & 1) * ct::kEpsPlane, xa + 3, y0, z0, L, Lm);
         // a2 plane of the next step's product (its buffer's last reader, the
         // split two steps back, finished before the last block barrier)
@@ -971,13 +1011,16 @@ mp_contract_tc_kernel(ContractArgs A, const __grid_constant__ CUtensorMap a2map)
           uint64_t* bar = &bars[(st + 1) & 1];
           tc::fence_proxy_async_smem();
           tc::mbar_arrive_expect_tx(bar, tcc::kRawBytes);
-          tc::tma_load_4d(araw + ((st + 1) & 1) * (tcc::kRawBytes / 4), &a2map, bar, 0, z0, y0, (xa - 1) & Lm);
+          if (kBM)
+            tc::tma_load_4d(araw + ((st + 1) & 1) * (tcc::kRawBytes / 4), &a2map, bar, 2 * z0, y0, (xa - 1) & Lm, 0);
+          else
+            tc::tma_load_4d(araw + ((st + 1) & 1) * (tcc::kRawBytes / 4), &a2map, bar, 0, z0, y0, (xa - 1) & Lm);
         }
       }
       cp_async_commit();
       __syncthreads();
       {
-        const float2* ap = abuf + (st & 1) * ct::kA3Plane;
+        const float2* ap = abuf + (st & 1) * tcc::kA3Buf;
         const float* hp0 = hring + (st % 3) * hf::kHPlane;
         const float* hp1 = hring + ((st + 1) % 3) * hf::kHPlane;
         const float* hp2 = hring + ((st + 2) % 3) * hf::kHPlane;
@@ -990,7 +1033,9 @@ mp_contract_tc_kernel(ContractArgs A, const __grid_constant__ CUtensorMap a2map)
         for (int r = 0; r < 6; ++r) {
           float2 av[6];
 #pragma unroll
-          for (int k = 0; k < 6; ++k) av[k] = ap[((cy + r) * ct::HZ + cz + k) * kBinStride + b];
+          for (int k = 0; k < 6; ++k)
+            av[k] = kBM ? ap[b * tcc::kA3P + (cy + r) * ct::HZ + cz + k]
+                        : ap[((cy + r) * ct::HZ + cz + k) * kBinStride + b];
           // Rz_{l1z}(row, cz + dz) = sum_{l2z} Gamma[l1z][l2z] a3(row, cz + dz + l1z - l2z)
           float2 rz[2][3];
 #pragma unroll
@@ -1044,9 +1089,21 @@ mp_contract_tc_kernel(ContractArgs A, const __grid_constant__ CUtensorMap a2map)
           if (A.conj_src) g = make_float2(A.sign * g.x, -A.sign * g.y);
           tc_put_pair(gbf, (cy + (c >> 1)) * ct::TZ + cz + (c & 1), b, g.x, g.y);
         }
-        const int cell = tid >> 2, q = tid & 3;
+        // this thread's operand row (cell) and bins 4q .. 4q+3; with bin-major
+        // planes ([bin][cell] in shared memory) a warp takes 32 cells of one q
+        const int cell = kBM ? (tid & 63) : (tid >> 2), q = kBM ? (tid >> 6) : (tid & 3);
         float v[8];
-        if (tma_a2) {
+        if (kBM) {
+          const uint32_t par = (st & 1) ? tma_ph1 : tma_ph0;
+          if (!tc::mbar_wait(&bars[st & 1], par)) *s_abort = 1;  // a2 plane (TMA)
+          const float* src = araw + (st & 1) * (tcc::kRawBytes / 4) + cell * 2;
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            const float2 p = *reinterpret_cast<const float2*>(src + (4 * q + i) * 128);
+            v[2 * i] = p.x;
+            v[2 * i + 1] = p.y;
+          }
+        } else if (tma_a2) {
           const uint32_t par = (st & 1) ? tma_ph1 : tma_ph0;
           if (!tc::mbar_wait(&bars[st & 1], par)) *s_abort = 1;  // a2 plane (TMA)
           const float4* src = reinterpret_cast<const float4*>(araw + (st & 1) * (tcc::kRawBytes / 4) + cell * 32 + 8 * q);
@@ -1340,25 +1397,30 @@ struct FieldsCtx {
   int L, nsm;
   long long N;
   cudaStream_t s;
+  bool bin_major;
 };
 
+// bin_major: the caller's fields_out holds the batch as cuFFT leaves it,
+// [nb][L^3] (no interleave, and the workspace needs no bin-major copy).
 int fields_setup(const void* half_spec, int J, int l, int m, int nb, const double* phi_power, void* fields_out,
-                 void* workspace, size_t workspace_bytes, void* stream, FieldsCtx* ctx) {
+                 void* workspace, size_t workspace_bytes, void* stream, FieldsCtx* ctx, bool bin_major = false) {
   if (!half_spec || !phi_power || !fields_out) return fail(HERMES_ERR_INVALID, "multipole_fields: NULL argument");
   if (l < 0 || l > kMaxEll || m < -l || m > l) return fail(HERMES_ERR_INVALID, "multipole_fields: bad (l=%d, m=%d)", l, m);
+  if (nb < 1 || nb > kMaxBins) return fail(HERMES_ERR_INVALID, "multipole_fields: nb=%d outside [1,%d]", nb, kMaxBins);
   size_t need = 0;
-  int rc = hermes_multipole_workspace_size(J, nb, &need);
+  int rc = hermes_multipole_workspace_size(J, bin_major ? 1 : nb, &need);
   if (rc) return rc;
   if (!workspace || workspace_bytes < need) return fail(HERMES_ERR_WORKSPACE, "multipole_fields: workspace %zu < %zu", workspace_bytes, need);
   ctx->L = 1 << J;
   ctx->N = 1LL << (3 * J);
   ctx->s = hermes::as_stream(stream);
   ctx->nsm = sm_count();
-  const MpWs w = carve_ws(workspace, workspace_bytes, J, nb);
+  ctx->bin_major = bin_major;
+  const MpWs w = carve_ws(workspace, workspace_bytes, J, bin_major ? 1 : nb);
   ctx->T = w.T;
   ctx->Pf = w.Pf;
   ctx->out = static_cast<float2*>(fields_out);
-  ctx->binmajor = nb > 1 ? w.binmajor : ctx->out;
+  ctx->binmajor = (nb > 1 && !bin_major) ? w.binmajor : ctx->out;
   mp_power_to_f32<<<(ctx->L + 1 + 255) / 256, 256, 0, ctx->s>>>(phi_power, ctx->L + 1, ctx->Pf);
   HERMES_LAUNCH_CHECK("mp_power_to_f32");
   return HERMES_OK;
@@ -1392,7 +1454,7 @@ int fields_run(const FieldsCtx& ctx, const void* half_spec, int J, int l, int m,
   r = cufftExecC2C(h, reinterpret_cast<cufftComplex*>(ctx.binmajor), reinterpret_cast<cufftComplex*>(ctx.binmajor),
                    CUFFT_INVERSE);
   if (r != CUFFT_SUCCESS) return fail(HERMES_ERR_CUFFT, "cufftExecC2C failed: %d", (int)r);
-  if (nb > 1) {
+  if (nb > 1 && !ctx.bin_major) {
     long long nblk = ctx.N / kIlCells;
     if (nblk > (long long)ctx.nsm * 16) nblk = (long long)ctx.nsm * 16;
     mp_interleave_kernel<<<(int)nblk, 256, 0, s>>>(ctx.binmajor, nb, ctx.N, ctx.out);
@@ -1402,12 +1464,13 @@ int fields_run(const FieldsCtx& ctx, const void* half_spec, int J, int l, int m,
 }
 }  // namespace
 
-extern "C" int hermes_multipole_fields(const void* half_spec, int J, int l, int m, const double* radii,
-                                       int nb, const double* phi_power, void* fields_out, void* workspace,
-                                       size_t workspace_bytes, void* stream) {
+static int fields_radii(const void* half_spec, int J, int l, int m, const double* radii, int nb,
+                        const double* phi_power, void* fields_out, void* workspace, size_t workspace_bytes,
+                        void* stream, bool bin_major) {
   if (!radii) return fail(HERMES_ERR_INVALID, "multipole_fields: NULL argument");
   FieldsCtx ctx;
-  int rc = fields_setup(half_spec, J, l, m, nb, phi_power, fields_out, workspace, workspace_bytes, stream, &ctx);
+  int rc = fields_setup(half_spec, J, l, m, nb, phi_power, fields_out, workspace, workspace_bytes, stream, &ctx,
+                        bin_major);
   if (rc) return rc;
   RhoArgs hrho;
   for (int b = 0; b < kMaxBins; ++b) hrho.v[2 * b] = hrho.v[2 * b + 1] = 0.f;
@@ -1422,14 +1485,28 @@ extern "C" int hermes_multipole_fields(const void* half_spec, int J, int l, int 
   return fields_run(ctx, half_spec, J, l, m, nb);
 }
 
-extern "C" int hermes_multipole_fields_window(const void* half_spec, int J, int l, int m,
-                                              const hermes_window_t* bins, int nb, const double* phi_power,
-                                              void* fields_out, void* workspace, size_t workspace_bytes,
-                                              void* stream) {
+extern "C" int hermes_multipole_fields(const void* half_spec, int J, int l, int m, const double* radii,
+                                       int nb, const double* phi_power, void* fields_out, void* workspace,
+                                       size_t workspace_bytes, void* stream) {
+  return fields_radii(half_spec, J, l, m, radii, nb, phi_power, fields_out, workspace, workspace_bytes, stream,
+                      false);
+}
+
+extern "C" int hermes_multipole_fields_bm(const void* half_spec, int J, int l, int m, const double* radii,
+                                          int nb, const double* phi_power, void* fields_out, void* workspace,
+                                          size_t workspace_bytes, void* stream) {
+  return fields_radii(half_spec, J, l, m, radii, nb, phi_power, fields_out, workspace, workspace_bytes, stream,
+                      true);
+}
+
+static int fields_window(const void* half_spec, int J, int l, int m, const hermes_window_t* bins, int nb,
+                         const double* phi_power, void* fields_out, void* workspace, size_t workspace_bytes,
+                         void* stream, bool bin_major) {
   if (!bins) return fail(HERMES_ERR_INVALID, "multipole_fields_window: NULL argument");
   if (nb < 1 || nb > kMaxBins) return fail(HERMES_ERR_INVALID, "multipole_fields_window: nb=%d", nb);
   FieldsCtx ctx;
-  int rc = fields_setup(half_spec, J, l, m, nb, phi_power, fields_out, workspace, workspace_bytes, stream, &ctx);
+  int rc = fields_setup(half_spec, J, l, m, nb, phi_power, fields_out, workspace, workspace_bytes, stream, &ctx,
+                        bin_major);
   if (rc) return rc;
   IsoWins wins;
   memset(&wins, 0, sizeof(wins));
@@ -1446,16 +1523,32 @@ extern "C" int hermes_multipole_fields_window(const void* half_spec, int J, int 
   return fields_run(ctx, half_spec, J, l, m, nb);
 }
 
-extern "C" int hermes_multipole_fields_table(const void* half_spec, int J, int l, int m, const double* tables,
-                                             const int64_t* offsets, const int32_t* sizes, const double* k_max,
-                                             double grid_to_physical, int nb, const double* phi_power,
-                                             void* fields_out, void* workspace, size_t workspace_bytes,
-                                             void* stream) {
+extern "C" int hermes_multipole_fields_window(const void* half_spec, int J, int l, int m,
+                                              const hermes_window_t* bins, int nb, const double* phi_power,
+                                              void* fields_out, void* workspace, size_t workspace_bytes,
+                                              void* stream) {
+  return fields_window(half_spec, J, l, m, bins, nb, phi_power, fields_out, workspace, workspace_bytes, stream,
+                       false);
+}
+
+extern "C" int hermes_multipole_fields_window_bm(const void* half_spec, int J, int l, int m,
+                                                 const hermes_window_t* bins, int nb, const double* phi_power,
+                                                 void* fields_out, void* workspace, size_t workspace_bytes,
+                                                 void* stream) {
+  return fields_window(half_spec, J, l, m, bins, nb, phi_power, fields_out, workspace, workspace_bytes, stream,
+                       true);
+}
+
+static int fields_table(const void* half_spec, int J, int l, int m, const double* tables, const int64_t* offsets,
+                        const int32_t* sizes, const double* k_max, double grid_to_physical, int nb,
+                        const double* phi_power, void* fields_out, void* workspace, size_t workspace_bytes,
+                        void* stream, bool bin_major) {
   if (!tables || !offsets || !sizes || !k_max) return fail(HERMES_ERR_INVALID, "multipole_fields_table: NULL argument");
   if (nb < 1 || nb > kMaxBins) return fail(HERMES_ERR_INVALID, "multipole_fields_table: nb=%d", nb);
   if (!(grid_to_physical > 0.0)) return fail(HERMES_ERR_INVALID, "multipole_fields_table: grid_to_physical must be > 0");
   FieldsCtx ctx;
-  int rc = fields_setup(half_spec, J, l, m, nb, phi_power, fields_out, workspace, workspace_bytes, stream, &ctx);
+  int rc = fields_setup(half_spec, J, l, m, nb, phi_power, fields_out, workspace, workspace_bytes, stream, &ctx,
+                        bin_major);
   if (rc) return rc;
   TabArgs ta;
   memset(&ta, 0, sizeof(ta));
@@ -1470,6 +1563,24 @@ extern "C" int hermes_multipole_fields_table(const void* half_spec, int J, int l
   mp_tab_table_kernel<<<ctx.nsm * 8, 256, 0, ctx.s>>>(ctx.T, 3 * ctx.L * ctx.L, tables, ta, nb);
   HERMES_LAUNCH_CHECK("mp_tab_table_kernel");
   return fields_run(ctx, half_spec, J, l, m, nb);
+}
+
+extern "C" int hermes_multipole_fields_table(const void* half_spec, int J, int l, int m, const double* tables,
+                                             const int64_t* offsets, const int32_t* sizes, const double* k_max,
+                                             double grid_to_physical, int nb, const double* phi_power,
+                                             void* fields_out, void* workspace, size_t workspace_bytes,
+                                             void* stream) {
+  return fields_table(half_spec, J, l, m, tables, offsets, sizes, k_max, grid_to_physical, nb, phi_power,
+                      fields_out, workspace, workspace_bytes, stream, false);
+}
+
+extern "C" int hermes_multipole_fields_table_bm(const void* half_spec, int J, int l, int m, const double* tables,
+                                                const int64_t* offsets, const int32_t* sizes, const double* k_max,
+                                                double grid_to_physical, int nb, const double* phi_power,
+                                                void* fields_out, void* workspace, size_t workspace_bytes,
+                                                void* stream) {
+  return fields_table(half_spec, J, l, m, tables, offsets, sizes, k_max, grid_to_physical, nb, phi_power,
+                      fields_out, workspace, workspace_bytes, stream, true);
 }
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no link
@@ -1505,12 +1616,32 @@ static int make_a2_map(const void* fields, int L, CUtensorMap* map) {
   return HERMES_OK;
 }
 
-enum { kEngineTensor = 0, kEngineSimt = 1 };
+// 4-D tensor map over bin-major fields [bin][x][y][z] (float32 view: z as 2L
+// floats), box 16 floats (8 z) x 8 (y) x 1 (x) x 16 (bins; bins >= nb read
+// as zeros): one contraction tile's a2 plane as [bin][8 y][8 z] complex.
+static int make_a2_map_bm(const void* fields, int L, int nb, CUtensorMap* map) {
+  auto enc = tensor_map_encoder();
+  if (!enc) return fail(HERMES_ERR_CUDA, "cuTensorMapEncodeTiled is unavailable");
+  const cuuint64_t dims[4] = {2 * (cuuint64_t)L, (cuuint64_t)L, (cuuint64_t)L, (cuuint64_t)nb};
+  const cuuint64_t row = sizeof(float) * 2 * (cuuint64_t)L;
+  const cuuint64_t strides[3] = {row, row * L, row * L * L};
+  const cuuint32_t box[4] = {2 * ct::TZ, ct::TY, 1, kBinStride};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<void*>(fields), dims, strides, box, estr,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(HERMES_ERR_CUDA, "cuTensorMapEncodeTiled failed: %d", (int)r);
+  return HERMES_OK;
+}
+
+enum { kEngineTensor = 0, kEngineSimt = 1, kEngineTensorBinMajor = 2 };
 
 // Launches the contraction and the float64 reduction into dout [16][16][2]
 // (already multiplied by `scale`), with no host synchronisation.  engine:
 // tensor-core bin product (mp_contract_tc_kernel) or FP32 CUDA cores
-// (mp_contract_kernel).
+// (mp_contract_kernel) on the fields layout of hermes_multipole_fields, or
+// the tensor-core kernel on the bin-major layout of
+// hermes_multipole_fields_bm.
 static int mp_contract_launch(const float* eps1, const void* fields2, int nb2, const void* fields3, int nb3,
                               int conj_sign, const double* gamma, int J, int chunk_x, int ctas_per_sm, double scale,
                               double* dout, void* workspace, size_t workspace_bytes, cudaStream_t s, int engine) {
@@ -1538,12 +1669,15 @@ static int mp_contract_launch(const float* eps1, const void* fields2, int nb2, c
   if (!workspace || workspace_bytes < need)
     return fail(HERMES_ERR_WORKSPACE, "multipole_contract: workspace %zu < %zu", workspace_bytes, need);
   const MpWs w = carve_ws(workspace, workspace_bytes, J, 1);
-  static bool smem_set[2][64] = {{false}};
+  static bool smem_set[3][64] = {{false}};
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 0 || dev >= 64 || !smem_set[engine][dev]) {  // once per device, before any stream capture
     if (engine == kEngineTensor)
-      HERMES_CUDA_TRY(cudaFuncSetAttribute(mp_contract_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+      HERMES_CUDA_TRY(cudaFuncSetAttribute(mp_contract_tc_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)tcc::kSmem));
+    else if (engine == kEngineTensorBinMajor)
+      HERMES_CUDA_TRY(cudaFuncSetAttribute(mp_contract_tc_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)tcc::kSmem));
     else
       HERMES_CUDA_TRY(cudaFuncSetAttribute(mp_contract_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1557,6 +1691,8 @@ static int mp_contract_launch(const float* eps1, const void* fields2, int nb2, c
   A.src3 = static_cast<const float2*>(conj_src ? fields2 : fields3);
   A.s2 = nb2 == 1 ? 1 : kBinStride;
   A.s3 = conj_src ? A.s2 : (nb3 == 1 ? 1 : kBinStride);
+  A.bstride = 1LL << (3 * J);
+  A.nb3s = nb3;
   A.conj_src = conj_src;
   A.sign = (float)conj_sign;
   A.J = J;
@@ -1568,15 +1704,21 @@ static int mp_contract_launch(const float* eps1, const void* fields2, int nb2, c
   int nblk = ctas_per_sm * sm_count();
   if (nblk > n_items) nblk = n_items;
   if (nblk > 1024) nblk = 1024;
-  if (engine == kEngineTensor) {
+  if (engine == kEngineTensor || engine == kEngineTensorBinMajor) {
     CUtensorMap map;
     memset(&map, 0, sizeof(map));
-    if (A.s2 == kBinStride) {
+    if (engine == kEngineTensorBinMajor) {
+      rc = make_a2_map_bm(fields2, L, nb2, &map);
+      if (rc) return rc;
+    } else if (A.s2 == kBinStride) {
       rc = make_a2_map(fields2, L, &map);
       if (rc) return rc;
     }
     HERMES_CUDA_TRY(cudaMemsetAsync(w.status, 0, sizeof(int), s));
-    mp_contract_tc_kernel<<<nblk, ct::kThreads, tcc::kSmem, s>>>(A, map);
+    if (engine == kEngineTensorBinMajor)
+      mp_contract_tc_kernel<true><<<nblk, ct::kThreads, tcc::kSmem, s>>>(A, map);
+    else
+      mp_contract_tc_kernel<false><<<nblk, ct::kThreads, tcc::kSmem, s>>>(A, map);
     HERMES_LAUNCH_CHECK("mp_contract_tc_kernel");
   } else {
     mp_contract_kernel<<<nblk, ct::kThreads, ct::kSmem, s>>>(A);
@@ -1641,6 +1783,14 @@ extern "C" int hermes_multipole_contract_simt_async(const float* eps1, const voi
                                                     void* workspace, size_t workspace_bytes, void* stream) {
   return contract_async(eps1, fields2, nb2, fields3, nb3, conj_sign, gamma, J, chunk_x, ctas_per_sm, dev_out,
                         workspace, workspace_bytes, stream, kEngineSimt);
+}
+
+extern "C" int hermes_multipole_contract_bm_async(const float* eps1, const void* fields2, int nb2,
+                                                  const void* fields3, int nb3, int conj_sign, const double* gamma,
+                                                  int J, int chunk_x, int ctas_per_sm, double* dev_out,
+                                                  void* workspace, size_t workspace_bytes, void* stream) {
+  return contract_async(eps1, fields2, nb2, fields3, nb3, conj_sign, gamma, J, chunk_x, ctas_per_sm, dev_out,
+                        workspace, workspace_bytes, stream, kEngineTensorBinMajor);
 }
 
 extern "C" int hermes_multipole_contract_status(const void* workspace, size_t workspace_bytes, int J, int* status,

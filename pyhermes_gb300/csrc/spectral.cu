@@ -584,17 +584,31 @@ pair_products_cylz_kernel(PPArgs a, const WinDev* __restrict__ wins, const doubl
     for (int zc = 0; zc < H; zc += kCylZ) {
       const int zn = min(kCylZ, H - zc);
       __syncwarp();
+      // lane i stages z-plane zc + i of all CW columns: per column the lanes
+      // read consecutive modes (coalesced), the CW loads are in flight
+      // together, and the plane's products are written as 128-bit rows
 #pragma unroll
-      for (int c = 0; c < CW; ++c) {
-        const long long mb = (col0 + c) * H + zc;
-        for (int i = lane; i < zn; i += 32) {
+      for (int ii = 0; ii < kCylZ / 32; ++ii) {
+        const int i = lane + 32 * ii;
+        if (i < zn) {
           const int z = zc + i;
           const float wgt = (z == 0 || z == L / 2) ? 1.f : 2.f;
+          float tv[NP][CW];
 #pragma unroll
-          for (int p = 0; p < NP; ++p) {
-            const float2 u = a.si[p][mb + i], v = a.sj[p][mb + i];
-            Tw[(i * NP + p) * CW + c] = (a.exclude_k0 && mb + i == 0) ? 0.f : wgt * (u.x * v.x + u.y * v.y);
+          for (int c = 0; c < CW; ++c) {
+            const long long m = (col0 + c) * H + z;
+#pragma unroll
+            for (int p = 0; p < NP; ++p) {
+              const float2 u = a.si[p][m], v = a.sj[p][m];
+              tv[p][c] = (a.exclude_k0 && m == 0) ? 0.f : wgt * (u.x * v.x + u.y * v.y);
+            }
           }
+#pragma unroll
+          for (int p = 0; p < NP; ++p)
+#pragma unroll
+            for (int c4 = 0; c4 < CW; c4 += 4)
+              *reinterpret_cast<float4*>(Tw + (i * NP + p) * CW + c4) =
+                  make_float4(tv[p][c4], tv[p][c4 + 1], tv[p][c4 + 2], tv[p][c4 + 3]);
         }
       }
       __syncwarp();

@@ -67,23 +67,37 @@ def _ws_bytes(J, nb):
 BIN_STRIDE = 16
 
 
-def multipole_fields(half_spec, J, l, m, radii_grid, phi_power, out=None, ws=None):
+def _fields_out(J, nb, bin_major, dev):
+    N = 1 << (3 * J)
+    shape = (N,) if nb == 1 else ((nb, N) if bin_major else (N, BIN_STRIDE))
+    return torch.empty(shape, dtype=torch.complex64, device=dev)
+
+
+def fields_ws_bytes(J, nb, bin_major=False):
+    """Workspace bytes of the fields calls: the bin-major layout needs no
+    bin-major staging copy."""
+    return _ws_bytes(J, 1 if bin_major else nb)
+
+
+def multipole_fields(half_spec, J, l, m, radii_grid, phi_power, out=None, ws=None, bin_major=False):
     """a_lm^b = ifftn(fftn(eps) K_lm^b) for thin-shell radii (grid units).
 
     Returns complex64 [L^3, 16] (bin-interleaved; bins >= nb unused) for
-    several radii, or [L^3] for a single radius."""
+    several radii, or [L^3] for a single radius.  bin_major=True returns
+    [nb, L^3] as the inverse FFT leaves it (hermes_multipole_fields_bm: no
+    interleave pass, no bin-major workspace copy), the layout the tensor-core
+    contraction reads with bin_major=True."""
     nb = len(radii_grid)
-    N = 1 << (3 * J)
     dev = half_spec.device
     if out is None:
-        shape = (N,) if nb == 1 else (N, BIN_STRIDE)
-        out = torch.empty(shape, dtype=torch.complex64, device=dev)
+        out = _fields_out(J, nb, bin_major, dev)
     if ws is None:
-        ws = _workspace(_ws_bytes(J, nb), dev)
+        ws = _workspace(fields_ws_bytes(J, nb, bin_major), dev)
     radii = (ctypes.c_double * nb)(*[float(r) for r in radii_grid])
-    _lib.check(_lib.load().hermes_multipole_fields(_ptr(half_spec), J, int(l), int(m), radii, nb, _ptr(phi_power),
-                                                   _ptr(out), _ptr(ws), ws.numel(), _stream_ptr(dev)),
-               "hermes_multipole_fields")
+    lib = _lib.load()
+    fn = lib.hermes_multipole_fields_bm if bin_major else lib.hermes_multipole_fields
+    _lib.check(fn(_ptr(half_spec), J, int(l), int(m), radii, nb, _ptr(phi_power), _ptr(out), _ptr(ws), ws.numel(),
+                  _stream_ptr(dev)), "hermes_multipole_fields")
     return out
 
 
@@ -116,11 +130,11 @@ def as_bin(b):
     return b if isinstance(b, BinSpec) else BinSpec("shell", {"R": float(b)})
 
 
-def multipole_fields_bins(half_spec, J, l, m, bins, box_size, phi_power, out=None, ws=None):
+def multipole_fields_bins(half_spec, J, l, m, bins, box_size, phi_power, out=None, ws=None, bin_major=False):
     """a_lm^b for radial bins of any supported profile (shell, sphere,
     thick_shell, gaussian, gaussian_shell, custom_real, custom_kspace), in the
-    layout of multipole_fields.  The GPU path per bin follows
-    radial_multipole_windows.py:269-313: j_l for shells, the analytic
+    layout of multipole_fields (bin_major as there).  The GPU path per bin
+    follows radial_multipole_windows.py:269-313: j_l for shells, the analytic
     monopole transfer for l = 0, else a host table of U_l(k)."""
     from . import radial_profiles as rp
 
@@ -130,24 +144,29 @@ def multipole_fields_bins(half_spec, J, l, m, bins, box_size, phi_power, out=Non
     g2p = L / float(box_size)
     per_bin = [rp.profile_mode(b.type, b.len_args, l) for b in bins]
     if len(set(per_bin)) > 1:
-        # bins on different profile paths: one call per path, its columns
-        # gathered into the shared [cell][BIN_STRIDE] layout
+        # bins on different profile paths: one call per path, its bins
+        # gathered into the shared layout
         if out is None:
-            out = torch.zeros((L ** 3, BIN_STRIDE), dtype=torch.complex64, device=half_spec.device)
+            out = torch.zeros((nb, L ** 3) if bin_major else (L ** 3, BIN_STRIDE), dtype=torch.complex64,
+                              device=half_spec.device)
         for path in dict.fromkeys(per_bin):
             idx = [i for i, p in enumerate(per_bin) if p == path]
-            part = multipole_fields_bins(half_spec, J, l, m, [bins[i] for i in idx], box_size, phi_power, ws=ws)
-            out[:, idx] = part.view(L ** 3, 1) if part.dim() == 1 else part[:, :len(idx)]
+            part = multipole_fields_bins(half_spec, J, l, m, [bins[i] for i in idx], box_size, phi_power, ws=ws,
+                                         bin_major=bin_major)
+            if bin_major:
+                out[idx] = part.view(1, L ** 3) if part.dim() == 1 else part
+            else:
+                out[:, idx] = part.view(L ** 3, 1) if part.dim() == 1 else part[:, :len(idx)]
         return out
     mode = per_bin[0]
     if mode == "shell":
         radii = [(b.len_args["R_shell"] if b.type == "gaussian_shell" else b.len_args["R"]) * g2p for b in bins]
-        return multipole_fields(half_spec, J, l, m, radii, phi_power, out=out, ws=ws)
+        return multipole_fields(half_spec, J, l, m, radii, phi_power, out=out, ws=ws, bin_major=bin_major)
     dev = half_spec.device
     if out is None:
-        out = torch.empty((L ** 3,) if nb == 1 else (L ** 3, BIN_STRIDE), dtype=torch.complex64, device=dev)
+        out = _fields_out(J, nb, bin_major, dev)
     if ws is None:
-        ws = _workspace(_ws_bytes(J, nb), dev)
+        ws = _workspace(fields_ws_bytes(J, nb, bin_major), dev)
     lib = _lib.load()
     if mode == "analytic":
         from .window import WIN_ARGS, WIN_CODES, HermesWindow
@@ -159,9 +178,9 @@ def multipole_fields_bins(half_spec, J, l, m, bins, box_size, phi_power, out=Non
                 arr[k].len[i] = float(b.len_args[nm]) * g2p
             arr[k].los[2] = 1.0
             arr[k].scale = 1.0
-        _lib.check(lib.hermes_multipole_fields_window(_ptr(half_spec), J, int(l), int(m), arr, nb, _ptr(phi_power),
-                                                      _ptr(out), _ptr(ws), ws.numel(), _stream_ptr(dev)),
-                   "hermes_multipole_fields_window")
+        fn = lib.hermes_multipole_fields_window_bm if bin_major else lib.hermes_multipole_fields_window
+        _lib.check(fn(_ptr(half_spec), J, int(l), int(m), arr, nb, _ptr(phi_power), _ptr(out), _ptr(ws), ws.numel(),
+                      _stream_ptr(dev)), "hermes_multipole_fields_window")
         return out
     k_max = math.sqrt(3.0) * g2p
     tabs = [rp.build_radial_multipole_table(b.type, b.len_args, l, k_max, b.profile) for b in bins]
@@ -169,11 +188,10 @@ def multipole_fields_bins(half_spec, J, l, m, bins, box_size, phi_power, out=Non
     offs = np.concatenate([[0], np.cumsum(sizes[:-1])]).astype(np.int64)
     kms = np.array([km for km, _ in tabs], dtype=np.float64)
     dt = torch.as_tensor(np.concatenate([t for _, t in tabs]), dtype=torch.float64, device=dev)
-    _lib.check(lib.hermes_multipole_fields_table(_ptr(half_spec), J, int(l), int(m), _ptr(dt),
-                                                 offs.ctypes.data_as(ctypes.c_void_p),
-                                                 sizes.ctypes.data_as(ctypes.c_void_p),
-                                                 kms.ctypes.data_as(ctypes.c_void_p), g2p, nb, _ptr(phi_power),
-                                                 _ptr(out), _ptr(ws), ws.numel(), _stream_ptr(dev)),
+    fn = lib.hermes_multipole_fields_table_bm if bin_major else lib.hermes_multipole_fields_table
+    _lib.check(fn(_ptr(half_spec), J, int(l), int(m), _ptr(dt), offs.ctypes.data_as(ctypes.c_void_p),
+                  sizes.ctypes.data_as(ctypes.c_void_p), kms.ctypes.data_as(ctypes.c_void_p), g2p, nb,
+                  _ptr(phi_power), _ptr(out), _ptr(ws), ws.numel(), _stream_ptr(dev)),
                "hermes_multipole_fields_table")
     return out  # dt is released in stream order after the table kernel
 
@@ -238,20 +256,27 @@ ENGINES = ("tensor", "simt")
 
 
 def multipole_contract_async(eps1, fields2, nb2, gamma_c, J, dev_out, fields3=None, nb3=None, conj_sign=1,
-                             chunk_x=0, ctas_per_sm=0, ws=None, engine="tensor"):
+                             chunk_x=0, ctas_per_sm=0, ws=None, engine="tensor", bin_major=False):
     """hermes_multipole_contract_async: S (times 4 pi / L^3) into the device
     float64 tensor dev_out [16, 16, 2] on the current stream, no host sync.
     gamma_c: a ctypes double[9] (kept alive by the caller during capture).
     engine: 'tensor' (bin x bin product on tcgen05, BF16x3 operands) or 'simt'
-    (the all-FP32 CUDA-core kernel)."""
+    (the all-FP32 CUDA-core kernel).  bin_major: fields in the [nb, L^3]
+    layout of multipole_fields(bin_major=True) (tensor engine,
+    hermes_multipole_contract_bm_async)."""
     if engine not in ENGINES:
         raise ValueError(f"engine must be one of {ENGINES}")
+    if bin_major and engine != "tensor":
+        raise ValueError("bin-major fields are read by the tensor engine only")
     nb3 = nb2 if fields3 is None else nb3
     dev = eps1.device
     if ws is None:
-        ws = _workspace(_ws_bytes(J, max(nb2, nb3)), dev)
+        ws = _workspace(_ws_bytes(J, 1 if bin_major else max(nb2, nb3)), dev)
     lib = _lib.load()
-    fn = lib.hermes_multipole_contract_async if engine == "tensor" else lib.hermes_multipole_contract_simt_async
+    if bin_major:
+        fn = lib.hermes_multipole_contract_bm_async
+    else:
+        fn = lib.hermes_multipole_contract_async if engine == "tensor" else lib.hermes_multipole_contract_simt_async
     _lib.check(fn(_ptr(eps1), _ptr(fields2), nb2, _ptr(fields3), nb3, int(conj_sign), gamma_c, J, int(chunk_x),
                   int(ctas_per_sm), _ptr(dev_out), _ptr(ws), ws.numel(), _stream_ptr(dev)),
                "hermes_multipole_contract_async")
@@ -270,13 +295,13 @@ def contract_status(J, ws=None, device="cuda"):
 
 
 def multipole_contract_engine(eps1, fields2, nb2, gamma, J, fields3=None, nb3=None, conj_sign=1, engine="tensor",
-                              chunk_x=0, ctas_per_sm=0):
+                              chunk_x=0, ctas_per_sm=0, bin_major=False):
     """S[b2, b3] complex128 from a chosen engine (async launch + one read)."""
     nb3 = nb2 if fields3 is None else nb3
     g = (ctypes.c_double * 9)(*np.asarray(gamma, dtype=np.float64).ravel())
     out = torch.zeros((MAX_BINS, MAX_BINS, 2), dtype=torch.float64, device=eps1.device)
     multipole_contract_async(eps1, fields2, nb2, g, J, out, fields3=fields3, nb3=nb3, conj_sign=conj_sign,
-                             chunk_x=chunk_x, ctas_per_sm=ctas_per_sm, engine=engine)
+                             chunk_x=chunk_x, ctas_per_sm=ctas_per_sm, engine=engine, bin_major=bin_major)
     o = out[:nb2, :nb3].cpu().numpy()
     return o[..., 0] + 1j * o[..., 1]
 
@@ -319,10 +344,12 @@ class GraphedMultipole:
         L = self.L
         self.eps = torch.empty((L, L, L), dtype=torch.float32, device=self.dev)
         self.spec = torch.empty((L, L, L // 2 + 1), dtype=torch.complex64, device=self.dev)
-        self.fields = torch.empty((L ** 3, BIN_STRIDE), dtype=torch.complex64, device=self.dev)
+        # bin-major fields [nb, L^3], as the inverse FFT leaves them
+        self.fields = torch.empty((len(self.grid), L ** 3), dtype=torch.complex64, device=self.dev)
         self.out = torch.zeros((len(self.lm), MAX_BINS, MAX_BINS, 2), dtype=torch.float64, device=self.dev)
         # own workspace: a captured graph must never see the shared one reallocated
-        self.ws = torch.empty(max(_ws_bytes(self.J, len(self.grid)), 256), dtype=torch.uint8, device=self.dev)
+        self.ws = torch.empty(max(fields_ws_bytes(self.J, len(self.grid), True), 256), dtype=torch.uint8,
+                              device=self.dev)
         self.chunk_x, self.ctas = int(chunk_x), int(ctas_per_sm)
         self.use_graph = bool(use_graph)
         self.graph = None
@@ -332,10 +359,10 @@ class GraphedMultipole:
         _lib.check(lib.hermes_fft_r2c(_ptr(self.eps), _ptr(self.spec), self.J, _stream_ptr(self.dev)), "hermes_fft_r2c")
         nb = len(self.grid)
         for k, (l, m) in enumerate(self.lm):
-            multipole_fields(self.spec, self.J, l, m, self.grid, self.P, out=self.fields, ws=self.ws)
+            multipole_fields(self.spec, self.J, l, m, self.grid, self.P, out=self.fields, ws=self.ws, bin_major=True)
             multipole_contract_async(self.eps, self.fields, nb, self.gamma, self.J, self.out[k],
                                      conj_sign=(-1) ** ((l + m) % 2), chunk_x=self.chunk_x,
-                                     ctas_per_sm=self.ctas, ws=self.ws)
+                                     ctas_per_sm=self.ctas, ws=self.ws, bin_major=True)
 
     def summands(self, delta):
         """S_lm[i, j] (complex128 [n_lm, nb, nb]) for the field delta."""
@@ -386,6 +413,7 @@ class MultipoleEngine:
         if engine not in ENGINES:
             raise ValueError(f"engine must be one of {ENGINES}")
         self.engine = engine
+        self.bin_major = engine == "tensor"
         self.J = int(J)
         self.L = 1 << self.J
         self.box = float(box_size)
@@ -404,7 +432,8 @@ class MultipoleEngine:
         self.timing = {"fields_s": 0.0, "contract_s": 0.0}
 
     def _fields(self, spec, l, m, bins):
-        return multipole_fields_bins(spec, self.J, l, m, bins, self.box, self.P)
+        # the tensor engine reads the bin-major layout the inverse FFT writes
+        return multipole_fields_bins(spec, self.J, l, m, bins, self.box, self.P, bin_major=self.bin_major)
 
     def summands(self, l, m, r12_phys, r13_phys):
         """S_m[i, j] for two lists of radial bins (thin-shell radii in physical
@@ -423,13 +452,14 @@ class MultipoleEngine:
                     t1 = time.perf_counter()
                     self.timing["fields_s"] += t1 - t0
                     S = multipole_contract_engine(self.eps1, f2, len(c12), self.gamma, self.J,
-                                                  conj_sign=(-1) ** ((l + m) % 2), engine=self.engine)
+                                                  conj_sign=(-1) ** ((l + m) % 2), engine=self.engine,
+                                                  bin_major=self.bin_major)
                 else:
                     f3 = self._fields(self.spec3, l, -m, c13)
                     t1 = time.perf_counter()
                     self.timing["fields_s"] += t1 - t0
                     S = multipole_contract_engine(self.eps1, f2, len(c12), self.gamma, self.J, fields3=f3,
-                                                  nb3=len(c13), engine=self.engine)
+                                                  nb3=len(c13), engine=self.engine, bin_major=self.bin_major)
                     del f3
                 self.timing["contract_s"] += time.perf_counter() - t1
                 t0 = time.perf_counter()

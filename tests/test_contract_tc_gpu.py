@@ -100,3 +100,43 @@ def test_tensor_engine_many_bins_matches_fp32_kernel(J, chunk_x, ctas):
     assert _rel(tc, simt) < 1e-5, _rel(tc, simt)
     tc2 = mp.multipole_contract_engine(et, f, 15, GAM, J, engine="tensor", **kw)
     assert np.array_equal(tc, tc2)
+
+
+@pytest.mark.parametrize("J,chunk_x,ctas", [(6, 0, 0), (7, 32, 1)])
+def test_bin_major_path_is_bit_identical(J, chunk_x, ctas):
+    """Fields in the bin-major layout the inverse FFT writes (no interleave)
+    hold the same values as the interleaved layout, and the tensor-core
+    contraction reading them gives bit-identical S: shared field with 15 and
+    with 1 radius, separate a3 fields with nb3 != nb2, and a3 of one radius."""
+    L = 1 << J
+    g = torch.Generator(device="cuda").manual_seed(100 + J)
+    et = torch.randn((L, L, L), generator=g, device="cuda", dtype=torch.float32)
+    P = phi_power_device(PHI, L, 1, 1024, "cuda")
+    spec = rfft_field(et)
+    radii = list(np.linspace(1.0, 0.3 * L, 15))
+    l, m = 5, 3
+    fi = mp.multipole_fields(spec, J, l, m, radii, P)
+    fb = mp.multipole_fields(spec, J, l, m, radii, P, bin_major=True)
+    assert fb.shape == (15, L ** 3)
+    assert torch.equal(fb, fi[:, :15].t())
+    kw = dict(chunk_x=chunk_x, ctas_per_sm=ctas)
+    s_i = mp.multipole_contract_engine(et, fi, 15, GAM, J, conj_sign=-1, **kw)
+    s_b = mp.multipole_contract_engine(et, fb, 15, GAM, J, conj_sign=-1, bin_major=True, **kw)
+    assert mp.contract_status(J) == 0
+    assert np.array_equal(s_i, s_b)
+    r3 = radii[2:9]
+    gi = mp.multipole_fields(spec, J, l, -m, r3, P)
+    gb = mp.multipole_fields(spec, J, l, -m, r3, P, bin_major=True)
+    s_i = mp.multipole_contract_engine(et, fi, 15, GAM, J, fields3=gi, nb3=7, **kw)
+    s_b = mp.multipole_contract_engine(et, fb, 15, GAM, J, fields3=gb, nb3=7, bin_major=True, **kw)
+    assert np.array_equal(s_i, s_b)
+    h_i = mp.multipole_fields(spec, J, l, -m, [radii[4]], P)
+    h_b = mp.multipole_fields(spec, J, l, -m, [radii[4]], P, bin_major=True)
+    assert torch.equal(h_i, h_b)
+    s_i = mp.multipole_contract_engine(et, fi, 15, GAM, J, fields3=h_i, nb3=1, **kw)
+    s_b = mp.multipole_contract_engine(et, fb, 15, GAM, J, fields3=h_b, nb3=1, bin_major=True, **kw)
+    assert np.array_equal(s_i, s_b)
+    s_i = mp.multipole_contract_engine(et, h_i, 1, GAM, J, fields3=gi, nb3=7, **kw)
+    s_b = mp.multipole_contract_engine(et, h_b, 1, GAM, J, fields3=gb, nb3=7, bin_major=True, **kw)
+    assert np.array_equal(s_i, s_b)
+    assert mp.contract_status(J) == 0
