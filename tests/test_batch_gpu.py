@@ -3,8 +3,9 @@
 The batch shares bin windows, runs four catalogues' pair products in one
 pass and replays one CUDA graph of the multipole (l, m) loop per J with an
 autotuned contraction tile.  2PCF results must match the one-at-a-time path
-to 1e-9 relative (same kernels); 3PCF products to 1e-5 relative (the
-autotuned tile changes the float32 grouping of the cell sums).  A second
+to 1e-9 relative (same kernels); 3PCF products to 1e-4 relative, the
+bound of the mixed-precision (tensor-core) contraction: the autotuned tile
+changes which cells one work item's FP32 tensor-memory accumulator sums.  A second
 replay of the captured graph must reproduce the first exactly.
 """
 import numpy as np
@@ -30,8 +31,8 @@ def test_batch_pipeline_matches_one_at_a_time():
     assert set(bp.tiles) == {5, 6}
     for r, g in zip(ref, got):
         assert _rel(g["xi"], r["xi"]) < 1e-9
-        assert _rel(g["delta_ddd_l"], r["delta_ddd_l"]) < 1e-5
-        assert _rel(g["zeta_l"], r["zeta_l"]) < 1e-5
+        assert _rel(g["delta_ddd_l"], r["delta_ddd_l"]) < 1e-4
+        assert _rel(g["zeta_l"], r["zeta_l"]) < 1e-4
     again = bp.run(cats)
     for g, a in zip(got, again):
         np.testing.assert_array_equal(g["delta_ddd_l"], a["delta_ddd_l"])
