@@ -62,7 +62,7 @@ def build(force=False, verbose=False, extra_flags=()):
     extra = list(extra_flags)
     if verbose:
         extra += ["-Xptxas", "-v"]
-    with concurrent.futures.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
+    with concurrent.futures.ThreadPoolExecutor(max_workers=max(1, min(16, os.cpu_count() or 1, len(srcs)))) as ex:
         results = list(ex.map(lambda s: _compile(s, extra), srcs))
     if verbose:
         for (_, log), s in zip(results, srcs):

@@ -887,19 +887,32 @@ __device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
 }
 
 // a3 plane x_a from bin-major fields (bin b at src3 + b * bstride) -> buf
-// [16][kA3P] float2; bins nb3 .. 15 are written as zeros.
+// [16][kA3P] float2; bins nb3 .. 15 are written as zeros.  Thread t copies
+// bin t >> 4, cells (t & 15) + 16 i (i < 9) of the 12 x 12 plane, so the bin
+// base is computed once and the (row, column) of the next cell is one step
+// on (16 cells = one row of 12 and 4 columns).
 __device__ __forceinline__ void ct_stage_a3_bm(const float2* __restrict__ src3, long long bstride, int nb3,
                                                float2* buf, int xa, int y0, int z0, int L, int Lm) {
-  constexpr int kPlane = ct::HY * ct::HZ;
-  const long long xb = (long long)(xa & Lm) * L;
-  for (int c = threadIdx.x; c < kBinStride * kPlane; c += ct::kThreads) {
-    const int bb = c / kPlane, cell = c - bb * kPlane;
-    const int hy = cell / ct::HZ, hz = cell - hy * ct::HZ;
-    float2* dst = buf + bb * tcc::kA3P + cell;
-    if (bb < nb3)
-      cp_async8(dst, src3 + bb * bstride + (xb + ((y0 - 2 + hy) & Lm)) * L + ((z0 - 2 + hz) & Lm));
-    else
-      *dst = make_float2(0.f, 0.f);
+  static_assert(ct::kThreads == 16 * kBinStride && ct::HY * ct::HZ == 16 * 9 && ct::HZ == 12, "a3 staging map");
+  const int bb = threadIdx.x >> 4, j = threadIdx.x & 15;
+  float2* dst = buf + bb * tcc::kA3P + j;
+  if (bb < nb3) {
+    const float2* src = src3 + bb * bstride + (long long)(xa & Lm) * L * L;
+    int hy = j >= ct::HZ ? 1 : 0;
+    int hz = j - hy * ct::HZ;
+#pragma unroll 1
+    for (int i = 0; i < 9; ++i) {
+      cp_async8(dst + 16 * i, src + ((y0 - 2 + hy) & Lm) * L + ((z0 - 2 + hz) & Lm));
+      hz += 4;
+      hy += 1;
+      if (hz >= ct::HZ) {
+        hz -= ct::HZ;
+        hy += 1;
+      }
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < 9; ++i) dst[16 * i] = make_float2(0.f, 0.f);
   }
 }
 

@@ -1,0 +1,11 @@
+// pair_products_kernel<1>: 1 spectrum pair(s) per pass (see pair_products.cuh).
+#include "pair_products.cuh"
+
+namespace hermes {
+
+HERMES_PP_LAUNCHER(1) {
+  pair_products_kernel<1><<<grid, kPPThreads, smem, s>>>(a, wins, pd, partial, k0);
+  return cudaGetLastError();
+}
+
+}  // namespace hermes
