@@ -841,9 +841,11 @@ constexpr int kRawBytes = 64 * kBinStride * 8;             // TMA a2 plane: 64 c
 constexpr int kTmemCols = 128;                             // D: 96 columns used
 constexpr int kN = 96;
 // a3 plane buffer: [cell][16] (bin-interleaved fields) or [16][kA3P]
-// (bin-major fields; kA3P = 145 = 1 mod 16 puts the 16 bins of one cell on
-// distinct bank pairs)
-constexpr int kA3P = ct::HY * ct::HZ + 1;
+// (bin-major fields).  kA3P = 146: rows stay 16-byte aligned, so a plane is
+// staged with 16-byte copies and a thread reads two cells of its bin with
+// one 16-byte load; the 16 bins of one cell start 4 banks apart, so a
+// quarter-warp's 16-byte loads cover all 32 banks once (no conflict).
+constexpr int kA3P = ct::HY * ct::HZ + 2;
 constexpr int kA3Buf = kBinStride * kA3P;
 static_assert(kA3Buf >= ct::kA3Plane, "a3 buffer");
 constexpr uint32_t kIdesc = hermes::tc::idesc_bf16_f32(128, kN, true, true);
@@ -887,32 +889,37 @@ __device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
 }
 
 // a3 plane x_a from bin-major fields (bin b at src3 + b * bstride) -> buf
-// [16][kA3P] float2; bins nb3 .. 15 are written as zeros.  Thread t copies
-// bin t >> 4, cells (t & 15) + 16 i (i < 9) of the 12 x 12 plane, so the bin
-// base is computed once and the (row, column) of the next cell is one step
-// on (16 cells = one row of 12 and 4 columns).
+// [16][kA3P] float2; bins nb3 .. 15 are written as zeros.  The copies are
+// 16 bytes, two cells (2p, 2p + 1) of one row: with z0 a multiple of 8 the
+// pair starts at an even z and never straddles the periodic wrap, so both
+// ends are 16-byte aligned.  Thread t copies bin t >> 4, pairs
+// p = (t & 15) + 16 i of the 72 in the 12 x 12 plane; the (row, pair
+// column) of the next one is a fixed step (16 pairs = two rows of 6 and 4).
 __device__ __forceinline__ void ct_stage_a3_bm(const float2* __restrict__ src3, long long bstride, int nb3,
                                                float2* buf, int xa, int y0, int z0, int L, int Lm) {
-  static_assert(ct::kThreads == 16 * kBinStride && ct::HY * ct::HZ == 16 * 9 && ct::HZ == 12, "a3 staging map");
+  static_assert(ct::kThreads == 16 * kBinStride && ct::HY * ct::HZ == 144 && ct::HZ == 12 && ct::TZ % 8 == 0,
+                "a3 staging map");
+  constexpr int kPairs = ct::HY * ct::HZ / 2;  // 72
   const int bb = threadIdx.x >> 4, j = threadIdx.x & 15;
-  float2* dst = buf + bb * tcc::kA3P + j;
+  float2* dst = buf + bb * tcc::kA3P + 2 * j;
+  const int n = j < kPairs - 64 ? 5 : 4;
   if (bb < nb3) {
     const float2* src = src3 + bb * bstride + (long long)(xa & Lm) * L * L;
-    int hy = j >= ct::HZ ? 1 : 0;
-    int hz = j - hy * ct::HZ;
+    int hy = j / 6;
+    int hz = 2 * (j - 6 * hy);
 #pragma unroll 1
-    for (int i = 0; i < 9; ++i) {
-      cp_async8(dst + 16 * i, src + ((y0 - 2 + hy) & Lm) * L + ((z0 - 2 + hz) & Lm));
-      hz += 4;
-      hy += 1;
+    for (int i = 0; i < n; ++i) {
+      cp_async16(dst + 32 * i, src + ((y0 - 2 + hy) & Lm) * L + ((z0 - 2 + hz) & Lm));
+      hz += 8;
+      hy += 2;
       if (hz >= ct::HZ) {
         hz -= ct::HZ;
         hy += 1;
       }
     }
   } else {
-#pragma unroll
-    for (int i = 0; i < 9; ++i) dst[16 * i] = make_float2(0.f, 0.f);
+#pragma unroll 1
+    for (int i = 0; i < n; ++i) *reinterpret_cast<float4*>(dst + 32 * i) = make_float4(0.f, 0.f, 0.f, 0.f);
   }
 }
 
@@ -1045,10 +1052,18 @@ mp_contract_tc_kernel(ContractArgs A, const __grid_constant__ CUtensorMap a2map)
 #pragma unroll
         for (int r = 0; r < 6; ++r) {
           float2 av[6];
+          if (kBM) {  // two cells per 16-byte load (cz even, kA3P even)
+            const float4* row4 = reinterpret_cast<const float4*>(ap + b * tcc::kA3P + (cy + r) * ct::HZ + cz);
 #pragma unroll
-          for (int k = 0; k < 6; ++k)
-            av[k] = kBM ? ap[b * tcc::kA3P + (cy + r) * ct::HZ + cz + k]
-                        : ap[((cy + r) * ct::HZ + cz + k) * kBinStride + b];
+            for (int k = 0; k < 3; ++k) {
+              const float4 p = row4[k];
+              av[2 * k] = make_float2(p.x, p.y);
+              av[2 * k + 1] = make_float2(p.z, p.w);
+            }
+          } else {
+#pragma unroll
+            for (int k = 0; k < 6; ++k) av[k] = ap[((cy + r) * ct::HZ + cz + k) * kBinStride + b];
+          }
           // Rz_{l1z}(row, cz + dz) = sum_{l2z} Gamma[l1z][l2z] a3(row, cz + dz + l1z - l2z)
           float2 rz[2][3];
 #pragma unroll
