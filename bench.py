@@ -316,52 +316,66 @@ def deposit_field(pos_t, w_t, J, phi_t, ws):
 
 
 def deposit_bench(dev, lib, kernels, phi, flush, steps):
-    """The 4M-point J=9 deposit: Mparticles/s and the accumulate kernel roofline."""
+    """The 4M-point J=9 deposit: Mparticles/s and the accumulate kernel
+    roofline, with the tile the deposit autotuner picks for this catalogue
+    (the default 8x16x32 tile timed beside it)."""
     import torch
 
-    from pyhermes_gb300 import _lib, synthetic
+    from pyhermes_gb300 import _lib, autotune, synthetic
 
     pos_np, w_np = synthetic.lognormal_catalogue(DEP_N, box=BOX, device=dev)
     pos = torch.as_tensor(pos_np, device=dev)
     pw = torch.as_tensor(w_np / w_np.sum(), device=dev)
     L = 1 << DEP_J
     eps = torch.empty((L, L, L), dtype=torch.float32, device=dev)
-    buf = kernels.DepositWorkspace(dev).get(DEP_N, DEP_J)
     sptr = torch.cuda.current_stream(dev).cuda_stream
     P = ctypes.c_void_p
-
-    def sort():
-        _lib.check(lib.hermes_deposit_sort(P(pos.data_ptr()), P(pw.data_ptr()), DEP_N, DEP_J, BOX,
-                                           P(phi.data_ptr()), phi.numel(), 1024, P(buf.data_ptr()),
-                                           buf.numel(), sptr), "sort")
-
-    def accumulate():
-        _lib.check(lib.hermes_deposit_accumulate(DEP_N, DEP_J, BOX, P(phi.data_ptr()), phi.numel(), 1024,
-                                                 P(eps.data_ptr()), None, None, P(buf.data_ptr()),
-                                                 buf.numel(), sptr), "accumulate")
-
-    for _ in range(3):
-        sort()
-        accumulate()
     stream = torch.cuda.current_stream(dev)
-    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(steps)]
-    torch.cuda.synchronize(dev)
-    for k in range(steps):
-        flush.zero_()
-        ev[k][0].record(stream)
-        sort()
-        ev[k][1].record(stream)
-        accumulate()
-        ev[k][2].record(stream)
-    torch.cuda.synchronize(dev)
-    step_ms = [e[0].elapsed_time(e[2]) for e in ev]
-    acc_ms = sum(e[1].elapsed_time(e[2]) for e in ev) / steps
+
+    def measure():
+        buf = kernels.DepositWorkspace(dev).get(DEP_N, DEP_J)  # sized for the level's current tile
+
+        def sort():
+            _lib.check(lib.hermes_deposit_sort(P(pos.data_ptr()), P(pw.data_ptr()), DEP_N, DEP_J, BOX,
+                                               P(phi.data_ptr()), phi.numel(), 1024, P(buf.data_ptr()),
+                                               buf.numel(), sptr), "sort")
+
+        def accumulate():
+            _lib.check(lib.hermes_deposit_accumulate(DEP_N, DEP_J, BOX, P(phi.data_ptr()), phi.numel(), 1024,
+                                                     P(eps.data_ptr()), None, None, P(buf.data_ptr()),
+                                                     buf.numel(), sptr), "accumulate")
+
+        for _ in range(3):
+            sort()
+            accumulate()
+        ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(steps)]
+        torch.cuda.synchronize(dev)
+        for k in range(steps):
+            flush.zero_()
+            ev[k][0].record(stream)
+            sort()
+            ev[k][1].record(stream)
+            accumulate()
+            ev[k][2].record(stream)
+        torch.cuda.synchronize(dev)
+        step_ms = sum(e[0].elapsed_time(e[2]) for e in ev) / steps
+        acc_ms = sum(e[1].elapsed_time(e[2]) for e in ev) / steps
+        return step_ms, acc_ms
+
+    autotune.set_deposit_tile(DEP_J, (0, 0, 0))
+    default_step, default_acc = measure()
+    tile, tile_ms = autotune.tune_deposit(pos, pw, DEP_J, BOX, phi)
+    step_ms, acc_ms = measure()
+    autotune.set_deposit_tile(DEP_J, (0, 0, 0))
     hbm, _, kind = load_peaks()
     alg = DEP_N * 16 + L ** 3 * 4
     ach = alg / (acc_ms / 1e3) / 1e9
     return {"metric": "deposit Mparticles/s (4M lognormal points, J=9, float32 field)",
-            "value": DEP_N / (sum(step_ms) / steps / 1e3) / 1e6, "unit": "Mparticles/s",
-            "ms_per_step": sum(step_ms) / steps, "launches_per_step": 7,
+            "value": DEP_N / (step_ms / 1e3) / 1e6, "unit": "Mparticles/s",
+            "ms_per_step": step_ms, "launches_per_step": 7,
+            "tile": "x".join(map(str, tile)), "tile_ms_per_deposit": tile_ms,
+            "default_tile": {"tile": "8x16x32", "ms_per_step": default_step, "accumulate_ms": default_acc,
+                             "value": DEP_N / (default_step / 1e3) / 1e6},
             "roofline": {"kernel": "dep_accum_kernel", "bound": "hbm", "achieved": ach, "peak": hbm,
                          "peak_kind": kind, "unit": "GB/s", "frac": ach / hbm,
                          "traffic": profile_traffic("dep_accum_kernel"),
@@ -380,7 +394,7 @@ def c4_bench(dev, phi_np):
     l <= 1 per J and scaled by samples and (l, m) terms."""
     import torch
 
-    from pyhermes_gb300 import batch
+    from pyhermes_gb300 import autotune, batch
     from pyhermes_gb300 import multipole as mp
 
     cats = batch.c4_catalogues(64, box=BOX, device=dev)
@@ -392,6 +406,9 @@ def c4_bench(dev, phi_np):
     res_b = bp.run(cats)
     torch.cuda.synchronize(dev)
     t_b = time.perf_counter() - t0
+    # the one-at-a-time path runs with the default deposit tiles
+    for j in (7, 8, 9):
+        autotune.set_deposit_tile(j, (0, 0, 0))
     batch.run_one_at_a_time(warm, box=BOX, device=dev)
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
@@ -430,6 +447,7 @@ def c4_bench(dev, phi_np):
             "points_total": int(sum(len(c["weights"]) for c in cats)),
             "max_rel_diff_zeta_batched_vs_one_at_a_time": diff, "max_rel_diff_xi": diff_xi,
             "tiles": {str(k): {"chunk_x": v["chunk_x"], "ctas_per_sm": v["ctas_per_sm"]} for k, v in bp.tiles.items()},
+            "deposit_tiles": {str(k): v["tile"] for k, v in bp.deposit_tiles.items()},
             "graph": "one CUDA graph per J: rFFT + 28 x (radial multipole fields + contraction)"}
 
 

@@ -82,7 +82,9 @@ int hermes_deposit_accumulate(int64_t n, int J, double box, const double* phi,
  * it until exit).  Limits: n <= 131072 particles, J <= 8; larger requests
  * return HERMES_ERR_INVALID.  The first call on a device looks up the
  * array's device address (cudaGetSymbolAddress), so make that first call
- * before any stream capture.  All calls share the one array: calls whose
+ * before any stream capture; the address is kept for the life of the
+ * process, so it is not valid after cudaDeviceReset or in a second CUDA
+ * context on the same device.  All calls share the one array: calls whose
  * work overlaps on the GPU (other streams, other host threads) race. */
 int hermes_deposit_noalloc(const double* pos, const double* w, int64_t n, int J,
                            double box, const double* phi, int n_phi, int phi_res,
@@ -92,6 +94,19 @@ int hermes_deposit_noalloc(const double* pos, const double* w, int64_t n, int J,
  * workspace of the last hermes_deposit issued with it. */
 int hermes_deposit_status(const void* workspace, int64_t* n_rejected,
                           void* stream);
+/* Tile shape (cells along x, y, z) of the deposit accumulation at grid level
+ * J, for hermes_deposit, hermes_deposit_sort / _accumulate and
+ * hermes_deposit_workspace_size from this call on, process-wide.  No
+ * counterpart in the reference (its deposit has no tiles): it is the control
+ * the deposit tile autotuner sets.  Powers of two; x and y in [4, 128], z in
+ * [4, 128]; at most 16384 cells; (0, 0, 0) restores the default 8 x 16 x 32.
+ * A tile larger than the grid is clipped to it.  The field is the same bit
+ * for bit for every tile (integer fixed-point sums); the workspace size
+ * depends on the tile, so query it after setting the tile, and do not change
+ * the tile of a level while another thread deposits at it.
+ * hermes_deposit_noalloc always uses the default tile. */
+int hermes_deposit_set_tile(int J, int tx, int ty, int tz);
+int hermes_deposit_get_tile(int J, int* tx, int* ty, int* tz);
 
 /* ---- spectral windows ------------------------------------------------------
  * Built-in window transfer functions (utils/window_functions.py:441-458),

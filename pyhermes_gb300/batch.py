@@ -18,7 +18,9 @@ what is batched is the GPU work:
   multipole fields and the contraction -- is one CUDA graph per J
   (``GraphedMultipole``), replayed per catalogue with no host round trip
   inside; its contraction tile (x-chunk, CTAs per SM) comes from
-  ``autotune.tune_contract``.
+  ``autotune.tune_contract``;
+* the deposit tile of each J is tuned on the group's first catalogue
+  (``autotune.tune_deposit``; the field does not depend on it).
 
 ``run_one_at_a_time`` is the unbatched path through the public classes.
 ``c4_catalogues`` builds the uneven catalogue set (sizes log-uniform in
@@ -109,6 +111,7 @@ class BatchPipeline:
         self.use_graph = use_graph
         self.engines = {}
         self.tiles = {}
+        self.deposit_tiles = {}
         self.timing = {}
 
     def _engine(self, J, phi):
@@ -121,6 +124,15 @@ class BatchPipeline:
                                                   ctas_per_sm=ctas, use_graph=self.use_graph)
         return self.engines[J]
 
+    def _tune_deposit(self, J, cat):
+        from .phi import sample_scaling_function
+
+        pos = torch.as_tensor(np.asarray(cat["pos"], dtype=np.float64), device=self.device)
+        w = torch.as_tensor(np.asarray(cat["weights"], dtype=np.float64), device=self.device)
+        phi = torch.as_tensor(sample_scaling_function(), device=self.device)
+        tile, ms = autotune.tune_deposit(pos, w, J, self.box, phi)
+        self.deposit_tiles[J] = {"tile": "x".join(map(str, tile)), "ms": ms}
+
     def run(self, cats, group_size=4):
         """Results in input order: dicts with xi, delta_dd, delta_ddd_l, zeta_l."""
         results = [None] * len(cats)
@@ -130,6 +142,8 @@ class BatchPipeline:
             by_j.setdefault(cats[i]["J"], []).append(i)
         pairs = [(a, b) for a in self.radii for b in self.radii]
         for J, idxs in by_j.items():
+            if self.autotune_tiles and J not in self.deposit_tiles:
+                self._tune_deposit(J, cats[idxs[0]])
             windows = None
             for g0 in range(0, len(idxs), group_size):
                 grp = idxs[g0:g0 + group_size]

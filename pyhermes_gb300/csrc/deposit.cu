@@ -23,6 +23,7 @@
 // neighbour tile, so a CTA reads only records that reach it.
 #include <math.h>
 
+#include <atomic>
 #include <mutex>
 
 #include "hermes_common.cuh"
@@ -30,7 +31,15 @@
 namespace {
 
 constexpr int kMaxSupport = 4;
-constexpr int kTileX = 8, kTileY = 16, kTileZ = 32;
+constexpr int kTileX = 8, kTileY = 16, kTileZ = 32;  // default tile (cells)
+constexpr int kMaxTileCells = 16384;                  // 128 KB int64 + 64 KB counts of shared memory
+constexpr int kMaxJ = 10;
+
+// Tile shape per grid level J chosen by hermes_deposit_set_tile (0 = the
+// default), packed as tx | ty << 8 | tz << 16 (each a power of two <= 128).
+std::atomic<int> g_tile[kMaxJ + 1];
+
+int pack_tile(int tx, int ty, int tz) { return tx | (ty << 8) | (tz << 16); }
 constexpr int kAccThreads = 256;
 constexpr int kScanChunk = 4096;  // elements per scan block (1024 threads x 4)
 constexpr unsigned kRejected = 0xFFFFFFFFu;
@@ -616,8 +625,9 @@ struct DepPlan {
   size_t ws_bytes;
 };
 
-int dep_plan(int64_t n, int J, int S, int res, DepPlan* p) {
-  if (J < 2 || J > 10) return hermes::fail(HERMES_ERR_INVALID, "deposit: J=%d outside [2,10]", J);
+// tile: packed tile shape, 0 for the default.
+int dep_plan(int64_t n, int J, int S, int res, DepPlan* p, int tile) {
+  if (J < 2 || J > kMaxJ) return hermes::fail(HERMES_ERR_INVALID, "deposit: J=%d outside [2,%d]", J, kMaxJ);
   if (n < 0 || n > 0x7FFFFFFFLL) return hermes::fail(HERMES_ERR_INVALID, "deposit: n=%lld outside [0,2^31)", (long long)n);
   if (S < 1 || S > kMaxSupport) return hermes::fail(HERMES_ERR_INVALID, "deposit: phi support %d outside [1,%d]", S, kMaxSupport);
   if (res < 1 || res > 1024) return hermes::fail(HERMES_ERR_INVALID, "deposit: phi_res %d outside [1,1024]", res);
@@ -625,9 +635,11 @@ int dep_plan(int64_t n, int J, int S, int res, DepPlan* p) {
   g.L = 1 << J;
   g.S = S;
   g.res = res;
-  g.tx = g.L < kTileX ? g.L : kTileX;
-  g.ty = g.L < kTileY ? g.L : kTileY;
-  g.tz = g.L < kTileZ ? g.L : kTileZ;
+  const int tx = tile ? (tile & 0xFF) : kTileX, ty = tile ? ((tile >> 8) & 0xFF) : kTileY,
+            tz = tile ? ((tile >> 16) & 0xFF) : kTileZ;
+  g.tx = g.L < tx ? g.L : tx;
+  g.ty = g.L < ty ? g.L : ty;
+  g.tz = g.L < tz ? g.L : tz;
   if (S - 1 > g.tx) return hermes::fail(HERMES_ERR_INVALID, "deposit: grid too small for support");
   g.res_log2 = (res & (res - 1)) == 0 ? __builtin_ctz((unsigned)res) : -1;
   g.tx_log2 = __builtin_ctz((unsigned)g.tx);
@@ -652,15 +664,49 @@ int dep_plan(int64_t n, int J, int S, int res, DepPlan* p) {
   return HERMES_OK;
 }
 
-}  // namespace
+// the tile set for level J (0: default)
+int tile_for(int J) { return (J >= 0 && J <= kMaxJ) ? g_tile[J].load(std::memory_order_relaxed) : 0; }
 
-extern "C" int hermes_deposit_workspace_size(int64_t n, int J, size_t* bytes) {
+int workspace_size(int64_t n, int J, int tile, size_t* bytes) {
   if (!bytes) return hermes::fail(HERMES_ERR_INVALID, "deposit: bytes is NULL");
   DepPlan p;
-  int rc = dep_plan(n, J, 3, 1024, &p);
+  int rc = dep_plan(n, J, 3, 1024, &p, tile);
   if (rc) return rc;
   *bytes = p.ws_bytes;
   return HERMES_OK;
+}
+
+}  // namespace
+
+extern "C" int hermes_deposit_set_tile(int J, int tx, int ty, int tz) {
+  if (J < 2 || J > kMaxJ) return hermes::fail(HERMES_ERR_INVALID, "deposit_set_tile: J=%d outside [2,%d]", J, kMaxJ);
+  if (tx == 0 && ty == 0 && tz == 0) {
+    g_tile[J].store(0);
+    return HERMES_OK;
+  }
+  auto pow2 = [](int v) { return v > 0 && (v & (v - 1)) == 0; };
+  if (!pow2(tx) || !pow2(ty) || !pow2(tz) || tx < kMaxSupport || ty < kMaxSupport || tz < 4 || tx > 128 ||
+      ty > 128 || tz > 128 || tx * ty * tz > kMaxTileCells)
+    return hermes::fail(HERMES_ERR_INVALID,
+                        "deposit_set_tile: tile %dx%dx%d must be powers of two, x and y in [%d, 128], z in [4, 128], "
+                        "at most %d cells", tx, ty, tz, kMaxSupport, kMaxTileCells);
+  g_tile[J].store(pack_tile(tx, ty, tz));
+  return HERMES_OK;
+}
+
+extern "C" int hermes_deposit_get_tile(int J, int* tx, int* ty, int* tz) {
+  if (J < 2 || J > kMaxJ || !tx || !ty || !tz) return hermes::fail(HERMES_ERR_INVALID, "deposit_get_tile: bad argument");
+  const int t = tile_for(J);
+  const int L = 1 << J;
+  const int x = t ? (t & 0xFF) : kTileX, y = t ? ((t >> 8) & 0xFF) : kTileY, z = t ? ((t >> 16) & 0xFF) : kTileZ;
+  *tx = x < L ? x : L;
+  *ty = y < L ? y : L;
+  *tz = z < L ? z : L;
+  return HERMES_OK;
+}
+
+extern "C" int hermes_deposit_workspace_size(int64_t n, int J, size_t* bytes) {
+  return workspace_size(n, J, tile_for(J), bytes);
 }
 
 namespace {
@@ -677,11 +723,11 @@ struct DepBuffers {
 };
 
 int dep_prepare(int64_t n, int J, double box, int n_phi, int phi_res, const double* phi,
-                void* workspace, size_t workspace_bytes, DepPlan* p, DepBuffers* b) {
+                void* workspace, size_t workspace_bytes, DepPlan* p, DepBuffers* b, int tile) {
   if (!(box > 0.0) || !isfinite(box)) return hermes::fail(HERMES_ERR_INVALID, "deposit: box must be finite and > 0");
   if (!phi || phi_res <= 0 || n_phi <= 0 || n_phi % phi_res)
     return hermes::fail(HERMES_ERR_INVALID, "deposit: n_phi=%d must be a positive multiple of phi_res=%d", n_phi, phi_res);
-  int rc = dep_plan(n, J, n_phi / phi_res, phi_res, p);
+  int rc = dep_plan(n, J, n_phi / phi_res, phi_res, p, tile);
   if (rc) return rc;
   p->g.scale = (double)p->g.L / box;
   if (!workspace || workspace_bytes < p->ws_bytes)
@@ -698,15 +744,12 @@ int dep_prepare(int64_t n, int J, double box, int n_phi, int phi_res, const doub
   return HERMES_OK;
 }
 
-}  // namespace
-
-extern "C" int hermes_deposit_sort(const double* pos, const double* w, int64_t n, int J,
-                                   double box, const double* phi, int n_phi, int phi_res,
-                                   void* workspace, size_t workspace_bytes, void* stream) {
+int deposit_sort(const double* pos, const double* w, int64_t n, int J, double box, const double* phi, int n_phi,
+                 int phi_res, void* workspace, size_t workspace_bytes, void* stream, int tile) {
   if (n > 0 && (!pos || !w)) return hermes::fail(HERMES_ERR_INVALID, "deposit: pos/w NULL");
   DepPlan p;
   DepBuffers b;
-  int rc = dep_prepare(n, J, box, n_phi, phi_res, phi, workspace, workspace_bytes, &p, &b);
+  int rc = dep_prepare(n, J, box, n_phi, phi_res, phi, workspace, workspace_bytes, &p, &b, tile);
   if (rc) return rc;
   cudaStream_t s = hermes::as_stream(stream);
   HERMES_CUDA_TRY(cudaMemsetAsync(b.st, 0, sizeof(DepStatus), s));
@@ -736,15 +779,14 @@ extern "C" int hermes_deposit_sort(const double* pos, const double* w, int64_t n
   return HERMES_OK;
 }
 
-extern "C" int hermes_deposit_accumulate(int64_t n, int J, double box, const double* phi,
-                                         int n_phi, int phi_res, float* eps_out,
-                                         double* eps_f64_out, uint32_t* counts_out,
-                                         void* workspace, size_t workspace_bytes, void* stream) {
+int deposit_accumulate(int64_t n, int J, double box, const double* phi, int n_phi, int phi_res, float* eps_out,
+                       double* eps_f64_out, uint32_t* counts_out, void* workspace, size_t workspace_bytes,
+                       void* stream, int tile) {
   if ((eps_out == nullptr) == (eps_f64_out == nullptr))
     return hermes::fail(HERMES_ERR_INVALID, "deposit: give exactly one of eps_out / eps_f64_out");
   DepPlan p;
   DepBuffers b;
-  int rc = dep_prepare(n, J, box, n_phi, phi_res, phi, workspace, workspace_bytes, &p, &b);
+  int rc = dep_prepare(n, J, box, n_phi, phi_res, phi, workspace, workspace_bytes, &p, &b, tile);
   if (rc) return rc;
   cudaStream_t s = hermes::as_stream(stream);
   const int ncell = p.g.tx * p.g.ty * p.g.tz;
@@ -766,16 +808,39 @@ extern "C" int hermes_deposit_accumulate(int64_t n, int J, double box, const dou
   return HERMES_OK;
 }
 
+int deposit_full(const double* pos, const double* w, int64_t n, int J, double box, const double* phi, int n_phi,
+                 int phi_res, float* eps_out, double* eps_f64_out, uint32_t* counts_out, void* workspace,
+                 size_t workspace_bytes, void* stream, int tile) {
+  if ((eps_out == nullptr) == (eps_f64_out == nullptr))
+    return hermes::fail(HERMES_ERR_INVALID, "deposit: give exactly one of eps_out / eps_f64_out");
+  int rc = deposit_sort(pos, w, n, J, box, phi, n_phi, phi_res, workspace, workspace_bytes, stream, tile);
+  if (rc) return rc;
+  return deposit_accumulate(n, J, box, phi, n_phi, phi_res, eps_out, eps_f64_out, counts_out, workspace,
+                            workspace_bytes, stream, tile);
+}
+
+}  // namespace
+
+extern "C" int hermes_deposit_sort(const double* pos, const double* w, int64_t n, int J,
+                                   double box, const double* phi, int n_phi, int phi_res,
+                                   void* workspace, size_t workspace_bytes, void* stream) {
+  return deposit_sort(pos, w, n, J, box, phi, n_phi, phi_res, workspace, workspace_bytes, stream, tile_for(J));
+}
+
+extern "C" int hermes_deposit_accumulate(int64_t n, int J, double box, const double* phi,
+                                         int n_phi, int phi_res, float* eps_out,
+                                         double* eps_f64_out, uint32_t* counts_out,
+                                         void* workspace, size_t workspace_bytes, void* stream) {
+  return deposit_accumulate(n, J, box, phi, n_phi, phi_res, eps_out, eps_f64_out, counts_out, workspace,
+                            workspace_bytes, stream, tile_for(J));
+}
+
 extern "C" int hermes_deposit(const double* pos, const double* w, int64_t n, int J,
                               double box, const double* phi, int n_phi, int phi_res,
                               float* eps_out, double* eps_f64_out, uint32_t* counts_out,
                               void* workspace, size_t workspace_bytes, void* stream) {
-  if ((eps_out == nullptr) == (eps_f64_out == nullptr))
-    return hermes::fail(HERMES_ERR_INVALID, "deposit: give exactly one of eps_out / eps_f64_out");
-  int rc = hermes_deposit_sort(pos, w, n, J, box, phi, n_phi, phi_res, workspace, workspace_bytes, stream);
-  if (rc) return rc;
-  return hermes_deposit_accumulate(n, J, box, phi, n_phi, phi_res, eps_out, eps_f64_out, counts_out,
-                                   workspace, workspace_bytes, stream);
+  return deposit_full(pos, w, n, J, box, phi, n_phi, phi_res, eps_out, eps_f64_out, counts_out, workspace,
+                      workspace_bytes, stream, tile_for(J));
 }
 
 extern "C" int hermes_deposit_status(const void* workspace, int64_t* n_rejected, void* stream) {
@@ -840,7 +905,7 @@ extern "C" int hermes_deposit_noalloc(const double* pos, const double* w, int64_
     return hermes::fail(HERMES_ERR_INVALID, "deposit_noalloc: J=%d above %d (the built-in scratch limit)", J,
                         kNoAllocMaxJ);
   size_t need = 0;
-  int rc = hermes_deposit_workspace_size(n, J, &need);
+  int rc = workspace_size(n, J, 0, &need);  // always the default tile (the limits above assume it)
   if (rc) return rc;
   if (need > kNoAllocScratchBytes)
     return hermes::fail(HERMES_ERR_INVALID, "deposit_noalloc: needs %zu scratch bytes, built-in array has %zu",
@@ -850,6 +915,6 @@ extern "C" int hermes_deposit_noalloc(const double* pos, const double* w, int64_
   if (rc) return rc;
   // hermes_deposit_sort clears the status word and bucket counts it relies on;
   // everything else in the scratch is written before it is read.
-  return hermes_deposit(pos, w, n, J, box, phi, n_phi, phi_res, eps_out, eps_f64_out, counts_out, scratch,
-                        kNoAllocScratchBytes, stream);
+  return deposit_full(pos, w, n, J, box, phi, n_phi, phi_res, eps_out, eps_f64_out, counts_out, scratch,
+                      kNoAllocScratchBytes, stream, 0);
 }

@@ -29,6 +29,7 @@ def test_batch_pipeline_matches_one_at_a_time():
     bp = batch.BatchPipeline(lmax=2, radii=radii, edges=edges)
     got = bp.run(cats)
     assert set(bp.tiles) == {5, 6}
+    assert set(bp.deposit_tiles) == {5, 6}
     for r, g in zip(ref, got):
         assert _rel(g["xi"], r["xi"]) < 1e-9
         assert _rel(g["delta_ddd_l"], r["delta_ddd_l"]) < 1e-4

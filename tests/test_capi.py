@@ -35,3 +35,34 @@ def test_version_and_error_paths(lib):
     assert rc == -1
     assert b"J=15" in lib.hermes_last_error()
     assert lib.hermes_deposit_workspace_size(1000, 7, None) == -1
+
+
+def test_deposit_tile_setting(lib):
+    """The per-level deposit tile: validated, read back (clipped to the grid),
+    reflected in the workspace size, and reset to the default."""
+    t = [ctypes.c_int(0) for _ in range(3)]
+    refs = [ctypes.byref(v) for v in t]
+    assert lib.hermes_deposit_get_tile(7, *refs) == 0
+    assert [v.value for v in t] == [8, 16, 32]
+    base = ctypes.c_size_t(0)
+    assert lib.hermes_deposit_workspace_size(100000, 7, ctypes.byref(base)) == 0
+    try:
+        assert lib.hermes_deposit_set_tile(7, 4, 8, 16) == 0
+        assert lib.hermes_deposit_get_tile(7, *refs) == 0
+        assert [v.value for v in t] == [4, 8, 16]
+        small = ctypes.c_size_t(0)
+        assert lib.hermes_deposit_workspace_size(100000, 7, ctypes.byref(small)) == 0
+        assert small.value > base.value  # more tiles, more bucket counters
+        assert lib.hermes_deposit_set_tile(3, 16, 16, 32) == 0  # clipped to L = 8 on read
+        assert lib.hermes_deposit_get_tile(3, *refs) == 0
+        assert [v.value for v in t] == [8, 8, 8]
+        for bad in [(7, 3, 16, 32), (7, 2, 16, 32), (7, 8, 16, 2), (7, 256, 16, 32), (7, 32, 32, 32),
+                    (11, 8, 16, 32), (1, 8, 16, 32)]:
+            assert lib.hermes_deposit_set_tile(*bad) == -1, bad
+            assert b"deposit_set_tile" in lib.hermes_last_error()
+    finally:
+        assert lib.hermes_deposit_set_tile(7, 0, 0, 0) == 0
+        assert lib.hermes_deposit_set_tile(3, 0, 0, 0) == 0
+    again = ctypes.c_size_t(0)
+    assert lib.hermes_deposit_workspace_size(100000, 7, ctypes.byref(again)) == 0
+    assert again.value == base.value
