@@ -535,15 +535,19 @@ def mc_bench(dev, phi_np, steps):
     rng = np.random.default_rng(7)
     cen = torch.as_tensor(rng.uniform(0.0, L, (MC_CENTRES, 3)), device=dev)
     off = mc3pcf.rotation_offsets(50.0 * sc, 80.0 * sc, 0.5, MC_ROT, rng=np.random.RandomState(8))
-    for _ in range(2):
-        mc3pcf.triplet_sum(lp.e1, lp.e2, lp.e3, DEP_J, cen, off, lp.phi_t)
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
-    for a, b in ev:
-        a.record(stream)
-        mc3pcf.triplet_sum(lp.e1, lp.e2, lp.e3, DEP_J, cen, off, lp.phi_t)
-        b.record(stream)
-    torch.cuda.synchronize(dev)
-    t_tr = sum(a.elapsed_time(b) for a, b in ev) / len(ev) / 1e3
+    def time_triplets(bricks):
+        for _ in range(2):
+            mc3pcf.triplet_sum(lp.e1, lp.e2, lp.e3, DEP_J, cen, off, lp.phi_t, bricks=bricks)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        for a, b in ev:
+            a.record(stream)
+            mc3pcf.triplet_sum(lp.e1, lp.e2, lp.e3, DEP_J, cen, off, lp.phi_t, bricks=bricks)
+            b.record(stream)
+        torch.cuda.synchronize(dev)
+        return sum(a.elapsed_time(b) for a, b in ev) / len(ev) / 1e3
+
+    t_c_order = time_triplets(False)  # fields in C order, as the reference stores them
+    t_tr = time_triplets(True)        # brick-layout copies (the default path)
     ntr = MC_CENTRES * MC_ROT
     hbm, _, kind = load_peaks()
     ach = ntr * 324 / t_tr / 1e9
@@ -584,12 +588,14 @@ def mc_bench(dev, phi_np, steps):
                      "efficiency_equal_wall_time": (se_u ** 2 * t_u) / (se_l ** 2 * t_l)})
     return {"metric": "uniform-MC triplet samples/s (J=9 lognormal field from 4e6 points)",
             "value": ntr / t_tr, "unit": "triplets/s", "ms_per_launch": t_tr * 1e3,
+            "c_order_fields": {"value": ntr / t_c_order, "ms_per_launch": t_c_order * 1e3},
             "sample": f"{MC_CENTRES} centres x {MC_ROT} rotations, r12=50, r13=80 Mpc/h, mu=0.5",
-            "roofline": {"kernel": "mc_triplet_kernel", "bound": "hbm", "achieved": ach, "peak": hbm,
+            "roofline": {"kernel": "mc_triplet_kernel<bricks>", "bound": "hbm", "achieved": ach, "peak": hbm,
                          "peak_kind": kind, "unit": "GB/s", "frac": ach / hbm,
                          "algorithmic_bytes_per_triplet": 324,
                          "traffic": profile_traffic("mc_triplet_kernel"),
-                         "note": "3 x 27 float32 gathers per triplet over Morton-ordered centres"},
+                         "note": "3 x 27 float32 gathers per triplet over Morton-ordered centres, fields in "
+                                 "2x2x2 bricks (one 32-byte sector each)"},
             "learned_proposal": {"train_samples": len(configs) * n_cen_train * n_rot_train,
                                  "train_s": t_train, "loss_first_last": [losses[0], losses[-1]],
                                  "pool_factor": pool_factor, "replicates": replicates, "tests": rows}}

@@ -371,6 +371,27 @@ int hermes_mc_sample(const float* eps1, const float* eps2, const float* eps3, in
                      const double* phi, int n_phi, int phi_res, double* sums_out,
                      void* workspace, size_t workspace_bytes, void* stream);
 
+/* The Monte Carlo gathers on fields in a brick layout (no counterpart in the
+ * reference, whose fields are C order): hermes_field_to_bricks copies a
+ * float32 [L^3] C-order field into 2 x 2 x 2 bricks of 32 bytes (one DRAM
+ * sector; bricks in C order of the brick coordinates, the 8 cells of a
+ * brick in (x, y, z) bit order), so a 27-point interpolation reads exactly 8
+ * sectors instead of 9 rows of 1-2 sectors.  hermes_mc_triplets_bricks and
+ * hermes_mc_sample_bricks take the same arguments as hermes_mc_triplets and
+ * hermes_mc_sample with eps1..eps3 in that layout and return the same values
+ * bit for bit (the same float32 products in the same order). */
+int hermes_field_to_bricks(const float* field, int J, float* bricks, void* stream);
+int hermes_mc_triplets_bricks(const float* eps1, const float* eps2, const float* eps3, int J,
+                              const double* centers, const double* center_w, int64_t n_centers,
+                              const double* offsets, int n_rot, const double* phi, int n_phi,
+                              int phi_res, double rho1, double* sum_out, float* samples_out,
+                              void* workspace, size_t workspace_bytes, void* stream);
+int hermes_mc_sample_bricks(const float* eps1, const float* eps2, const float* eps3, int J,
+                            const double* pool, int64_t M, const int64_t* idx, const double* weights,
+                            const double* offsets, int64_t n, double R1, double R2, double mu,
+                            uint64_t seed, const double* phi, int n_phi, int phi_res,
+                            double* sums_out, void* workspace, size_t workspace_bytes, void* stream);
+
 /* ---- learned proposal network (no reference counterpart) ---------------------
  * A tanh MLP with dims[0] inputs, dims[n_layers] outputs, widths <= 128:
  * params = per layer W [in][out] then b [out] (float32).  forward writes

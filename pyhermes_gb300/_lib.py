@@ -68,6 +68,12 @@ SIGNATURES = {
     "hermes_interp": (_c_int, [_p, _c_int, _p, _c_i64, _p, _c_int, _c_int, _dbl, _dbl, _dbl, _p, _p, _c_sz, _p]),
     "hermes_mc_triplets": (_c_int, [_p, _p, _p, _c_int, _p, _p, _c_i64, _p, _c_int, _p, _c_int, _c_int, _dbl,
                                     ctypes.POINTER(_dbl), _p, _p, _c_sz, _p]),
+    "hermes_mc_triplets_bricks": (_c_int, [_p, _p, _p, _c_int, _p, _p, _c_i64, _p, _c_int, _p, _c_int, _c_int, _dbl,
+                                           ctypes.POINTER(_dbl), _p, _p, _c_sz, _p]),
+    "hermes_mc_sample_bricks": (_c_int, [_p, _p, _p, _c_int, _p, ctypes.c_int64, _p, _p, _p, ctypes.c_int64,
+                                         ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_uint64, _p,
+                                         _c_int, _c_int, _p, _p, _c_sz, _p]),
+    "hermes_field_to_bricks": (_c_int, [_p, _c_int, _p, _p]),
     "hermes_mlp_infer_tc": (_c_int, [_p, _p, _c_int, _p, _c_i64, _p, _p, _p]),
     "hermes_poisson_grad": (_c_int, [_p, _p, _c_i64, _p, ctypes.POINTER(_dbl), _p, _p]),
     "hermes_mlp_param_count": (_c_int, [_p, _c_int, ctypes.POINTER(_c_i64)]),

@@ -25,7 +25,21 @@ __device__ __forceinline__ void mc_axis(double s, int res, int L, int& c, int& f
   f = fi < 0 ? 0 : (fi >= res ? res - 1 : fi);
 }
 
+// Index of cell (x, y, z) of an L^3 field: C order (z fastest), or the brick
+// layout of hermes_field_to_bricks: 2 x 2 x 2 bricks of 32 bytes (one DRAM
+// sector) in C order of the brick coordinates, the 8 cells of a brick in
+// (x, y, z) bit order.  A 3 x 3 x 3 stencil then touches exactly 8 sectors,
+// against 9 rows of 1-2 sectors each in C order.
+template <bool kBricks>
+__device__ __forceinline__ size_t mc_cell(int x, int y, int z, int J) {
+  if (!kBricks) return (((size_t)x << J) + y) << J | (size_t)z;
+  const int h = J - 1;
+  const size_t brick = ((((size_t)(x >> 1) << h) + (y >> 1)) << h) + (z >> 1);
+  return brick << 3 | (size_t)((x & 1) << 2 | (y & 1) << 1 | (z & 1));
+}
+
 // 27-point interpolation of a float32 field at scaled position (sx, sy, sz).
+template <bool kBricks = false>
 __device__ __forceinline__ float mc_interp(const float* __restrict__ grid, const float* __restrict__ phis, int res,
                                            int J, double sx, double sy, double sz) {
   const int L = 1 << J;
@@ -43,11 +57,10 @@ __device__ __forceinline__ float mc_interp(const float* __restrict__ grid, const
     for (int b = 0; b < 3; ++b) {
       const int yg = (cy - b) & m;
       const float py = phis[fy + b * res];
-      const float* row = grid + (((size_t)xg << J) + yg) * (size_t)L;
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         const int zg = (cz - c) & m;
-        acc += __ldg(row + zg) * px * py * phis[fz + c * res];
+        acc += __ldg(grid + mc_cell<kBricks>(xg, yg, zg, J)) * px * py * phis[fz + c * res];
       }
     }
   }
@@ -68,6 +81,8 @@ __global__ void mc_interp_kernel(const float* __restrict__ grid, int J, const do
 // sum_i w_i n1_i sum_r n2(x_i + d2_r) n3(x_i + d3_r); n1 = eps1 interpolated
 // (box-random centres) or rho1 (particle centres: eps1 == NULL).  When
 // samples != NULL also writes the per-(centre, rotation) products f_ir.
+// kBricks: the fields are in the brick layout (mc_cell).
+template <bool kBricks>
 __global__ void __launch_bounds__(256)
 mc_triplet_kernel(const float* __restrict__ eps1, const float* __restrict__ eps2, const float* __restrict__ eps3,
                   int J, const double* __restrict__ centers, const double* __restrict__ cw, int64_t nc,
@@ -76,13 +91,13 @@ mc_triplet_kernel(const float* __restrict__ eps1, const float* __restrict__ eps2
   double acc = 0.0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += (int64_t)gridDim.x * blockDim.x) {
     const double x = centers[3 * i], y = centers[3 * i + 1], z = centers[3 * i + 2];
-    const float n1 = eps1 ? mc_interp(eps1, phis, res, J, x, y, z) : (float)rho1;
+    const float n1 = eps1 ? mc_interp<kBricks>(eps1, phis, res, J, x, y, z) : (float)rho1;
     const float w = cw ? (float)cw[i] : 1.f;
     float s = 0.f;
     for (int r = 0; r < n_rot; ++r) {
       const double* o = offsets + 6 * r;
-      const float n2 = mc_interp(eps2, phis, res, J, x + o[0], y + o[1], z + o[2]);
-      const float n3 = mc_interp(eps3, phis, res, J, x + o[3], y + o[4], z + o[5]);
+      const float n2 = mc_interp<kBricks>(eps2, phis, res, J, x + o[0], y + o[1], z + o[2]);
+      const float n3 = mc_interp<kBricks>(eps3, phis, res, J, x + o[3], y + o[4], z + o[5]);
       const float f = w * n1 * n2 * n3;
       if (samples) samples[i * n_rot + r] = f;
       s += f;
@@ -156,6 +171,7 @@ __device__ __forceinline__ void mc_triangle(double R1, double R2, double mu, dou
 // [n][6] or drawn (phi, cos theta1, alpha uniform, as the reference's three
 // uniforms); value f_k = w_k n1(c) n2(c + o1) n3(c + o2) (w_k = 1 when w is
 // NULL).  Block partial sums of f and f^2.
+template <bool kBricks>
 __global__ void __launch_bounds__(256)
 mc_sample_kernel(const float* __restrict__ eps1, const float* __restrict__ eps2, const float* __restrict__ eps3,
                  int J, const double* __restrict__ pool, long long M, const long long* __restrict__ idx,
@@ -182,9 +198,9 @@ mc_sample_kernel(const float* __restrict__ eps1, const float* __restrict__ eps2,
       mc_triangle(R1, R2, mu, a, 2.0 * bb - 1.0, c, o);
     }
     const double x = pool[3 * i], y = pool[3 * i + 1], z = pool[3 * i + 2];
-    const float n1 = mc_interp(eps1, phis, res, J, x, y, z);
-    const float n2 = mc_interp(eps2, phis, res, J, x + o[0], y + o[1], z + o[2]);
-    const float n3 = mc_interp(eps3, phis, res, J, x + o[3], y + o[4], z + o[5]);
+    const float n1 = mc_interp<kBricks>(eps1, phis, res, J, x, y, z);
+    const float n2 = mc_interp<kBricks>(eps2, phis, res, J, x + o[0], y + o[1], z + o[2]);
+    const float n3 = mc_interp<kBricks>(eps3, phis, res, J, x + o[3], y + o[4], z + o[5]);
     double f = (double)(n1 * n2 * n3);
     if (w) f *= w[k];
     acc += f;
@@ -204,6 +220,23 @@ mc_sample_kernel(const float* __restrict__ eps1, const float* __restrict__ eps2,
   if (threadIdx.x == 0) {
     partial[blockIdx.x] = sh[0][0];
     partial[gridDim.x + blockIdx.x] = sh[1][0];
+  }
+}
+
+// dst[mc_cell<true>(x, y, z)] = src[mc_cell<false>(x, y, z)]: one thread per
+// destination element, so the writes are contiguous; a warp's 32 reads are
+// 4 bricks = 8 rows of 2 cells.
+__global__ void mc_to_bricks_kernel(const float* __restrict__ src, int J, float* __restrict__ dst) {
+  const size_t n = (size_t)1 << (3 * J);
+  const int h = J - 1;
+  const size_t hm = ((size_t)1 << h) - 1;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const size_t brick = i >> 3;
+    const int c = (int)(i & 7);
+    const int x = (int)(((brick >> (2 * h)) & hm) << 1) | (c >> 2);
+    const int y = (int)(((brick >> h) & hm) << 1) | ((c >> 1) & 1);
+    const int z = (int)((brick & hm) << 1) | (c & 1);
+    dst[i] = __ldg(src + mc_cell<false>(x, y, z, J));
   }
 }
 
@@ -256,11 +289,10 @@ extern "C" int hermes_interp(const float* grid, int J, const double* scaled_pos,
   return HERMES_OK;
 }
 
-extern "C" int hermes_mc_triplets(const float* eps1, const float* eps2, const float* eps3, int J,
-                                  const double* centers, const double* center_w, int64_t n_centers,
-                                  const double* offsets, int n_rot, const double* phi, int n_phi, int phi_res,
-                                  double rho1, double* sum_out, float* samples_out, void* workspace,
-                                  size_t workspace_bytes, void* stream) {
+static int mc_triplets(const float* eps1, const float* eps2, const float* eps3, int J, const double* centers,
+                       const double* center_w, int64_t n_centers, const double* offsets, int n_rot, const double* phi,
+                       int n_phi, int phi_res, double rho1, double* sum_out, float* samples_out, void* workspace,
+                       size_t workspace_bytes, void* stream, bool bricks) {
   if (!eps2 || !eps3 || !sum_out || (n_centers > 0 && !centers) || (n_rot > 0 && !offsets))
     return fail(HERMES_ERR_INVALID, "mc_triplets: NULL argument");
   if (J < 2 || J > 10) return fail(HERMES_ERR_INVALID, "mc_triplets: J=%d outside [2,10]", J);
@@ -271,8 +303,12 @@ extern "C" int hermes_mc_triplets(const float* eps1, const float* eps2, const fl
   int rc = mc_prepare(phi, n_phi, phi_res, workspace, workspace_bytes, &phis, &partial, s);
   if (rc) return rc;
   const int g = mc_grid();
-  mc_triplet_kernel<<<g, 256, 0, s>>>(eps1, eps2, eps3, J, centers, center_w, n_centers, offsets, n_rot, phis,
-                                      phi_res, rho1, partial, samples_out);
+  if (bricks)
+    mc_triplet_kernel<true><<<g, 256, 0, s>>>(eps1, eps2, eps3, J, centers, center_w, n_centers, offsets, n_rot, phis,
+                                              phi_res, rho1, partial, samples_out);
+  else
+    mc_triplet_kernel<false><<<g, 256, 0, s>>>(eps1, eps2, eps3, J, centers, center_w, n_centers, offsets, n_rot,
+                                               phis, phi_res, rho1, partial, samples_out);
   HERMES_LAUNCH_CHECK("mc_triplet_kernel");
   mc_sum_kernel<<<1, 256, 0, s>>>(partial, g, partial + g);
   HERMES_LAUNCH_CHECK("mc_sum_kernel");
@@ -281,11 +317,10 @@ extern "C" int hermes_mc_triplets(const float* eps1, const float* eps2, const fl
   return HERMES_OK;
 }
 
-extern "C" int hermes_mc_sample(const float* eps1, const float* eps2, const float* eps3, int J, const double* pool,
-                                int64_t M, const int64_t* idx, const double* weights, const double* offsets,
-                                int64_t n, double R1, double R2, double mu, uint64_t seed, const double* phi,
-                                int n_phi, int phi_res, double* sums_out, void* workspace, size_t workspace_bytes,
-                                void* stream) {
+static int mc_sample(const float* eps1, const float* eps2, const float* eps3, int J, const double* pool, int64_t M,
+                     const int64_t* idx, const double* weights, const double* offsets, int64_t n, double R1, double R2,
+                     double mu, uint64_t seed, const double* phi, int n_phi, int phi_res, double* sums_out,
+                     void* workspace, size_t workspace_bytes, void* stream, bool bricks) {
   if (!eps1 || !eps2 || !eps3 || !sums_out) return fail(HERMES_ERR_INVALID, "mc_sample: NULL argument");
   if (J < 2 || J > 10) return fail(HERMES_ERR_INVALID, "mc_sample: J=%d outside [2,10]", J);
   if (n < 0 || M < 0) return fail(HERMES_ERR_INVALID, "mc_sample: negative count");
@@ -296,9 +331,14 @@ extern "C" int hermes_mc_sample(const float* eps1, const float* eps2, const floa
   int rc = mc_prepare(phi, n_phi, phi_res, workspace, workspace_bytes, &phis, &partial, s);
   if (rc) return rc;
   const int g = mc_grid();
-  mc_sample_kernel<<<g, 256, 0, s>>>(eps1, eps2, eps3, J, pool, (long long)M, reinterpret_cast<const long long*>(idx),
-                                     weights, offsets, (long long)n, R1, R2, mu, (unsigned long long)seed, phis,
-                                     phi_res, partial);
+  if (bricks)
+    mc_sample_kernel<true><<<g, 256, 0, s>>>(eps1, eps2, eps3, J, pool, (long long)M,
+                                             reinterpret_cast<const long long*>(idx), weights, offsets, (long long)n,
+                                             R1, R2, mu, (unsigned long long)seed, phis, phi_res, partial);
+  else
+    mc_sample_kernel<false><<<g, 256, 0, s>>>(eps1, eps2, eps3, J, pool, (long long)M,
+                                              reinterpret_cast<const long long*>(idx), weights, offsets, (long long)n,
+                                              R1, R2, mu, (unsigned long long)seed, phis, phi_res, partial);
   HERMES_LAUNCH_CHECK("mc_sample_kernel");
   mc_sum_kernel<<<1, 256, 0, s>>>(partial, g, partial + 2 * g);
   HERMES_LAUNCH_CHECK("mc_sum_kernel");
@@ -306,5 +346,50 @@ extern "C" int hermes_mc_sample(const float* eps1, const float* eps2, const floa
   HERMES_LAUNCH_CHECK("mc_sum_kernel");
   HERMES_CUDA_TRY(cudaMemcpyAsync(sums_out, partial + 2 * g, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
   HERMES_CUDA_TRY(cudaStreamSynchronize(s));
+  return HERMES_OK;
+}
+
+extern "C" int hermes_mc_triplets(const float* eps1, const float* eps2, const float* eps3, int J,
+                                  const double* centers, const double* center_w, int64_t n_centers,
+                                  const double* offsets, int n_rot, const double* phi, int n_phi, int phi_res,
+                                  double rho1, double* sum_out, float* samples_out, void* workspace,
+                                  size_t workspace_bytes, void* stream) {
+  return mc_triplets(eps1, eps2, eps3, J, centers, center_w, n_centers, offsets, n_rot, phi, n_phi, phi_res, rho1,
+                     sum_out, samples_out, workspace, workspace_bytes, stream, false);
+}
+
+extern "C" int hermes_mc_triplets_bricks(const float* eps1, const float* eps2, const float* eps3, int J,
+                                         const double* centers, const double* center_w, int64_t n_centers,
+                                         const double* offsets, int n_rot, const double* phi, int n_phi, int phi_res,
+                                         double rho1, double* sum_out, float* samples_out, void* workspace,
+                                         size_t workspace_bytes, void* stream) {
+  return mc_triplets(eps1, eps2, eps3, J, centers, center_w, n_centers, offsets, n_rot, phi, n_phi, phi_res, rho1,
+                     sum_out, samples_out, workspace, workspace_bytes, stream, true);
+}
+
+extern "C" int hermes_mc_sample(const float* eps1, const float* eps2, const float* eps3, int J, const double* pool,
+                                int64_t M, const int64_t* idx, const double* weights, const double* offsets,
+                                int64_t n, double R1, double R2, double mu, uint64_t seed, const double* phi,
+                                int n_phi, int phi_res, double* sums_out, void* workspace, size_t workspace_bytes,
+                                void* stream) {
+  return mc_sample(eps1, eps2, eps3, J, pool, M, idx, weights, offsets, n, R1, R2, mu, seed, phi, n_phi, phi_res,
+                   sums_out, workspace, workspace_bytes, stream, false);
+}
+
+extern "C" int hermes_mc_sample_bricks(const float* eps1, const float* eps2, const float* eps3, int J,
+                                       const double* pool, int64_t M, const int64_t* idx, const double* weights,
+                                       const double* offsets, int64_t n, double R1, double R2, double mu,
+                                       uint64_t seed, const double* phi, int n_phi, int phi_res, double* sums_out,
+                                       void* workspace, size_t workspace_bytes, void* stream) {
+  return mc_sample(eps1, eps2, eps3, J, pool, M, idx, weights, offsets, n, R1, R2, mu, seed, phi, n_phi, phi_res,
+                   sums_out, workspace, workspace_bytes, stream, true);
+}
+
+extern "C" int hermes_field_to_bricks(const float* field, int J, float* bricks, void* stream) {
+  if (!field || !bricks) return fail(HERMES_ERR_INVALID, "field_to_bricks: NULL argument");
+  if (J < 2 || J > 10) return fail(HERMES_ERR_INVALID, "field_to_bricks: J=%d outside [2,10]", J);
+  if (field == bricks) return fail(HERMES_ERR_INVALID, "field_to_bricks: the copy cannot be in place");
+  mc_to_bricks_kernel<<<mc_grid(), 256, 0, hermes::as_stream(stream)>>>(field, J, bricks);
+  HERMES_LAUNCH_CHECK("mc_to_bricks_kernel");
   return HERMES_OK;
 }

@@ -28,6 +28,7 @@ import ctypes
 import logging
 import math
 import time
+import weakref
 
 import numpy as np
 import torch
@@ -51,6 +52,32 @@ def _mc_workspace(device):
         _lib.check(_lib.load().hermes_mc_workspace_size(ctypes.byref(n)), "mc_workspace_size")
         _WS[key] = torch.empty(n.value, dtype=torch.uint8, device=device)
     return _WS[key]
+
+
+_BRICKS = {}
+_BRICKS_KEEP = 6
+
+
+def field_bricks(eps, J):
+    """The brick-layout copy of a float32 [L^3] field (hermes_field_to_bricks),
+    cached per (storage, version, J) so repeated Monte Carlo calls on the same
+    field convert it once; the last few are kept."""
+    if eps is None:
+        return None
+    key = (eps.device.type, eps.device.index, eps.data_ptr(), eps._version, int(J))
+    hit = _BRICKS.get(key)
+    if hit is not None and hit[0]() is eps:
+        return hit[1]
+    L = 1 << int(J)
+    if eps.dtype != torch.float32 or not eps.is_contiguous() or eps.numel() != L ** 3:
+        raise ValueError("field_bricks needs a contiguous float32 field of L^3 cells")
+    out = torch.empty(L ** 3, dtype=torch.float32, device=eps.device)
+    _lib.check(_lib.load().hermes_field_to_bricks(_ptr(eps), int(J), _ptr(out), _stream_ptr(eps.device)),
+               "hermes_field_to_bricks")
+    if len(_BRICKS) >= _BRICKS_KEEP:
+        _BRICKS.pop(next(iter(_BRICKS)))
+    _BRICKS[key] = (weakref.ref(eps), out)
+    return out
 
 
 def generate_triangle_offsets(R1, R2, mu, phi, costheta1, alpha):
@@ -111,12 +138,14 @@ def morton_order(centers, L):
 
 
 def triplet_sum(eps1, eps2, eps3, J, centers, offsets, phi_t, center_w=None, rho1=0.0, samples=False,
-                locality=True):
+                locality=True, bricks=True):
     """sum_i w_i n1_i sum_r n2 n3 (float64) and optionally the per-triplet
     products.  With locality (and no per-triplet output) the centres are put
     in Morton order first: every centre uses the same rotation offsets, so
     neighbouring threads then gather neighbouring cells from L2 (the sum is
-    over all centres, so only its rounding order changes)."""
+    over all centres, so only its rounding order changes).  With bricks the
+    gathers read brick-layout copies of the fields (field_bricks; the same
+    values bit for bit, fewer DRAM sectors per gather)."""
     dev = eps2.device
     c = torch.as_tensor(np.ascontiguousarray(centers), dtype=torch.float64, device=dev) \
         if not isinstance(centers, torch.Tensor) else centers
@@ -131,9 +160,13 @@ def triplet_sum(eps1, eps2, eps3, J, centers, offsets, phi_t, center_w=None, rho
     smp = torch.empty((nc, nr), dtype=torch.float32, device=dev) if samples else None
     ws = _mc_workspace(dev)
     out = ctypes.c_double(0.0)
-    rc = _lib.load().hermes_mc_triplets(_ptr(eps1), _ptr(eps2), _ptr(eps3), J, _ptr(c), _ptr(w), nc, _ptr(o), nr,
-                                        _ptr(phi_t), phi_t.numel(), phi_t.numel() // 3, float(rho1),
-                                        ctypes.byref(out), _ptr(smp), _ptr(ws), ws.numel(), _stream_ptr(dev))
+    lib = _lib.load()
+    fn = lib.hermes_mc_triplets
+    if bricks:
+        eps1, eps2, eps3 = (field_bricks(e, J) for e in (eps1, eps2, eps3))
+        fn = lib.hermes_mc_triplets_bricks
+    rc = fn(_ptr(eps1), _ptr(eps2), _ptr(eps3), J, _ptr(c), _ptr(w), nc, _ptr(o), nr, _ptr(phi_t), phi_t.numel(),
+            phi_t.numel() // 3, float(rho1), ctypes.byref(out), _ptr(smp), _ptr(ws), ws.numel(), _stream_ptr(dev))
     _lib.check(rc, "hermes_mc_triplets")
     return out.value, smp
 
@@ -151,7 +184,8 @@ def interp(grid, J, scaled_pos, phi_t, offset=(0.0, 0.0, 0.0)):
     return out
 
 
-def mc_sample(eps1, eps2, eps3, J, pool, phi_t, R1, R2, mu, n, seed=0, idx=None, weights=None, offsets=None):
+def mc_sample(eps1, eps2, eps3, J, pool, phi_t, R1, R2, mu, n, seed=0, idx=None, weights=None, offsets=None,
+              bricks=True):
     """(sum f, sum f^2) in float64 over n one-rotation triplets f = w n1 n2 n3
     (hermes_mc_sample): centre pool[idx[k]] (uniform from the pool when idx
     is None), offsets given [n, 6] or drawn on the device for the triangle
@@ -159,10 +193,14 @@ def mc_sample(eps1, eps2, eps3, J, pool, phi_t, R1, R2, mu, n, seed=0, idx=None,
     dev = eps2.device
     out = (ctypes.c_double * 2)()
     ws = _mc_workspace(dev)
-    rc = _lib.load().hermes_mc_sample(_ptr(eps1), _ptr(eps2), _ptr(eps3), J, _ptr(pool), pool.shape[0], _ptr(idx),
-                                      _ptr(weights), _ptr(offsets), int(n), float(R1), float(R2), float(mu),
-                                      int(seed) & ((1 << 64) - 1), _ptr(phi_t), phi_t.numel(), phi_t.numel() // 3,
-                                      out, _ptr(ws), ws.numel(), _stream_ptr(dev))
+    lib = _lib.load()
+    fn = lib.hermes_mc_sample
+    if bricks:
+        eps1, eps2, eps3 = (field_bricks(e, J) for e in (eps1, eps2, eps3))
+        fn = lib.hermes_mc_sample_bricks
+    rc = fn(_ptr(eps1), _ptr(eps2), _ptr(eps3), J, _ptr(pool), pool.shape[0], _ptr(idx), _ptr(weights),
+            _ptr(offsets), int(n), float(R1), float(R2), float(mu), int(seed) & ((1 << 64) - 1), _ptr(phi_t),
+            phi_t.numel(), phi_t.numel() // 3, out, _ptr(ws), ws.numel(), _stream_ptr(dev))
     _lib.check(rc, "hermes_mc_sample")
     return out[0], out[1]
 

@@ -270,3 +270,32 @@ def test_mc_sample_matches_interp_path_and_draws_unbiased_rotations():
     mc_u, se_cu = lp.centre_estimate(2.0, 4.0, 0.3, 20_000, 32, seed=31, uniform=True)
     mc_l, se_cl = lp.centre_estimate(2.0, 4.0, 0.3, 20_000, 32, seed=32)
     assert abs(mc_l - mc_u) < 5 * np.sqrt(se_cu ** 2 + se_cl ** 2), (mc_u, mc_l, se_cu, se_cl)
+
+
+@pytest.mark.parametrize("J", [4, 7])
+def test_brick_layout_gathers_are_bit_identical(J):
+    """hermes_field_to_bricks puts cell (x, y, z) at brick (x/2, y/2, z/2),
+    slot (x%2, y%2, z%2); the brick-layout triplet and single-sample kernels
+    read the same float32 values in the same order, so their float64 sums and
+    per-triplet products equal the C-order kernels' exactly."""
+    L = 1 << J
+    g = torch.Generator(device="cuda").manual_seed(J)
+    eps = [torch.rand((L, L, L), generator=g, device="cuda", dtype=torch.float32) for _ in range(3)]
+    bricks = mc3pcf.field_bricks(eps[1], J)
+    want = eps[1].view(L // 2, 2, L // 2, 2, L // 2, 2).permute(0, 2, 4, 1, 3, 5).reshape(-1)
+    assert torch.equal(bricks, want)
+    assert mc3pcf.field_bricks(eps[1], J) is bricks  # cached
+    rng = np.random.default_rng(J)
+    phi_t = torch.as_tensor(PHI, device="cuda")
+    centres = torch.as_tensor(rng.uniform(0.0, L, (5000, 3)), device="cuda")
+    off = mc3pcf.rotation_offsets(0.2 * L, 0.3 * L, 0.4, 7, rng=np.random.RandomState(J))
+    for e1 in (eps[0], None):
+        a, sa = mc3pcf.triplet_sum(e1, eps[1], eps[2], J, centres, off, phi_t, rho1=1.5, samples=True, bricks=False)
+        b, sb = mc3pcf.triplet_sum(e1, eps[1], eps[2], J, centres, off, phi_t, rho1=1.5, samples=True, bricks=True)
+        assert a == b
+        assert torch.equal(sa, sb)
+    a = mc3pcf.mc_sample(eps[0], eps[1], eps[2], J, centres, phi_t, 0.2 * L, 0.3 * L, 0.4, 20000, seed=9,
+                         bricks=False)
+    b = mc3pcf.mc_sample(eps[0], eps[1], eps[2], J, centres, phi_t, 0.2 * L, 0.3 * L, 0.4, 20000, seed=9,
+                         bricks=True)
+    assert a == b
