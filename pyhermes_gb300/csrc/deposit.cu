@@ -504,23 +504,26 @@ dep_accum_kernel(const DepRec* __restrict__ sorted, const unsigned* __restrict__
         py[s] = __ldg(&phif[fy + g.res * s]);
         pz[s] = __ldg(&phif[fz + g.res * s]);
       }
+      // every lane runs all S^3 terms and predicates the adds on the term's
+      // cell lying in this tile (no divergent skips between the lanes'
+      // particles)
 #pragma unroll
       for (int a = 0; a < S; ++a) {
-        if (lx[a] >= g.tx) continue;
+        const bool va = lx[a] < g.tx;
 #pragma unroll
         for (int b = 0; b < S; ++b) {
-          if (ly[b] >= g.ty) continue;
+          const bool vb = va && ly[b] < g.ty;
           const float pxy = px[a] * py[b];
           const int row = (lx[a] << tyzl) + (ly[b] << tzl);
 #pragma unroll
           for (int c = 0; c < S; ++c) {
-            if (lz[c] >= g.tz) continue;
+            const bool v = vb && lz[c] < g.tz;
             int qh;
             unsigned ql;
             split_q(pxy * pz[c] * scale_f, two_sb, inv_two_sb, lo_one, qh, ql);
             const int cell = row + lz[c];
-            if (ql != 0u) atomicAdd(&acc_lo[cell], ql);
-            if (qh != 0) atomicAdd(&acc_hi[cell], qh);
+            if (v && ql != 0u) atomicAdd(&acc_lo[cell], ql);
+            if (v && qh != 0) atomicAdd(&acc_hi[cell], qh);
           }
         }
       }
@@ -552,18 +555,18 @@ dep_accum_kernel(const DepRec* __restrict__ sorted, const unsigned* __restrict__
     }
 #pragma unroll
     for (int a = 0; a < S; ++a) {
-      if (lx[a] >= g.tx) continue;
+      const bool va = lx[a] < g.tx;
 #pragma unroll
       for (int b = 0; b < S; ++b) {
-        if (ly[b] >= g.ty) continue;
+        const bool vb = va && ly[b] < g.ty;
         const float pxy = px[a] * py[b];
         const int row = (lx[a] << tyzl) + (ly[b] << tzl);
 #pragma unroll
         for (int c = 0; c < S; ++c) {
-          if (lz[c] >= g.tz) continue;
+          const bool v = vb && lz[c] < g.tz;
           const long long q = f32_to_ll_rn(pxy * pz[c] * scale_f);
-          atomicAdd(reinterpret_cast<unsigned long long*>(&acc[row + lz[c]]),
-                    static_cast<unsigned long long>(q));
+          if (v && q != 0)
+            atomicAdd(reinterpret_cast<unsigned long long*>(&acc[row + lz[c]]), static_cast<unsigned long long>(q));
         }
       }
     }
