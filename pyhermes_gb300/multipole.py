@@ -435,6 +435,30 @@ class MultipoleEngine:
         # the tensor engine reads the bin-major layout the inverse FFT writes
         return multipole_fields_bins(spec, self.J, l, m, bins, self.box, self.P, bin_major=self.bin_major)
 
+    def summands_shared(self, lms, bins):
+        """S_lm[i, j] for every (l, m) in lms over one list of at most 16 bins
+        shared by vertices 2 and 3 (a_{l,-m} from the conjugate of a_lm),
+        complex128 [len(lms), nb, nb]: every fields pass and contraction is
+        queued on the current stream into one device array, which is read
+        back once (no host round trip per (l, m))."""
+        bins = [as_bin(b) for b in bins]
+        nb = len(bins)
+        if not (self.same23 and 1 <= nb <= MAX_BINS):
+            raise ValueError("summands_shared needs vertices 2 and 3 to share the field and 1..16 bins")
+        g = (ctypes.c_double * 9)(*np.asarray(self.gamma, dtype=np.float64).ravel())
+        out = torch.zeros((len(lms), MAX_BINS, MAX_BINS, 2), dtype=torch.float64, device=self.dev)
+        t0 = time.perf_counter()
+        for k, (l, m) in enumerate(lms):
+            f = self._fields(self.spec2, l, m, bins)
+            multipole_contract_async(self.eps1, f, nb, g, self.J, out[k], conj_sign=(-1) ** ((l + m) % 2),
+                                     engine=self.engine, bin_major=self.bin_major)
+            del f  # released in stream order, after the contraction that reads it
+        o = out[:, :nb, :nb].cpu().numpy()
+        # the fields passes and contractions run queued together; their time
+        # is counted under contract_s
+        self.timing["contract_s"] += time.perf_counter() - t0
+        return o[..., 0] + 1j * o[..., 1]
+
     def summands(self, l, m, r12_phys, r13_phys):
         """S_m[i, j] for two lists of radial bins (thin-shell radii in physical
         units, or BinSpec), complex128 [n12, n13]."""
@@ -483,8 +507,16 @@ class MultipoleEngine:
             r12 = r13 = both
             i12 = i13 = {r: i for i, r in enumerate(both)}
         res = np.zeros((len(pairs), l_max - l_min + 1))
+        shared = None
+        if self.same23 and r12 == r13 and len(r12) <= MAX_BINS:
+            lms = [(l, m) for l in range(l_min, l_max + 1) for m in range(l + 1)]
+            S = self.summands_shared(lms, r12)
+            shared = {lm: S[k] for k, lm in enumerate(lms)}
         for li, l in enumerate(range(l_min, l_max + 1)):
-            Sm = [self.summands(l, m, r12, r13) for m in range(0, l + 1)]
+            if shared is not None:
+                Sm = [shared[(l, m)] for m in range(0, l + 1)]
+            else:
+                Sm = [self.summands(l, m, r12, r13) for m in range(0, l + 1)]
             for s, (a, b) in enumerate(pairs):
                 res[s, li] = combine_multipole_m_terms([Sm[m][i12[a], i13[b]] for m in range(l + 1)], l)
         return res
