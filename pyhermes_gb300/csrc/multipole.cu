@@ -269,9 +269,9 @@ __device__ __forceinline__ float2 ylm_at(const YlmConst& Y, int a, int b, int c,
 template <int NB4>
 __device__ __forceinline__ void mp_window_sum(int x, int y, int z, int L, const float* __restrict__ P,
                                               const float4* __restrict__ T4, const YlmConst& Y,
-                                              float (&accr)[4 * NB4], float (&acci)[4 * NB4]) {
+                                              float2 (&acc)[4 * NB4]) {
 #pragma unroll
-  for (int b = 0; b < 4 * NB4; ++b) accr[b] = acci[b] = 0.f;
+  for (int b = 0; b < 4 * NB4; ++b) acc[b] = make_float2(0.f, 0.f);
   const int ia[2] = {x - L, x}, ib[2] = {y - L, y}, ic[2] = {z - L, z};
   const float pa[2] = {P[L - x], P[x]}, pb[2] = {P[L - y], P[y]}, pc[2] = {P[L - z], P[z]};
 #pragma unroll
@@ -283,19 +283,15 @@ __device__ __forceinline__ void mp_window_sum(int x, int y, int z, int L, const 
         const int n2 = ia[i] * ia[i] + ib[j] * ib[j] + ic[k] * ic[k];
         const float pw = pa[i] * pb[j] * pc[k];
         const float2 yv = ylm_at(Y, ia[i], ib[j], ic[k], n2);
-        const float yr = pw * yv.x, yi = pw * yv.y;
+        const float2 yw = make_float2(pw * yv.x, pw * yv.y);  // (Re, Im) of P Y, one paired FMA per bin
         const float4* tr = T4 + (long long)n2 * (kBinStride / 4);
 #pragma unroll
         for (int q = 0; q < NB4; ++q) {
           const float4 jl = __ldg(tr + q);
-          accr[4 * q + 0] = fmaf(jl.x, yr, accr[4 * q + 0]);
-          acci[4 * q + 0] = fmaf(jl.x, yi, acci[4 * q + 0]);
-          accr[4 * q + 1] = fmaf(jl.y, yr, accr[4 * q + 1]);
-          acci[4 * q + 1] = fmaf(jl.y, yi, acci[4 * q + 1]);
-          accr[4 * q + 2] = fmaf(jl.z, yr, accr[4 * q + 2]);
-          acci[4 * q + 2] = fmaf(jl.z, yi, acci[4 * q + 2]);
-          accr[4 * q + 3] = fmaf(jl.w, yr, accr[4 * q + 3]);
-          acci[4 * q + 3] = fmaf(jl.w, yi, acci[4 * q + 3]);
+          acc[4 * q + 0] = __ffma2_rn(make_float2(jl.x, jl.x), yw, acc[4 * q + 0]);
+          acc[4 * q + 1] = __ffma2_rn(make_float2(jl.y, jl.y), yw, acc[4 * q + 1]);
+          acc[4 * q + 2] = __ffma2_rn(make_float2(jl.z, jl.z), yw, acc[4 * q + 2]);
+          acc[4 * q + 3] = __ffma2_rn(make_float2(jl.w, jl.w), yw, acc[4 * q + 3]);
         }
       }
 }
@@ -331,8 +327,8 @@ mp_prepass_quad_kernel(const float2* __restrict__ half, int J, const float* __re
        w += (long long)gridDim.x * blockDim.x) {
     const int z = (int)(w % H), li = (int)(w / H);
     const int x = 1 + li / Q1, y = 1 + li % Q1;
-    float accr[NB], acci[NB];
-    mp_window_sum<NB4>(x, y, z, L, P, T4, Y, accr, acci);
+    float2 acc[NB];
+    mp_window_sum<NB4>(x, y, z, L, P, T4, Y, acc);
     const bool mirror = z != 0 && z != L / 2;
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
@@ -345,7 +341,7 @@ mp_prepass_quad_kernel(const float2* __restrict__ half, int J, const float* __re
 #pragma unroll
       for (int b = 0; b < NB; ++b) {
         if (b < nb) {
-          const float kr = cr * accr[b], ki = ci * acci[b];
+          const float kr = cr * acc[b].x, ki = ci * acc[b].y;
           out[b * N + idx] = make_float2(er * kr - ei * ki, er * ki + ei * kr);
         }
       }
@@ -355,7 +351,7 @@ mp_prepass_quad_kernel(const float2* __restrict__ half, int J, const float* __re
 #pragma unroll
         for (int b = 0; b < NB; ++b) {
           if (b < nb) {
-            const float kr = lsign * cr * accr[b], ki = lsign * ci * acci[b];
+            const float kr = lsign * cr * acc[b].x, ki = lsign * ci * acc[b].y;
             out[b * N + idm] = make_float2(mr * kr - mi * ki, mr * ki + mi * kr);
           }
         }
@@ -390,29 +386,29 @@ mp_prepass_edge_kernel(const float2* __restrict__ half, int J, const float* __re
       if (x >= L / 2) ++x;
     }
     const float2 e = half[((long long)x * L + y) * H + z];
-    float accr[NB], acci[NB];
-    mp_window_sum<NB4>(x, y, z, L, P, T4, Y, accr, acci);
+    float2 acc[NB];
+    mp_window_sum<NB4>(x, y, z, L, P, T4, Y, acc);
     const float er = e.x * inv_n, ei = e.y * inv_n;
     const long long idx = ((long long)x * L + y) * L + z;
 #pragma unroll
     for (int b = 0; b < NB; ++b)
-      if (b < nb) out[b * N + idx] = make_float2(er * accr[b] - ei * acci[b], er * acci[b] + ei * accr[b]);
+      if (b < nb) out[b * N + idx] = make_float2(er * acc[b].x - ei * acc[b].y, er * acc[b].y + ei * acc[b].x);
     if (z == 0 || z == L / 2) continue;
     const int xm = (L - x) & Lm, ym = (L - y) & Lm, zm = L - z;
     if (x == 0 || y == 0) {
-      mp_window_sum<NB4>(xm, ym, zm, L, P, T4, Y, accr, acci);
+      mp_window_sum<NB4>(xm, ym, zm, L, P, T4, Y, acc);
     } else {
 #pragma unroll
       for (int b = 0; b < NB; ++b) {
-        accr[b] *= lsign;
-        acci[b] *= lsign;
+        acc[b].x *= lsign;
+        acc[b].y *= lsign;
       }
     }
     const float mr = e.x * inv_n, mi = -(e.y * inv_n);  // conj(eps_hat(k)) / L^3
     const long long idm = ((long long)xm * L + ym) * L + zm;
 #pragma unroll
     for (int b = 0; b < NB; ++b)
-      if (b < nb) out[b * N + idm] = make_float2(mr * accr[b] - mi * acci[b], mr * acci[b] + mi * accr[b]);
+      if (b < nb) out[b * N + idm] = make_float2(mr * acc[b].x - mi * acc[b].y, mr * acc[b].y + mi * acc[b].x);
   }
 }
 

@@ -468,13 +468,12 @@ pair_products_cylz_kernel(PPArgs a, const WinDev* __restrict__ wins, const doubl
   const long long ncol = (long long)L * L;  // a multiple of CW
   for (long long col0 = ((long long)blockIdx.x * kWarps + wid) * CW; col0 < ncol;
        col0 += (long long)gridDim.x * kWarps * CW) {
-    float fac[CW][2][NP];
+    // (bin 2 lane, bin 2 lane + 1) sums of each column, updated by paired FMAs
+    float2 fac[CW][NP];
 #pragma unroll
     for (int c = 0; c < CW; ++c)
 #pragma unroll
-      for (int j = 0; j < 2; ++j)
-#pragma unroll
-        for (int p = 0; p < NP; ++p) fac[c][j][p] = 0.f;
+      for (int p = 0; p < NP; ++p) fac[c][p] = make_float2(0.f, 0.f);
     float t00[NP];
     for (int zc = 0; zc < H; zc += kCylZ) {
       const int zn = min(kCylZ, H - zc);
@@ -527,10 +526,7 @@ pair_products_cylz_kernel(PPArgs a, const WinDev* __restrict__ wins, const doubl
             tv[c4 + 3] = t4.w;
           }
 #pragma unroll
-          for (int c = 0; c < CW; ++c) {
-            fac[c][0][p] = fmaf(tv[c], bz.x, fac[c][0][p]);
-            fac[c][1][p] = fmaf(tv[c], bz.y, fac[c][1][p]);
-          }
+          for (int c = 0; c < CW; ++c) fac[c][p] = __ffma2_rn(make_float2(tv[c], tv[c]), bz, fac[c][p]);
         }
       }
     }
@@ -545,7 +541,7 @@ pair_products_cylz_kernel(PPArgs a, const WinDev* __restrict__ wins, const doubl
       for (int j = 0; j < 2; ++j)
 #pragma unroll
         for (int p = 0; p < NP; ++p) {
-          float f = fac[c][j][p];
+          float f = j == 0 ? fac[c][p].x : fac[c][p].y;
           if (col == 0 && zk[j]) f -= t00[p] * B[2 * lane + j];  // K(0,0,0) forced to 0
           acc[j][p] += (double)aj[j] * (double)f;
         }
