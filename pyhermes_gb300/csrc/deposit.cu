@@ -357,8 +357,20 @@ __device__ __forceinline__ void split_q(float v, float two_sb, float inv_two_sb,
   }
 }
 
+// The split point sb of the two-word accumulation for a tile reached by T
+// records (0: int64 atomics), see dep_accum_kernel.
+__device__ __forceinline__ int split_bits(unsigned total, const DepStatus* __restrict__ st) {
+  const int clog = total > 1u ? 32 - __clz((int)(total - 1u)) : 0;  // ceil(log2 T)
+  const int cand = 32 - clog;
+  if (cand < 8 || cand > 31) return 0;
+  const double pm = (double)__uint_as_float(st->phimax_bits);
+  const double qmax = (double)__uint_as_float(st->wmax_bits) * pm * pm * pm * st->scale_d;
+  // factor 2 margin for the float32 rounding of each product
+  return (double)total * (2.0 * ldexp(qmax, -cand) + 1.0) < 2147483648.0 ? cand : 0;
+}
+
 template <int S, bool kF64Out>
-__global__ void __launch_bounds__(kAccThreads)
+__global__ void __launch_bounds__(kAccThreads, 5)
 dep_accum_kernel(const DepRec* __restrict__ sorted, const unsigned* __restrict__ offsets,
                  const float* __restrict__ phif, DepGeom g,
                  const DepStatus* __restrict__ st, float* __restrict__ out32,
@@ -368,7 +380,7 @@ dep_accum_kernel(const DepRec* __restrict__ sorted, const unsigned* __restrict__
   long long* acc = reinterpret_cast<long long*>(smem);
   unsigned* cnt = reinterpret_cast<unsigned*>(acc + ncell);
   __shared__ unsigned r_start[64], r_pref[65], r_home[64];
-  __shared__ int n_ranges;
+  __shared__ int n_ranges, s_sb;
 
   const int tile = blockIdx.x;
   const int hz = tile % g.ntz, hy = (tile / g.ntz) % g.nty, hx = tile / (g.ntz * g.nty);
@@ -431,6 +443,7 @@ dep_accum_kernel(const DepRec* __restrict__ sorted, const unsigned* __restrict__
       const int nr = __popc(v0) + __popc(v1);
       r_pref[nr] = inc;
       n_ranges = nr;
+      s_sb = split_bits(inc, st);
     }
   }
   __syncthreads();
@@ -467,17 +480,7 @@ dep_accum_kernel(const DepRec* __restrict__ sorted, const unsigned* __restrict__
   // Otherwise (dense tiles) sb = 0 and the tile uses int64 atomics.  The
   // same bound gives |q| / 2^sb < 2^31 for every contribution, which
   // split_q needs.
-  int sb = 0;
-  {
-    const int clog = total > 1u ? 32 - __clz((int)(total - 1u)) : 0;  // ceil(log2 T)
-    const int cand = 32 - clog;
-    if (cand >= 8 && cand <= 31) {
-      const double pm = (double)__uint_as_float(st->phimax_bits);
-      const double qmax = (double)__uint_as_float(st->wmax_bits) * pm * pm * pm * st->scale_d;
-      // factor 2 margin for the float32 rounding of each product
-      if ((double)total * (2.0 * ldexp(qmax, -cand) + 1.0) < 2147483648.0) sb = cand;
-    }
-  }
+  const int sb = s_sb;  // chosen once per tile by the range-table warp (float64 is slow on this part)
   if (sb > 0) {
     unsigned* acc_lo = reinterpret_cast<unsigned*>(acc);
     int* acc_hi = reinterpret_cast<int*>(acc) + ncell;

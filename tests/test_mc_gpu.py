@@ -299,3 +299,39 @@ def test_brick_layout_gathers_are_bit_identical(J):
     b = mc3pcf.mc_sample(eps[0], eps[1], eps[2], J, centres, phi_t, 0.2 * L, 0.3 * L, 0.4, 20000, seed=9,
                          bricks=True)
     assert a == b
+
+
+def test_interp_indices_follow_the_reference_at_boundaries():
+    """hermes_interp gathers the 27 cells around floor(s) with the phi samples
+    at int((s - floor(s)) * res), both in the reference's float64 arithmetic
+    (the kernel reads them from the float64 bits of s when 0 <= s < 2^30).
+    Against a float64 restatement, for coordinates on and beside cell and
+    sample boundaries, tiny, negative (offset) and ordinary ones: a cell or
+    sample index off by one would move a value by ~1e-3 or more, far above
+    the float32 tolerance of 2e-6."""
+    J, L, res = 5, 32, 1024
+    rng = np.random.default_rng(3)
+    grid = rng.standard_normal((L, L, L)).astype(np.float32)
+    phis = np.asarray(PHI, dtype=np.float32).astype(np.float64)
+    k = np.arange(0, 4 * res)
+    edge = np.concatenate([k / res, np.nextafter(k / res, 0.0), np.nextafter(k / res, 1e9)])[:3000]
+    pos = np.stack([rng.uniform(0.0, L, 6000), rng.uniform(0.0, L, 6000), rng.uniform(0.0, L, 6000)], axis=1)
+    pos[:3000, 0] = edge
+    pos[3000:3100, 1] = rng.uniform(0.0, 1e-9, 100)
+    pos[3100:3200] = np.floor(pos[3100:3200])
+    off = (-7.25, 0.5, -0.3)  # makes some coordinates negative
+    got = mc3pcf.interp(torch.as_tensor(grid, device="cuda"), J, torch.as_tensor(pos, device="cuda"),
+                        torch.as_tensor(PHI, device="cuda"), offset=off).cpu().numpy()
+    s = pos + np.asarray(off)
+    c = np.floor(s).astype(np.int64)
+    f = np.clip(((s - np.floor(s)) * res).astype(np.int64), 0, res - 1)
+    g64 = grid.astype(np.float64)
+    want = np.zeros(len(pos))
+    for a in range(3):
+        px = phis[f[:, 0] + a * res]
+        for b in range(3):
+            py = phis[f[:, 1] + b * res]
+            for cc in range(3):
+                v = g64[(c[:, 0] - a) % L, (c[:, 1] - b) % L, (c[:, 2] - cc) % L]
+                want += v * px * py * phis[f[:, 2] + cc * res]
+    np.testing.assert_allclose(got, want, rtol=0, atol=2e-6)
