@@ -108,6 +108,16 @@ int hermes_deposit_status(const void* workspace, int64_t* n_rejected,
 int hermes_deposit_set_tile(int J, int tx, int ty, int tz);
 int hermes_deposit_get_tile(int J, int* tx, int* ty, int* tz);
 
+/* The scaling function's precomputes on the device, as
+ * utils/wavelet_grid.py:94-118 fourier_power_spectrum (power_out[n] =
+ * |phi_hat(n / L)|^2, n = 0 .. L * bandwidth, L * bandwidth + 1 float64) and
+ * utils/corr3pcf_multipoles.py:22-30 cal_gamma (gamma_out[l1 * S + l2],
+ * S = n_phi / phi_res <= 5, float64).  phi: device float64 [n_phi]; either
+ * output may be NULL.  The Python layer keeps its host copy of these small
+ * tables (cached per phi); this is the same computation for C callers. */
+int hermes_phi_prepare(const double* phi, int n_phi, int phi_res, int L, int bandwidth,
+                       double* power_out, double* gamma_out, void* stream);
+
 /* ---- spectral windows ------------------------------------------------------
  * Built-in window transfer functions (utils/window_functions.py:441-458),
  * evaluated on the fly inside the passes below instead of being materialised

@@ -30,6 +30,7 @@ SIGNATURES = {
                                            _p, _c_sz, _p]),
     "hermes_deposit_status": (_c_int, [_p, ctypes.POINTER(_c_i64), _p]),
     "hermes_deposit_set_tile": (_c_int, [_c_int, _c_int, _c_int, _c_int]),
+    "hermes_phi_prepare": (_c_int, [_p, _c_int, _c_int, _c_int, _c_int, _p, _p, _p]),
     "hermes_deposit_get_tile": (_c_int, [_c_int, ctypes.POINTER(_c_int), ctypes.POINTER(_c_int),
                                          ctypes.POINTER(_c_int)]),
     "hermes_deposit_noalloc": (_c_int, [_p, _p, _c_i64, _c_int, _dbl, _p, _c_int, _c_int, _p, _p, _p, _p]),

@@ -66,3 +66,8 @@ def test_deposit_tile_setting(lib):
     again = ctypes.c_size_t(0)
     assert lib.hermes_deposit_workspace_size(100000, 7, ctypes.byref(again)) == 0
     assert again.value == base.value
+
+
+def test_phi_prepare_rejects_bad_arguments(lib):
+    assert lib.hermes_phi_prepare(None, 3072, 1024, 64, 1, None, None, None) == -1
+    assert b"phi is NULL" in lib.hermes_last_error()
