@@ -879,11 +879,6 @@ __device__ __forceinline__ void tc_put_pair(unsigned char* op, int cell, int b, 
   *reinterpret_cast<uint32_t*>(op + tcc::kAtomCol + row + hermes::tc::sw128_offset(r, b >> 2) + byte) = l;
 }
 
-__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
-}
-
 // a3 plane x_a from bin-major fields (bin b at src3 + b * bstride) -> buf
 // [16][kA3P] float2; bins nb3 .. 15 are written as zeros.  The copies are
 // 16 bytes, two cells (2p, 2p + 1) of one row: with z0 a multiple of 8 the
