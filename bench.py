@@ -27,9 +27,11 @@ per (l, m), against the measured bf16 peak; `fields_roofline` = the fields
 pass of one (l, m) against HBM.  `traffic` values come from
 profiles/ncu_traffic.json (the ncu command and case are recorded there).
 `deposit` = the 4M-point J=9 deposit (Mparticles/s, HBM roofline of the
-accumulate kernel).  `mc3pcf` = Monte Carlo 3PCF on a J=9 lognormal field:
-uniform-MC triplets/s and the learned importance-sampling proposal against
-uniform sampling (variance per sample, bias, equal-wall-time efficiency).
+accumulate kernel) with the tile the deposit autotuner picks, the default
+tile timed beside it.  `mc3pcf` = Monte Carlo 3PCF on a J=9 lognormal field:
+uniform-MC triplets/s on brick-layout fields (C-order fields timed beside
+it) and the learned importance-sampling proposal against uniform sampling
+(variance per sample, bias, equal-wall-time efficiency).
 `c2_window_2pcf` = `field @ W` (gaussian R=10) and the 30x10 (s, mu) ring
 2PCF on the 4M-point J=9 field, with their HBM rooflines.  `c4_batched` =
 64 uneven catalogues through the batched pipeline against the same public
