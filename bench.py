@@ -871,6 +871,7 @@ def run_gb300(args, ws, rank, local):
         del f2
     hbm, bf16, kind = load_peaks()
     flops = 8.0 * 15 * 15 * 27 * L ** 3
+    stencil_flops = 81 * 2 * 2 * 16 * L ** 3 * (128 + 4) / 128
     achieved = flops / t_con["tensor"] / 1e12
     fld_bytes = L * L * (L // 2 + 1) * 8 + L ** 3 * 15 * 8
 
@@ -924,7 +925,14 @@ def run_gb300(args, ws, rank, local):
                      "executes_on": ("stencil on FP32 paired-FMA pipes; bin x bin product on tcgen05 "
                                      "(BF16x3 operands, FP32 accumulate in TMEM)"),
                      "algorithmic_flops": flops, "ms_per_launch": t_con["tensor"] * 1e3,
-                     "ms_per_launch_simt_engine": t_con["simt"] * 1e3},
+                     "ms_per_launch_simt_engine": t_con["simt"] * 1e3,
+                     # what bounds the kernel: the FP32 stencil on the CUDA cores (81 paired
+                     # complex x real FMAs per cell, bin lane and x-plane; 16 bin lanes; the
+                     # 4-plane halo of each 128-plane x-chunk) against the nominal FP32 peak
+                     # (152 SMs x 128 lanes x 2 FLOP x 2.07 GHz)
+                     "stencil_fp32": {"flops": stencil_flops, "achieved_tflops": stencil_flops / t_con["tensor"] / 1e12,
+                                      "nominal_peak_tflops": 80.6,
+                                      "frac": stencil_flops / t_con["tensor"] / 1e12 / 80.6}},
         "fields_roofline": {"kernels": "mp_jl_table + mp_prepass_quad/edge + cuFFT C2C x15 (bin-major output, "
                                        "read as is by the tensor-core contraction)",
                             "bound": "hbm", "ms_per_lm": t_fld["bin_major"] * 1e3, "algorithmic_bytes": fld_bytes,
