@@ -335,6 +335,18 @@ __device__ __forceinline__ float ll_to_f32(long long a) {
   return fmaf(hi, 4294967296.0f, lo);
 }
 
+// ll_to_f32(HI * 2^sb + LO) from the two words in 32-bit integer arithmetic
+// (8 <= sb <= 31; LO is the unsigned sum of many parts, so any 32-bit
+// value): HI * 2^sb has upper 32 bits HI >> (32 - sb) (arithmetic shift:
+// floor division) and lower 32 bits HI << sb; adding LO to the lower word
+// carries one into the upper word when the 32-bit sum wraps.  The two words
+// are those of the int64 total, so the result is the same float bit for bit.
+__device__ __forceinline__ float split_to_f32(int hi, unsigned lo, int sb) {
+  const unsigned low = ((unsigned)hi << sb) + lo;
+  const int up = (hi >> (32 - sb)) + (low < lo ? 1 : 0);
+  return fmaf((float)up, 4294967296.0f, (float)low);
+}
+
 // The (hi, lo) words of q = f32_to_ll_rn(v) split at bit sb, for
 // |q| < 2^(31 + sb), in 32-bit arithmetic: with a = |v|, qa = floor(a) +
 // (a - floor(a) >= 1/2) is the same round-half-away magnitude (floor(a) and
@@ -584,6 +596,15 @@ dep_accum_kernel(const DepRec* __restrict__ sorted, const unsigned* __restrict__
   for (int i = 4 * threadIdx.x; i < ncell; i += 4 * blockDim.x) {
     const int lz_ = i & (g.tz - 1), ly_ = (i >> tzl) & (g.ty - 1), lx_ = i >> tyzl;
     const size_t gi = ((size_t)(x0 + lx_) * g.L + (y0 + ly_)) * g.L + (z0 + lz_);
+    if (!kF64Out && sb > 0) {  // float32 field from the two words, no 64-bit arithmetic
+      const uint4 l4 = *reinterpret_cast<const uint4*>(reinterpret_cast<const unsigned*>(acc) + i);
+      const int4 h4 = *reinterpret_cast<const int4*>(reinterpret_cast<const int*>(acc) + ncell + i);
+      *reinterpret_cast<float4*>(out32 + gi) =
+          make_float4(split_to_f32(h4.x, l4.x, sb) * inv_f, split_to_f32(h4.y, l4.y, sb) * inv_f,
+                      split_to_f32(h4.z, l4.z, sb) * inv_f, split_to_f32(h4.w, l4.w, sb) * inv_f);
+      if (counts_out) *reinterpret_cast<uint4*>(counts_out + gi) = *reinterpret_cast<const uint4*>(cnt + i);
+      continue;
+    }
     longlong2 a01, a23;
     if (sb > 0) {  // cell total = HI * 2^sb + LO
       const uint4 l4 = *reinterpret_cast<const uint4*>(reinterpret_cast<const unsigned*>(acc) + i);

@@ -530,6 +530,13 @@ pair_products_cylz_kernel(PPArgs a, const WinDev* __restrict__ wins, const doubl
         }
       }
     }
+    // the task's CW columns are summed in float32 and added to the float64
+    // total once per task (float64 throughput is low on this part)
+    float task[2][NP];
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+      for (int p = 0; p < NP; ++p) task[j][p] = 0.f;
 #pragma unroll
     for (int c = 0; c < CW; ++c) {
       const long long col = col0 + c;
@@ -543,9 +550,13 @@ pair_products_cylz_kernel(PPArgs a, const WinDev* __restrict__ wins, const doubl
         for (int p = 0; p < NP; ++p) {
           float f = j == 0 ? fac[c][p].x : fac[c][p].y;
           if (col == 0 && zk[j]) f -= t00[p] * B[2 * lane + j];  // K(0,0,0) forced to 0
-          acc[j][p] += (double)aj[j] * (double)f;
+          task[j][p] = fmaf(aj[j], f, task[j][p]);
         }
     }
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+      for (int p = 0; p < NP; ++p) acc[j][p] += (double)task[j][p];
   }
   // block reduction over warps (fixed order -> deterministic)
 #pragma unroll
