@@ -324,6 +324,26 @@ int hermes_multipole_contract_bm_async(const float* eps1, const void* fields2, i
                                        const double* gamma, int J, int chunk_x, int ctas_per_sm,
                                        double* dev_out, void* workspace, size_t workspace_bytes,
                                        void* stream);
+/* Degree pairs (no reference counterpart; together they replace the m = 0
+ * terms of degrees l and l + 1 in the loop of calc_DDD_multipole,
+ * utils/corr3pcf_multipoles.py:512-555, for thin shells on the bin-major
+ * layout).  For m = 0 the field a_{l,0} is real for even l and imaginary
+ * for odd l, so one complex field carries both degrees of a pair.
+ * hermes_multipole_fields_pair_bm: l even (l + 1 <= 40); fields_out =
+ * a_{l,0} + a_{l+1,0} for the nb radii, complex64 [nb][L^3], one prepass
+ * and one batched inverse FFT (workspace: hermes_multipole_workspace_size(J,
+ * 1)).  HERMES_ERR_INVALID for odd or out-of-range l.
+ * hermes_multipole_contract_pair_bm_async: on those fields, dev_out[b2][b3]
+ * = (S_{l,0}[b2][b3], S_{l+1,0}[b2][b3]), each the m = 0 summand that
+ * hermes_multipole_contract_bm_async gives for its degree alone (real; the
+ * imaginary parts there are rounding), scaled the same way. */
+int hermes_multipole_fields_pair_bm(const void* half_spec, int J, int l, const double* radii, int nb,
+                                    const double* phi_power, void* fields_out, void* workspace,
+                                    size_t workspace_bytes, void* stream);
+int hermes_multipole_contract_pair_bm_async(const float* eps1, const void* fields, int nb,
+                                            const double* gamma, int J, int chunk_x, int ctas_per_sm,
+                                            double* dev_out, void* workspace, size_t workspace_bytes,
+                                            void* stream);
 int hermes_multipole_contract_plain(const float* eps1, const void* a2, const void* a3,
                                     const double* gamma, int J, double* out,
                                     void* workspace, size_t workspace_bytes, void* stream);

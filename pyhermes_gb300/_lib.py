@@ -59,6 +59,9 @@ SIGNATURES = {
                                                   _p, _c_sz, _p]),
     "hermes_multipole_contract_bm_async": (_c_int, [_p, _p, _c_int, _p, _c_int, _c_int, _p, _c_int, _c_int, _c_int,
                                                     _p, _p, _c_sz, _p]),
+    "hermes_multipole_fields_pair_bm": (_c_int, [_p, _c_int, _c_int, _p, _c_int, _p, _p, _p, _c_sz, _p]),
+    "hermes_multipole_contract_pair_bm_async": (_c_int, [_p, _p, _c_int, _p, _c_int, _c_int, _c_int, _p, _p, _c_sz,
+                                                         _p]),
     "hermes_multipole_contract_status": (_c_int, [_p, _c_sz, _c_int, ctypes.POINTER(_c_int), _p]),
     "hermes_multipole_contract_plain": (_c_int, [_p, _p, _p, _p, _c_int, _p, _p, _c_sz, _p]),
     "hermes_mixing_solve": (_c_int, [_p, _p, _p, _c_int, _c_int, _p, _p, _p, _p]),

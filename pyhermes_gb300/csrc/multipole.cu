@@ -218,6 +218,7 @@ struct YlmConst {
   float pmm;         // (-1)^m (2m-1)!!
   int neg_m;         // requested m < 0
   float neg_sign;    // (-1)^|m|
+  float norm_lo;     // pairs (m = 0, degrees l - 1 and l): norm of degree l - 1
   // upward recurrence P_e = ca[e] ct P_{e-1} - cb[e] P_{e-2}, e = m+2 .. l:
   // ca = (2e-1)/(e-m), cb = (e+m-1)/(e-m) (float64 on the host, then float)
   float ca[kMaxEll + 1], cb[kMaxEll + 1];
@@ -264,12 +265,29 @@ __device__ __forceinline__ float2 ylm_at(const YlmConst& Y, int a, int b, int c,
   return make_float2(yr, yi);
 }
 
+// (Y_{l-1,0}(k), Y_{l,0}(k)) for Y made for (l, 0) with norm_lo set: one
+// Legendre recurrence gives both degrees, each the same float value
+// ylm_at gives for it alone.
+__device__ __forceinline__ float2 ylm_pair_at(const YlmConst& Y, int c, int n2) {
+  if (n2 == 0) return make_float2(Y.l == 1 ? kFourPiInvSqrt : 0.f, 0.f);
+  const float ct = (float)c * rsqrtf((float)n2);
+  float p2 = 1.f, p1 = ct;  // P_0, P_1
+  for (int e = 2; e <= Y.l; ++e) {
+    const float pl = Y.ca[e] * ct * p1 - Y.cb[e] * p2;
+    p2 = p1;
+    p1 = pl;
+  }
+  return make_float2(Y.norm_lo * p2, Y.norm * p1);
+}
+
 // acc[b] = K_lm^b(x, y, z) = sum over the 8 images (a, b', c) (each axis
 // index i in {i - L, i}) of Pphi(|a|) Pphi(|b'|) Pphi(|c|) j_l(|k|) Y_lm(k).
-template <int NB4>
+// kPair: acc[b] = (K_{l-1,0}^b, K_{l,0}^b) from the tables T4 (degree
+// l - 1) and T4b (degree l), Y made for (l, 0) with norm_lo.
+template <int NB4, bool kPair = false>
 __device__ __forceinline__ void mp_window_sum(int x, int y, int z, int L, const float* __restrict__ P,
-                                              const float4* __restrict__ T4, const YlmConst& Y,
-                                              float2 (&acc)[4 * NB4]) {
+                                              const float4* __restrict__ T4, const float4* __restrict__ T4b,
+                                              const YlmConst& Y, float2 (&acc)[4 * NB4]) {
 #pragma unroll
   for (int b = 0; b < 4 * NB4; ++b) acc[b] = make_float2(0.f, 0.f);
   const int ia[2] = {x - L, x}, ib[2] = {y - L, y}, ic[2] = {z - L, z};
@@ -282,16 +300,28 @@ __device__ __forceinline__ void mp_window_sum(int x, int y, int z, int L, const 
       for (int k = 0; k < 2; ++k) {
         const int n2 = ia[i] * ia[i] + ib[j] * ib[j] + ic[k] * ic[k];
         const float pw = pa[i] * pb[j] * pc[k];
-        const float2 yv = ylm_at(Y, ia[i], ib[j], ic[k], n2);
+        const float2 yv = kPair ? ylm_pair_at(Y, ic[k], n2) : ylm_at(Y, ia[i], ib[j], ic[k], n2);
         const float2 yw = make_float2(pw * yv.x, pw * yv.y);  // (Re, Im) of P Y, one paired FMA per bin
         const float4* tr = T4 + (long long)n2 * (kBinStride / 4);
+        if (kPair) {
+          const float4* trb = T4b + (long long)n2 * (kBinStride / 4);
 #pragma unroll
-        for (int q = 0; q < NB4; ++q) {
-          const float4 jl = __ldg(tr + q);
-          acc[4 * q + 0] = __ffma2_rn(make_float2(jl.x, jl.x), yw, acc[4 * q + 0]);
-          acc[4 * q + 1] = __ffma2_rn(make_float2(jl.y, jl.y), yw, acc[4 * q + 1]);
-          acc[4 * q + 2] = __ffma2_rn(make_float2(jl.z, jl.z), yw, acc[4 * q + 2]);
-          acc[4 * q + 3] = __ffma2_rn(make_float2(jl.w, jl.w), yw, acc[4 * q + 3]);
+          for (int q = 0; q < NB4; ++q) {
+            const float4 ja = __ldg(tr + q), jb = __ldg(trb + q);
+            acc[4 * q + 0] = __ffma2_rn(make_float2(ja.x, jb.x), yw, acc[4 * q + 0]);
+            acc[4 * q + 1] = __ffma2_rn(make_float2(ja.y, jb.y), yw, acc[4 * q + 1]);
+            acc[4 * q + 2] = __ffma2_rn(make_float2(ja.z, jb.z), yw, acc[4 * q + 2]);
+            acc[4 * q + 3] = __ffma2_rn(make_float2(ja.w, jb.w), yw, acc[4 * q + 3]);
+          }
+        } else {
+#pragma unroll
+          for (int q = 0; q < NB4; ++q) {
+            const float4 jl = __ldg(tr + q);
+            acc[4 * q + 0] = __ffma2_rn(make_float2(jl.x, jl.x), yw, acc[4 * q + 0]);
+            acc[4 * q + 1] = __ffma2_rn(make_float2(jl.y, jl.y), yw, acc[4 * q + 1]);
+            acc[4 * q + 2] = __ffma2_rn(make_float2(jl.z, jl.z), yw, acc[4 * q + 2]);
+            acc[4 * q + 3] = __ffma2_rn(make_float2(jl.w, jl.w), yw, acc[4 * q + 3]);
+          }
         }
       }
 }
@@ -314,10 +344,18 @@ __device__ __forceinline__ void mp_window_sum(int x, int y, int z, int L, const 
 // window evaluation serves the four reflected lines (x, y), (L-x, y),
 // (x, L-y), (L-x, L-y) at z and, for z not 0 or L/2, their inversions at
 // L - z (the inversion of line a is line 3 - a).
-template <int NB4>
+//
+// kPair: the window is K_{l-1,0} + K_{l,0} for odd l (Y made for (l, 0)
+// with norm_lo, tables T4 for l - 1 and T4b for l).  Both terms are real and
+// reflection-symmetric; under inversion the even one keeps its sign and the
+// odd one flips it, so -k gets K_{l-1,0} - K_{l,0}.  The inverse FFT then
+// gives a_{l-1,0} + a_{l,0}: the real field a_{l-1,0} in the real part and
+// a_{l,0}, which is imaginary, in the imaginary part.
+template <int NB4, bool kPair = false>
 __global__ void __launch_bounds__(256)
 mp_prepass_quad_kernel(const float2* __restrict__ half, int J, const float* __restrict__ P,
-                       const float4* __restrict__ T4, YlmConst Y, int nb, float2* __restrict__ out, float inv_n) {
+                       const float4* __restrict__ T4, const float4* __restrict__ T4b, YlmConst Y, int nb,
+                       float2* __restrict__ out, float inv_n) {
   constexpr int NB = 4 * NB4;
   const int L = 1 << J, H = L / 2 + 1, Q1 = L / 2 - 1;
   const long long N = 1LL << (3 * J);
@@ -328,8 +366,35 @@ mp_prepass_quad_kernel(const float2* __restrict__ half, int J, const float* __re
     const int z = (int)(w % H), li = (int)(w / H);
     const int x = 1 + li / Q1, y = 1 + li % Q1;
     float2 acc[NB];
-    mp_window_sum<NB4>(x, y, z, L, P, T4, Y, acc);
+    mp_window_sum<NB4, kPair>(x, y, z, L, P, T4, T4b, Y, acc);
     const bool mirror = z != 0 && z != L / 2;
+    if (kPair) {
+#pragma unroll
+      for (int a = 0; a < 4; ++a) {
+        const int xa = (a & 1) ? L - x : x, ya = (a & 2) ? L - y : y;
+        const float2 e = half[((long long)xa * L + ya) * H + z];
+        const float er = e.x * inv_n, ei = e.y * inv_n;
+        const long long idx = ((long long)xa * L + ya) * L + z;
+#pragma unroll
+        for (int b = 0; b < NB; ++b) {
+          if (b < nb) {
+            const float k = acc[b].x + acc[b].y;
+            out[b * N + idx] = make_float2(er * k, ei * k);
+          }
+        }
+        if (mirror) {
+          const long long idm = ((long long)(L - xa) * L + (L - ya)) * L + (L - z);
+#pragma unroll
+          for (int b = 0; b < NB; ++b) {
+            if (b < nb) {
+              const float k = acc[b].x - acc[b].y;
+              out[b * N + idm] = make_float2(er * k, -ei * k);  // conj(eps_hat(k)) K(-k) / L^3
+            }
+          }
+        }
+      }
+      continue;
+    }
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
       const int xa = (a & 1) ? L - x : x, ya = (a & 2) ? L - y : y;
@@ -363,10 +428,11 @@ mp_prepass_quad_kernel(const float2* __restrict__ half, int J, const float* __re
 // Edge lines, x in {0, L/2} or y in {0, L/2} (4L - 4 lines): one thread per
 // half-spectrum mode, which also writes its inversion when z is not 0 or
 // L/2, evaluating it on the x = 0 and y = 0 lines.
-template <int NB4>
+template <int NB4, bool kPair = false>
 __global__ void __launch_bounds__(256)
 mp_prepass_edge_kernel(const float2* __restrict__ half, int J, const float* __restrict__ P,
-                       const float4* __restrict__ T4, YlmConst Y, int nb, float2* __restrict__ out, float inv_n) {
+                       const float4* __restrict__ T4, const float4* __restrict__ T4b, YlmConst Y, int nb,
+                       float2* __restrict__ out, float inv_n) {
   constexpr int NB = 4 * NB4;
   const int L = 1 << J, H = L / 2 + 1, Lm = L - 1;
   const long long N = 1LL << (3 * J);
@@ -387,16 +453,27 @@ mp_prepass_edge_kernel(const float2* __restrict__ half, int J, const float* __re
     }
     const float2 e = half[((long long)x * L + y) * H + z];
     float2 acc[NB];
-    mp_window_sum<NB4>(x, y, z, L, P, T4, Y, acc);
+    mp_window_sum<NB4, kPair>(x, y, z, L, P, T4, T4b, Y, acc);
     const float er = e.x * inv_n, ei = e.y * inv_n;
     const long long idx = ((long long)x * L + y) * L + z;
 #pragma unroll
-    for (int b = 0; b < NB; ++b)
-      if (b < nb) out[b * N + idx] = make_float2(er * acc[b].x - ei * acc[b].y, er * acc[b].y + ei * acc[b].x);
+    for (int b = 0; b < NB; ++b) {
+      if (b < nb) {
+        if (kPair) {
+          const float k = acc[b].x + acc[b].y;
+          out[b * N + idx] = make_float2(er * k, ei * k);
+        } else {
+          out[b * N + idx] = make_float2(er * acc[b].x - ei * acc[b].y, er * acc[b].y + ei * acc[b].x);
+        }
+      }
+    }
     if (z == 0 || z == L / 2) continue;
     const int xm = (L - x) & Lm, ym = (L - y) & Lm, zm = L - z;
     if (x == 0 || y == 0) {
-      mp_window_sum<NB4>(xm, ym, zm, L, P, T4, Y, acc);
+      mp_window_sum<NB4, kPair>(xm, ym, zm, L, P, T4, T4b, Y, acc);
+    } else if (kPair) {  // K_{l-1,0} keeps its sign under inversion, K_{l,0} flips it
+#pragma unroll
+      for (int b = 0; b < NB; ++b) acc[b].y = -acc[b].y;
     } else {
 #pragma unroll
       for (int b = 0; b < NB; ++b) {
@@ -407,8 +484,16 @@ mp_prepass_edge_kernel(const float2* __restrict__ half, int J, const float* __re
     const float mr = e.x * inv_n, mi = -(e.y * inv_n);  // conj(eps_hat(k)) / L^3
     const long long idm = ((long long)xm * L + ym) * L + zm;
 #pragma unroll
-    for (int b = 0; b < NB; ++b)
-      if (b < nb) out[b * N + idm] = make_float2(mr * acc[b].x - mi * acc[b].y, mr * acc[b].y + mi * acc[b].x);
+    for (int b = 0; b < NB; ++b) {
+      if (b < nb) {
+        if (kPair) {
+          const float k = acc[b].x + acc[b].y;
+          out[b * N + idm] = make_float2(mr * k, mi * k);
+        } else {
+          out[b * N + idm] = make_float2(mr * acc[b].x - mi * acc[b].y, mr * acc[b].y + mi * acc[b].x);
+        }
+      }
+    }
   }
 }
 
@@ -495,6 +580,7 @@ struct ContractArgs {
   int nb3s;          // bin-major fields: bins of the a3 source to stage
   int conj_src;      // a3 = sign * conj(src3)
   float sign;
+  int packed;        // tensor-core kernel: S = (sum Re a2 Re G, sum Im a2 Im G), not a2 G
   int J, CX;
   GammaC gm;
   double* partial;   // [gridDim.x][16][16][2]
@@ -1212,8 +1298,13 @@ mp_contract_tc_kernel(ContractArgs A, const __grid_constant__ CUtensorMap a2map)
       for (int sp = 0; sp < 3; ++sp) {
         const float* rr = stage + (sp * 32 + 2 * b2) * 33 + 2 * b3;
         const float* ri = rr + 33;  // row of the imaginary part of a2
-        sr += (double)rr[0] - (double)ri[1];
-        si += (double)rr[1] + (double)ri[0];
+        if (A.packed) {  // the two real products, each its own sum
+          sr += (double)rr[0];
+          si += (double)ri[1];
+        } else {
+          sr += (double)rr[0] - (double)ri[1];
+          si += (double)rr[1] + (double)ri[0];
+        }
       }
       dacc[(b2 * kMaxBins + b3) * 2] += sr;
       dacc[(b2 * kMaxBins + b3) * 2 + 1] += si;
@@ -1346,6 +1437,7 @@ YlmConst make_ylm(int l, int m) {
   Y.pmm = (float)pmm;
   Y.neg_m = m < 0 ? 1 : 0;
   Y.neg_sign = (mp % 2 == 1) ? -1.f : 1.f;
+  Y.norm_lo = 0.f;
   for (int e = 0; e <= kMaxEll; ++e) {
     Y.ca[e] = Y.cb[e] = 0.f;
     if (e >= mp + 2 && e <= l) {
@@ -1353,6 +1445,13 @@ YlmConst make_ylm(int l, int m) {
       Y.cb[e] = (float)((double)(e + mp - 1) / (double)(e - mp));
     }
   }
+  return Y;
+}
+
+// the pair (l - 1, 0), (l, 0) for odd l: Y of (l, 0) plus the norm of l - 1
+YlmConst make_ylm_pair(int l) {
+  YlmConst Y = make_ylm(l, 0);
+  Y.norm_lo = make_ylm(l - 1, 0).norm;
   return Y;
 }
 
@@ -1369,6 +1468,7 @@ namespace {
 // The one workspace layout of the fields and contraction calls.
 struct MpWs {
   float* T;          // radial table [n2][16]
+  float* T2;         // second radial table (pairs of degrees)
   float* Pf;         // phi power, float
   double* partial;   // per-block partial sums [1024][16][16][2]
   double* dout;      // reduced S [16][16][2]
@@ -1381,6 +1481,7 @@ MpWs carve_ws(void* ws, size_t cap, int J, int nb) {
   MpWs w;
   c.take<float>(2 * kMaxBins);  // rho double-float (kept for layout stability)
   w.T = c.take<float>(table_floats(J));
+  w.T2 = c.take<float>(table_floats(J));
   w.Pf = c.take<float>((1 << J) + 1);
   w.partial = c.take<double>((size_t)1024 * kMaxBins * kMaxBins * 2);
   w.dout = c.take<double>((size_t)kMaxBins * kMaxBins * 2);
@@ -1410,6 +1511,7 @@ namespace {
 // batched inverse FFT and the interleave.
 struct FieldsCtx {
   float* T;
+  float* T2;
   float* Pf;
   float2* binmajor;
   float2* out;
@@ -1437,6 +1539,7 @@ int fields_setup(const void* half_spec, int J, int l, int m, int nb, const doubl
   ctx->bin_major = bin_major;
   const MpWs w = carve_ws(workspace, workspace_bytes, J, bin_major ? 1 : nb);
   ctx->T = w.T;
+  ctx->T2 = w.T2;
   ctx->Pf = w.Pf;
   ctx->out = static_cast<float2*>(fields_out);
   ctx->binmajor = (nb > 1 && !bin_major) ? w.binmajor : ctx->out;
@@ -1445,25 +1548,34 @@ int fields_setup(const void* half_spec, int J, int l, int m, int nb, const doubl
   return HERMES_OK;
 }
 
-int fields_run(const FieldsCtx& ctx, const void* half_spec, int J, int l, int m, int nb) {
+// pair: the window K_{l,0} + K_{l+1,0} for even l, with the radial tables
+// of l in ctx.T and of l + 1 in ctx.T2 (m is 0).
+int fields_run(const FieldsCtx& ctx, const void* half_spec, int J, int l, int m, int nb, bool pair = false) {
   cudaStream_t s = ctx.s;
-  const YlmConst Y = make_ylm(l, m);
+  const YlmConst Y = pair ? make_ylm_pair(l + 1) : make_ylm(l, m);
   const float inv_n = (float)(1.0 / (double)ctx.N);
   const int grid = ctx.nsm * 8;
   const float2* half = static_cast<const float2*>(half_spec);
   const float4* T4 = reinterpret_cast<const float4*>(ctx.T);
+  const float4* T4b = reinterpret_cast<const float4*>(ctx.T2);
   const long long we = (long long)(4 * ctx.L - 4) * (ctx.L / 2 + 1);
   const int grid_e = (int)std::min<long long>(grid, (we + 255) / 256);
-  if (nb <= 4) {
-    mp_prepass_quad_kernel<1><<<grid, 256, 0, s>>>(half, J, ctx.Pf, T4, Y, nb, ctx.binmajor, inv_n);
-    mp_prepass_edge_kernel<1><<<grid_e, 256, 0, s>>>(half, J, ctx.Pf, T4, Y, nb, ctx.binmajor, inv_n);
-  } else if (nb <= 8) {
-    mp_prepass_quad_kernel<2><<<grid, 256, 0, s>>>(half, J, ctx.Pf, T4, Y, nb, ctx.binmajor, inv_n);
-    mp_prepass_edge_kernel<2><<<grid_e, 256, 0, s>>>(half, J, ctx.Pf, T4, Y, nb, ctx.binmajor, inv_n);
+#define HERMES_PREPASS(NB4, PAIR)                                                                               \
+  do {                                                                                                          \
+    mp_prepass_quad_kernel<NB4, PAIR><<<grid, 256, 0, s>>>(half, J, ctx.Pf, T4, T4b, Y, nb, ctx.binmajor, inv_n); \
+    mp_prepass_edge_kernel<NB4, PAIR><<<grid_e, 256, 0, s>>>(half, J, ctx.Pf, T4, T4b, Y, nb, ctx.binmajor,      \
+                                                            inv_n);                                            \
+  } while (0)
+  if (pair) {
+    if (nb <= 4) HERMES_PREPASS(1, true);
+    else if (nb <= 8) HERMES_PREPASS(2, true);
+    else HERMES_PREPASS(4, true);
   } else {
-    mp_prepass_quad_kernel<4><<<grid, 256, 0, s>>>(half, J, ctx.Pf, T4, Y, nb, ctx.binmajor, inv_n);
-    mp_prepass_edge_kernel<4><<<grid_e, 256, 0, s>>>(half, J, ctx.Pf, T4, Y, nb, ctx.binmajor, inv_n);
+    if (nb <= 4) HERMES_PREPASS(1, false);
+    else if (nb <= 8) HERMES_PREPASS(2, false);
+    else HERMES_PREPASS(4, false);
   }
+#undef HERMES_PREPASS
   HERMES_LAUNCH_CHECK("mp_prepass_kernel");
   cufftHandle h;
   int rc = hermes::get_plan_c2c_batch(J, nb, &h);
@@ -1485,7 +1597,7 @@ int fields_run(const FieldsCtx& ctx, const void* half_spec, int J, int l, int m,
 
 static int fields_radii(const void* half_spec, int J, int l, int m, const double* radii, int nb,
                         const double* phi_power, void* fields_out, void* workspace, size_t workspace_bytes,
-                        void* stream, bool bin_major) {
+                        void* stream, bool bin_major, bool pair = false) {
   if (!radii) return fail(HERMES_ERR_INVALID, "multipole_fields: NULL argument");
   FieldsCtx ctx;
   int rc = fields_setup(half_spec, J, l, m, nb, phi_power, fields_out, workspace, workspace_bytes, stream, &ctx,
@@ -1501,7 +1613,11 @@ static int fields_radii(const void* half_spec, int J, int l, int m, const double
   }
   mp_jl_table_kernel<<<ctx.nsm * 8, 256, 0, ctx.s>>>(ctx.T, 3 * ctx.L * ctx.L, hrho, nb, l);
   HERMES_LAUNCH_CHECK("mp_jl_table_kernel");
-  return fields_run(ctx, half_spec, J, l, m, nb);
+  if (pair) {
+    mp_jl_table_kernel<<<ctx.nsm * 8, 256, 0, ctx.s>>>(ctx.T2, 3 * ctx.L * ctx.L, hrho, nb, l + 1);
+    HERMES_LAUNCH_CHECK("mp_jl_table_kernel");
+  }
+  return fields_run(ctx, half_spec, J, l, m, nb, pair);
 }
 
 extern "C" int hermes_multipole_fields(const void* half_spec, int J, int l, int m, const double* radii,
@@ -1516,6 +1632,15 @@ extern "C" int hermes_multipole_fields_bm(const void* half_spec, int J, int l, i
                                           size_t workspace_bytes, void* stream) {
   return fields_radii(half_spec, J, l, m, radii, nb, phi_power, fields_out, workspace, workspace_bytes, stream,
                       true);
+}
+
+extern "C" int hermes_multipole_fields_pair_bm(const void* half_spec, int J, int l, const double* radii, int nb,
+                                               const double* phi_power, void* fields_out, void* workspace,
+                                               size_t workspace_bytes, void* stream) {
+  if (l < 0 || l + 1 > kMaxEll || (l & 1))
+    return fail(HERMES_ERR_INVALID, "multipole_fields_pair: l=%d must be even and below %d", l, kMaxEll);
+  return fields_radii(half_spec, J, l, 0, radii, nb, phi_power, fields_out, workspace, workspace_bytes, stream,
+                      true, true);
 }
 
 static int fields_window(const void* half_spec, int J, int l, int m, const hermes_window_t* bins, int nb,
@@ -1663,7 +1788,8 @@ enum { kEngineTensor = 0, kEngineSimt = 1, kEngineTensorBinMajor = 2 };
 // hermes_multipole_fields_bm.
 static int mp_contract_launch(const float* eps1, const void* fields2, int nb2, const void* fields3, int nb3,
                               int conj_sign, const double* gamma, int J, int chunk_x, int ctas_per_sm, double scale,
-                              double* dout, void* workspace, size_t workspace_bytes, cudaStream_t s, int engine) {
+                              double* dout, void* workspace, size_t workspace_bytes, cudaStream_t s, int engine,
+                              int packed = 0) {
   if (!eps1 || !fields2 || !gamma || !dout) return fail(HERMES_ERR_INVALID, "multipole_contract: NULL argument");
   if (nb2 < 1 || nb2 > kMaxBins) return fail(HERMES_ERR_INVALID, "multipole_contract: nb2=%d", nb2);
   const int conj_src = fields3 == nullptr;
@@ -1714,6 +1840,7 @@ static int mp_contract_launch(const float* eps1, const void* fields2, int nb2, c
   A.nb3s = nb3;
   A.conj_src = conj_src;
   A.sign = (float)conj_sign;
+  A.packed = packed;
   A.J = J;
   A.CX = chunk_x;
   A.gm = make_gamma(gamma);
@@ -1782,10 +1909,10 @@ extern "C" int hermes_multipole_contract(const float* eps1, const void* fields2,
 
 static int contract_async(const float* eps1, const void* fields2, int nb2, const void* fields3, int nb3,
                           int conj_sign, const double* gamma, int J, int chunk_x, int ctas_per_sm, double* dev_out,
-                          void* workspace, size_t workspace_bytes, void* stream, int engine) {
+                          void* workspace, size_t workspace_bytes, void* stream, int engine, int packed = 0) {
   const double scale = 4.0 * 3.141592653589793 / (double)(1LL << (3 * (J < 0 ? 0 : (J > 10 ? 10 : J))));
   return mp_contract_launch(eps1, fields2, nb2, fields3, nb3, conj_sign, gamma, J, chunk_x, ctas_per_sm, scale,
-                            dev_out, workspace, workspace_bytes, hermes::as_stream(stream), engine);
+                            dev_out, workspace, workspace_bytes, hermes::as_stream(stream), engine, packed);
 }
 
 extern "C" int hermes_multipole_contract_async(const float* eps1, const void* fields2, int nb2, const void* fields3,
@@ -1810,6 +1937,19 @@ extern "C" int hermes_multipole_contract_bm_async(const float* eps1, const void*
                                                   void* workspace, size_t workspace_bytes, void* stream) {
   return contract_async(eps1, fields2, nb2, fields3, nb3, conj_sign, gamma, J, chunk_x, ctas_per_sm, dev_out,
                         workspace, workspace_bytes, stream, kEngineTensorBinMajor);
+}
+
+// fields = a_{l,0} + a_{l+1,0} from hermes_multipole_fields_pair_bm: with
+// a3 = conj(fields), the real part of a2 G is sum a_{l,0} G(a_{l,0}) =
+// S_{l,0} and the product of the imaginary parts is
+// sum (a_{l+1,0}/i) G(-a_{l+1,0}/i) = sum a_{l+1,0} G(a_{l+1,0}) = S_{l+1,0},
+// read as separate blocks of the tensor-core accumulator.
+extern "C" int hermes_multipole_contract_pair_bm_async(const float* eps1, const void* fields, int nb,
+                                                       const double* gamma, int J, int chunk_x, int ctas_per_sm,
+                                                       double* dev_out, void* workspace, size_t workspace_bytes,
+                                                       void* stream) {
+  return contract_async(eps1, fields, nb, nullptr, nb, 1, gamma, J, chunk_x, ctas_per_sm, dev_out, workspace,
+                        workspace_bytes, stream, kEngineTensorBinMajor, 1);
 }
 
 extern "C" int hermes_multipole_contract_status(const void* workspace, size_t workspace_bytes, int J, int* status,

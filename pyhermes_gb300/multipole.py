@@ -101,6 +101,45 @@ def multipole_fields(half_spec, J, l, m, radii_grid, phi_power, out=None, ws=Non
     return out
 
 
+def multipole_fields_pair(half_spec, J, l, radii_grid, phi_power, out=None, ws=None):
+    """a_{l,0} + a_{l+1,0} for even l and thin-shell radii (grid units),
+    bin-major complex64 [nb, L^3] (hermes_multipole_fields_pair_bm): the real
+    field a_{l,0} in the real part and the imaginary field a_{l+1,0} in the
+    imaginary part, from one prepass and one inverse FFT."""
+    nb = len(radii_grid)
+    dev = half_spec.device
+    if out is None:
+        out = torch.empty((nb, 1 << (3 * J)), dtype=torch.complex64, device=dev)
+    if ws is None:
+        ws = _workspace(fields_ws_bytes(J, nb, True), dev)
+    radii = (ctypes.c_double * nb)(*[float(r) for r in radii_grid])
+    _lib.check(_lib.load().hermes_multipole_fields_pair_bm(_ptr(half_spec), J, int(l), radii, nb, _ptr(phi_power),
+                                                           _ptr(out), _ptr(ws), ws.numel(), _stream_ptr(dev)),
+               "hermes_multipole_fields_pair_bm")
+    return out
+
+
+def multipole_contract_pair_async(eps1, fields, nb, gamma_c, J, dev_out, chunk_x=0, ctas_per_sm=0, ws=None):
+    """hermes_multipole_contract_pair_bm_async: dev_out[b2, b3] = (S_{l,0},
+    S_{l+1,0}) (times 4 pi / L^3) from the fields of multipole_fields_pair."""
+    dev = eps1.device
+    if ws is None:
+        ws = _workspace(_ws_bytes(J, 1), dev)
+    _lib.check(_lib.load().hermes_multipole_contract_pair_bm_async(_ptr(eps1), _ptr(fields), nb, gamma_c, J,
+                                                                   int(chunk_x), int(ctas_per_sm), _ptr(dev_out),
+                                                                   _ptr(ws), ws.numel(), _stream_ptr(dev)),
+               "hermes_multipole_contract_pair_bm_async")
+    return dev_out
+
+
+def degree_pairs(lms):
+    """Even l with (l, 0) and (l + 1, 0) both in lms: the m = 0 terms one
+    paired fields pass and contraction serve (a_{l,0} is real for even l and
+    imaginary for odd l, so one complex field carries both)."""
+    have = set(lms)
+    return [l for l in sorted({l for l, _ in lms}) if l % 2 == 0 and (l, 0) in have and (l + 1, 0) in have]
+
+
 class BinSpec:
     """One radial bin of a multipole window: radial profile type, physical
     len_args and the binning window's other_args (profile configuration)."""
@@ -329,7 +368,7 @@ class GraphedMultipole:
     contraction tile choices (see autotune.tune_contract)."""
 
     def __init__(self, J, box_size, radii_phys, l_max, phi_array, device, phi_resolution=1024, chunk_x=0,
-                 ctas_per_sm=0, use_graph=True):
+                 ctas_per_sm=0, use_graph=True, pair_degrees=True):
         self.J, self.L, self.box = int(J), 1 << int(J), float(box_size)
         self.dev = torch.device(device)
         self.radii = [float(r) for r in radii_phys]
@@ -338,6 +377,8 @@ class GraphedMultipole:
         self.grid = [r * self.L / self.box for r in self.radii]
         self.l_max = int(l_max)
         self.lm = [(l, m) for l in range(self.l_max + 1) for m in range(l + 1)]
+        # m = 0 terms of degrees (l, l + 1) from one paired fields pass and contraction
+        self.pairs = degree_pairs(self.lm) if pair_degrees else []
         phi = np.asarray(phi_array, dtype=np.float64)
         self.gamma = (ctypes.c_double * 9)(*cal_gamma(phi, phi.shape[0] // phi_resolution, phi_resolution).ravel())
         self.P = phi_power_device(phi, self.L, 1, phi_resolution, self.dev)
@@ -346,7 +387,8 @@ class GraphedMultipole:
         self.spec = torch.empty((L, L, L // 2 + 1), dtype=torch.complex64, device=self.dev)
         # bin-major fields [nb, L^3], as the inverse FFT leaves them
         self.fields = torch.empty((len(self.grid), L ** 3), dtype=torch.complex64, device=self.dev)
-        self.out = torch.zeros((len(self.lm), MAX_BINS, MAX_BINS, 2), dtype=torch.float64, device=self.dev)
+        self.out = torch.zeros((len(self.lm) + len(self.pairs), MAX_BINS, MAX_BINS, 2), dtype=torch.float64,
+                               device=self.dev)
         # own workspace: a captured graph must never see the shared one reallocated
         self.ws = torch.empty(max(fields_ws_bytes(self.J, len(self.grid), True), 256), dtype=torch.uint8,
                               device=self.dev)
@@ -358,7 +400,14 @@ class GraphedMultipole:
         lib = _lib.load()
         _lib.check(lib.hermes_fft_r2c(_ptr(self.eps), _ptr(self.spec), self.J, _stream_ptr(self.dev)), "hermes_fft_r2c")
         nb = len(self.grid)
+        for j, l in enumerate(self.pairs):
+            multipole_fields_pair(self.spec, self.J, l, self.grid, self.P, out=self.fields, ws=self.ws)
+            multipole_contract_pair_async(self.eps, self.fields, nb, self.gamma, self.J, self.out[len(self.lm) + j],
+                                          chunk_x=self.chunk_x, ctas_per_sm=self.ctas, ws=self.ws)
+        paired = {(l + d, 0) for l in self.pairs for d in (0, 1)}
         for k, (l, m) in enumerate(self.lm):
+            if (l, m) in paired:
+                continue
             multipole_fields(self.spec, self.J, l, m, self.grid, self.P, out=self.fields, ws=self.ws, bin_major=True)
             multipole_contract_async(self.eps, self.fields, nb, self.gamma, self.J, self.out[k],
                                      conj_sign=(-1) ** ((l + m) % 2), chunk_x=self.chunk_x,
@@ -380,7 +429,13 @@ class GraphedMultipole:
             self.graph.replay()
         nb = len(self.grid)
         o = self.out[:, :nb, :nb].cpu().numpy()
-        return o[..., 0] + 1j * o[..., 1]
+        n = len(self.lm)
+        S = o[:n, ..., 0] + 1j * o[:n, ..., 1]
+        k_of = {lm: k for k, lm in enumerate(self.lm)}
+        for j, l in enumerate(self.pairs):
+            S[k_of[(l, 0)]] = o[n + j, ..., 0]
+            S[k_of[(l + 1, 0)]] = o[n + j, ..., 1]
+        return S
 
     def ddd(self, delta, pairs, l_min=0):
         """DDD_l [n_samples, n_l] for (r12, r13) samples drawn from the radii
@@ -409,10 +464,13 @@ class MultipoleEngine:
     """Batched multipole contraction of three fields over radius pairs."""
 
     def __init__(self, eps1, eps2, eps3, phi_array, J, box_size, phi_resolution=1024, share23=None,
-                 engine="tensor"):
+                 engine="tensor", pair_degrees=True):
         if engine not in ENGINES:
             raise ValueError(f"engine must be one of {ENGINES}")
         self.engine = engine
+        # m = 0 terms of degrees (l, l + 1) from one paired fields pass and
+        # contraction (summands_shared, tensor engine, thin shells)
+        self.pair_degrees = bool(pair_degrees)
         self.bin_major = engine == "tensor"
         self.J = int(J)
         self.L = 1 << self.J
@@ -446,9 +504,18 @@ class MultipoleEngine:
         if not (self.same23 and 1 <= nb <= MAX_BINS):
             raise ValueError("summands_shared needs vertices 2 and 3 to share the field and 1..16 bins")
         g = (ctypes.c_double * 9)(*np.asarray(self.gamma, dtype=np.float64).ravel())
-        out = torch.zeros((len(lms), MAX_BINS, MAX_BINS, 2), dtype=torch.float64, device=self.dev)
+        k_of = {lm: k for k, lm in enumerate(lms)}
+        pairs = self._degree_pairs(lms, bins)
+        paired = {(l + d, 0) for l in pairs for d in (0, 1)}
+        out = torch.zeros((len(lms) + len(pairs), MAX_BINS, MAX_BINS, 2), dtype=torch.float64, device=self.dev)
         t0 = time.perf_counter()
+        for j, l in enumerate(pairs):
+            f = multipole_fields_pair(self.spec2, self.J, l, self._grid(bins), self.P)
+            multipole_contract_pair_async(self.eps1, f, nb, g, self.J, out[len(lms) + j])
+            del f
         for k, (l, m) in enumerate(lms):
+            if (l, m) in paired:
+                continue
             f = self._fields(self.spec2, l, m, bins)
             multipole_contract_async(self.eps1, f, nb, g, self.J, out[k], conj_sign=(-1) ** ((l + m) % 2),
                                      engine=self.engine, bin_major=self.bin_major)
@@ -457,7 +524,26 @@ class MultipoleEngine:
         # the fields passes and contractions run queued together; their time
         # is counted under contract_s
         self.timing["contract_s"] += time.perf_counter() - t0
-        return o[..., 0] + 1j * o[..., 1]
+        S = o[:len(lms), ..., 0] + 1j * o[:len(lms), ..., 1]
+        for j, l in enumerate(pairs):
+            S[k_of[(l, 0)]] = o[len(lms) + j, ..., 0]
+            S[k_of[(l + 1, 0)]] = o[len(lms) + j, ..., 1]
+        return S
+
+    def _grid(self, bins):
+        """Thin-shell radii of bins in grid units."""
+        g2p = self.L / self.box
+        return [(b.len_args["R_shell"] if b.type == "gaussian_shell" else b.len_args["R"]) * g2p for b in bins]
+
+    def _degree_pairs(self, lms, bins):
+        """degree_pairs(lms) where the paired kernels apply: tensor engine,
+        thin-shell bins."""
+        if not (self.bin_major and self.pair_degrees):
+            return []
+        from . import radial_profiles as rp
+
+        return [l for l in degree_pairs(lms)
+                if all(rp.profile_mode(b.type, b.len_args, d) == "shell" for b in bins for d in (l, l + 1))]
 
     def summands(self, l, m, r12_phys, r13_phys):
         """S_m[i, j] for two lists of radial bins (thin-shell radii in physical

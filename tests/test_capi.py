@@ -71,3 +71,11 @@ def test_deposit_tile_setting(lib):
 def test_phi_prepare_rejects_bad_arguments(lib):
     assert lib.hermes_phi_prepare(None, 3072, 1024, 64, 1, None, None, None) == -1
     assert b"phi is NULL" in lib.hermes_last_error()
+
+
+def test_degree_pair_entries_reject_bad_arguments(lib):
+    # odd or out-of-range degrees are refused before any device work
+    for l in (1, 3, -2, 40):
+        assert lib.hermes_multipole_fields_pair_bm(None, 7, l, None, 4, None, None, None, 0, None) == -1, l
+        assert b"multipole_fields_pair" in lib.hermes_last_error()
+    assert lib.hermes_multipole_contract_pair_bm_async(None, None, 4, None, 7, 0, 0, None, None, 0, None) == -1
