@@ -344,6 +344,18 @@ int hermes_multipole_contract_pair_bm_async(const float* eps1, const void* field
                                             const double* gamma, int J, int chunk_x, int ctas_per_sm,
                                             double* dev_out, void* workspace, size_t workspace_bytes,
                                             void* stream);
+/* The inverse 3-D FFT of the multipole fields (replaces the ifftn of
+ * _stream_convolution_fields, utils/corr3pcf_multipoles.py:267-321).
+ * hermes_multipole_set_fft: 0 = cuFFT's batched 3-D plan; 1 (default) = at
+ * J = 9, cuFFT's 1-D z lines followed by hermes_fft512_strided_inverse over
+ * y and x (other J keep the 3-D plan).  Returns the previous mode,
+ * HERMES_ERR_INVALID outside [0, 1].  Process-wide.
+ * hermes_fft512_strided_inverse: in-place unnormalised inverse 512-point
+ * FFTs (e^{+2 pi i n k / 512}, as CUFFT_INVERSE) along axis 0 (x, element
+ * stride 512^2) or 1 (y, stride 512) of nfields (1..64) complex64 fields
+ * [512][512][512]. */
+int hermes_multipole_set_fft(int mode);
+int hermes_fft512_strided_inverse(void* data, int nfields, int axis, void* stream);
 int hermes_multipole_contract_plain(const float* eps1, const void* a2, const void* a3,
                                     const double* gamma, int J, double* out,
                                     void* workspace, size_t workspace_bytes, void* stream);

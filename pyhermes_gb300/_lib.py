@@ -59,6 +59,8 @@ SIGNATURES = {
                                                   _p, _c_sz, _p]),
     "hermes_multipole_contract_bm_async": (_c_int, [_p, _p, _c_int, _p, _c_int, _c_int, _p, _c_int, _c_int, _c_int,
                                                     _p, _p, _c_sz, _p]),
+    "hermes_multipole_set_fft": (_c_int, [_c_int]),
+    "hermes_fft512_strided_inverse": (_c_int, [_p, _c_int, _c_int, _p]),
     "hermes_multipole_fields_pair_bm": (_c_int, [_p, _c_int, _c_int, _p, _c_int, _p, _p, _p, _c_sz, _p]),
     "hermes_multipole_contract_pair_bm_async": (_c_int, [_p, _p, _c_int, _p, _c_int, _c_int, _c_int, _p, _p, _c_sz,
                                                          _p]),

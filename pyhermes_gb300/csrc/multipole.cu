@@ -28,6 +28,7 @@
 #include <cufft.h>
 
 #include <algorithm>
+#include <atomic>
 #include <map>
 #include <mutex>
 #include <tuple>
@@ -41,6 +42,8 @@
 
 namespace hermes {
 int get_plan_c2c_batch(int J, int batch, cufftHandle* out);
+int get_plan_c2c_lines(int J, int fields, cufftHandle* out);
+int fft512_strided_inverse(float2* data, int nf, int axis, cudaStream_t s);
 int prepare_window(const hermes_window_t& in, int L, WinDev* out);
 }
 
@@ -1548,6 +1551,12 @@ int fields_setup(const void* half_spec, int J, int l, int m, int nb, const doubl
   return HERMES_OK;
 }
 
+// Inverse 3-D FFT of the fields: 0 = cuFFT's 3-D plan; 1 (default) = at
+// J = 9, cuFFT's 1-D z lines (contiguous, near HBM speed) then
+// fft512_strided_inverse over y and x in place of cuFFT's strided passes
+// (15 fields: 19.95 ms per fields call against 25.7 ms).
+std::atomic<int> g_fft_mode{1};
+
 // pair: the window K_{l,0} + K_{l+1,0} for even l, with the radial tables
 // of l in ctx.T and of l + 1 in ctx.T2 (m is 0).
 int fields_run(const FieldsCtx& ctx, const void* half_spec, int J, int l, int m, int nb, bool pair = false) {
@@ -1577,14 +1586,22 @@ int fields_run(const FieldsCtx& ctx, const void* half_spec, int J, int l, int m,
   }
 #undef HERMES_PREPASS
   HERMES_LAUNCH_CHECK("mp_prepass_kernel");
+  const int fft_mode = g_fft_mode.load();
+  const bool own = J == 9 && fft_mode != 0;
   cufftHandle h;
-  int rc = hermes::get_plan_c2c_batch(J, nb, &h);
+  int rc = own ? hermes::get_plan_c2c_lines(J, nb, &h) : hermes::get_plan_c2c_batch(J, nb, &h);
   if (rc) return rc;
   cufftResult r = cufftSetStream(h, s);
   if (r != CUFFT_SUCCESS) return fail(HERMES_ERR_CUFFT, "cufftSetStream failed: %d", (int)r);
   r = cufftExecC2C(h, reinterpret_cast<cufftComplex*>(ctx.binmajor), reinterpret_cast<cufftComplex*>(ctx.binmajor),
                    CUFFT_INVERSE);
   if (r != CUFFT_SUCCESS) return fail(HERMES_ERR_CUFFT, "cufftExecC2C failed: %d", (int)r);
+  if (own) {  // z lines by cuFFT above, then the y and x passes
+    rc = hermes::fft512_strided_inverse(ctx.binmajor, nb, 1, s);
+    if (rc) return rc;
+    rc = hermes::fft512_strided_inverse(ctx.binmajor, nb, 0, s);
+    if (rc) return rc;
+  }
   if (nb > 1 && !ctx.bin_major) {
     long long nblk = ctx.N / kIlCells;
     if (nblk > (long long)ctx.nsm * 16) nblk = (long long)ctx.nsm * 16;
@@ -1632,6 +1649,11 @@ extern "C" int hermes_multipole_fields_bm(const void* half_spec, int J, int l, i
                                           size_t workspace_bytes, void* stream) {
   return fields_radii(half_spec, J, l, m, radii, nb, phi_power, fields_out, workspace, workspace_bytes, stream,
                       true);
+}
+
+extern "C" int hermes_multipole_set_fft(int mode) {
+  if (mode < 0 || mode > 1) return fail(HERMES_ERR_INVALID, "multipole_set_fft: mode=%d outside [0, 1]", mode);
+  return g_fft_mode.exchange(mode);
 }
 
 extern "C" int hermes_multipole_fields_pair_bm(const void* half_spec, int J, int l, const double* radii, int nb,

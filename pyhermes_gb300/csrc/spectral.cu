@@ -22,7 +22,7 @@
 namespace hermes {
 
 // ---- cuFFT plan cache ----------------------------------------------------
-enum PlanKind { kR2C = 0, kC2R = 1, kC2C = 2 };
+enum PlanKind { kR2C = 0, kC2R = 1, kC2C = 2, kC2CLines = 3 };
 
 static std::mutex g_plan_mu;
 static std::map<std::tuple<int, int, int, int>, cufftHandle> g_plans;
@@ -39,6 +39,14 @@ int get_plan(int J, PlanKind kind, int batch, cufftHandle* out) {
   }
   cufftHandle h;
   const int L = 1 << J;
+  if (kind == kC2CLines) {  // 1-D transforms of the batch * L^2 contiguous z lines
+    int n1[1] = {L};
+    cufftResult r = cufftPlanMany(&h, 1, n1, nullptr, 1, L, nullptr, 1, L, CUFFT_C2C, batch * L * L);
+    if (r != CUFFT_SUCCESS) return fail(HERMES_ERR_CUFFT, "cufftPlanMany(lines, J=%d, batch=%d) failed: %d", J, batch, (int)r);
+    g_plans[key] = h;
+    *out = h;
+    return HERMES_OK;
+  }
   int n[3] = {L, L, L};
   cufftType t = kind == kR2C ? CUFFT_R2C : (kind == kC2R ? CUFFT_C2R : CUFFT_C2C);
   long long dist_in = kind == kC2R ? (long long)L * L * (L / 2 + 1) : (long long)L * L * L;
@@ -50,11 +58,12 @@ int get_plan(int J, PlanKind kind, int batch, cufftHandle* out) {
   return HERMES_OK;
 }
 
-// Batched C2C plan over `batch` interleaved fields: element (cell, b) at
-// cell * stride + b (stride >= batch), i.e. istride = stride, idist = 1.
-
 // Batched contiguous complex-to-complex plan (batch fields of L^3, distance L^3).
 int get_plan_c2c_batch(int J, int batch, cufftHandle* out) { return get_plan(J, kC2C, batch, out); }
+
+// 1-D complex-to-complex plan over the z lines (length L, contiguous) of
+// `fields` fields of L^3.
+int get_plan_c2c_lines(int J, int fields, cufftHandle* out) { return get_plan(J, kC2CLines, fields, out); }
 
 #define HERMES_CUFFT_TRY(expr)                                                   \
   do {                                                                           \

@@ -79,3 +79,13 @@ def test_degree_pair_entries_reject_bad_arguments(lib):
         assert lib.hermes_multipole_fields_pair_bm(None, 7, l, None, 4, None, None, None, 0, None) == -1, l
         assert b"multipole_fields_pair" in lib.hermes_last_error()
     assert lib.hermes_multipole_contract_pair_bm_async(None, None, 4, None, 7, 0, 0, None, None, 0, None) == -1
+
+
+def test_fft_mode_switch(lib):
+    prev = lib.hermes_multipole_set_fft(0)
+    assert prev in (0, 1)
+    assert lib.hermes_multipole_set_fft(prev) == 0
+    for bad in (-1, 2):
+        assert lib.hermes_multipole_set_fft(bad) == -1
+        assert b"multipole_set_fft" in lib.hermes_last_error()
+    assert lib.hermes_fft512_strided_inverse(None, 1, 0, None) == -1
