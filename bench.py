@@ -933,8 +933,9 @@ def run_gb300(args, ws, rank, local):
                      "stencil_fp32": {"flops": stencil_flops, "achieved_tflops": stencil_flops / t_con["tensor"] / 1e12,
                                       "nominal_peak_tflops": 80.6,
                                       "frac": stencil_flops / t_con["tensor"] / 1e12 / 80.6}},
-        "fields_roofline": {"kernels": "mp_jl_table + mp_prepass_quad/edge + cuFFT C2C x15 (bin-major output, "
-                                       "read as is by the tensor-core contraction)",
+        "fields_roofline": {"kernels": "mp_jl_table + mp_prepass_quad/edge + inverse FFT of 15 fields (cuFFT 1-D z "
+                                       "lines, fft512_cols_kernel over y and x; bin-major output, read as is by the "
+                                       "tensor-core contraction)",
                             "bound": "hbm", "ms_per_lm": t_fld["bin_major"] * 1e3, "algorithmic_bytes": fld_bytes,
                             "achieved": fld_bytes / t_fld["bin_major"] / 1e9, "peak": hbm, "peak_kind": kind,
                             "unit": "GB/s", "frac": fld_bytes / t_fld["bin_major"] / 1e9 / hbm,
