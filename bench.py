@@ -817,10 +817,11 @@ def run_gb300(args, ws, rank, local):
     value = t_total / (args.steps * ws)
     zeta = np.asarray(res.zeta_l)
 
-    # our kernels per step: 2 deposits x 7; per product per (l, m): fields (power, j_l table,
-    # interior and edge prepass; the inverse FFT is cuFFT, its bin-major output is read as is) +
-    # contract (tensor-core contraction, reduce); the mixing solve
-    kernel_launches = args.steps * (14 + 2 * N_LM * 6 + 1)
+    # our kernels per step: 2 deposits x 7; per product, per single (l, m) term 8 (fields: power,
+    # j_l table, interior and edge prepass, the y and x FFT passes after cuFFT's z lines; contract:
+    # tensor-core contraction, reduce) and per degree pair 9 (a second j_l table); the mixing solve
+    n_pairs = len(mp.degree_pairs([(l, m) for l in range(MP_LMAX + 1) for m in range(l + 1)]))
+    kernel_launches = args.steps * (14 + 2 * ((N_LM - 2 * n_pairs) * 8 + n_pairs * 9) + 1)
 
     # end to end: catalogues in pinned host memory, copies inside the timed region
     h = [torch.as_tensor(a).pin_memory() for a in (dpos_np, dw_np, rpos_np, rw_np)]
