@@ -230,8 +230,10 @@ int hermes_pair_products(const void* const* spectra, int n_spec, const int32_t* 
  * reference's per-cell loop form (workspace >= 16*(#SM*8+1) bytes).
  *
  * hermes_multipole_workspace_size(J, nb): bytes of device workspace for
- * fields/contract calls with up to nb bins (for nb > 1 this includes the
- * nb * L^3 complex64 bin-major fields that cuFFT transforms).
+ * fields/contract calls with up to nb bins: two radial tables of
+ * (3 L^2 + 1) x 16 floats (the second for degree pairs), the contraction's
+ * partial sums and, for nb > 1, the nb * L^3 complex64 bin-major fields
+ * that the inverse FFT transforms before the interleave.
  */
 int hermes_multipole_workspace_size(int J, int nb, size_t* bytes);
 int hermes_multipole_fields(const void* half_spec, int J, int l, int m,
