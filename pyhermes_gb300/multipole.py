@@ -498,7 +498,9 @@ class MultipoleEngine:
         shared by vertices 2 and 3 (a_{l,-m} from the conjugate of a_lm),
         complex128 [len(lms), nb, nb]: every fields pass and contraction is
         queued on the current stream into one device array, which is read
-        back once (no host round trip per (l, m))."""
+        back once (no host round trip per (l, m)).  With the tensor engine
+        and thin-shell bins, the m = 0 terms of degrees (l, l + 1), l even,
+        share one paired fields pass and contraction (degree_pairs)."""
         bins = [as_bin(b) for b in bins]
         nb = len(bins)
         if not (self.same23 and 1 <= nb <= MAX_BINS):
