@@ -108,8 +108,9 @@ def project_scaling_grid_numba(positions, weights, phi_array, phi_resolution=102
     pos = torch.as_tensor(np.ascontiguousarray(positions, dtype=np.float64), device=dev)
     if pos.ndim != 2 or pos.shape[1] != 3:
         raise ValueError(f"positions must have shape (n, 3), got {tuple(pos.shape)}")
-    w = torch.as_tensor(np.ascontiguousarray(np.broadcast_to(np.asarray(weights, dtype=np.float64),
-                                                             (pos.shape[0],))), device=dev)
+    # a writable copy: a broadcast of an already full-size array is a read-only view
+    w = torch.as_tensor(np.array(np.broadcast_to(np.asarray(weights, dtype=np.float64), (pos.shape[0],))),
+                        device=dev)
     phi = torch.as_tensor(np.ascontiguousarray(phi_array, dtype=np.float64), device=dev)
     eps, _, _ = kernels.deposit(pos, w, int(J), float(box_size), phi, int(phi_resolution),
                                 out_dtype=torch.float64)
